@@ -1,0 +1,286 @@
+"""Benchmark of the banded Smith-Waterman scoring stage (SW scoring-stage
+microbench): 1,000,000 banded candidate regions from synthetic protein data
+of 2,000 queries x 200,000 subjects (log-normal lengths, BLOSUM62 background,
+10 % planted homologs), band half-widths 8-128, BLOSUM62 with gap open 11 /
+extend 1, per-position query bias.  Metric: GCUPS (in-band cells counted as
+the reference counts them / second), every score bit-exact.
+
+One JSON line on rank 0.  `value`: device-resident jobs and scores (whole
+pipeline: classify, sort, pair, packed int16 kernel, int32 kernel), L2
+flushed between steps.  `e2e`: the same call through the C ABI with pinned
+host buffers (job upload and score download inside the timed region).
+`--impl reference` times the CPU oracle (the reference algorithm restated in
+C, all host threads) on bounded samples of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "banded SW GCUPS (bit-exact)"
+ALGO_OPS_PER_CELL = 11  # E: 2 sub + max, F: 2 sub + max, H: add + 3 max, best: max
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--jobs", type=int, default=1_000_000)
+    ap.add_argument("--queries", type=int, default=2000)
+    ap.add_argument("--subjects", type=int, default=200_000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample size (seconds of work)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(seed, nq, ns, nj):
+    from saber_gb300 import synth
+    qs, ss, planted = synth.protein_db(seed, nq, ns)
+    bias = synth.query_bias(seed + 1, qs)
+    jobs = synth.band_jobs(seed + 2, qs, ss, planted, nj)
+    return qs, ss, planted, bias, jobs
+
+
+def config_dict(a, world):
+    return {"workload": "sw-scoring-microbench: %d banded regions, %d queries x %d subjects, half-widths 8-128, "
+                        "BLOSUM62 11/1, query bias" % (a.jobs, a.queries, a.subjects),
+            "jobs_per_gpu": a.jobs, "queries": a.queries, "subjects": a.subjects, "seed": a.seed,
+            "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(qs, ss, bias, jobs, matrix, seconds):
+    """The oracle port on all host cores over a bounded sample of the jobs."""
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
+    n = min(jobs.size, 4000)
+    t0 = time.perf_counter()
+    _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs[:n], matrix, 11, 1, threads)
+    dt = time.perf_counter() - t0
+    rate = cells / max(dt, 1e-9)
+    want_cells = rate * seconds
+    per_job = cells / max(n, 1)
+    n2 = int(min(jobs.size, max(n, want_cells / max(per_job, 1))))
+    t0 = time.perf_counter()
+    _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs[:n2], matrix, 11, 1, threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(cells / dt / 1e9, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
+            "sample": "first %d of the %d jobs (%.3g cells, %.1f s), scalar C oracle (banded.rs restatement), "
+                      "%d threads" % (n2, jobs.size, cells, dt, threads)}
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    from saber_gb300.scoring import matrix
+    from oracle import oracle as orc
+    qs, ss, planted, bias, jobs = workload(a.seed, a.queries, a.subjects, a.jobs)
+    mat = matrix("BLOSUM62")
+    threads = os.cpu_count() or 1
+    per_step = 30000
+    rng = np.random.default_rng(a.seed + 9)
+    tot_cells, tot_t = 0, 0.0
+    for step in range(a.warmup + a.steps):
+        sel = jobs[rng.integers(0, jobs.size, size=min(per_step, jobs.size))]
+        t0 = time.perf_counter()
+        _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, sel, mat, 11, 1, threads)
+        dt = time.perf_counter() - t0
+        if step >= a.warmup:
+            tot_cells += cells
+            tot_t += dt
+    v = tot_cells / tot_t / 1e9
+    out = {"metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": "GCUPS", "n_gpus": world,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(tot_t / a.steps * 1e3, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic", "config": config_dict(a, world),
+           "cpu_baseline": {"value": round(v, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
+                            "sample": "%d random jobs per step of the same workload, scalar C restatement of "
+                                      "banded_score (the reference is Rust; no cargo here)" % per_step},
+           "e2e": {"value": round(v, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(a, rank, world, local_rank):
+    import torch
+    from saber_gb300 import Device
+    from saber_gb300.gpu import JOB_DTYPE
+    from saber_gb300.scoring import matrix
+    torch.cuda.set_device(local_rank)
+    seed = a.seed + 1000 * rank
+    qs, ss, planted, bias, jobs = workload(seed, a.queries, a.subjects, a.jobs)
+    mat = matrix("BLOSUM62")
+    dev = Device(local_rank)
+    dev.set_scheme(mat, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    stream = torch.cuda.ExternalStream(dev.stream, device=local_rank)
+    d_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).to("cuda:%d" % local_rank)
+    d_scores = torch.empty(jobs.size, dtype=torch.int32, device="cuda:%d" % local_rank)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda:%d" % local_rank)
+    dpx_peak, i32_peak = dev.probe_int_peak()
+
+    def step_dev():
+        return dev.score_band_jobs_dev(d_jobs.data_ptr(), jobs.size, d_scores.data_ptr())
+
+    for _ in range(a.warmup):
+        step_dev()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local_rank)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    tot_ms, fast_ms, cells, fast_cells, launches, lib_launches, rescored = 0.0, 0.0, 0, 0, 0, 0, 0
+    for _ in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        st = step_dev()
+        ev1.record(stream)
+        ev1.synchronize()
+        tot_ms += ev0.elapsed_time(ev1)
+        fast_ms += st["t_fast_ms"]
+        cells += st["banded_cells"]
+        fast_cells += st["fast_cells"]
+        launches += st["kernel_launches"]
+        lib_launches += st["library_launches"]
+        rescored += st["i16_rescored"]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t = torch.tensor([tot_ms], dtype=torch.float64)
+    c = torch.tensor([float(cells)], dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+    value = c.item() / (t.item() * 1e-3) / 1e9
+
+    # end to end: pinned host jobs in, scores out, through the C ABI
+    h_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).pin_memory()
+    h_scores = torch.empty(jobs.size, dtype=torch.int32).pin_memory()
+    for _ in range(max(1, a.warmup)):
+        dev.score_band_jobs_ptr(h_jobs.data_ptr(), jobs.size, h_scores.data_ptr())
+    e2e_s = 0.0
+    for _ in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev.score_band_jobs_ptr(h_jobs.data_ptr(), jobs.size, h_scores.data_ptr())
+        e2e_s += time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e = c.item() / te.item() / 1e9
+    same = bool(np.array_equal(h_scores.numpy(), d_scores.cpu().numpy()))
+
+    if rank != 0:
+        return
+    fast_s = fast_ms * 1e-3
+    achieved = fast_cells * ALGO_OPS_PER_CELL / fast_s / 1e12 if fast_s > 0 else None
+    peak = dpx_peak * 2 / 1e12
+    out = {"metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": round(tot_ms / a.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int16 (int32 rescore)", "data": "synthetic",
+           "config": config_dict(a, world),
+           "e2e": {"value": round(e2e, 2), "unit": "GCUPS", "h2d_bytes_per_step": int(jobs.nbytes),
+                   "d2h_bytes_per_step": int(jobs.size * 4), "matches_device_path": same},
+           "roofline": {"bound": "int", "kernel": "k_band_fast",
+                        "achieved": round(achieved, 3) if achieved else None, "peak": round(peak, 3),
+                        "unit": "Tops/s", "frac": round(achieved / peak, 3) if achieved else None,
+                        "traffic": None,
+                        "basis": "11 algorithmic int ops per in-band cell; peak = measured DPX s16x2 "
+                                 "lane-instructions/s x 2 (probe kernel, this run)",
+                        "fast_kernel_gcups": round(fast_cells / fast_s / 1e9, 2) if fast_s > 0 else None,
+                        "fast_share_of_step": round(fast_ms / tot_ms, 3) if tot_ms else None,
+                        "int32_max_lane_ops_per_s": i32_peak},
+           "clocks": clk, "gpu_launches": int(launches),
+           "library_launches": int(lib_launches), "i16_rescored": int(rescored),
+           "cells_per_step": int(cells // max(a.steps, 1))}
+    if not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(qs, ss, bias, jobs, mat, a.cpu_seconds)
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("gloo")
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+    else:
+        run_ours(a, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,158 @@
+/*
+ * saber_gpu.h — C ABI of the GB300 seed-and-extend scoring library
+ * (libsaber_gb300.so).
+ *
+ * Plain C types only: opaque handle, caller-owned buffers, int status codes
+ * (0 = ok, negative = error; the message is in saber_gpu_last_error).  No
+ * exception crosses the ABI.  One CUDA stream per handle; calls on one handle
+ * are serialised by an internal mutex (as the reference's CUDA backend
+ * serialises launches, src/gpu/cuda.rs:37,144); separate handles are
+ * independent.  There is no CPU fallback: a call that cannot run on the GPU
+ * returns an error.
+ *
+ * Encodings and conventions (src/gpu/mod.rs:9-26):
+ *   - residues are canonical alignment codes (protein ARNDCQEGHILKMFPSTWYVBZX*
+ *     -> 0..23, nucleotide ACGTN -> 0..4); codes >= 24 are scored as X (22);
+ *   - substitution matrix: 24x24 int32, row = query code, column = subject code;
+ *   - gaps (SABER convention): a gap of length k costs open + (k-1)*extend;
+ *   - bias[i] (int8) is added to every aligned column of query position i;
+ *   - scores are exact int32, never saturated.
+ *
+ * Bands are diagonal bands lo <= j - i <= hi in window coordinates (i query
+ * position, j position in the subject window), as src/algorithm/banded.rs:29-54.
+ */
+#ifndef SABER_GPU_H
+#define SABER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SABER_OK 0
+#define SABER_ERR_ARG (-1)      /* invalid argument */
+#define SABER_ERR_CUDA (-2)     /* CUDA runtime / launch error */
+#define SABER_ERR_NOMEM (-3)    /* device allocation failed */
+#define SABER_ERR_STATE (-4)    /* missing prerequisite (no DB, no queries, ...) */
+#define SABER_ERR_CAP (-5)      /* traceback direction matrix over the byte cap */
+#define SABER_ERR_DEVICE (-6)   /* a device-side check failed (error word set) */
+
+typedef struct saber_gpu saber_gpu;
+
+/* One banded scoring job: the query, a subject window inside the loaded
+ * database and the band its alignment must stay in.  Mirrors the reference's
+ * BandJob (src/algorithm/band_simd8.rs:27-33) plus the query/window
+ * addressing that Engine::score_windows does per region
+ * (src/search/engine.rs:1045-1054).  32 bytes. */
+typedef struct {
+    uint32_t query;     /* index into the loaded query set */
+    uint32_t subject;   /* subject id (informational; not read by the kernels) */
+    uint64_t win_begin; /* absolute residue offset of the window start in the DB */
+    uint32_t win_len;   /* window length n */
+    int32_t band_lo;    /* band, relative to the window: band_lo <= j - i <= band_hi */
+    int32_t band_hi;
+    uint32_t flags;     /* reserved, 0 */
+} saber_band_job;
+
+/* Work counters of the last scoring call (names follow the reference's
+ * Counters, src/search/engine.rs:205-282, where they exist). */
+typedef struct {
+    uint64_t jobs;            /* jobs scored */
+    uint64_t banded_cells;    /* in-band cells, counted as banded.rs:123-131 */
+    uint64_t fast_cells;      /* the part of banded_cells in jobs of the packed int16 kernel */
+    uint64_t fast_jobs;       /* jobs taken by the packed int16 kernel */
+    uint64_t generic_jobs;    /* jobs scored directly in int32 (narrow bands) */
+    uint64_t i16_rescored;    /* int16 results at the overflow limit, rescored in int32 */
+    uint64_t empty_jobs;      /* empty band / window / query: score 0 */
+    uint64_t kernel_launches; /* this library's own kernels launched by the call */
+    uint64_t library_launches;/* CUB sort / scan / select kernels launched by the call */
+    double t_prep_ms;         /* device time: classify, sort, pairing (CUDA events) */
+    double t_fast_ms;         /* device time of the packed int16 kernel */
+    double t_generic_ms;      /* device time of the int32 kernel */
+} saber_score_stats;
+
+/* ---- handle ---------------------------------------------------------- */
+
+/* Opens device `device` and creates the handle's stream.  Replaces
+ * try_init_backend / CudaBackend::new_on_device (src/gpu/mod.rs:63-77,
+ * src/gpu/cuda.rs:45-51). */
+int saber_gpu_open(int device, saber_gpu** out);
+int saber_gpu_close(saber_gpu* h);
+/* Last error message of this handle ("" when none).  Valid until the next call. */
+const char* saber_gpu_last_error(const saber_gpu* h);
+/* The CUDA stream (cudaStream_t) all work of this handle runs on. */
+void* saber_gpu_stream(saber_gpu* h);
+
+/* Scoring scheme for the following calls.  Replaces the `matrix` and `gaps`
+ * arguments of ScoreBackend::score_windows (src/gpu/mod.rs:51-58) and the
+ * banded Scheme (src/algorithm/banded.rs:21-27).  Requires
+ * 0 <= gap_extend <= gap_open <= 1000. */
+int saber_gpu_set_scheme(saber_gpu* h, const int32_t* matrix576, int32_t gap_open,
+                         int32_t gap_extend);
+
+/* Uploads the database residues (codes) and subject offsets (nsub + 1
+ * entries, offsets[0] = 0).  Replaces the residue access of SeedIndex
+ * (src/search/index.rs:644,701-717) for the device path. */
+int saber_gpu_load_db(saber_gpu* h, const uint8_t* residues, uint64_t n_residues,
+                      const uint64_t* offsets, uint64_t nsub);
+
+/* Uploads a query set: codes, offsets (nq + 1 entries) and the per-position
+ * composition bias (same offsets; NULL = no bias).  Builds the device query
+ * profiles for the current scheme.  Replaces the per-query QueryPrep inputs
+ * (src/search/engine.rs:497-510) that the scoring stage reads. */
+int saber_gpu_load_queries(saber_gpu* h, const uint8_t* codes, const uint64_t* offsets,
+                           const int8_t* bias, uint32_t nq);
+
+/* ---- banded scoring (score only) -------------------------------------
+ * Exact score of every job, identical to the reference's banded_score /
+ * score_banded_many (src/algorithm/banded.rs:408-449,
+ * src/algorithm/band_simd8.rs:78-185): the optimal local alignment inside
+ * the clipped band; 0 for an empty band, window or query. */
+
+/* Host buffers: copies the jobs in and the scores out on the handle's stream
+ * (end-to-end path). */
+int saber_gpu_score_band_jobs(saber_gpu* h, const saber_band_job* jobs, uint64_t njobs,
+                              int32_t* scores, saber_score_stats* stats);
+
+/* Device buffers: d_jobs and d_scores are device pointers; the call enqueues
+ * on the handle's stream and returns after the work is queued and its
+ * bookkeeping read back (one small device-to-host read). */
+int saber_gpu_score_band_jobs_dev(saber_gpu* h, const saber_band_job* d_jobs, uint64_t njobs,
+                                  int32_t* d_scores, saber_score_stats* stats);
+
+/* One query against many banded subject windows, host buffers, caller order:
+ * the signature of score_banded_many (src/algorithm/band_simd8.rs:78-86) in C.
+ * subjects: concatenated windows with offsets (njobs + 1); bands: lo/hi per job. */
+int saber_gpu_score_banded_many(saber_gpu* h, const uint8_t* query, uint32_t m,
+                                const int8_t* bias, const uint8_t* subjects,
+                                const uint64_t* sub_offsets, const int64_t* band_lo,
+                                const int64_t* band_hi, uint64_t njobs, int32_t* scores);
+
+/* ScoreBackend::score_windows (src/gpu/mod.rs:51-58, src/gpu/cuda.rs:112-155):
+ * full-window local SW score of one query against every window, in input
+ * order, with its own matrix and gaps (the handle's scheme is not changed). */
+int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m,
+                            const int8_t* bias, const uint8_t* windows,
+                            const uint64_t* win_offsets, uint32_t nwin,
+                            const int32_t* matrix576, int32_t gap_open, int32_t gap_extend,
+                            int32_t* scores);
+
+/* Measures the integer-pipe peak of this GPU for the roofline: throughput of
+ * the DPX packed-int16 max/add-max instructions the scoring kernel uses
+ * (lane-instructions per second; each does two 16-bit operations) and of plain
+ * int32 max instructions.  No reference counterpart (measurement utility). */
+int saber_gpu_probe_int_peak(saber_gpu* h, double* dpx_s16x2_lane_ops_per_s,
+                             double* i32_lane_ops_per_s);
+
+/* In-band cell count of one job after clipping the band to the m x n
+ * rectangle, counted as the reference counts banded cells (the row_range span
+ * summed over rows, src/algorithm/banded.rs:123-131,208).  Host-only helper;
+ * needs no GPU. */
+uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

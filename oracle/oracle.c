@@ -1,0 +1,433 @@
+/*
+ * CPU oracle (test infrastructure only) — see oracle.h for scope and pinning.
+ * Restates the reference's scalar algorithms; each function cites the
+ * reference file:line it follows.
+ */
+#include "oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* alphabet.rs:39-41: codes >= 24 are scored as X (22). */
+static inline int code_index(uint8_t c) { return c < 24 ? (int)c : 22; }
+
+/* banded.rs:121 */
+#define NEG32 (INT32_MIN / 4)
+
+static inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+static inline int32_t max32(int32_t a, int32_t b) { return a > b ? a : b; }
+
+int64_t orc_sw_reference(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                         const int32_t* matrix, const int8_t* bias,
+                         int64_t go, int64_t ge, uint64_t* q_end, uint64_t* s_end) {
+    /* reference.rs:15-52 */
+    *q_end = 0;
+    *s_end = 0;
+    if (m == 0 || n == 0) return 0;
+    const int64_t neg = INT64_MIN / 4;
+    size_t w = n + 1;
+    int64_t* h = (int64_t*)calloc((m + 1) * w, sizeof(int64_t));
+    int64_t* e = (int64_t*)malloc((m + 1) * w * sizeof(int64_t));
+    int64_t* f = (int64_t*)malloc((m + 1) * w * sizeof(int64_t));
+    for (size_t t = 0; t < (m + 1) * w; t++) { e[t] = neg; f[t] = neg; }
+    int64_t best = 0;
+    uint64_t bi = 0, bj = 0;
+    for (size_t i = 1; i <= m; i++) {
+        int qi = code_index(q[i - 1]);
+        int64_t b = bias ? (int64_t)bias[i - 1] : 0;
+        for (size_t j = 1; j <= n; j++) {
+            int sj = code_index(s[j - 1]);
+            int64_t ee = max64(h[i * w + j - 1] - go, e[i * w + j - 1] - ge);
+            int64_t ff = max64(h[(i - 1) * w + j] - go, f[(i - 1) * w + j] - ge);
+            int64_t dd = h[(i - 1) * w + j - 1] + (int64_t)matrix[qi * 24 + sj] + b;
+            int64_t v = max64(max64(max64(0, ee), ff), dd);
+            e[i * w + j] = ee;
+            f[i * w + j] = ff;
+            h[i * w + j] = v;
+            if (v > best) { best = v; bi = i; bj = j; }
+        }
+    }
+    free(h); free(e); free(f);
+    *q_end = bi;
+    *s_end = bj;
+    return best;
+}
+
+int orc_score_alignment(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                        uint64_t q_start, uint64_t s_start,
+                        const uint8_t* ops, const uint32_t* lens, uint32_t n_ops,
+                        const int32_t* matrix, const int8_t* bias,
+                        int64_t go, int64_t ge,
+                        int64_t* score, uint64_t* q_end, uint64_t* s_end) {
+    /* reference.rs:58-103 */
+    uint64_t i = q_start, j = s_start;
+    int64_t sc = 0;
+    for (uint32_t t = 0; t < n_ops; t++) {
+        uint64_t len = lens[t];
+        switch (ops[t]) {
+        case 'M':
+            for (uint64_t k = 0; k < len; k++) {
+                if (i >= m || j >= n) return -1;
+                int64_t b = bias ? (int64_t)bias[i] : 0;
+                sc += (int64_t)matrix[code_index(q[i]) * 24 + code_index(s[j])] + b;
+                i++; j++;
+            }
+            break;
+        case 'I':
+            if (len == 0 || i + len > m) return -1;
+            sc -= go + ((int64_t)len - 1) * ge;
+            i += len;
+            break;
+        case 'D':
+            if (len == 0 || j + len > n) return -1;
+            sc -= go + ((int64_t)len - 1) * ge;
+            j += len;
+            break;
+        default:
+            return -1;
+        }
+    }
+    *score = sc;
+    *q_end = i;
+    *s_end = j;
+    return 0;
+}
+
+/* banded.rs:45-47 (Band::clip) and 41-43 (width). */
+static void band_clip(int64_t* lo, int64_t* hi, size_t m, size_t n) {
+    int64_t l = *lo, h = *hi;
+    if (l < -((int64_t)m - 1)) l = -((int64_t)m - 1);
+    if (h > (int64_t)n - 1) h = (int64_t)n - 1;
+    *lo = l;
+    *hi = h;
+}
+
+/* banded.rs:123-131 (row_range): k in [kmin, kmax], j = i + lo + k. */
+static int row_range(int64_t i, int64_t lo, int64_t w, int64_t n, int64_t* kmin, int64_t* kmax) {
+    int64_t a = -(i + lo);
+    if (a < 0) a = 0;
+    int64_t b = n - 1 - i - lo;
+    if (b > w - 1) b = w - 1;
+    *kmin = a;
+    *kmax = b;
+    return a <= b;
+}
+
+void orc_banded_score(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                      const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                      orc_band_score* out) {
+    /* banded.rs:134-224 */
+    out->score = 0; out->q_end = 0; out->s_end = 0; out->cells = 0;
+    if (m == 0 || n == 0 || hi < lo) return;
+    band_clip(&lo, &hi, m, n);
+    int64_t w = hi - lo + 1;
+    if (w <= 0) return;
+    int32_t* hp = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* fp = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* hc = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* fc = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    for (int64_t k = 0; k <= w; k++) { hp[k] = fp[k] = hc[k] = fc[k] = NEG32; }
+    const int32_t go = sc.gap_open, ge = sc.gap_extend;
+    uint64_t cells = 0;
+    int32_t best = 0;
+    uint64_t bq = 0, bs = 0;
+    for (int64_t i = 0; i < (int64_t)m; i++) {
+        int64_t kmin, kmax;
+        if (!row_range(i, lo, w, (int64_t)n, &kmin, &kmax)) {
+            for (int64_t k = 0; k < w; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+        } else {
+            const int32_t* row = sc.matrix + code_index(q[i]) * 24;
+            int32_t b = bias ? (int32_t)bias[i] : 0;
+            int32_t e = NEG32, h_left = NEG32;
+            int64_t base = i + lo;
+            for (int64_t k = kmin; k <= kmax; k++) {
+                int64_t j = base + k;
+                int32_t ecand = max32(h_left - go, e - ge);
+                e = k > kmin ? ecand : NEG32;
+                int32_t f = i >= 1 ? max32(hp[k + 1] - go, fp[k + 1] - ge) : NEG32;
+                int32_t hd = (i >= 1 && j >= 1) ? hp[k] : 0;
+                int32_t diag = hd + row[code_index(s[j])] + b;
+                int32_t h = max32(max32(max32(diag, e), f), 0);
+                hc[k] = h;
+                fc[k] = f;
+                h_left = h;
+                if (h > best) { best = h; bq = (uint64_t)i + 1; bs = (uint64_t)j + 1; }
+            }
+            cells += (uint64_t)(kmax - kmin + 1);
+            for (int64_t k = 0; k < kmin; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+            for (int64_t k = kmax + 1; k < w; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+        }
+        int32_t* t;
+        t = hp; hp = hc; hc = t;
+        t = fp; fp = fc; fc = t;
+    }
+    out->score = best;
+    out->q_end = bq;
+    out->s_end = bs;
+    out->cells = cells;
+    free(hp); free(fp); free(hc); free(fc);
+}
+
+/* Shared DP of banded_align_scalar (banded.rs:250-326); fills dir, returns
+ * best (score, i, k) and cells.  stop_at: banded_simd.rs:594-596. */
+static void banded_dir_dp(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                          const int8_t* bias, orc_scheme sc, int64_t lo, int64_t w,
+                          uint8_t* dir, int32_t stop_at,
+                          int32_t* best_score, int64_t* best_i, int64_t* best_k, uint64_t* cells_out) {
+    int32_t* hp = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* fp = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* hc = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    int32_t* fc = (int32_t*)malloc((size_t)(w + 1) * sizeof(int32_t));
+    for (int64_t k = 0; k <= w; k++) { hp[k] = fp[k] = hc[k] = fc[k] = NEG32; }
+    const int32_t go = sc.gap_open, ge = sc.gap_extend;
+    int32_t bsc = 0;
+    int64_t bi = 0, bk = 0;
+    uint64_t cells = 0;
+    for (int64_t i = 0; i < (int64_t)m; i++) {
+        int64_t kmin, kmax;
+        if (!row_range(i, lo, w, (int64_t)n, &kmin, &kmax)) {
+            for (int64_t k = 0; k < w; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+        } else {
+            const int32_t* row = sc.matrix + code_index(q[i]) * 24;
+            int32_t b = bias ? (int32_t)bias[i] : 0;
+            int32_t e = NEG32, h_left = NEG32;
+            int64_t base = i + lo;
+            uint8_t* dirrow = dir + (size_t)(i * w);
+            for (int64_t k = kmin; k <= kmax; k++) {
+                int64_t j = base + k;
+                int32_t eo = h_left - go;
+                int32_t ee = e - ge;
+                uint8_t e_ext = ee > eo;
+                e = k > kmin ? max32(ee, eo) : NEG32;
+                int32_t fo = hp[k + 1] - go;
+                int32_t fe = fp[k + 1] - ge;
+                uint8_t f_ext = fe > fo;
+                int32_t f = i >= 1 ? max32(fe, fo) : NEG32;
+                int32_t hd = (i >= 1 && j >= 1) ? hp[k] : 0;
+                int32_t diag = hd + row[code_index(s[j])] + b;
+                uint8_t c1 = diag > 0;
+                int32_t h1 = max32(diag, 0);
+                uint8_t c2 = e > h1;
+                int32_t h2 = max32(h1, e);
+                uint8_t c3 = f > h2;
+                int32_t h = max32(h2, f);
+                uint8_t org = c3 ? 3 : (c2 ? 2 : c1);
+                hc[k] = h;
+                fc[k] = f;
+                dirrow[k] = (uint8_t)(org | (e_ext << 2) | (f_ext << 3));
+                h_left = h;
+                if (h > bsc) { bsc = h; bi = i; bk = k; }
+            }
+            cells += (uint64_t)(kmax - kmin + 1);
+            for (int64_t k = 0; k < kmin; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+            for (int64_t k = kmax + 1; k < w; k++) { hc[k] = NEG32; fc[k] = NEG32; }
+        }
+        int32_t* t;
+        t = hp; hp = hc; hc = t;
+        t = fp; fp = fc; fc = t;
+        if (bsc >= stop_at) break;
+    }
+    *best_score = bsc;
+    *best_i = bi;
+    *best_k = bk;
+    *cells_out = cells;
+    free(hp); free(fp); free(hc); free(fc);
+}
+
+uint64_t orc_banded_dir(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                        const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                        uint8_t* dir, uint64_t dir_cap, int64_t* clipped_lo) {
+    if (m == 0 || n == 0 || hi < lo) return 0;
+    band_clip(&lo, &hi, m, n);
+    int64_t w = hi - lo + 1;
+    if (w <= 0 || (uint64_t)(m * (uint64_t)w) > dir_cap) return 0;
+    memset(dir, 0xFF, (size_t)(m * (uint64_t)w));
+    int32_t bsc; int64_t bi, bk; uint64_t cells;
+    banded_dir_dp(q, m, s, n, bias, sc, lo, w, dir, INT32_MAX, &bsc, &bi, &bk, &cells);
+    *clipped_lo = lo;
+    return (uint64_t)w;
+}
+
+int orc_banded_align(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                     const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                     uint64_t max_dir_bytes, int32_t stop_at,
+                     orc_alignment* out, uint8_t* ops, uint32_t* lens, uint32_t ops_cap) {
+    /* banded.rs:227-332 */
+    memset(out, 0, sizeof(*out));
+    if (m == 0 || n == 0 || hi < lo) return 0;
+    band_clip(&lo, &hi, m, n);
+    int64_t w = hi - lo + 1;
+    if (w <= 0) return 0;
+    uint64_t need = (uint64_t)m * (uint64_t)w;
+    if (need > max_dir_bytes) return -2;
+    uint8_t* dir = (uint8_t*)calloc((size_t)need, 1);
+    int32_t bsc; int64_t bi, bk; uint64_t cells;
+    banded_dir_dp(q, m, s, n, bias, sc, lo, w, dir, stop_at, &bsc, &bi, &bk, &cells);
+    if (bsc <= 0) { free(dir); out->cells = cells; return 0; }
+
+    /* walk, banded.rs:336-403 */
+    uint64_t q_end = (uint64_t)bi + 1;
+    uint64_t s_end = (uint64_t)(bi + lo + bk) + 1;
+    size_t cap = (size_t)(m + n + 2);
+    uint8_t* opbuf = (uint8_t*)malloc(cap);
+    size_t nop = 0;
+    int state = 0; /* 0 = H, 1 = E (query gap, 'D'), 2 = F (subject gap, 'I') */
+    int64_t i = bi, k = bk;
+    for (;;) {
+        uint8_t d = dir[(size_t)(i * w + k)];
+        if (state == 0) {
+            uint8_t org = d & 3;
+            if (org == 0) break;
+            if (org == 1) {
+                opbuf[nop++] = 'M';
+                int64_t j = i + lo + k;
+                if (i == 0 || j == 0) break;
+                i -= 1;
+            } else if (org == 2) {
+                state = 1;
+            } else {
+                state = 2;
+            }
+        } else if (state == 1) {
+            opbuf[nop++] = 'D';
+            int ext = (d & 4) != 0;
+            k -= 1;
+            if (!ext) state = 0;
+        } else {
+            opbuf[nop++] = 'I';
+            int ext = (d & 8) != 0;
+            i -= 1;
+            k += 1;
+            if (!ext) state = 0;
+        }
+    }
+    /* reverse, derive start coordinates, run-length encode */
+    uint64_t qs = q_end, ss = s_end;
+    uint32_t runs = 0;
+    uint8_t* rop = (uint8_t*)malloc(nop + 1);
+    uint32_t* rlen = (uint32_t*)malloc((nop + 1) * sizeof(uint32_t));
+    for (size_t t = 0; t < nop; t++) {
+        uint8_t op = opbuf[nop - 1 - t];
+        if (op == 'M') { qs--; ss--; }
+        else if (op == 'I') qs--;
+        else ss--;
+        if (runs > 0 && rop[runs - 1] == op) {
+            rlen[runs - 1]++;
+        } else {
+            rop[runs] = op;
+            rlen[runs] = 1;
+            runs++;
+        }
+    }
+    int rc = 1;
+    if (runs > ops_cap || !ops || !lens) {
+        rc = -3;
+    } else {
+        memcpy(ops, rop, runs);
+        memcpy(lens, rlen, runs * sizeof(uint32_t));
+    }
+    free(rop);
+    free(rlen);
+    free(opbuf);
+    free(dir);
+    out->score = bsc;
+    out->q_start = qs;
+    out->q_end = q_end;
+    out->s_start = ss;
+    out->s_end = s_end;
+    out->cells = cells;
+    out->n_ops = runs;
+    return rc;
+}
+
+int32_t orc_ungapped_xdrop(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                           uint64_t qp, uint64_t sp, const int32_t* matrix,
+                           const int8_t* bias, int32_t x,
+                           uint64_t* q_lo, uint64_t* q_hi) {
+    /* engine.rs:2460-2494 */
+    int32_t best_r = 0, cur = 0;
+    uint64_t end = qp;
+    uint64_t i = qp, j = sp;
+    while (i < m && j < n) {
+        cur += matrix[code_index(q[i]) * 24 + code_index(s[j])] + (bias ? (int32_t)bias[i] : 0);
+        i++; j++;
+        if (cur > best_r) { best_r = cur; end = i; }
+        else if (cur < best_r - x) break;
+    }
+    int32_t best_l = 0;
+    cur = 0;
+    uint64_t start = qp;
+    int64_t ii = (int64_t)qp - 1, jj = (int64_t)sp - 1;
+    while (ii >= 0 && jj >= 0) {
+        cur += matrix[code_index(q[ii]) * 24 + code_index(s[jj])] + (bias ? (int32_t)bias[ii] : 0);
+        if (cur > best_l) { best_l = cur; start = (uint64_t)ii; }
+        else if (cur < best_l - x) break;
+        ii--; jj--;
+    }
+    *q_lo = start;
+    *q_hi = end > qp ? end : qp;
+    return best_r + best_l;
+}
+
+/* ---- batched jobs ------------------------------------------------------ */
+
+typedef struct {
+    const uint8_t* residues;
+    const uint8_t* qcodes;
+    const uint64_t* qoffs;
+    const int8_t* qbias;
+    const orc_band_job* jobs;
+    uint64_t njobs;
+    orc_scheme sc;
+    int32_t* scores;
+    uint64_t next;          /* shared work counter (atomic) */
+    uint64_t cells;         /* summed under atomic add */
+} batch_ctx;
+
+static void* batch_worker(void* arg) {
+    batch_ctx* c = (batch_ctx*)arg;
+    uint64_t local_cells = 0;
+    for (;;) {
+        uint64_t b = __atomic_fetch_add(&c->next, 64, __ATOMIC_RELAXED);
+        if (b >= c->njobs) break;
+        uint64_t e = b + 64 < c->njobs ? b + 64 : c->njobs;
+        for (uint64_t t = b; t < e; t++) {
+            const orc_band_job* jb = &c->jobs[t];
+            uint64_t q0 = c->qoffs[jb->query], q1 = c->qoffs[jb->query + 1];
+            orc_band_score o;
+            orc_banded_score(c->qcodes + q0, (size_t)(q1 - q0),
+                             c->residues + jb->win_begin, jb->win_len,
+                             c->qbias ? c->qbias + q0 : NULL, c->sc,
+                             jb->band_lo, jb->band_hi, &o);
+            c->scores[t] = o.score;
+            local_cells += o.cells;
+        }
+    }
+    __atomic_fetch_add(&c->cells, local_cells, __ATOMIC_RELAXED);
+    return NULL;
+}
+
+int orc_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
+                        const uint64_t* qoffs, const int8_t* qbias,
+                        const orc_band_job* jobs, uint64_t njobs,
+                        const int32_t* matrix, int32_t gap_open, int32_t gap_extend,
+                        int32_t* scores, int threads, uint64_t* cells_out) {
+    batch_ctx c;
+    c.residues = residues; c.qcodes = qcodes; c.qoffs = qoffs; c.qbias = qbias;
+    c.jobs = jobs; c.njobs = njobs; c.scores = scores;
+    c.sc.matrix = matrix; c.sc.gap_open = gap_open; c.sc.gap_extend = gap_extend;
+    c.next = 0; c.cells = 0;
+    if (threads < 1) threads = 1;
+    if (threads > 512) threads = 512;
+    pthread_t tid[512];
+    int started = 0;
+    for (int t = 1; t < threads; t++) {
+        if (pthread_create(&tid[t], NULL, batch_worker, &c) == 0) started = t;
+        else break;
+    }
+    batch_worker(&c);
+    for (int t = 1; t <= started; t++) pthread_join(tid[t], NULL);
+    if (cells_out) *cells_out = c.cells;
+    return 0;
+}

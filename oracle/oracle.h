@@ -1,0 +1,123 @@
+/*
+ * CPU oracle for the seed-and-extend scoring path — TEST INFRASTRUCTURE ONLY.
+ *
+ * This is a plain-C restatement of the reference (SABER 1.4.0, Rust) scalar
+ * algorithms that the GPU path must reproduce bit for bit.  It is used by the
+ * tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, and
+ * only as the checker or as the timed CPU reference — never by the product
+ * library.  Every function cites the reference file:line it follows (paths
+ * relative to the reference crate root).
+ *
+ * Pinning: the full-window SW score is pinned against the reference's own
+ * compiled kernel (src/gpu/kernels/sw.cu, built here by oracle/Makefile into
+ * oracle/_ref) on the reference's test-vector generator
+ * (examples/gpu_vectors.rs), committed as tests/golden/sw_vectors.json, and
+ * against the known answers of the reference unit tests
+ * (reference.rs:128-146, banded.rs:716-731, gpu/mod.rs:178-182).
+ */
+#ifndef SABER_ORACLE_H
+#define SABER_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scoring scheme: 24x24 matrix in NCBI order (row = query code, column =
+ * subject code), SABER gap convention (a gap of length k costs
+ * open + (k-1)*extend).  banded.rs:21-27. */
+typedef struct {
+    const int32_t* matrix; /* 576 entries, row-major */
+    int32_t gap_open;
+    int32_t gap_extend;
+} orc_scheme;
+
+/* banded.rs:90-99 */
+typedef struct {
+    int32_t score;
+    uint64_t q_end;  /* exclusive end of the first (row-major) optimal cell */
+    uint64_t s_end;
+    uint64_t cells;  /* evaluated in-band cells */
+} orc_band_score;
+
+/* banded.rs:101-113.  ops are (op, len) run-length pairs, op in 'M','I','D'. */
+typedef struct {
+    int32_t score;
+    uint64_t q_start, q_end, s_start, s_end; /* 0-based, half open */
+    uint64_t cells;
+    uint32_t n_ops;
+} orc_alignment;
+
+/* reference.rs:15-52: full-matrix Gotoh SW in i64; first row-major maximum. */
+int64_t orc_sw_reference(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                         const int32_t* matrix, const int8_t* bias,
+                         int64_t gap_open, int64_t gap_extend,
+                         uint64_t* q_end, uint64_t* s_end);
+
+/* reference.rs:58-103.  Returns 0 and fills score/ends, or -1 when the ops
+ * run past a sequence end or hold an unknown op. */
+int orc_score_alignment(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                        uint64_t q_start, uint64_t s_start,
+                        const uint8_t* ops, const uint32_t* lens, uint32_t n_ops,
+                        const int32_t* matrix, const int8_t* bias,
+                        int64_t gap_open, int64_t gap_extend,
+                        int64_t* score, uint64_t* q_end, uint64_t* s_end);
+
+/* banded.rs:134-224 (banded_score_scalar).  Band is lo <= j - i <= hi. */
+void orc_banded_score(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                      const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                      orc_band_score* out);
+
+/* banded.rs:227-332 + walk banded.rs:336-403, with the stop_at early exit of
+ * the dispatched kernel (banded_simd.rs:594-596: rows after the first whose
+ * best reaches stop_at are not computed; the alignment is unchanged, only
+ * `cells` shrinks).
+ * Returns 1 and fills `out`/ops on an alignment, 0 when the best score is
+ * 0 (Ok(None)), -2 when m*w exceeds max_dir_bytes (Err(need)), -3 when the
+ * ops buffer is too small.  ops/lens receive at most ops_cap runs. */
+int orc_banded_align(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                     const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                     uint64_t max_dir_bytes, int32_t stop_at,
+                     orc_alignment* out, uint8_t* ops, uint32_t* lens, uint32_t ops_cap);
+
+/* Direction bytes of the scalar traceback kernel (banded.rs:287-313), for
+ * tests that compare per-cell origins: dir receives m*w bytes (row i, band
+ * offset k at dir[i*w+k]); cells outside the row range are left 0xFF.
+ * Returns the clipped width w (0 when empty). */
+uint64_t orc_banded_dir(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                        const int8_t* bias, orc_scheme sc, int64_t lo, int64_t hi,
+                        uint8_t* dir, uint64_t dir_cap, int64_t* clipped_lo);
+
+/* engine.rs:2460-2494 (ungapped_xdrop): returns score; q range [*q_lo, *q_hi). */
+int32_t orc_ungapped_xdrop(const uint8_t* q, size_t m, const uint8_t* s, size_t n,
+                           uint64_t qp, uint64_t sp, const int32_t* matrix,
+                           const int8_t* bias, int32_t x,
+                           uint64_t* q_lo, uint64_t* q_hi);
+
+/* ---- batched banded jobs (CPU baseline and parity driver) ---------------
+ * Same job layout as the GPU library (include/saber_gpu.h, saber_band_job). */
+typedef struct {
+    uint32_t query;     /* index into the query set */
+    uint32_t subject;   /* subject id (informational) */
+    uint64_t win_begin; /* absolute residue offset of the window start */
+    uint32_t win_len;   /* window length n */
+    int32_t band_lo;    /* band relative to the window, j - i */
+    int32_t band_hi;
+    uint32_t flags;
+} orc_band_job;
+
+/* Scores every job with orc_banded_score (score only; score_banded_many's
+ * contract, band_simd8.rs:75-185) using `threads` POSIX threads.
+ * cells_out (optional) receives the total in-band cells. */
+int orc_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
+                        const uint64_t* qoffs, const int8_t* qbias,
+                        const orc_band_job* jobs, uint64_t njobs,
+                        const int32_t* matrix, int32_t gap_open, int32_t gap_extend,
+                        int32_t* scores, int threads, uint64_t* cells_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

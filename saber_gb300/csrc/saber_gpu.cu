@@ -1,0 +1,716 @@
+// C-ABI runtime of libsaber_gb300.so: handle, device-resident database and
+// query sets, and the banded scoring pipeline
+//   classify -> radix sort (query, width) -> pair equal-width jobs ->
+//   warp tasks -> packed int16 kernel -> int32 kernel (narrow bands and
+//   int16 overflows)
+// all on the handle's stream.  See include/saber_gpu.h for the contract.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "band_common.cuh"
+#include "saber_gpu.h"
+
+namespace saber {
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    // grow-only; contents are not preserved
+    cudaError_t reserve(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+struct QuerySet {
+    uint32_t nq = 0;
+    std::vector<uint64_t> offs;  // host copy
+    DevBuf codes, offsets, bias, prof, prof_off, prof_mpad;
+    bool has = false;
+    bool has_bias = false;
+};
+
+// Residues + subject offsets + a query set with profiles for one scheme.
+struct Dataset {
+    DevBuf res, soff;
+    uint64_t n_res = 0, nsub = 0;
+    bool has_db = false;
+    QuerySet qs;
+};
+
+struct Scheme {
+    int32_t matrix[576];
+    int32_t go = 11, ge = 1;
+    bool has = false;
+    DevBuf d_matrix;
+};
+
+}  // namespace saber
+
+struct saber_gpu {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+    int sm_count = 0;
+    // the handle's scheme and dataset (set_scheme / load_db / load_queries)
+    saber::Scheme scheme;
+    saber::Dataset main;
+    // per-call scheme and dataset of the one-query entry points
+    saber::Scheme eph_scheme;
+    saber::Dataset eph;
+    // per-call scratch
+    saber::DevBuf keys_in, keys_out, vals_in, vals_out, aux, aux2, flags, pairs, pair_pos, wtask,
+        counts, stats, cub_tmp, bufs, slabs, list, jobs_dev, scores_dev;
+};
+
+namespace saber {
+
+static int fail(saber_gpu* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    h->err = buf;
+    return code;
+}
+
+#define CU(h, call)                                                                       \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return ::saber::fail((h), SABER_ERR_CUDA, "%s: %s (%s:%d)", #call,            \
+                                 cudaGetErrorString(e_), __FILE__, __LINE__);             \
+    } while (0)
+#define CUALLOC(h, buf, bytes)                                                            \
+    do {                                                                                  \
+        cudaError_t e_ = (buf).reserve(bytes);                                            \
+        if (e_ != cudaSuccess)                                                            \
+            return ::saber::fail((h), SABER_ERR_NOMEM, "device allocation of %zu bytes: %s", \
+                                 (size_t)(bytes), cudaGetErrorString(e_));                \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// small kernels
+// ---------------------------------------------------------------------------
+__global__ void k_canon(uint8_t* __restrict__ r, uint64_t n) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        uint8_t c = r[i];
+        if (c >= 24) r[i] = 22;  // alphabet.rs:39-41
+    }
+}
+
+// Query profile P[c][i] = S(q_i, c) + bias_i for c < 24 and i < m, the
+// sentinel score elsewhere (row 24 and rows past the query end).  The
+// reference builds the same per-query table for its ungapped extension
+// (engine.rs:387-388) and a per-subject one in its int16 kernel
+// (banded_simd.rs:425-469).
+__global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __restrict__ qoffs,
+                          const int8_t* __restrict__ bias, const int32_t* __restrict__ matrix,
+                          const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
+                          int16_t* __restrict__ prof) {
+    const uint32_t q = blockIdx.x;
+    const uint64_t q0 = qoffs[q];
+    const int m = (int)(qoffs[q + 1] - q0);
+    const int mpad = (int)prof_mpad[q];
+    int16_t* P = prof + prof_off[q];
+    for (int t = threadIdx.x; t < kProfRows * mpad; t += blockDim.x) {
+        int c = t / mpad, i = t - c * mpad;
+        int v = kSent16;
+        if (c < 24 && i < m) {
+            int qc = codes[q0 + i];
+            if (qc >= 24) qc = 22;
+            v = matrix[qc * 24 + c] + (bias ? (int)bias[q0 + i] : 0);
+        }
+        P[t] = (int16_t)v;
+    }
+}
+
+// stats layout (uint64): 0 cells, 1 wmax_fast, 2 wmax_gen, 3 bad job count, 4 fast cells
+// counts layout (uint32): 0 n_fast, 1 n_gen, 2 n_pairs, 3 n_wtasks, 4 n_empty,
+//                         5 generic list count (class 1 + rescued), 6 wt counter
+__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs,
+                           const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
+                           uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                           int32_t* __restrict__ scores, uint32_t* __restrict__ counts,
+                           unsigned long long* __restrict__ stats) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t cells = 0, fcells = 0;
+    uint32_t c0 = 0, c1 = 0, c2 = 0, bad = 0;
+    unsigned long long wf = 0, wg = 0;
+    for (; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
+        saber_band_job j = jobs[t];
+        vals[t] = (uint32_t)t;
+        bool ok = j.query < nq && j.win_begin + (uint64_t)j.win_len <= n_res;
+        int64_t m = ok ? (int64_t)(qoffs[j.query + 1] - qoffs[j.query]) : 0;
+        int64_t lo = j.band_lo, hi = j.band_hi;
+        int64_t w = ok ? clip_band(m, j.win_len, lo, hi) : 0;
+        if (!ok) bad++;
+        if (w == 0) {
+            scores[t] = 0;
+            keys[t] = 2ull << 62;
+            c2++;
+        } else {
+            uint64_t jc = band_cells(m, j.win_len, lo, hi);
+            cells += jc;
+            if (w < kStripRows || w >= (1 << 24)) {
+                keys[t] = (1ull << 62) | t;
+                c1++;
+                wg = max(wg, (unsigned long long)w);
+            } else {
+                keys[t] = ((uint64_t)j.query << 24) | (uint64_t)w;
+                c0++;
+                fcells += jc;
+                wf = max(wf, (unsigned long long)w);
+            }
+        }
+    }
+    atomicAdd(&counts[0], c0);
+    atomicAdd(&counts[1], c1);
+    atomicAdd(&counts[4], c2);
+    atomicAdd(&stats[0], (unsigned long long)cells);
+    atomicMax(&stats[1], wf);
+    atomicMax(&stats[2], wg);
+    atomicAdd(&stats[3], (unsigned long long)bad);
+    atomicAdd(&stats[4], (unsigned long long)fcells);
+}
+
+// run_start candidates: position p when the sorted key changes at p.
+__global__ void k_run_marks(const uint64_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ mark) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    mark[p] = (p == 0 || keys[p] != keys[p - 1]) ? p : 0u;
+}
+
+// flag every second position of a run (the first job of each pair).
+__global__ void k_pair_flags(const uint32_t* __restrict__ run_start, uint32_t n, uint8_t* __restrict__ flag) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    flag[p] = ((p - run_start[p]) & 1u) == 0;
+}
+
+__global__ void k_make_pairs(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pos,
+                             const uint32_t* __restrict__ counts, uint32_t n_fast,
+                             uint2* __restrict__ pairs, uint32_t* __restrict__ qmark) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t np = counts[2];
+    if (i >= np) return;
+    uint32_t p = pos[i];
+    bool two = p + 1 < n_fast && keys[p + 1] == keys[p];
+    pairs[i] = make_uint2(p, two ? 2u : 1u);
+    uint64_t q = keys[p] >> 24;
+    bool newq = i == 0 || (keys[pos[i - 1]] >> 24) != q;
+    qmark[i] = newq ? i : 0u;
+}
+
+__global__ void k_wtask_flags(const uint32_t* __restrict__ qstart, const uint32_t* __restrict__ counts,
+                              uint8_t* __restrict__ flag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= counts[2]) return;
+    flag[i] = ((i - qstart[i]) & 31u) == 0;
+}
+
+struct MaxOp {
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
+};
+
+static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
+    uint64_t b = (n + t - 1) / t;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+
+// ---------------------------------------------------------------------------
+// the scoring pipeline (device-resident jobs and scores)
+// ---------------------------------------------------------------------------
+static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, const saber_band_job* d_jobs,
+                          uint64_t njobs, int32_t* d_scores, saber_score_stats* st) {
+    if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (!ds.has_db) return fail(h, SABER_ERR_STATE, "no database loaded");
+    if (!ds.qs.has) return fail(h, SABER_ERR_STATE, "no query set loaded");
+    if (njobs >= (1ull << 31))
+        return fail(h, SABER_ERR_ARG, "too many jobs in one call (%llu)", (unsigned long long)njobs);
+    saber_score_stats local{};
+    if (njobs == 0) {
+        if (st) *st = local;
+        return SABER_OK;
+    }
+    cudaStream_t s = h->stream;
+    const uint32_t n = (uint32_t)njobs;
+    CUALLOC(h, h->keys_in, njobs * 8);
+    CUALLOC(h, h->keys_out, njobs * 8);
+    CUALLOC(h, h->vals_in, njobs * 4);
+    CUALLOC(h, h->vals_out, njobs * 4);
+    CUALLOC(h, h->aux, njobs * 4);
+    CUALLOC(h, h->aux2, njobs * 4);
+    CUALLOC(h, h->flags, njobs);
+    CUALLOC(h, h->pairs, njobs * 8);
+    CUALLOC(h, h->pair_pos, njobs * 4);
+    CUALLOC(h, h->wtask, njobs * 4);
+    CUALLOC(h, h->counts, 16 * 4);
+    CUALLOC(h, h->stats, 8 * 8);
+    CUALLOC(h, h->list, njobs * 4);
+    uint32_t* counts = h->counts.as<uint32_t>();
+    unsigned long long* stats = h->stats.as<unsigned long long>();
+    CU(h, cudaMemsetAsync(counts, 0, 16 * 4, s));
+    CU(h, cudaMemsetAsync(stats, 0, 8 * 8, s));
+
+    const QuerySet& qs = ds.qs;
+    cudaEvent_t ev[4];
+    for (int i = 0; i < 4; i++) CU(h, cudaEventCreate(&ev[i]));
+    struct EvGuard {
+        cudaEvent_t* e;
+        ~EvGuard() {
+            for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]);
+        }
+    } evg{ev};
+    CU(h, cudaEventRecord(ev[0], s));
+    k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
+        d_jobs, njobs, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res, h->keys_in.as<uint64_t>(),
+        h->vals_in.as<uint32_t>(), d_scores, counts, stats);
+    CU(h, cudaGetLastError());
+    local.kernel_launches++;
+
+    // CUB temp storage: the max over the ops used below.
+    size_t t_sort = 0, t_scan = 0, t_sel = 0;
+    CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t_sort, h->keys_in.as<uint64_t>(),
+                                          h->keys_out.as<uint64_t>(), h->vals_in.as<uint32_t>(),
+                                          h->vals_out.as<uint32_t>(), (int)n, 0, 64, s));
+    CU(h, cub::DeviceScan::InclusiveScan(nullptr, t_scan, h->aux.as<uint32_t>(), h->aux2.as<uint32_t>(),
+                                         MaxOp(), (int)n, s));
+    CU(h, cub::DeviceSelect::Flagged(nullptr, t_sel, thrust::counting_iterator<uint32_t>(0),
+                                     h->flags.as<uint8_t>(), h->pair_pos.as<uint32_t>(), counts + 2,
+                                     (int)n, s));
+    size_t t_max = std::max(t_sort, std::max(t_scan, t_sel));
+    CUALLOC(h, h->cub_tmp, t_max);
+    size_t tb = h->cub_tmp.cap;
+    CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->keys_in.as<uint64_t>(),
+                                          h->keys_out.as<uint64_t>(), h->vals_in.as<uint32_t>(),
+                                          h->vals_out.as<uint32_t>(), (int)n, 0, 64, s));
+    local.library_launches += 9;  // onesweep radix sort: histogram + 8 digit passes
+
+    // one small read-back: class counts and widths size the scratch
+    uint32_t hc[8];
+    unsigned long long hs[5];
+    CU(h, cudaMemcpyAsync(hc, counts, 8 * 4, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaMemcpyAsync(hs, stats, 5 * 8, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaStreamSynchronize(s));
+    if (hs[3] != 0)
+        return fail(h, SABER_ERR_ARG, "%llu job(s) reference a query or window outside the loaded data", hs[3]);
+    const uint32_t n_fast = hc[0], n_gen = hc[1];
+    local.jobs = njobs;
+    local.banded_cells = hs[0];
+    local.fast_cells = hs[4];
+    local.fast_jobs = n_fast;
+    local.generic_jobs = n_gen;
+    local.empty_jobs = hc[4];
+    const uint64_t wmax_fast = hs[1];
+    const uint64_t wmax_all = std::max<uint64_t>(hs[1], hs[2]);
+
+    const uint32_t* order = h->vals_out.as<uint32_t>();
+    // generic list: class-1 jobs, then int16 overflows appended by the fast kernel
+    if (n_gen)
+        CU(h, cudaMemcpyAsync(h->list.as<uint32_t>(), order + n_fast, (size_t)n_gen * 4, cudaMemcpyDeviceToDevice, s));
+    CU(h, cudaMemcpyAsync(counts + 5, &n_gen, 4, cudaMemcpyHostToDevice, s));
+
+    if (n_fast) {
+        const unsigned T = 256;
+        // pairs of equal (query, width): run starts by a max-scan of change marks
+        uint32_t* aux = h->aux.as<uint32_t>();
+        uint32_t* aux2 = h->aux2.as<uint32_t>();
+        k_run_marks<<<nblocks(n_fast, T), T, 0, s>>>(h->keys_out.as<uint64_t>(), n_fast, aux);
+        CU(h, cub::DeviceScan::InclusiveScan(h->cub_tmp.p, tb, aux, aux2, MaxOp(), (int)n_fast, s));
+        k_pair_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, n_fast, h->flags.as<uint8_t>());
+        CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
+                                         h->flags.as<uint8_t>(), h->pair_pos.as<uint32_t>(), counts + 2,
+                                         (int)n_fast, s));
+        k_make_pairs<<<nblocks(n_fast, T), T, 0, s>>>(h->keys_out.as<uint64_t>(), h->pair_pos.as<uint32_t>(), counts,
+                                                      n_fast, h->pairs.as<uint2>(), aux);
+        // warp tasks: 32 consecutive pairs of one query
+        CU(h, cub::DeviceScan::InclusiveScan(h->cub_tmp.p, tb, aux, aux2, MaxOp(), (int)n_fast, s));
+        k_wtask_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, counts, h->flags.as<uint8_t>());
+        CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
+                                         h->flags.as<uint8_t>(), h->wtask.as<uint32_t>(), counts + 3, (int)n_fast,
+                                         s));
+        CU(h, cudaGetLastError());
+        local.kernel_launches += 4;   // run marks, pair flags, make pairs, warp-task flags
+        local.library_launches += 8;  // two scans and two selects (two kernels each)
+
+        // persistent warps; one boundary buffer of (wmax + 1) x 32 lanes per warp
+        const int bps = band_fast_blocks_per_sm();
+        const unsigned grid = (unsigned)(h->sm_count * bps);
+        const uint64_t warps = (uint64_t)grid * 256 / 32;
+        const uint32_t stride = (uint32_t)(wmax_fast + 1);
+        CUALLOC(h, h->bufs, warps * stride * 32 * sizeof(uint2));
+        FastArgs a;
+        a.res = ds.res.as<uint8_t>();
+        a.prof = qs.prof.as<int16_t>();
+        a.prof_off = qs.prof_off.as<uint64_t>();
+        a.prof_mpad = qs.prof_mpad.as<uint32_t>();
+        a.qoffs = qs.offsets.as<uint64_t>();
+        a.jobs = d_jobs;
+        a.order = order;
+        a.pairs = h->pairs.as<uint2>();
+        a.wtask_pair = h->wtask.as<uint32_t>();
+        a.counts = counts;
+        a.wt_counter = counts + 6;
+        a.bufs = h->bufs.as<uint2>();
+        a.buf_stride = stride;
+        a.go = sch.go;
+        a.ge = sch.ge;
+        a.scores = d_scores;
+        a.rescue = h->list.as<uint32_t>();
+        a.rescue_count = counts + 5;
+        CU(h, cudaEventRecord(ev[1], s));
+        CU(h, launch_band_fast(grid, s, a));
+        CU(h, cudaEventRecord(ev[2], s));
+        local.kernel_launches++;
+    } else {
+        CU(h, cudaEventRecord(ev[1], s));
+        CU(h, cudaEventRecord(ev[2], s));
+    }
+    {
+        // int32 kernel over narrow bands and rescued jobs (count read on the device)
+        const unsigned T = 128;
+        const unsigned grid = (unsigned)(h->sm_count * 4);
+        const uint64_t threads = (uint64_t)grid * T;
+        const uint32_t stride = (uint32_t)(wmax_all + 1);
+        CUALLOC(h, h->slabs, threads * stride * 4 * sizeof(int32_t));
+        GenericArgs a;
+        a.res = ds.res.as<uint8_t>();
+        a.prof = qs.prof.as<int16_t>();
+        a.prof_off = qs.prof_off.as<uint64_t>();
+        a.prof_mpad = qs.prof_mpad.as<uint32_t>();
+        a.qoffs = qs.offsets.as<uint64_t>();
+        a.jobs = d_jobs;
+        a.list = h->list.as<uint32_t>();
+        a.list_count = counts + 5;
+        a.slabs = h->slabs.as<int32_t>();
+        a.slab_stride = stride;
+        a.go = sch.go;
+        a.ge = sch.ge;
+        a.scores = d_scores;
+        CU(h, launch_band_generic(grid, T, s, a));
+        CU(h, cudaEventRecord(ev[3], s));
+        local.kernel_launches++;
+    }
+    uint32_t glist = 0;
+    CU(h, cudaMemcpyAsync(&glist, counts + 5, 4, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaStreamSynchronize(s));
+    local.i16_rescored = glist - n_gen;
+    float t01 = 0, t12 = 0, t23 = 0;
+    CU(h, cudaEventElapsedTime(&t01, ev[0], ev[1]));
+    CU(h, cudaEventElapsedTime(&t12, ev[1], ev[2]));
+    CU(h, cudaEventElapsedTime(&t23, ev[2], ev[3]));
+    local.t_prep_ms = t01;
+    local.t_fast_ms = t12;
+    local.t_generic_ms = t23;
+    if (st) *st = local;
+    return SABER_OK;
+}
+
+static int build_profiles(saber_gpu* h, const Scheme& sch, QuerySet& q) {
+    if (!q.has || !sch.has || q.nq == 0) return SABER_OK;
+    k_profile<<<q.nq, 256, 0, h->stream>>>(q.codes.as<uint8_t>(), q.offsets.as<uint64_t>(),
+                                           q.has_bias ? q.bias.as<int8_t>() : nullptr, sch.d_matrix.as<int32_t>(),
+                                           q.prof_off.as<uint64_t>(), q.prof_mpad.as<uint32_t>(), q.prof.as<int16_t>());
+    CU(h, cudaGetLastError());
+    CU(h, cudaStreamSynchronize(h->stream));
+    return SABER_OK;
+}
+
+static int load_queries(saber_gpu* h, const Scheme& sch, QuerySet& q, const uint8_t* codes, const uint64_t* offsets,
+                        const int8_t* bias, uint32_t nq) {
+    if (!offsets) return fail(h, SABER_ERR_ARG, "null query offsets");
+    if (offsets[0] != 0) return fail(h, SABER_ERR_ARG, "query offsets must start at 0");
+    for (uint32_t i = 0; i < nq; i++)
+        if (offsets[i + 1] < offsets[i]) return fail(h, SABER_ERR_ARG, "query offsets must be non-decreasing");
+    const uint64_t total = offsets[nq];
+    if (total && !codes) return fail(h, SABER_ERR_ARG, "null query codes");
+    q.has = false;
+    q.nq = nq;
+    q.offs.assign(offsets, offsets + nq + 1);
+    std::vector<uint64_t> poff(nq ? nq : 1, 0);
+    std::vector<uint32_t> pm(nq ? nq : 1, kStripRows);
+    uint64_t acc = 0;
+    for (uint32_t i = 0; i < nq; i++) {
+        uint64_t m = offsets[i + 1] - offsets[i];
+        uint64_t mpad = (m + kStripRows - 1) / kStripRows * kStripRows;
+        if (mpad == 0) mpad = kStripRows;
+        if (mpad > (1ull << 30)) return fail(h, SABER_ERR_ARG, "query %u too long", i);
+        poff[i] = acc;
+        pm[i] = (uint32_t)mpad;
+        acc += (uint64_t)kProfRows * mpad;
+    }
+    CUALLOC(h, q.codes, total + 16);
+    CUALLOC(h, q.offsets, (uint64_t)(nq + 1) * 8);
+    CUALLOC(h, q.prof_off, poff.size() * 8);
+    CUALLOC(h, q.prof_mpad, pm.size() * 4);
+    CUALLOC(h, q.prof, acc * 2 + 16);
+    cudaStream_t s = h->stream;
+    if (total) CU(h, cudaMemcpyAsync(q.codes.p, codes, total, cudaMemcpyHostToDevice, s));
+    CU(h, cudaMemcpyAsync(q.offsets.p, offsets, (uint64_t)(nq + 1) * 8, cudaMemcpyHostToDevice, s));
+    CU(h, cudaMemcpyAsync(q.prof_off.p, poff.data(), poff.size() * 8, cudaMemcpyHostToDevice, s));
+    CU(h, cudaMemcpyAsync(q.prof_mpad.p, pm.data(), pm.size() * 4, cudaMemcpyHostToDevice, s));
+    q.has_bias = bias != nullptr && total > 0;
+    if (q.has_bias) {
+        CUALLOC(h, q.bias, total + 16);
+        CU(h, cudaMemcpyAsync(q.bias.p, bias, total, cudaMemcpyHostToDevice, s));
+    }
+    CU(h, cudaStreamSynchronize(s));
+    q.has = true;
+    return build_profiles(h, sch, q);
+}
+
+static int load_db(saber_gpu* h, Dataset& ds, const uint8_t* residues, uint64_t n_res, const uint64_t* offsets,
+                   uint64_t nsub) {
+    if ((!residues && n_res) || !offsets) return fail(h, SABER_ERR_ARG, "null database arrays");
+    if (offsets[0] != 0 || offsets[nsub] != n_res)
+        return fail(h, SABER_ERR_ARG, "subject offsets must run from 0 to n_residues");
+    for (uint64_t i = 0; i < nsub; i++)
+        if (offsets[i + 1] < offsets[i]) return fail(h, SABER_ERR_ARG, "subject offsets must be non-decreasing");
+    ds.has_db = false;
+    CUALLOC(h, ds.res, n_res + 64);
+    CUALLOC(h, ds.soff, (nsub + 1) * 8);
+    cudaStream_t s = h->stream;
+    if (n_res) CU(h, cudaMemcpyAsync(ds.res.p, residues, n_res, cudaMemcpyHostToDevice, s));
+    CU(h, cudaMemsetAsync(ds.res.as<uint8_t>() + n_res, 22, 64, s));
+    CU(h, cudaMemcpyAsync(ds.soff.p, offsets, (nsub + 1) * 8, cudaMemcpyHostToDevice, s));
+    if (n_res) {
+        k_canon<<<nblocks(n_res, 256, h->sm_count * 16), 256, 0, s>>>(ds.res.as<uint8_t>(), n_res);
+        CU(h, cudaGetLastError());
+    }
+    CU(h, cudaStreamSynchronize(s));
+    ds.n_res = n_res;
+    ds.nsub = nsub;
+    ds.has_db = true;
+    return SABER_OK;
+}
+
+static int set_scheme(saber_gpu* h, Scheme& sch, const int32_t* matrix, int32_t go, int32_t ge) {
+    if (!matrix) return fail(h, SABER_ERR_ARG, "null matrix");
+    if (ge < 0 || go < ge || go > 1000) return fail(h, SABER_ERR_ARG, "gap costs need 0 <= extend <= open <= 1000");
+    for (int i = 0; i < 576; i++)
+        if (matrix[i] < -512 || matrix[i] > 512)
+            return fail(h, SABER_ERR_ARG, "substitution scores must lie in [-512, 512]");
+    memcpy(sch.matrix, matrix, sizeof(sch.matrix));
+    sch.go = go;
+    sch.ge = ge;
+    sch.has = false;
+    CUALLOC(h, sch.d_matrix, 576 * 4);
+    CU(h, cudaMemcpyAsync(sch.d_matrix.p, sch.matrix, 576 * 4, cudaMemcpyHostToDevice, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    sch.has = true;
+    return SABER_OK;
+}
+
+// One query against many windows on the per-call dataset (score_banded_many
+// and ScoreBackend::score_windows): the windows become the per-call database.
+static int one_query_jobs(saber_gpu* h, const Scheme& sch, const uint8_t* query, uint32_t m, const int8_t* bias,
+                          const uint8_t* subjects, const uint64_t* offs, const int64_t* blo, const int64_t* bhi,
+                          uint64_t njobs, bool full, int32_t* scores) {
+    if (njobs == 0) return SABER_OK;
+    if (!offs || (!query && m)) return fail(h, SABER_ERR_ARG, "null argument");
+    Dataset& ds = h->eph;
+    int rc = load_db(h, ds, subjects, offs[njobs], offs, njobs);
+    if (rc != SABER_OK) return rc;
+    uint64_t qoff[2] = {0, m};
+    rc = load_queries(h, sch, ds.qs, query, qoff, bias, 1);
+    if (rc != SABER_OK) return rc;
+    std::vector<saber_band_job> jobs(njobs);
+    for (uint64_t t = 0; t < njobs; t++) {
+        saber_band_job& j = jobs[t];
+        uint64_t n = offs[t + 1] - offs[t];
+        if (n > 0x7FFFFFFFull) return fail(h, SABER_ERR_ARG, "window %llu too long", (unsigned long long)t);
+        j.query = 0;
+        j.subject = (uint32_t)t;
+        j.win_begin = offs[t];
+        j.win_len = (uint32_t)n;
+        int64_t lo = full ? -(int64_t)m : blo[t];
+        int64_t hi = full ? (int64_t)n : bhi[t];
+        // clip in 64 bits first (Band::clip never widens) so any band fits int32
+        if (lo < -(int64_t)m) lo = -(int64_t)m;
+        if (hi > (int64_t)n) hi = (int64_t)n;
+        if (hi < lo) {
+            lo = 1;
+            hi = 0;
+        }
+        j.band_lo = (int32_t)lo;
+        j.band_hi = (int32_t)hi;
+        j.flags = 0;
+    }
+    CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
+    CUALLOC(h, h->scores_dev, njobs * 4);
+    CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs.data(), njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice,
+                          h->stream));
+    rc = score_pipeline(h, sch, ds, h->jobs_dev.as<saber_band_job>(), njobs, h->scores_dev.as<int32_t>(), nullptr);
+    if (rc != SABER_OK) return rc;
+    CU(h, cudaMemcpyAsync(scores, h->scores_dev.p, njobs * 4, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    return SABER_OK;
+}
+
+}  // namespace saber
+
+using namespace saber;
+
+extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx, double* i32);
+
+// ---------------------------------------------------------------------------
+// exported C ABI
+// ---------------------------------------------------------------------------
+#define ENTER(h)                          \
+    if (!(h)) return SABER_ERR_ARG;       \
+    std::lock_guard<std::mutex> g_((h)->mu); \
+    cudaSetDevice((h)->device);           \
+    (h)->err.clear()
+
+extern "C" {
+
+int saber_gpu_open(int device, saber_gpu** out) {
+    if (!out) return SABER_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return SABER_ERR_CUDA;
+    if (device < 0 || device >= ndev) return SABER_ERR_ARG;
+    saber_gpu* h = new saber_gpu();
+    h->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        delete h;
+        return SABER_ERR_CUDA;
+    }
+    *out = h;
+    return SABER_OK;
+}
+
+int saber_gpu_close(saber_gpu* h) {
+    if (!h) return SABER_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return SABER_OK;
+}
+
+const char* saber_gpu_last_error(const saber_gpu* h) { return h ? h->err.c_str() : "null handle"; }
+
+void* saber_gpu_stream(saber_gpu* h) { return h ? (void*)h->stream : nullptr; }
+
+int saber_gpu_set_scheme(saber_gpu* h, const int32_t* matrix576, int32_t go, int32_t ge) {
+    ENTER(h);
+    int rc = set_scheme(h, h->scheme, matrix576, go, ge);
+    if (rc == SABER_OK) rc = build_profiles(h, h->scheme, h->main.qs);
+    return rc;
+}
+
+int saber_gpu_load_db(saber_gpu* h, const uint8_t* residues, uint64_t n_res, const uint64_t* offsets,
+                      uint64_t nsub) {
+    ENTER(h);
+    return load_db(h, h->main, residues, n_res, offsets, nsub);
+}
+
+int saber_gpu_load_queries(saber_gpu* h, const uint8_t* codes, const uint64_t* offsets, const int8_t* bias,
+                           uint32_t nq) {
+    ENTER(h);
+    return load_queries(h, h->scheme, h->main.qs, codes, offsets, bias, nq);
+}
+
+int saber_gpu_score_band_jobs_dev(saber_gpu* h, const saber_band_job* d_jobs, uint64_t njobs, int32_t* d_scores,
+                                  saber_score_stats* stats) {
+    ENTER(h);
+    if (njobs && (!d_jobs || !d_scores)) return fail(h, SABER_ERR_ARG, "null job or score buffer");
+    return score_pipeline(h, h->scheme, h->main, d_jobs, njobs, d_scores, stats);
+}
+
+int saber_gpu_score_band_jobs(saber_gpu* h, const saber_band_job* jobs, uint64_t njobs, int32_t* scores,
+                              saber_score_stats* stats) {
+    ENTER(h);
+    if (njobs && (!jobs || !scores)) return fail(h, SABER_ERR_ARG, "null job or score buffer");
+    if (njobs == 0) {
+        if (stats) *stats = saber_score_stats{};
+        return SABER_OK;
+    }
+    CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
+    CUALLOC(h, h->scores_dev, njobs * 4);
+    CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice, h->stream));
+    int rc = score_pipeline(h, h->scheme, h->main, h->jobs_dev.as<saber_band_job>(), njobs,
+                            h->scores_dev.as<int32_t>(), stats);
+    if (rc != SABER_OK) return rc;
+    CU(h, cudaMemcpyAsync(scores, h->scores_dev.p, njobs * 4, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    return SABER_OK;
+}
+
+int saber_gpu_score_banded_many(saber_gpu* h, const uint8_t* query, uint32_t m, const int8_t* bias,
+                                const uint8_t* subjects, const uint64_t* sub_offsets, const int64_t* band_lo,
+                                const int64_t* band_hi, uint64_t njobs, int32_t* scores) {
+    ENTER(h);
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (njobs && (!band_lo || !band_hi || !scores)) return fail(h, SABER_ERR_ARG, "null argument");
+    return one_query_jobs(h, h->scheme, query, m, bias, subjects, sub_offsets, band_lo, band_hi, njobs, false,
+                          scores);
+}
+
+int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m, const int8_t* bias,
+                            const uint8_t* windows, const uint64_t* win_offsets, uint32_t nwin,
+                            const int32_t* matrix576, int32_t go, int32_t ge, int32_t* scores) {
+    ENTER(h);
+    if (nwin && !scores) return fail(h, SABER_ERR_ARG, "null argument");
+    int rc = set_scheme(h, h->eph_scheme, matrix576, go, ge);
+    if (rc != SABER_OK) return rc;
+    return one_query_jobs(h, h->eph_scheme, query, m, bias, windows, win_offsets, nullptr, nullptr, nwin, true,
+                          scores);
+}
+
+int saber_gpu_probe_int_peak(saber_gpu* h, double* dpx, double* i32) {
+    ENTER(h);
+    int rc = saber_probe_int_peak_impl(h->device, h->stream, dpx, i32);
+    if (rc != SABER_OK) return fail(h, rc, "integer peak probe failed");
+    return SABER_OK;
+}
+
+uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi) {
+    int64_t lo = band_lo, hi = band_hi;
+    if (clip_band((int64_t)m, (int64_t)n, lo, hi) == 0) return 0;
+    return band_cells((int64_t)m, (int64_t)n, lo, hi);
+}
+
+}  // extern "C"

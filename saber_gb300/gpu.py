@@ -1,0 +1,240 @@
+"""ctypes binding of libsaber_gb300.so (the C ABI in include/saber_gpu.h).
+
+Host-side mirror of the reference's scoring interfaces:
+
+* :class:`CudaBackend` — ``ScoreBackend`` (src/gpu/mod.rs:45-59): ``name()``
+  and ``score_windows(query, bias, windows, matrix, gaps)``;
+* :func:`score_banded_many` — ``band_simd8::score_banded_many``
+  (src/algorithm/band_simd8.rs:78-185): one query, many banded windows;
+* :class:`Device` — the batched device path: a resident database and query
+  set, and :meth:`Device.score_band_jobs` over a whole query batch.
+
+There is no CPU fallback: without the compiled library every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+_LIB = None
+
+JOB_DTYPE = np.dtype([
+    ("query", "<u4"), ("subject", "<u4"), ("win_begin", "<u8"), ("win_len", "<u4"),
+    ("band_lo", "<i4"), ("band_hi", "<i4"), ("flags", "<u4"),
+])
+assert JOB_DTYPE.itemsize == 32
+
+
+class SaberGpuError(RuntimeError):
+    """A call of the C ABI returned an error status."""
+
+
+class ScoreStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "jobs", "banded_cells", "fast_cells", "fast_jobs", "generic_jobs", "i16_rescored", "empty_jobs",
+        "kernel_launches", "library_launches")] + [
+        (n, ctypes.c_double) for n in ("t_prep_ms", "t_fast_ms", "t_generic_ms")]
+
+    def as_dict(self):
+        return {n: (float(getattr(self, n)) if n.startswith("t_") else int(getattr(self, n)))
+                for n, _ in self._fields_}
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load_library():
+    """Load libsaber_gb300.so; raises if it has not been built (no fallback)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        raise SaberGpuError("libsaber_gb300.so is not built (%s); run "
+                            "`python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    lib = ctypes.CDLL(path)
+    P, U32, U64, I32, I64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64
+    sig = {
+        "saber_gpu_open": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
+        "saber_gpu_close": (ctypes.c_int, [P]),
+        "saber_gpu_last_error": (ctypes.c_char_p, [P]),
+        "saber_gpu_stream": (P, [P]),
+        "saber_gpu_set_scheme": (ctypes.c_int, [P, P, I32, I32]),
+        "saber_gpu_load_db": (ctypes.c_int, [P, P, U64, P, U64]),
+        "saber_gpu_load_queries": (ctypes.c_int, [P, P, P, P, U32]),
+        "saber_gpu_score_band_jobs": (ctypes.c_int, [P, P, U64, P, P]),
+        "saber_gpu_score_band_jobs_dev": (ctypes.c_int, [P, P, U64, P, P]),
+        "saber_gpu_score_banded_many": (ctypes.c_int, [P, P, U32, P, P, P, P, P, U64, P]),
+        "saber_gpu_score_windows": (ctypes.c_int, [P, P, U32, P, P, P, U32, P, I32, I32, P]),
+        "saber_band_cells": (U64, [U64, U64, I64, I64]),
+        "saber_gpu_probe_int_peak": (ctypes.c_int, [P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def band_cells(m, n, lo, hi):
+    """In-band cells of one job (reference counting; host-only)."""
+    return int(load_library().saber_band_cells(int(m), int(n), int(lo), int(hi)))
+
+
+def _flat_matrix(matrix):
+    mat = np.ascontiguousarray(np.asarray(matrix, dtype=np.int32).reshape(576))
+    return mat
+
+
+class Device:
+    """One handle of the C ABI: a CUDA stream plus device-resident data."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.saber_gpu_open(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise SaberGpuError("saber_gpu_open(%d) failed with status %d" % (device, rc))
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.lib.saber_gpu_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.lib.saber_gpu_last_error(self.h)
+            raise SaberGpuError("%s failed (%d): %s" % (what, rc, msg.decode() if msg else ""))
+
+    @property
+    def stream(self):
+        return self.lib.saber_gpu_stream(self.h)
+
+    def set_scheme(self, matrix, gap_open, gap_extend):
+        mat = _flat_matrix(matrix)
+        self._check(self.lib.saber_gpu_set_scheme(self.h, _ptr(mat), int(gap_open), int(gap_extend)),
+                    "set_scheme")
+
+    def load_db(self, residues, offsets):
+        res = np.ascontiguousarray(residues, dtype=np.uint8)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._check(self.lib.saber_gpu_load_db(self.h, _ptr(res), res.size, _ptr(off), off.size - 1), "load_db")
+
+    def load_queries(self, codes, offsets, bias=None):
+        c = np.ascontiguousarray(codes, dtype=np.uint8)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        b = None if bias is None else np.ascontiguousarray(bias, dtype=np.int8)
+        self._check(self.lib.saber_gpu_load_queries(self.h, _ptr(c), _ptr(off), _ptr(b), off.size - 1),
+                    "load_queries")
+
+    def score_band_jobs(self, jobs, out=None):
+        """Scores of host jobs (structured JOB_DTYPE array); host in, host out."""
+        jobs = np.ascontiguousarray(jobs, dtype=JOB_DTYPE)
+        if out is None:
+            out = np.empty(jobs.size, dtype=np.int32)
+        st = ScoreStats()
+        self._check(self.lib.saber_gpu_score_band_jobs(self.h, _ptr(jobs), jobs.size, _ptr(out), ctypes.byref(st)),
+                    "score_band_jobs")
+        return out, st.as_dict()
+
+    def score_band_jobs_ptr(self, jobs_ptr, njobs, scores_ptr):
+        """Host-buffer call with raw host pointers (e.g. pinned torch tensors)."""
+        st = ScoreStats()
+        self._check(self.lib.saber_gpu_score_band_jobs(self.h, ctypes.c_void_p(jobs_ptr), int(njobs),
+                                                       ctypes.c_void_p(scores_ptr), ctypes.byref(st)),
+                    "score_band_jobs")
+        return st.as_dict()
+
+    def score_band_jobs_dev(self, d_jobs_ptr, njobs, d_scores_ptr):
+        """Device-resident variant: raw device pointers (e.g. torch tensors' data_ptr())."""
+        st = ScoreStats()
+        self._check(self.lib.saber_gpu_score_band_jobs_dev(self.h, ctypes.c_void_p(d_jobs_ptr), int(njobs),
+                                                           ctypes.c_void_p(d_scores_ptr), ctypes.byref(st)),
+                    "score_band_jobs_dev")
+        return st.as_dict()
+
+    def probe_int_peak(self):
+        """(DPX s16x2 lane-instructions/s, int32 max lane-instructions/s) of this GPU."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.saber_gpu_probe_int_peak(self.h, ctypes.byref(a), ctypes.byref(b)), "probe_int_peak")
+        return a.value, b.value
+
+    def score_banded_many(self, query, bias, subjects, bands):
+        """One query against banded windows: list of (window codes, (lo, hi))."""
+        q = np.ascontiguousarray(query, dtype=np.uint8)
+        b = None if bias is None else np.ascontiguousarray(bias, dtype=np.int8)
+        wins = [np.asarray(s, dtype=np.uint8) for s in subjects]
+        offs = np.zeros(len(wins) + 1, dtype=np.uint64)
+        offs[1:] = np.cumsum([w.size for w in wins]) if wins else []
+        cat = np.concatenate(wins) if wins and offs[-1] > 0 else np.zeros(1, np.uint8)
+        lo = np.ascontiguousarray([x[0] for x in bands], dtype=np.int64)
+        hi = np.ascontiguousarray([x[1] for x in bands], dtype=np.int64)
+        out = np.empty(len(wins), dtype=np.int32)
+        self._check(self.lib.saber_gpu_score_banded_many(self.h, _ptr(q), q.size, _ptr(b), _ptr(cat), _ptr(offs),
+                                                         _ptr(lo), _ptr(hi), len(wins), _ptr(out)),
+                    "score_banded_many")
+        return out
+
+    def score_windows(self, query, bias, windows, matrix, gap_open, gap_extend):
+        q = np.ascontiguousarray(query, dtype=np.uint8)
+        b = None if bias is None else np.ascontiguousarray(bias, dtype=np.int8)
+        wins = [np.asarray(s, dtype=np.uint8) for s in windows]
+        offs = np.zeros(len(wins) + 1, dtype=np.uint64)
+        if wins:
+            offs[1:] = np.cumsum([w.size for w in wins])
+        cat = np.concatenate(wins) if wins and offs[-1] > 0 else np.zeros(1, np.uint8)
+        mat = _flat_matrix(matrix)
+        out = np.empty(len(wins), dtype=np.int32)
+        self._check(self.lib.saber_gpu_score_windows(self.h, _ptr(q), q.size, _ptr(b), _ptr(cat), _ptr(offs),
+                                                     len(wins), _ptr(mat), int(gap_open), int(gap_extend),
+                                                     _ptr(out)), "score_windows")
+        return out
+
+
+class CudaBackend:
+    """The reference's ``ScoreBackend`` (src/gpu/mod.rs:45-59) on the GB300 library.
+
+    ``score_windows`` returns exact int32 scores in input order or raises
+    :class:`SaberGpuError`; it never returns a saturated score.  Calls are
+    serialised per handle by the library (as src/gpu/cuda.rs:144 does with a
+    mutex)."""
+
+    def __init__(self, device=0):
+        self.dev = Device(device)
+
+    def name(self):
+        return "cuda-gb300"
+
+    def score_windows(self, query, bias, windows, matrix, gaps):
+        go, ge = gaps
+        return self.dev.score_windows(query, bias, windows, matrix, go, ge)
+
+
+def score_banded_many(dev, query, bias, jobs, scheme):
+    """``score_banded_many(query, bias, jobs, scheme)`` (band_simd8.rs:78): jobs
+    are (subject window, (lo, hi)) pairs, scheme is (matrix, gap_open, gap_extend)."""
+    matrix, go, ge = scheme
+    dev.set_scheme(matrix, go, ge)
+    return dev.score_banded_many(query, bias, [j[0] for j in jobs], [j[1] for j in jobs])

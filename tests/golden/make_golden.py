@@ -1,0 +1,154 @@
+"""Generate the golden fixtures under tests/golden/ (run in a container that
+has the reference tree; the fixtures are committed and the tests only read
+them).
+
+* matrices.json — the substitution tables of src/scoring/matrices.rs (the
+  public NCBI BLOSUM/PAM tables in NCBI order ARNDCQEGHILKMFPSTWYVBZX*),
+  parsed from the reference source; also copied to saber_gb300/data/.
+* sw_vectors.json — the test vectors of examples/gpu_vectors.rs (same
+  xorshift generator, seed 0xC0DA, same case mix), with expected scores
+  computed by the reference's own CUDA kernel source (src/gpu/kernels/sw.cu)
+  compiled for the host by oracle/Makefile (`make -C oracle ref`).
+
+Usage:  python tests/golden/make_golden.py [--ref-root /root/reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+NAMES = {
+    "BLOSUM45_MATRIX": "BLOSUM45", "BLOSUM50_MATRIX": "BLOSUM50",
+    "BLOSUM62_MATRIX": "BLOSUM62", "BLOSUM80_MATRIX": "BLOSUM80",
+    "BLOSUM90_MATRIX": "BLOSUM90", "PAM30_MATRIX": "PAM30",
+    "PAM70_MATRIX": "PAM70", "PAM250_MATRIX": "PAM250",
+}
+
+
+def parse_matrices(ref_root):
+    src = open(os.path.join(ref_root, "src/scoring/matrices.rs")).read()
+    out = {}
+    for const, name in NAMES.items():
+        m = re.search(r"const %s: \[\[i32; 24\]; 24\] = \[(.*?)\n\];" % const, src, re.S)
+        if not m:
+            raise SystemExit("matrix %s not found" % const)
+        rows = re.findall(r"\[([^\[\]]+)\]", m.group(1))
+        mat = [[int(v) for v in r.split(",") if v.strip()] for r in rows]
+        assert len(mat) == 24 and all(len(r) == 24 for r in mat), name
+        out[name] = mat
+    return out
+
+
+def nucleotide(match, mismatch):
+    # matrices.rs:85-91
+    mat = [[mismatch] * 24 for _ in range(24)]
+    for i in range(4):
+        mat[i][i] = match
+    return mat
+
+
+class XorShift:
+    """examples/gpu_vectors.rs:10-21"""
+
+    def __init__(self, seed):
+        self.s = seed
+
+    def next(self):
+        s = self.s
+        s ^= (s << 13) & 0xFFFFFFFFFFFFFFFF
+        s ^= s >> 7
+        s ^= (s << 17) & 0xFFFFFFFFFFFFFFFF
+        self.s = s
+        return s
+
+    def below(self, n):
+        return self.next() % n
+
+
+def gpu_vector_cases(mats):
+    """examples/gpu_vectors.rs:52-90"""
+    r = XorShift(0xC0DA)
+    blosum, pam, nt = mats["BLOSUM62"], mats["PAM30"], nucleotide(2, -3)
+    cases = []
+    for case in range(24):
+        m, mname, alpha, go, ge = [
+            (blosum, "BLOSUM62", 24, 11, 1), (pam, "PAM30", 20, 10, 1),
+            (nt, "NT_2_-3", 5, 7, 2), (blosum, "BLOSUM62", 24, 13, 2)][case % 4]
+        ql = 1 + r.below(300)
+        q = [r.below(alpha) for _ in range(ql)]
+        bias = [r.below(5) - 2 for _ in range(ql)] if case % 3 == 0 else None
+        nw = 1 + r.below(40)
+        wins = []
+        for k in range(nw):
+            if k % 5 == 0:
+                lo = r.below(ql)
+                hi = lo + r.below(ql - lo + 1)
+                w = []
+                for c in q[lo:hi]:
+                    if r.below(4) == 0:
+                        w.append(r.below(alpha))
+                    else:
+                        w.append(c)
+                wins.append(w)
+            else:
+                l = r.below(400)
+                wins.append([r.below(alpha) for _ in range(l)])
+        cases.append(dict(matrix=mname, gap_open=go, gap_extend=ge, query=q, bias=bias, windows=wins))
+    long = [17] * 4000
+    cases.append(dict(matrix="BLOSUM62", gap_open=11, gap_extend=1, query=long, bias=None,
+                      windows=[long, long[:3500]]))
+    cases.append(dict(matrix="BLOSUM62", gap_open=11, gap_extend=1, query=[0, 1, 2, 200, 4],
+                      bias=None, windows=[[0, 1, 2, 22, 4], [255, 255]]))
+    return cases
+
+
+def ref_scores(lib, case, mats):
+    mat = mats[case["matrix"]] if case["matrix"] in mats else nucleotide(2, -3)
+    flat = (ctypes.c_int32 * 576)(*[v for row in mat for v in row])
+    q = bytes(case["query"])
+    bias = case["bias"]
+    cb = (ctypes.c_int8 * len(bias))(*bias) if bias else None
+    subj = b"".join(bytes(w) for w in case["windows"])
+    offs = [0]
+    for w in case["windows"]:
+        offs.append(offs[-1] + len(w))
+    coffs = (ctypes.c_uint32 * len(offs))(*offs)
+    out = (ctypes.c_int32 * len(case["windows"]))()
+    lib.ref_sw_score_windows(q, len(q), cb, subj if subj else None, coffs, len(case["windows"]),
+                             flat, case["gap_open"], case["gap_extend"], out)
+    return list(out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-root", default="/root/reference")
+    a = ap.parse_args()
+    mats = parse_matrices(a.ref_root)
+    with open(os.path.join(HERE, "matrices.json"), "w") as f:
+        json.dump(mats, f)
+    data_dir = os.path.join(REPO, "saber_gb300", "data")
+    os.makedirs(data_dir, exist_ok=True)
+    shutil.copy(os.path.join(HERE, "matrices.json"), os.path.join(data_dir, "matrices.json"))
+
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref",
+                           "REF_ROOT=%s" % a.ref_root])
+    lib = ctypes.CDLL(os.path.join(REPO, "oracle", "_ref", "libref_sw.so"))
+    cases = gpu_vector_cases(mats)
+    for c in cases:
+        c["expected"] = ref_scores(lib, c, mats)
+    with open(os.path.join(HERE, "sw_vectors.json"), "w") as f:
+        json.dump({"source": "examples/gpu_vectors.rs generator; scores from src/gpu/kernels/sw.cu "
+                             "compiled for the host (oracle/_ref)", "cases": cases}, f)
+    n = sum(len(c["windows"]) for c in cases)
+    print("wrote %d cases, %d windows" % (len(cases), n), file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()

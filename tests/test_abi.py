@@ -1,0 +1,67 @@
+"""CPU tests of the C-ABI boundary: the library loads, exports every symbol
+declared in include/*.h, the header carries no framework types, and the
+host-only helpers work without a GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from saber_gb300 import gpu
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(saber_\w+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = _declared()
+    for want in ("saber_gpu_open", "saber_gpu_close", "saber_gpu_score_band_jobs", "saber_gpu_score_windows",
+                 "saber_gpu_score_banded_many", "saber_band_cells"):
+        assert want in names
+
+
+def test_headers_use_plain_c_types():
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        src = open(h).read()
+        assert "torch" not in src and "at::" not in src and "std::" not in src
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(gpu.lib_path())
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_band_cells_matches_oracle_cell_count():
+    rng = np.random.default_rng(11)
+    from saber_gb300.scoring import matrix
+    mat = matrix("BLOSUM62")
+    for _ in range(300):
+        m = int(rng.integers(1, 60))
+        n = int(rng.integers(1, 60))
+        lo = int(rng.integers(-80, 80))
+        hi = lo + int(rng.integers(-5, 90))
+        q = rng.integers(0, 20, m).astype(np.uint8)
+        s = rng.integers(0, 20, n).astype(np.uint8)
+        want = orc.banded_score(q, s, None, mat, 11, 1, lo, hi)[3]
+        assert gpu.band_cells(m, n, lo, hi) == want, (m, n, lo, hi)
+
+
+def test_open_without_gpu_reports_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(gpu.SaberGpuError):
+        gpu.Device(0)

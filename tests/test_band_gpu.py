@@ -1,0 +1,169 @@
+"""GPU parity tests of the banded scoring path: every score bit-exact against
+the oracle (integer work, no tolerance), through the C ABI."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from saber_gb300 import synth
+from saber_gb300.gpu import JOB_DTYPE, CudaBackend
+from saber_gb300.scoring import encode_protein, matrix, nucleotide
+from tests.refgen import Lcg
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+B62 = matrix("BLOSUM62")
+
+
+def _oracle_jobs(qs, ss, bias, jobs, mat, go, ge):
+    return orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs, mat, go, ge, threads=8)
+
+
+def _report(got, want, jobs):
+    bad = np.flatnonzero(got != want)
+    lines = []
+    for t in bad[:8]:
+        j = jobs[t]
+        lines.append("job %d q=%d n=%d band=[%d,%d] got %d want %d" % (
+            t, j["query"], j["win_len"], j["band_lo"], j["band_hi"], got[t], want[t]))
+    return "%d mismatches\n%s" % (bad.size, "\n".join(lines))
+
+
+def test_golden_vectors_through_score_backend():
+    """ScoreBackend::score_windows on the reference's gpu_vectors cases
+    (expected scores from the reference's own kernel source)."""
+    be = CudaBackend(0)
+    assert be.name()
+    with open(os.path.join(HERE, "golden", "sw_vectors.json")) as f:
+        cases = json.load(f)["cases"]
+    for c in cases:
+        mat = nucleotide(2, -3) if c["matrix"] == "NT_2_-3" else matrix(c["matrix"])
+        bias = None if c["bias"] is None else np.array(c["bias"], np.int8)
+        got = be.score_windows(np.array(c["query"], np.uint8), bias,
+                               [np.array(w, np.uint8) for w in c["windows"]], mat,
+                               (c["gap_open"], c["gap_extend"]))
+        assert list(got) == c["expected"], c["matrix"]
+
+
+@pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8)])
+def test_random_band_jobs_match_oracle(dev, gaps):
+    go, ge = gaps
+    qs, ss, planted = synth.protein_db(100 + go, 40, 3000)
+    bias = synth.query_bias(7, qs)
+    jobs = synth.band_jobs(200 + ge, qs, ss, planted, 6000, half_min=1, half_max=140)
+    dev.set_scheme(B62, go, ge)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    got, st = dev.score_band_jobs(jobs)
+    want, cells = _oracle_jobs(qs, ss, bias, jobs, B62, go, ge)
+    assert np.array_equal(got, want), _report(got, want, jobs)
+    assert st["banded_cells"] == cells
+    assert st["fast_jobs"] > 0 and st["generic_jobs"] > 0
+
+
+def test_device_resident_path_matches_host_path(dev):
+    torch = pytest.importorskip("torch")
+    qs, ss, planted = synth.protein_db(21, 30, 2000)
+    jobs = synth.band_jobs(22, qs, ss, planted, 4000)
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, None)
+    host, _ = dev.score_band_jobs(jobs)
+    dj = torch.from_numpy(jobs.view(np.uint8).copy()).cuda()
+    ds = torch.full((jobs.size,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    dev.score_band_jobs_dev(dj.data_ptr(), jobs.size, ds.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(ds.cpu().numpy(), host)
+    want, _ = _oracle_jobs(qs, ss, None, jobs, B62, 11, 1)
+    assert np.array_equal(host, want), _report(host, want, jobs)
+
+
+def test_int16_overflow_is_rescored_exactly(dev):
+    """Scores above the int16 range: W x 4000 (44 000, banded.rs:716-731) and
+    300 W (3300, band_simd8.rs:454-468) next to ordinary jobs."""
+    w4000 = np.full(4000, 17, np.uint8)
+    w300 = np.full(300, 17, np.uint8)
+    other = encode_protein("MKVLAAGIVGKLLA")
+    dev.set_scheme(B62, 11, 1)
+    got = dev.score_banded_many(w4000, None, [w4000, w4000[:3500], other, w300], [(-20, 20), (-40, 40), (-3, 3),
+                                                                                  (-5, 5)])
+    want = [orc.banded_score(w4000, s, None, B62, 11, 1, lo, hi)[0]
+            for s, (lo, hi) in zip([w4000, w4000[:3500], other, w300], [(-20, 20), (-40, 40), (-3, 3), (-5, 5)])]
+    assert list(got) == want
+    assert got[0] == 44000
+
+
+def test_score_banded_many_reference_cases(dev):
+    """band_simd8.rs:403-451 cases (same LCG): BLOSUM62/PAM30/BLOSUM45, gaps
+    11/1 and 7/2, bands up to 200 wide, with and without bias."""
+    for sysname in ("BLOSUM62", "PAM30", "BLOSUM45"):
+        mx = matrix(sysname)
+        r = Lcg(7)
+        for trial in range(40):
+            ql = 1 + r.next(220)
+            q = np.array([r.next(24) for _ in range(ql)], np.uint8)
+            bias = np.array([r.next(9) - 4 for _ in range(ql)], np.int8)
+            n = 1 + r.next(70)
+            subs = []
+            for k in range(n):
+                l = 1 + r.next(320)
+                s = np.array([r.next(24) for _ in range(l)], np.uint8)
+                if k % 3 == 0:
+                    o = r.next(l)
+                    for t in range(min(max(l - o, 0), ql)):
+                        if r.next(4) > 0:
+                            s[o + t] = q[t]
+                subs.append(s)
+            bands = []
+            for s in subs:
+                c = r.next(len(s) + ql) - ql
+                w = r.next(200 if trial % 5 == 0 else 90)
+                bands.append((c - w // 2, c + (w + 1) // 2))
+            for go, ge in ((11, 1), (7, 2)):
+                b = bias if trial % 2 == 0 else None
+                dev.set_scheme(mx, go, ge)
+                got = dev.score_banded_many(q, b, subs, bands)
+                want = [orc.banded_score(q, s, b, mx, go, ge, lo, hi)[0] for s, (lo, hi) in zip(subs, bands)]
+                assert list(got) == want, (sysname, trial, go, ge)
+
+
+def test_edge_cases(dev):
+    """Empty windows and queries, bands outside the rectangle, one-residue
+    queries, bands wider than the rectangle, codes >= 24 (scored as X)."""
+    rng = np.random.default_rng(5)
+    q = rng.integers(0, 24, 37).astype(np.uint8)
+    cases = [
+        (np.zeros(0, np.uint8), (-5, 5)),
+        (rng.integers(0, 24, 10).astype(np.uint8), (50, 60)),      # band right of the window
+        (rng.integers(0, 24, 10).astype(np.uint8), (-80, -60)),    # band left of the query
+        (rng.integers(0, 24, 10).astype(np.uint8), (5, 2)),        # hi < lo
+        (rng.integers(0, 24, 500).astype(np.uint8), (-1000, 1000)),
+        (rng.integers(0, 255, 300).astype(np.uint8), (-40, 60)),   # out-of-range codes
+        (q.copy(), (0, 0)),
+        (q.copy(), (-36, 36)),
+        (rng.integers(0, 24, 17).astype(np.uint8), (-3, 13)),
+    ]
+    dev.set_scheme(B62, 11, 1)
+    subs = [c[0] for c in cases]
+    bands = [c[1] for c in cases]
+    got = dev.score_banded_many(q, None, subs, bands)
+    want = [orc.banded_score(q, s, None, B62, 11, 1, lo, hi)[0] for s, (lo, hi) in zip(subs, bands)]
+    assert list(got) == want
+    one = np.array([17], np.uint8)
+    got1 = dev.score_banded_many(one, None, [q, one], [(-3, 40), (0, 0)])
+    assert list(got1) == [orc.banded_score(one, q, None, B62, 11, 1, -3, 40)[0], 11]
+
+
+def test_wide_full_window_bands(dev):
+    """Full-rectangle plans (band covers the window) of long pairs."""
+    qs, ss, planted = synth.protein_db(31, 6, 40, max_len=1500)
+    dev.set_scheme(B62, 11, 1)
+    for qi in range(len(qs)):
+        q = qs.seq(qi)
+        subs = [ss.seq(k) for k in range(len(ss))]
+        got = CudaBackend(0).score_windows(q, None, subs, B62, (11, 1))
+        want = [orc.banded_score(q, s, None, B62, 11, 1, -q.size, s.size)[0] for s in subs]
+        assert list(got) == want
