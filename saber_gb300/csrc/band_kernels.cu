@@ -194,6 +194,7 @@ __global__ void __launch_bounds__(256) k_band_fast(
         wt = __shfl_sync(0xffffffffu, wt, 0);
         if (wt >= n_wtasks) break;
         const uint32_t p0 = wtask_pair[wt];
+        if (p0 >= n_pairs) continue;  // defensive: never index past the pair list
         const uint32_t qid = jobs[order[pairs[p0].x]].query;
         const uint32_t p = p0 + lane;
         bool has_pair = p < n_pairs;

@@ -236,11 +236,13 @@ __global__ void k_make_pairs(const uint64_t* __restrict__ keys, const uint32_t* 
     qmark[i] = newq ? i : 0u;
 }
 
+// Every flag below n is written: positions past the pair count are cleared
+// (the select runs over all n entries).
 __global__ void k_wtask_flags(const uint32_t* __restrict__ qstart, const uint32_t* __restrict__ counts,
-                              uint8_t* __restrict__ flag) {
+                              uint32_t n, uint8_t* __restrict__ flag) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= counts[2]) return;
-    flag[i] = ((i - qstart[i]) & 31u) == 0;
+    if (i >= n) return;
+    flag[i] = i < counts[2] && ((i - qstart[i]) & 31u) == 0;
 }
 
 struct MaxOp {
@@ -362,7 +364,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
                                                       n_fast, h->pairs.as<uint2>(), aux);
         // warp tasks: 32 consecutive pairs of one query
         CU(h, cub::DeviceScan::InclusiveScan(h->cub_tmp.p, tb, aux, aux2, MaxOp(), (int)n_fast, s));
-        k_wtask_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, counts, h->flags.as<uint8_t>());
+        k_wtask_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, counts, n_fast, h->flags.as<uint8_t>());
         CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
                                          h->flags.as<uint8_t>(), h->wtask.as<uint32_t>(), counts + 3, (int)n_fast,
                                          s));
