@@ -139,6 +139,25 @@ int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m,
                             const int32_t* matrix576, int32_t gap_open, int32_t gap_extend,
                             int32_t* scores);
 
+/* Allocation-free variant of saber_gpu_score_band_jobs_dev.  No counterpart
+ * in the reference: it exists for callers that cannot allocate GPU memory at
+ * scoring time — code between the nodes of a CUDA graph being captured, a
+ * process whose device memory is held by another allocator or reserved in a
+ * fixed budget, a latency-bound path where the device synchronisation of a
+ * cudaMalloc is not acceptable.  It makes no cudaMalloc/cudaFree and calls no
+ * allocating library routine: it reads the handle's resident database, query
+ * set and scheme, the caller's device buffers d_jobs / d_scores, and uses a
+ * fixed 16 MiB scratch array compiled into the library (held by every GPU
+ * that loads the library until the process exits).  Scores equal those of the
+ * other entry points (int32 recurrence of banded.rs:134-224).
+ * max_band_width bounds the clipped band width of every job (1..4096; larger
+ * is rejected with SABER_ERR_ARG; a job wider than it makes the call return
+ * SABER_ERR_ARG).  The first call on a device looks up the scratch array's
+ * address; make it before any stream capture.  Every call shares the scratch
+ * and it keeps the last call's contents; calls that overlap on the GPU race. */
+int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs, uint64_t njobs,
+                                      int32_t max_band_width, int32_t* d_scores);
+
 /* Measures the integer-pipe peak of this GPU for the roofline: throughput of
  * the DPX packed-int16 max/add-max instructions the scoring kernel uses
  * (lane-instructions per second; each does two 16-bit operations) and of plain

@@ -88,6 +88,24 @@ struct GenericArgs {
     int go, ge;
     int32_t* scores;
 };
+// Allocation-free entry point (noalloc.cu).
+constexpr int32_t kNoAllocMaxBandWidth = 4096;
+struct NoAllocArgs {
+    const uint8_t* res;
+    const int16_t* prof;
+    const uint64_t* prof_off;
+    const uint32_t* prof_mpad;
+    const uint64_t* qoffs;
+    uint32_t nq;
+    uint64_t n_res;
+    const saber_band_job* jobs;
+    uint64_t njobs;
+    int32_t max_band_width;
+    int go, ge;
+    int32_t* scores;
+};
+int noalloc_score_band_jobs(int device, cudaStream_t s, const NoAllocArgs& a, const char** msg);
+
 int band_fast_blocks_per_sm();
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a);
 cudaError_t launch_band_generic(unsigned grid, unsigned block, cudaStream_t s, const GenericArgs& a);

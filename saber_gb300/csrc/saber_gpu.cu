@@ -709,6 +709,34 @@ int saber_gpu_probe_int_peak(saber_gpu* h, double* dpx, double* i32) {
     return SABER_OK;
 }
 
+int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs, uint64_t njobs,
+                                      int32_t max_band_width, int32_t* d_scores) {
+    ENTER(h);
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (!h->main.has_db) return fail(h, SABER_ERR_STATE, "no database loaded");
+    if (!h->main.qs.has) return fail(h, SABER_ERR_STATE, "no query set loaded");
+    if (njobs && (!d_jobs || !d_scores)) return fail(h, SABER_ERR_ARG, "null job or score buffer");
+    const QuerySet& qs = h->main.qs;
+    NoAllocArgs a;
+    a.res = h->main.res.as<uint8_t>();
+    a.prof = qs.prof.as<int16_t>();
+    a.prof_off = qs.prof_off.as<uint64_t>();
+    a.prof_mpad = qs.prof_mpad.as<uint32_t>();
+    a.qoffs = qs.offsets.as<uint64_t>();
+    a.nq = qs.nq;
+    a.n_res = h->main.n_res;
+    a.jobs = d_jobs;
+    a.njobs = njobs;
+    a.max_band_width = max_band_width;
+    a.go = h->scheme.go;
+    a.ge = h->scheme.ge;
+    a.scores = d_scores;
+    const char* msg = "";
+    int rc = noalloc_score_band_jobs(h->device, h->stream, a, &msg);
+    if (rc != SABER_OK) return fail(h, rc, "%s", msg);
+    return SABER_OK;
+}
+
 uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi) {
     int64_t lo = band_lo, hi = band_hi;
     if (clip_band((int64_t)m, (int64_t)n, lo, hi) == 0) return 0;

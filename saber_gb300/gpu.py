@@ -71,6 +71,7 @@ def load_library():
         "saber_gpu_score_windows": (ctypes.c_int, [P, P, U32, P, P, P, U32, P, I32, I32, P]),
         "saber_band_cells": (U64, [U64, U64, I64, I64]),
         "saber_gpu_probe_int_peak": (ctypes.c_int, [P, P, P]),
+        "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -174,6 +175,13 @@ class Device:
                                                            ctypes.c_void_p(d_scores_ptr), ctypes.byref(st)),
                     "score_band_jobs_dev")
         return st.as_dict()
+
+    def score_band_jobs_noalloc(self, d_jobs_ptr, njobs, max_band_width, d_scores_ptr):
+        """Allocation-free scoring of device-resident jobs (no device memory is
+        allocated by the call; scratch is a fixed 16 MiB array in the library)."""
+        self._check(self.lib.saber_gpu_score_band_jobs_noalloc(self.h, ctypes.c_void_p(d_jobs_ptr), int(njobs),
+                                                               int(max_band_width), ctypes.c_void_p(d_scores_ptr)),
+                    "score_band_jobs_noalloc")
 
     def probe_int_peak(self):
         """(DPX s16x2 lane-instructions/s, int32 max lane-instructions/s) of this GPU."""
