@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample size (seconds of work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--strip-rows", type=int, default=16, help="rows per strip of the int16 kernel (8 or 16)")
     return ap.parse_args()
 
 
@@ -56,7 +57,8 @@ def config_dict(a, world):
     return {"workload": "sw-scoring-microbench: %d banded regions, %d queries x %d subjects, half-widths 8-128, "
                         "BLOSUM62 11/1, query bias" % (a.jobs, a.queries, a.subjects),
             "jobs_per_gpu": a.jobs, "queries": a.queries, "subjects": a.subjects, "seed": a.seed,
-            "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
+            "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world,
+            "strip_rows": a.strip_rows}
 
 
 class Clocks:
@@ -171,6 +173,7 @@ def run_ours(a, rank, world, local_rank):
     qs, ss, planted, bias, jobs = workload(seed, a.queries, a.subjects, a.jobs)
     mat = matrix("BLOSUM62")
     dev = Device(local_rank)
+    dev.strip_rows = a.strip_rows
     dev.set_scheme(mat, 11, 1)
     dev.load_db(ss.codes, ss.offsets)
     dev.load_queries(qs.codes, qs.offsets, bias)

@@ -139,6 +139,12 @@ int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m,
                             const int32_t* matrix576, int32_t gap_open, int32_t gap_extend,
                             int32_t* scores);
 
+/* Tuning: rows per strip of the packed int16 scoring kernel (8 or 16,
+ * default 16).  Results do not depend on it.  No reference counterpart (the
+ * reference's AVX2 kernels have fixed vector widths). */
+int saber_gpu_set_strip_rows(saber_gpu* h, int32_t strip_rows);
+int32_t saber_gpu_get_strip_rows(saber_gpu* h);
+
 /* Allocation-free variant of saber_gpu_score_band_jobs_dev.  No counterpart
  * in the reference: it exists for callers that cannot allocate GPU memory at
  * scoring time — code between the nodes of a CUDA graph being captured, a

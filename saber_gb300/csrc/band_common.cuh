@@ -8,8 +8,10 @@
 namespace saber {
 
 // Rows per strip of the packed int16 kernel (one strip = R query rows swept
-// along the subject window; see band_kernels.cu).
+// along the subject window; see band_kernels.cu): 8 or 16, chosen per handle
+// (tuning); query profiles are padded to the largest.
 constexpr int kStripRows = 16;
+constexpr int kStripRowsMin = 8;
 // Residue code used for positions outside a window or a query: its profile
 // entries are kSent, so such cells never beat a real cell (banded.rs:123-131
 // excludes them; the kernels compute them harmlessly instead of branching).
@@ -63,8 +65,6 @@ struct FastArgs {
     const uint64_t* qoffs;
     const saber_band_job* jobs;
     const uint32_t* order;
-    const uint2* pairs;
-    const uint32_t* wtask_pair;
     const uint32_t* counts;
     uint32_t* wt_counter;
     uint2* bufs;
@@ -73,6 +73,7 @@ struct FastArgs {
     int32_t* scores;
     uint32_t* rescue;
     uint32_t* rescue_count;
+    int strip_rows;  // 8 or 16
 };
 struct GenericArgs {
     const uint8_t* res;
@@ -106,7 +107,7 @@ struct NoAllocArgs {
 };
 int noalloc_score_band_jobs(int device, cudaStream_t s, const NoAllocArgs& a, const char** msg);
 
-int band_fast_blocks_per_sm();
+int band_fast_blocks_per_sm(int strip_rows);
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a);
 cudaError_t launch_band_generic(unsigned grid, unsigned block, cudaStream_t s, const GenericArgs& a);
 

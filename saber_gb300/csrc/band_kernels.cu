@@ -7,24 +7,29 @@
 //   F(i,j) = max(H(i-1,j) - go, F(i-1,j) - ge)
 //   H(i,j) = max(0, H(i-1,j-1) + S(q_i,s_j) + bias_i, E(i,j), F(i,j))
 //
-// Fast kernel (k_band_fast): one warp takes 32 pairs of jobs of one query,
-// each lane two jobs held in the two int16 halves of every register (DPX
-// s16x2 max/add instructions), and sweeps the band as strips of R query rows
-// along the subject window.  Per strip the lane keeps H(i, j-1) and E(i, j-1)
-// of its R rows in registers; the H/F values of the row above the strip come
-// from a per-lane boundary buffer (indexed by band offset k = j - i - lo) in
-// global memory, laid out [k][lane] so a warp reads and writes 256 contiguous
-// bytes per step.  All lanes of a warp run the same column schedule, so the
-// rows entering the band at the left edge are handled by compile-time
-// unrolling and only the ragged right edge (different band widths) is masked.
-// Substitution scores come from a per-query profile P[c][i] = S(q_i, c) +
-// bias_i (int16, built at query upload) — one 16-byte load per 8 rows.
+// Fast kernel (k_band_fast<R>): a warp takes 64 jobs (consecutive in the
+// (strips, width, query) order the runtime sorts them in); each lane holds
+// two independent jobs in the two int16 halves of every register and
+// updates both with one DPX s16x2 instruction per operation.  A job is swept
+// as strips of R query rows along its subject window: per strip the lane
+// keeps H(i, j-1) and E(i, j-1) of its R rows in registers, and the H/F
+// values of the row above the strip come from a per-lane boundary buffer
+// indexed by band offset k = j - i - lo, laid out [k][lane] so the warp
+// reads and writes 256 contiguous bytes per step.  All lanes run the same
+// column schedule: the rows entering the band at its left edge are handled
+// by compile-time unrolling, the middle steps need no masks, and only the
+// right edge (band widths differ within a warp) is masked per half.  The
+// boundary value, residue codes and substitution scores of a step are
+// fetched one to two steps ahead.  Substitution scores come from per-query
+// profiles P[c][i] = S(q_i, c) + bias_i (int16, built at query upload): two
+// 16-byte loads per 8 rows and step.
 //
-// Cells outside the window (j < 0 or j >= n) and rows past the query end use
-// a sentinel code whose profile value is kSent16; such cells only ever hold
-// values below the band optimum and never feed an in-window cell (except the
-// j = -1 column, which holds exactly H = 0 as the reference's "hd = 0 when
-// j == 0" rule requires), so they need no masks.
+// Cells outside the window (j < 0 or j >= n), rows past the query end and
+// the strips of a half that has finished use a sentinel code / sentinel
+// profile whose value is kSent16: such cells only ever hold values below the
+// band optimum and never feed an in-window cell (except the j = -1 column,
+// which holds exactly H = 0 as the reference's "hd = 0 when j == 0" rule
+// requires), so they need no masks.
 //
 // A job whose int16 best reaches kLimit16 is re-run by the int32 kernel
 // (k_band_generic), as the reference re-runs its int16 kernel in int32
@@ -36,11 +41,20 @@
 namespace saber {
 
 __device__ __forceinline__ uint32_t pk2(int v) { return (uint32_t)(uint16_t)(int16_t)v * 0x10001u; }
-__device__ __forceinline__ uint32_t pk2(int lo, int hi) {
-    return (uint32_t)(uint16_t)(int16_t)lo | ((uint32_t)(uint16_t)(int16_t)hi << 16);
-}
 __device__ __forceinline__ int lo16(uint32_t v) { return (int)(int16_t)(v & 0xFFFFu); }
 __device__ __forceinline__ int hi16(uint32_t v) { return (int)(int16_t)(v >> 16); }
+
+// R int16 sentinel profile entries: the profile of a half whose job has no
+// strip left (16-byte aligned for the vector loads).
+__device__ __align__(16) int16_t g_sent_profile[64] = {
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
+    kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16};
 
 struct PackedConsts {
     uint32_t ngo2, nge2, neg2;
@@ -64,37 +78,80 @@ struct StripState {
     uint32_t E[R];   // E(row r, previous column)
 };
 
-struct LaneJob {
-    const uint8_t* win;  // window start (may be null when n == 0)
-    int n;               // window length
-    int lo;              // clipped band lo
-    int w;               // clipped band width
+// One job of a half: its window, clipped band and rows.
+struct HalfJob {
+    const int16_t* prof;  // query profile (rows c = 0..24, stride mpad)
+    const uint8_t* win;   // window start (unused when n == 0)
+    int mpad;
+    int n;                // window length (0: every column is a sentinel)
+    int lo;               // clipped band lo
+    int w;                // clipped band width
+    int s0;               // first strip
+    int ns;               // number of strips
 };
 
-__device__ __forceinline__ int load_code(const LaneJob& j, int col) {
-    return ((unsigned)col < (unsigned)j.n) ? (int)__ldg(j.win + col) : kSentCode;
+// Per-strip view of a half: profile row base for this strip's rows.
+struct HalfStrip {
+    const int16_t* rows;  // prof + i0 (sentinel block when the half is done)
+    const uint8_t* win;
+    int mpad;
+    int n;
+    int col0;             // window column of step 0 (= lo + i0)
+};
+
+__device__ __forceinline__ HalfStrip half_strip(const HalfJob& h, int t, int R) {
+    HalfStrip v;
+    if (t < h.ns) {
+        int i0 = (h.s0 + t) * R;
+        v.rows = h.prof + i0;
+        v.win = h.win;
+        v.mpad = h.mpad;
+        v.n = h.n;
+        v.col0 = h.lo + i0;
+    } else {
+        v.rows = g_sent_profile;
+        v.win = nullptr;
+        v.mpad = 0;
+        v.n = 0;
+        v.col0 = 0;
+    }
+    return v;
 }
 
-// Loads the packed substitution scores of R rows (starting at the strip's
-// first row) for the two halves' residue codes.
+__device__ __forceinline__ int load_code(const HalfStrip& h, int u) {
+    int col = h.col0 + u;
+    return ((unsigned)col < (unsigned)h.n) ? (int)__ldg(h.win + col) : kSentCode;
+}
+
+// Raw profile vectors of one step for both halves (R/8 x 16 bytes each).
 template <int R>
-__device__ __forceinline__ void load_sub(const int16_t* __restrict__ prof, int mpad, int i0, int ca,
-                                         int cb, uint32_t (&sub)[R]) {
-    const uint4* pa = reinterpret_cast<const uint4*>(prof + (size_t)ca * mpad + i0);
-    const uint4* pb = reinterpret_cast<const uint4*>(prof + (size_t)cb * mpad + i0);
+struct StepLoads {
+    uint4 a[R / 8];
+    uint4 b[R / 8];
+    uint2 top;  // (H, F) of the row above at band offset u + 1
+};
+
+template <int R>
+__device__ __forceinline__ void fetch_step(StepLoads<R>& L, const HalfStrip& ha, const HalfStrip& hb, int ca,
+                                           int cb, const uint2* __restrict__ buf, int kin) {
+    const uint4* pa = reinterpret_cast<const uint4*>(ha.rows + (size_t)ca * ha.mpad);
+    const uint4* pb = reinterpret_cast<const uint4*>(hb.rows + (size_t)cb * hb.mpad);
 #pragma unroll
     for (int g = 0; g < R / 8; g++) {
-        uint4 a = __ldg(pa + g);
-        uint4 b = __ldg(pb + g);
-        sub[8 * g + 0] = __byte_perm(a.x, b.x, 0x5410);
-        sub[8 * g + 1] = __byte_perm(a.x, b.x, 0x7632);
-        sub[8 * g + 2] = __byte_perm(a.y, b.y, 0x5410);
-        sub[8 * g + 3] = __byte_perm(a.y, b.y, 0x7632);
-        sub[8 * g + 4] = __byte_perm(a.z, b.z, 0x5410);
-        sub[8 * g + 5] = __byte_perm(a.z, b.z, 0x7632);
-        sub[8 * g + 6] = __byte_perm(a.w, b.w, 0x5410);
-        sub[8 * g + 7] = __byte_perm(a.w, b.w, 0x7632);
+        L.a[g] = __ldg(pa + g);
+        L.b[g] = __ldg(pb + g);
     }
+    L.top = buf[(size_t)kin * 32];
+}
+
+template <int R>
+__device__ __forceinline__ uint32_t sub_of(const StepLoads<R>& L, int r) {
+    const uint4& a = L.a[r / 8];
+    const uint4& b = L.b[r / 8];
+    const int q = (r % 8) / 2;
+    uint32_t x = q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : a.w;
+    uint32_t y = q == 0 ? b.x : q == 1 ? b.y : q == 2 ? b.z : b.w;
+    return (r & 1) ? __byte_perm(x, y, 0x7632) : __byte_perm(x, y, 0x5410);
 }
 
 // Mask of the halves whose row r is still inside its band at this step
@@ -109,21 +166,18 @@ __device__ __forceinline__ uint32_t ragged_mask(int r, int thr_a, int thr_b) {
 // (compile-time U); MODE 1: all rows, no masks; MODE 2: all rows, ragged
 // right-edge masks.
 template <int R, int MODE, int U>
-__device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, uint2* __restrict__ buf,
-                                           int u, int wmax, const uint32_t (&sub)[R],
-                                           const PackedConsts& c, uint32_t& best, int thr_a,
-                                           int thr_b) {
-    int kin = u + 1 <= wmax ? u + 1 : wmax;
-    uint2 top = buf[(size_t)kin * 32];
-    uint32_t Hup = top.x, Fup = top.y;
+__device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, uint2* __restrict__ buf, int u,
+                                           const StepLoads<R>& L, const PackedConsts& c, uint32_t& best,
+                                           int thr_a, int thr_b) {
+    uint32_t Hup = L.top.x, Fup = L.top.y;
     uint32_t diag = diag0;
-    diag0 = top.x;
+    diag0 = L.top.x;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (MODE == 0 && r > U) break;
         uint32_t H, F;
         uint32_t hold = st.Hd[r];
-        cell(st.E[r], hold, Hup, Fup, diag, sub[r], c, H, F);
+        cell(st.E[r], hold, Hup, Fup, diag, sub_of<R>(L, r), c, H, F);
         if (MODE == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
             H = (H & mk) | (c.neg2 & ~mk);
@@ -135,54 +189,79 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
         Fup = F;
         best = __vimax_s16x2_relu(best, H);
     }
-    if (MODE != 0 || U == R - 1) {
-        int kout = u - R + 1;
-        buf[(size_t)kout * 32] = make_uint2(Hup, Fup);
-    }
+    if (MODE != 0 || U == R - 1) buf[(size_t)(u - R + 1) * 32] = make_uint2(Hup, Fup);
+}
+
+// The pipelined column loop state of one strip: the loads of step u + 1 and
+// the residue codes of step u + 2 are in flight while step u computes.
+template <int R>
+struct Pipe {
+    StepLoads<R> cur, nxt;
+    int ca2, cb2;  // codes of step u + 2
+};
+
+template <int R>
+__device__ __forceinline__ void pipe_advance(Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
+                                             const uint2* buf, int u, int wmax) {
+    // called before computing step u: cur <- nxt (step u), issue step u + 1
+    p.cur = p.nxt;
+    int k1 = u + 2 <= wmax ? u + 2 : wmax;
+    fetch_step<R>(p.nxt, ha, hb, p.ca2, p.cb2, buf, k1);
+    p.ca2 = load_code(ha, u + 2);
+    p.cb2 = load_code(hb, u + 2);
 }
 
 template <int R, int U>
 struct LeftTriangle {
     __device__ __forceinline__ static void run(StripState<R>& st, uint32_t& diag0, uint2* buf, int wmax,
-                                               const int16_t* prof, int mpad, int i0,
-                                               const LaneJob& ja, const LaneJob& jb,
+                                               Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
                                                const PackedConsts& c, uint32_t& best) {
-        LeftTriangle<R, U - 1>::run(st, diag0, buf, wmax, prof, mpad, i0, ja, jb, c, best);
-        uint32_t sub[R];
-        int ca = load_code(ja, ja.lo + i0 + U);
-        int cb = load_code(jb, jb.lo + i0 + U);
-        load_sub<R>(prof, mpad, i0, ca, cb, sub);
-        strip_step<R, 0, U>(st, diag0, buf, U, wmax, sub, c, best, 0, 0);
+        LeftTriangle<R, U - 1>::run(st, diag0, buf, wmax, p, ha, hb, c, best);
+        pipe_advance<R>(p, ha, hb, buf, U, wmax);
+        strip_step<R, 0, U>(st, diag0, buf, U, p.cur, c, best, 0, 0);
     }
 };
 template <int R>
 struct LeftTriangle<R, -1> {
-    __device__ __forceinline__ static void run(StripState<R>&, uint32_t&, uint2*, int, const int16_t*, int,
-                                               int, const LaneJob&, const LaneJob&, const PackedConsts&,
-                                               uint32_t&) {}
+    __device__ __forceinline__ static void run(StripState<R>&, uint32_t&, uint2*, int, Pipe<R>&, const HalfStrip&,
+                                               const HalfStrip&, const PackedConsts&, uint32_t&) {}
 };
 
-struct FastTask {
-    uint32_t pair_begin;  // index of the first pair in the pair list
-};
+__device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, const int16_t* prof,
+                                          const uint64_t* prof_off, const uint32_t* prof_mpad,
+                                          const uint64_t* qoffs, const uint8_t* res, int R) {
+    const uint32_t q = j.query;
+    const int64_t m = (int64_t)(qoffs[q + 1] - qoffs[q]);
+    int64_t lo = j.band_lo, hi = j.band_hi;
+    int64_t w = clip_band(m, j.win_len, lo, hi);
+    h.prof = prof + prof_off[q];
+    h.mpad = (int)prof_mpad[q];
+    h.win = res + j.win_begin;
+    h.n = (int)j.win_len;
+    h.lo = (int)lo;
+    h.w = (int)w;
+    int64_t first = hi < 0 ? -hi : 0;
+    int64_t last = (int64_t)j.win_len - 1 - lo;
+    if (last > m - 1) last = m - 1;
+    h.s0 = (int)(first / R);
+    h.ns = (int)(last / R - first / R + 1);
+}
 
-// Persistent warps over warp tasks (32 pairs of one query each).
-// pairs[p] = (sorted position of the first job, 1 or 2 jobs).
+// Persistent warps over warp tasks: task t = sorted positions [64t, 64t + 64)
+// of the fast class; lane l takes positions 64t + 2l (low half) and + 1.
 template <int R>
-__global__ void __launch_bounds__(256) k_band_fast(
+__global__ void __launch_bounds__(256, 2) k_band_fast(
     const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
     const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
-    const uint32_t* __restrict__ order, const uint2* __restrict__ pairs,
-    const uint32_t* __restrict__ wtask_pair, const uint32_t* __restrict__ counts,
+    const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
     uint32_t* __restrict__ wt_counter, uint2* __restrict__ bufs, uint32_t buf_stride, int go, int ge,
-    int32_t* __restrict__ scores, uint32_t* __restrict__ rescue, uint32_t* __restrict__ rescue_count,
-    uint32_t rescue_base) {
+    int32_t* __restrict__ scores, uint32_t* __restrict__ rescue, uint32_t* __restrict__ rescue_count) {
     const int lane = threadIdx.x & 31;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint2* mybuf = bufs + (size_t)gwarp * buf_stride * 32 + lane;
-    const uint32_t n_wtasks = counts[3];
-    const uint32_t n_pairs = counts[2];
+    const uint32_t n_fast = counts[0];
+    const uint32_t n_wtasks = (n_fast + 63) / 64;
     PackedConsts c;
     c.ngo2 = pk2(-go);
     c.nge2 = pk2(-ge);
@@ -193,71 +272,29 @@ __global__ void __launch_bounds__(256) k_band_fast(
         if (lane == 0) wt = atomicAdd(wt_counter, 1u);
         wt = __shfl_sync(0xffffffffu, wt, 0);
         if (wt >= n_wtasks) break;
-        const uint32_t p0 = wtask_pair[wt];
-        if (p0 >= n_pairs) continue;  // defensive: never index past the pair list
-        const uint32_t qid = jobs[order[pairs[p0].x]].query;
-        const uint32_t p = p0 + lane;
-        bool has_pair = p < n_pairs;
-        uint2 pr = has_pair ? pairs[p] : make_uint2(0, 0);
-        uint32_t ja_idx = 0, jb_idx = 0;
-        bool has_a = false, has_b = false;
-        if (has_pair) {
-            ja_idx = order[pr.x];
-            has_a = jobs[ja_idx].query == qid;
-            if (has_a && pr.y == 2) {
-                jb_idx = order[pr.x + 1];
-                has_b = true;
-            }
-        }
-        const uint64_t q0 = qoffs[qid];
-        const int m = (int)(qoffs[qid + 1] - q0);
-        const int16_t* qprof = prof + prof_off[qid];
-        const int mpad = (int)prof_mpad[qid];
-
-        LaneJob ja{nullptr, 0, 0, 0}, jb{nullptr, 0, 0, 0};
-        int first_a = 1 << 30, last_a = -1, first_b = 1 << 30, last_b = -1;
-        if (has_a) {
-            saber_band_job jj = jobs[ja_idx];
-            int64_t lo = jj.band_lo, hi = jj.band_hi;
-            int64_t w = clip_band(m, jj.win_len, lo, hi);
-            ja.win = res + jj.win_begin;
-            ja.n = (int)jj.win_len;
-            ja.lo = (int)lo;
-            ja.w = (int)w;
-            first_a = (int)(hi < 0 ? -hi : 0);
-            int64_t la = (int64_t)jj.win_len - 1 - lo;
-            last_a = (int)(la < m - 1 ? la : m - 1);
-        }
-        if (has_b) {
-            saber_band_job jj = jobs[jb_idx];
-            int64_t lo = jj.band_lo, hi = jj.band_hi;
-            int64_t w = clip_band(m, jj.win_len, lo, hi);
-            jb.win = res + jj.win_begin;
-            jb.n = (int)jj.win_len;
-            jb.lo = (int)lo;
-            jb.w = (int)w;
-            first_b = (int)(hi < 0 ? -hi : 0);
-            int64_t lb = (int64_t)jj.win_len - 1 - lo;
-            last_b = (int)(lb < m - 1 ? lb : m - 1);
-        }
+        const uint32_t pa = wt * 64 + 2 * lane, pb = pa + 1;
+        const bool has_a = pa < n_fast, has_b = pb < n_fast;
+        const uint32_t ja_idx = has_a ? order[pa] : 0u;
+        const uint32_t jb_idx = has_b ? order[pb] : 0u;
+        HalfJob A{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0}, B{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0};
+        if (has_a) load_half(A, jobs[ja_idx], prof, prof_off, prof_mpad, qoffs, res, R);
+        if (has_b) load_half(B, jobs[jb_idx], prof, prof_off, prof_mpad, qoffs, res, R);
         const int big = 1 << 30;
-        int wmin_l = min(has_a ? ja.w : big, has_b ? jb.w : big);
-        int wmax_l = max(has_a ? ja.w : 0, has_b ? jb.w : 0);
-        const int wmin = __reduce_min_sync(0xffffffffu, wmin_l);
-        const int wmax = __reduce_max_sync(0xffffffffu, wmax_l);
-        if (!has_a) ja.w = wmin;
-        if (!has_b) jb.w = wmin;
-        const int s_first = __reduce_min_sync(0xffffffffu, min(first_a, first_b)) / R;
-        const int s_last = __reduce_max_sync(0xffffffffu, max(last_a, last_b)) / R;
+        const int wmin = __reduce_min_sync(0xffffffffu, min(has_a ? A.w : big, has_b ? B.w : big));
+        const int wmax = __reduce_max_sync(0xffffffffu, max(has_a ? A.w : 0, has_b ? B.w : 0));
+        const int nsmax = __reduce_max_sync(0xffffffffu, max(A.ns, B.ns));
+        if (!has_a) A.w = wmin;
+        if (!has_b) B.w = wmin;
 
-        // Boundary of the row above the first strip: H = 0 (the reference's
-        // hd = 0 on row 0), F unreachable; position wmax is outside every band.
+        // Boundary of the row above each job's first strip: H = 0 (the
+        // reference's hd = 0 on row 0), F unreachable; position wmax lies
+        // outside every band.
         for (int k = 0; k < wmax; k++) mybuf[(size_t)k * 32] = make_uint2(0u, c.neg2);
         mybuf[(size_t)wmax * 32] = make_uint2(c.neg2, c.neg2);
 
         uint32_t best = 0;
-        for (int s = s_first; s <= s_last; s++) {
-            const int i0 = s * R;
+        for (int t = 0; t < nsmax; t++) {
+            const HalfStrip ha = half_strip(A, t, R), hb = half_strip(B, t, R);
             StripState<R> st;
 #pragma unroll
             for (int r = 0; r < R; r++) {
@@ -265,41 +302,33 @@ __global__ void __launch_bounds__(256) k_band_fast(
                 st.E[r] = c.neg2;
             }
             uint32_t diag0 = mybuf[0].x;
-            LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, qprof, mpad, i0, ja, jb, c, best);
+            Pipe<R> p;
+            {
+                int ca0 = load_code(ha, 0), cb0 = load_code(hb, 0);
+                fetch_step<R>(p.nxt, ha, hb, ca0, cb0, mybuf, 1);
+                p.ca2 = load_code(ha, 1);
+                p.cb2 = load_code(hb, 1);
+            }
+            LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
             int u = R;
             for (; u < wmin; u++) {
-                uint32_t sub[R];
-                int ca = load_code(ja, ja.lo + i0 + u);
-                int cb = load_code(jb, jb.lo + i0 + u);
-                load_sub<R>(qprof, mpad, i0, ca, cb, sub);
-                strip_step<R, 1, 0>(st, diag0, mybuf, u, wmax, sub, c, best, 0, 0);
+                pipe_advance<R>(p, ha, hb, mybuf, u, wmax);
+                strip_step<R, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
             }
             const int uend = wmax + R - 1;
             for (; u < uend; u++) {
-                uint32_t sub[R];
-                int ca = load_code(ja, ja.lo + i0 + u);
-                int cb = load_code(jb, jb.lo + i0 + u);
-                load_sub<R>(qprof, mpad, i0, ca, cb, sub);
-                strip_step<R, 2, 0>(st, diag0, mybuf, u, wmax, sub, c, best, u - ja.w + 1,
-                                    u - jb.w + 1);
+                pipe_advance<R>(p, ha, hb, mybuf, u, wmax);
+                strip_step<R, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);
             }
         }
-        int sa = lo16(best), sb = hi16(best);
+        const int sa = lo16(best), sb = hi16(best);
         if (has_a) {
-            if (sa >= kLimit16) {
-                uint32_t slot = atomicAdd(rescue_count, 1u);
-                rescue[rescue_base + slot] = ja_idx;
-            } else {
-                scores[ja_idx] = sa;
-            }
+            if (sa >= kLimit16) rescue[atomicAdd(rescue_count, 1u)] = ja_idx;
+            else scores[ja_idx] = sa;
         }
         if (has_b) {
-            if (sb >= kLimit16) {
-                uint32_t slot = atomicAdd(rescue_count, 1u);
-                rescue[rescue_base + slot] = jb_idx;
-            } else {
-                scores[jb_idx] = sb;
-            }
+            if (sb >= kLimit16) rescue[atomicAdd(rescue_count, 1u)] = jb_idx;
+            else scores[jb_idx] = sb;
         }
     }
 }
@@ -395,18 +424,26 @@ __global__ void __launch_bounds__(128) k_band_generic(
 }
 
 // ---- host-side launch wrappers (the runtime TU calls these) ----
-int band_fast_blocks_per_sm() {
+template <int R>
+static int fast_blocks_per_sm() {
     int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_band_fast<kStripRows>, 256, 0) != cudaSuccess)
-        return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_band_fast<R>, 256, 0) != cudaSuccess) return 1;
     return bps < 1 ? 1 : bps;
 }
 
+int band_fast_blocks_per_sm(int strip_rows) {
+    return strip_rows == 8 ? fast_blocks_per_sm<8>() : fast_blocks_per_sm<16>();
+}
+
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a) {
-    k_band_fast<kStripRows><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs,
-                                                 a.order, a.pairs, a.wtask_pair, a.counts, a.wt_counter,
-                                                 a.bufs, a.buf_stride, a.go, a.ge, a.scores, a.rescue,
-                                                 a.rescue_count, 0u);
+    if (a.strip_rows == 8)
+        k_band_fast<8><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
+                                            a.counts, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                            a.rescue, a.rescue_count);
+    else
+        k_band_fast<16><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
+                                             a.counts, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                             a.rescue, a.rescue_count);
     return cudaGetLastError();
 }
 

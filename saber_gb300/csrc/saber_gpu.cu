@@ -1,11 +1,10 @@
 // C-ABI runtime of libsaber_gb300.so: handle, device-resident database and
 // query sets, and the banded scoring pipeline
-//   classify -> radix sort (query, width) -> pair equal-width jobs ->
-//   warp tasks -> packed int16 kernel -> int32 kernel (narrow bands and
+//   classify -> radix sort by (strips, width, query) -> packed int16 kernel
+//   (64 consecutive jobs per warp task) -> int32 kernel (narrow bands and
 //   int16 overflows)
 // all on the handle's stream.  See include/saber_gpu.h for the contract.
 #include <cub/cub.cuh>
-#include <thrust/iterator/counting_iterator.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -84,6 +83,7 @@ struct saber_gpu {
     std::mutex mu;
     std::string err;
     int sm_count = 0;
+    int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
     // the handle's scheme and dataset (set_scheme / load_db / load_queries)
     saber::Scheme scheme;
     saber::Dataset main;
@@ -91,8 +91,8 @@ struct saber_gpu {
     saber::Scheme eph_scheme;
     saber::Dataset eph;
     // per-call scratch
-    saber::DevBuf keys_in, keys_out, vals_in, vals_out, aux, aux2, flags, pairs, pair_pos, wtask,
-        counts, stats, cub_tmp, bufs, slabs, list, jobs_dev, scores_dev;
+    saber::DevBuf keys_in, keys_out, vals_in, vals_out, counts, stats, cub_tmp, bufs, slabs, list, jobs_dev,
+        scores_dev;
 };
 
 namespace saber {
@@ -160,9 +160,9 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
 }
 
 // stats layout (uint64): 0 cells, 1 wmax_fast, 2 wmax_gen, 3 bad job count, 4 fast cells
-// counts layout (uint32): 0 n_fast, 1 n_gen, 2 n_pairs, 3 n_wtasks, 4 n_empty,
+// counts layout (uint32): 0 n_fast, 1 n_gen, 4 n_empty,
 //                         5 generic list count (class 1 + rescued), 6 wt counter
-__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs,
+__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, int R,
                            const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
                            uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                            int32_t* __restrict__ scores, uint32_t* __restrict__ counts,
@@ -186,12 +186,19 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
         } else {
             uint64_t jc = band_cells(m, j.win_len, lo, hi);
             cells += jc;
-            if (w < kStripRows || w >= (1 << 24)) {
+            // strips of R rows holding the job's in-window rows
+            const int64_t first = hi < 0 ? -hi : 0;
+            int64_t last = (int64_t)j.win_len - 1 - lo;
+            if (last > m - 1) last = m - 1;
+            const int64_t ns = last / R - first / R + 1;
+            if (w < R || w >= (1 << 16) || ns >= (1 << 14)) {
                 keys[t] = (1ull << 62) | t;
                 c1++;
                 wg = max(wg, (unsigned long long)w);
             } else {
-                keys[t] = ((uint64_t)j.query << 24) | (uint64_t)w;
+                // fast class ordered by (strips, width, query): a warp's 64
+                // consecutive jobs then share their loop counts and widths
+                keys[t] = ((uint64_t)ns << 48) | ((uint64_t)w << 32) | (uint64_t)j.query;
                 c0++;
                 fcells += jc;
                 wf = max(wf, (unsigned long long)w);
@@ -207,47 +214,6 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
     atomicAdd(&stats[3], (unsigned long long)bad);
     atomicAdd(&stats[4], (unsigned long long)fcells);
 }
-
-// run_start candidates: position p when the sorted key changes at p.
-__global__ void k_run_marks(const uint64_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ mark) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    mark[p] = (p == 0 || keys[p] != keys[p - 1]) ? p : 0u;
-}
-
-// flag every second position of a run (the first job of each pair).
-__global__ void k_pair_flags(const uint32_t* __restrict__ run_start, uint32_t n, uint8_t* __restrict__ flag) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    flag[p] = ((p - run_start[p]) & 1u) == 0;
-}
-
-__global__ void k_make_pairs(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pos,
-                             const uint32_t* __restrict__ counts, uint32_t n_fast,
-                             uint2* __restrict__ pairs, uint32_t* __restrict__ qmark) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t np = counts[2];
-    if (i >= np) return;
-    uint32_t p = pos[i];
-    bool two = p + 1 < n_fast && keys[p + 1] == keys[p];
-    pairs[i] = make_uint2(p, two ? 2u : 1u);
-    uint64_t q = keys[p] >> 24;
-    bool newq = i == 0 || (keys[pos[i - 1]] >> 24) != q;
-    qmark[i] = newq ? i : 0u;
-}
-
-// Every flag below n is written: positions past the pair count are cleared
-// (the select runs over all n entries).
-__global__ void k_wtask_flags(const uint32_t* __restrict__ qstart, const uint32_t* __restrict__ counts,
-                              uint32_t n, uint8_t* __restrict__ flag) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    flag[i] = i < counts[2] && ((i - qstart[i]) & 31u) == 0;
-}
-
-struct MaxOp {
-    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
-};
 
 static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
     uint64_t b = (n + t - 1) / t;
@@ -277,12 +243,6 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     CUALLOC(h, h->keys_out, njobs * 8);
     CUALLOC(h, h->vals_in, njobs * 4);
     CUALLOC(h, h->vals_out, njobs * 4);
-    CUALLOC(h, h->aux, njobs * 4);
-    CUALLOC(h, h->aux2, njobs * 4);
-    CUALLOC(h, h->flags, njobs);
-    CUALLOC(h, h->pairs, njobs * 8);
-    CUALLOC(h, h->pair_pos, njobs * 4);
-    CUALLOC(h, h->wtask, njobs * 4);
     CUALLOC(h, h->counts, 16 * 4);
     CUALLOC(h, h->stats, 8 * 8);
     CUALLOC(h, h->list, njobs * 4);
@@ -302,23 +262,17 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res, h->keys_in.as<uint64_t>(),
+        d_jobs, njobs, h->strip_rows, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res, h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
     CU(h, cudaGetLastError());
     local.kernel_launches++;
 
-    // CUB temp storage: the max over the ops used below.
-    size_t t_sort = 0, t_scan = 0, t_sel = 0;
+    // CUB temp storage of the radix sort
+    size_t t_sort = 0;
     CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t_sort, h->keys_in.as<uint64_t>(),
                                           h->keys_out.as<uint64_t>(), h->vals_in.as<uint32_t>(),
                                           h->vals_out.as<uint32_t>(), (int)n, 0, 64, s));
-    CU(h, cub::DeviceScan::InclusiveScan(nullptr, t_scan, h->aux.as<uint32_t>(), h->aux2.as<uint32_t>(),
-                                         MaxOp(), (int)n, s));
-    CU(h, cub::DeviceSelect::Flagged(nullptr, t_sel, thrust::counting_iterator<uint32_t>(0),
-                                     h->flags.as<uint8_t>(), h->pair_pos.as<uint32_t>(), counts + 2,
-                                     (int)n, s));
-    size_t t_max = std::max(t_sort, std::max(t_scan, t_sel));
-    CUALLOC(h, h->cub_tmp, t_max);
+    CUALLOC(h, h->cub_tmp, t_sort);
     size_t tb = h->cub_tmp.cap;
     CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->keys_in.as<uint64_t>(),
                                           h->keys_out.as<uint64_t>(), h->vals_in.as<uint32_t>(),
@@ -350,30 +304,8 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     CU(h, cudaMemcpyAsync(counts + 5, &n_gen, 4, cudaMemcpyHostToDevice, s));
 
     if (n_fast) {
-        const unsigned T = 256;
-        // pairs of equal (query, width): run starts by a max-scan of change marks
-        uint32_t* aux = h->aux.as<uint32_t>();
-        uint32_t* aux2 = h->aux2.as<uint32_t>();
-        k_run_marks<<<nblocks(n_fast, T), T, 0, s>>>(h->keys_out.as<uint64_t>(), n_fast, aux);
-        CU(h, cub::DeviceScan::InclusiveScan(h->cub_tmp.p, tb, aux, aux2, MaxOp(), (int)n_fast, s));
-        k_pair_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, n_fast, h->flags.as<uint8_t>());
-        CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
-                                         h->flags.as<uint8_t>(), h->pair_pos.as<uint32_t>(), counts + 2,
-                                         (int)n_fast, s));
-        k_make_pairs<<<nblocks(n_fast, T), T, 0, s>>>(h->keys_out.as<uint64_t>(), h->pair_pos.as<uint32_t>(), counts,
-                                                      n_fast, h->pairs.as<uint2>(), aux);
-        // warp tasks: 32 consecutive pairs of one query
-        CU(h, cub::DeviceScan::InclusiveScan(h->cub_tmp.p, tb, aux, aux2, MaxOp(), (int)n_fast, s));
-        k_wtask_flags<<<nblocks(n_fast, T), T, 0, s>>>(aux2, counts, n_fast, h->flags.as<uint8_t>());
-        CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
-                                         h->flags.as<uint8_t>(), h->wtask.as<uint32_t>(), counts + 3, (int)n_fast,
-                                         s));
-        CU(h, cudaGetLastError());
-        local.kernel_launches += 4;   // run marks, pair flags, make pairs, warp-task flags
-        local.library_launches += 8;  // two scans and two selects (two kernels each)
-
         // persistent warps; one boundary buffer of (wmax + 1) x 32 lanes per warp
-        const int bps = band_fast_blocks_per_sm();
+        const int bps = band_fast_blocks_per_sm(h->strip_rows);
         const unsigned grid = (unsigned)(h->sm_count * bps);
         const uint64_t warps = (uint64_t)grid * 256 / 32;
         const uint32_t stride = (uint32_t)(wmax_fast + 1);
@@ -386,8 +318,6 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.qoffs = qs.offsets.as<uint64_t>();
         a.jobs = d_jobs;
         a.order = order;
-        a.pairs = h->pairs.as<uint2>();
-        a.wtask_pair = h->wtask.as<uint32_t>();
         a.counts = counts;
         a.wt_counter = counts + 6;
         a.bufs = h->bufs.as<uint2>();
@@ -397,6 +327,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.scores = d_scores;
         a.rescue = h->list.as<uint32_t>();
         a.rescue_count = counts + 5;
+        a.strip_rows = h->strip_rows;
         CU(h, cudaEventRecord(ev[1], s));
         CU(h, launch_band_fast(grid, s, a));
         CU(h, cudaEventRecord(ev[2], s));
@@ -736,6 +667,15 @@ int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs
     if (rc != SABER_OK) return fail(h, rc, "%s", msg);
     return SABER_OK;
 }
+
+int saber_gpu_set_strip_rows(saber_gpu* h, int32_t strip_rows) {
+    ENTER(h);
+    if (strip_rows != 8 && strip_rows != 16) return fail(h, SABER_ERR_ARG, "strip_rows must be 8 or 16");
+    h->strip_rows = strip_rows;
+    return SABER_OK;
+}
+
+int32_t saber_gpu_get_strip_rows(saber_gpu* h) { return h ? h->strip_rows : 0; }
 
 uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi) {
     int64_t lo = band_lo, hi = band_hi;

@@ -71,6 +71,8 @@ def load_library():
         "saber_gpu_score_windows": (ctypes.c_int, [P, P, U32, P, P, P, U32, P, I32, I32, P]),
         "saber_band_cells": (U64, [U64, U64, I64, I64]),
         "saber_gpu_probe_int_peak": (ctypes.c_int, [P, P, P]),
+        "saber_gpu_set_strip_rows": (ctypes.c_int, [P, I32]),
+        "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
     for name, (res, args) in sig.items():
@@ -182,6 +184,14 @@ class Device:
         self._check(self.lib.saber_gpu_score_band_jobs_noalloc(self.h, ctypes.c_void_p(d_jobs_ptr), int(njobs),
                                                                int(max_band_width), ctypes.c_void_p(d_scores_ptr)),
                     "score_band_jobs_noalloc")
+
+    @property
+    def strip_rows(self):
+        return int(self.lib.saber_gpu_get_strip_rows(self.h))
+
+    @strip_rows.setter
+    def strip_rows(self, r):
+        self._check(self.lib.saber_gpu_set_strip_rows(self.h, int(r)), "set_strip_rows")
 
     def probe_int_peak(self):
         """(DPX s16x2 lane-instructions/s, int32 max lane-instructions/s) of this GPU."""

@@ -47,12 +47,14 @@ def test_golden_vectors_through_score_backend():
         assert list(got) == c["expected"], c["matrix"]
 
 
+@pytest.mark.parametrize("strip_rows", [8, 16])
 @pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8)])
-def test_random_band_jobs_match_oracle(dev, gaps):
+def test_random_band_jobs_match_oracle(dev, gaps, strip_rows):
     go, ge = gaps
     qs, ss, planted = synth.protein_db(100 + go, 40, 3000)
     bias = synth.query_bias(7, qs)
     jobs = synth.band_jobs(200 + ge, qs, ss, planted, 6000, half_min=1, half_max=140)
+    dev.strip_rows = strip_rows
     dev.set_scheme(B62, go, ge)
     dev.load_db(ss.codes, ss.offsets)
     dev.load_queries(qs.codes, qs.offsets, bias)
