@@ -64,8 +64,8 @@ struct FastArgs {
     const uint32_t* prof_mpad;
     const uint64_t* qoffs;
     const saber_band_job* jobs;
-    const uint32_t* order;
-    const uint32_t* counts;
+    const uint32_t* order;  // sorted job indices of this launch's class
+    const uint32_t* n_ptr;  // device count of those jobs
     uint32_t* wt_counter;
     uint2* bufs;
     uint32_t buf_stride;

@@ -141,7 +141,7 @@ __device__ __forceinline__ void fetch_step(StepLoads<R>& L, const HalfStrip& ha,
         L.a[g] = __ldg(pa + g);
         L.b[g] = __ldg(pb + g);
     }
-    L.top = buf[(size_t)kin * 32];
+    L.top = __ldcg(buf + (size_t)kin * 32);  // boundary rows live in L2, not L1
 }
 
 template <int R>
@@ -189,7 +189,7 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
         Fup = F;
         best = __vimax_s16x2_relu(best, H);
     }
-    if (MODE != 0 || U == R - 1) buf[(size_t)(u - R + 1) * 32] = make_uint2(Hup, Fup);
+    if (MODE != 0 || U == R - 1) __stcg(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Fup));
 }
 
 // The pipelined column loop state of one strip: the loads of step u + 1 and
@@ -248,19 +248,20 @@ __device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, c
 }
 
 // Persistent warps over warp tasks: task t = sorted positions [64t, 64t + 64)
-// of the fast class; lane l takes positions 64t + 2l (low half) and + 1.
+// of the fast class, taken largest first; lane l takes positions 64t + 2l
+// (low half) and 64t + 2l + 1 (high half).
 template <int R>
 __global__ void __launch_bounds__(256, 2) k_band_fast(
     const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
     const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
-    const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
+    const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_ptr,
     uint32_t* __restrict__ wt_counter, uint2* __restrict__ bufs, uint32_t buf_stride, int go, int ge,
     int32_t* __restrict__ scores, uint32_t* __restrict__ rescue, uint32_t* __restrict__ rescue_count) {
     const int lane = threadIdx.x & 31;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint2* mybuf = bufs + (size_t)gwarp * buf_stride * 32 + lane;
-    const uint32_t n_fast = counts[0];
+    const uint32_t n_fast = *n_ptr;
     const uint32_t n_wtasks = (n_fast + 63) / 64;
     PackedConsts c;
     c.ngo2 = pk2(-go);
@@ -272,7 +273,9 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         if (lane == 0) wt = atomicAdd(wt_counter, 1u);
         wt = __shfl_sync(0xffffffffu, wt, 0);
         if (wt >= n_wtasks) break;
-        const uint32_t pa = wt * 64 + 2 * lane, pb = pa + 1;
+        // largest tasks first: the sort order is ascending in strips and width
+        const uint32_t task = n_wtasks - 1 - wt;
+        const uint32_t pa = task * 64 + 2 * lane, pb = pa + 1;
         const bool has_a = pa < n_fast, has_b = pb < n_fast;
         const uint32_t ja_idx = has_a ? order[pa] : 0u;
         const uint32_t jb_idx = has_b ? order[pb] : 0u;
@@ -289,8 +292,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         // Boundary of the row above each job's first strip: H = 0 (the
         // reference's hd = 0 on row 0), F unreachable; position wmax lies
         // outside every band.
-        for (int k = 0; k < wmax; k++) mybuf[(size_t)k * 32] = make_uint2(0u, c.neg2);
-        mybuf[(size_t)wmax * 32] = make_uint2(c.neg2, c.neg2);
+        for (int k = 0; k < wmax; k++) __stcg(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
+        __stcg(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
 
         uint32_t best = 0;
         for (int t = 0; t < nsmax; t++) {
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 st.Hd[r] = c.neg2;
                 st.E[r] = c.neg2;
             }
-            uint32_t diag0 = mybuf[0].x;
+            uint32_t diag0 = __ldcg(mybuf).x;
             Pipe<R> p;
             {
                 int ca0 = load_code(ha, 0), cb0 = load_code(hb, 0);
@@ -311,6 +314,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
             }
             LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
             int u = R;
+#pragma unroll 2
             for (; u < wmin; u++) {
                 pipe_advance<R>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
@@ -438,11 +442,11 @@ int band_fast_blocks_per_sm(int strip_rows) {
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a) {
     if (a.strip_rows == 8)
         k_band_fast<8><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                            a.counts, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                            a.n_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                             a.rescue, a.rescue_count);
     else
         k_band_fast<16><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                             a.counts, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                             a.n_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                              a.rescue, a.rescue_count);
     return cudaGetLastError();
 }

@@ -159,9 +159,20 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
     }
 }
 
-// stats layout (uint64): 0 cells, 1 wmax_fast, 2 wmax_gen, 3 bad job count, 4 fast cells
-// counts layout (uint32): 0 n_fast, 1 n_gen, 4 n_empty,
-//                         5 generic list count (class 1 + rescued), 6 wt counter
+// stats layout (uint64): 0 cells, 1 wmax of the R-row class, 2 wmax of the
+//   int32 class, 3 bad job count, 4 cells of the packed classes, 5 wmax of
+//   the 8-row class
+// counts layout (uint32): 0 jobs in the R-row class, 1 int32 class, 4 empty,
+//   5 int32 list length (class + rescued), 6 task counter of the R-row launch,
+//   7 jobs in the 8-row class, 8 task counter of the 8-row launch
+//
+// Classes (the top two key bits, so the sort makes them contiguous):
+//   0: width >= R (R = the handle's strip rows), packed int16 kernel with R rows
+//   1: 8 <= width < R when R = 16, packed int16 kernel with 8 rows
+//   2: narrower bands and out-of-range sizes, int32 kernel
+//   3: empty jobs (score 0, written here)
+// Packed-class keys order jobs by (strips, width, query) so that the 64
+// consecutive jobs of a warp task share their loop counts and widths.
 __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, int R,
                            const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
                            uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
@@ -169,8 +180,8 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
                            unsigned long long* __restrict__ stats) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t cells = 0, fcells = 0;
-    uint32_t c0 = 0, c1 = 0, c2 = 0, bad = 0;
-    unsigned long long wf = 0, wg = 0;
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, bad = 0;
+    unsigned long long w0 = 0, w1 = 0, w2 = 0;
     for (; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
         saber_band_job j = jobs[t];
         vals[t] = (uint32_t)t;
@@ -181,38 +192,51 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
         if (!ok) bad++;
         if (w == 0) {
             scores[t] = 0;
-            keys[t] = 2ull << 62;
+            keys[t] = 3ull << 62;
+            c3++;
+            continue;
+        }
+        const uint64_t jc = band_cells(m, j.win_len, lo, hi);
+        cells += jc;
+        // strips of `rows` rows holding the job's in-window rows
+        const int64_t first = hi < 0 ? -hi : 0;
+        int64_t last = (int64_t)j.win_len - 1 - lo;
+        if (last > m - 1) last = m - 1;
+        int cls = 2;
+        int rows = R;
+        if (w >= R) cls = 0;
+        else if (R > kStripRowsMin && w >= kStripRowsMin) {
+            cls = 1;
+            rows = kStripRowsMin;
+        }
+        const int64_t ns = last / rows - first / rows + 1;
+        if (cls != 2 && (w >= (1 << 16) || ns >= (1 << 14))) cls = 2;
+        if (cls == 2) {
+            keys[t] = (2ull << 62) | t;
             c2++;
+            w2 = max(w2, (unsigned long long)w);
         } else {
-            uint64_t jc = band_cells(m, j.win_len, lo, hi);
-            cells += jc;
-            // strips of R rows holding the job's in-window rows
-            const int64_t first = hi < 0 ? -hi : 0;
-            int64_t last = (int64_t)j.win_len - 1 - lo;
-            if (last > m - 1) last = m - 1;
-            const int64_t ns = last / R - first / R + 1;
-            if (w < R || w >= (1 << 16) || ns >= (1 << 14)) {
-                keys[t] = (1ull << 62) | t;
-                c1++;
-                wg = max(wg, (unsigned long long)w);
-            } else {
-                // fast class ordered by (strips, width, query): a warp's 64
-                // consecutive jobs then share their loop counts and widths
-                keys[t] = ((uint64_t)ns << 48) | ((uint64_t)w << 32) | (uint64_t)j.query;
+            keys[t] = ((uint64_t)cls << 62) | ((uint64_t)ns << 48) | ((uint64_t)w << 32) | (uint64_t)j.query;
+            fcells += jc;
+            if (cls == 0) {
                 c0++;
-                fcells += jc;
-                wf = max(wf, (unsigned long long)w);
+                w0 = max(w0, (unsigned long long)w);
+            } else {
+                c1++;
+                w1 = max(w1, (unsigned long long)w);
             }
         }
     }
     atomicAdd(&counts[0], c0);
-    atomicAdd(&counts[1], c1);
-    atomicAdd(&counts[4], c2);
+    atomicAdd(&counts[7], c1);
+    atomicAdd(&counts[1], c2);
+    atomicAdd(&counts[4], c3);
     atomicAdd(&stats[0], (unsigned long long)cells);
-    atomicMax(&stats[1], wf);
-    atomicMax(&stats[2], wg);
+    atomicMax(&stats[1], w0);
+    atomicMax(&stats[2], w2);
     atomicAdd(&stats[3], (unsigned long long)bad);
     atomicAdd(&stats[4], (unsigned long long)fcells);
+    atomicMax(&stats[5], w1);
 }
 
 static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
@@ -280,32 +304,39 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     local.library_launches += 9;  // onesweep radix sort: histogram + 8 digit passes
 
     // one small read-back: class counts and widths size the scratch
-    uint32_t hc[8];
-    unsigned long long hs[5];
-    CU(h, cudaMemcpyAsync(hc, counts, 8 * 4, cudaMemcpyDeviceToHost, s));
-    CU(h, cudaMemcpyAsync(hs, stats, 5 * 8, cudaMemcpyDeviceToHost, s));
+    uint32_t hc[10];
+    unsigned long long hs[6];
+    CU(h, cudaMemcpyAsync(hc, counts, 10 * 4, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaMemcpyAsync(hs, stats, 6 * 8, cudaMemcpyDeviceToHost, s));
     CU(h, cudaStreamSynchronize(s));
     if (hs[3] != 0)
         return fail(h, SABER_ERR_ARG, "%llu job(s) reference a query or window outside the loaded data", hs[3]);
-    const uint32_t n_fast = hc[0], n_gen = hc[1];
+    const uint32_t n_fast = hc[0], n_gen = hc[1], n_fast8 = hc[7];
     local.jobs = njobs;
     local.banded_cells = hs[0];
     local.fast_cells = hs[4];
-    local.fast_jobs = n_fast;
+    local.fast_jobs = n_fast + n_fast8;
     local.generic_jobs = n_gen;
     local.empty_jobs = hc[4];
-    const uint64_t wmax_fast = hs[1];
-    const uint64_t wmax_all = std::max<uint64_t>(hs[1], hs[2]);
+    const uint64_t wmax_fast = std::max<uint64_t>(hs[1], hs[5]);
+    const uint64_t wmax_all = std::max<uint64_t>(wmax_fast, hs[2]);
 
     const uint32_t* order = h->vals_out.as<uint32_t>();
     // generic list: class-1 jobs, then int16 overflows appended by the fast kernel
     if (n_gen)
-        CU(h, cudaMemcpyAsync(h->list.as<uint32_t>(), order + n_fast, (size_t)n_gen * 4, cudaMemcpyDeviceToDevice, s));
+        CU(h, cudaMemcpyAsync(h->list.as<uint32_t>(), order + n_fast + n_fast8, (size_t)n_gen * 4,
+                              cudaMemcpyDeviceToDevice, s));
     CU(h, cudaMemcpyAsync(counts + 5, &n_gen, 4, cudaMemcpyHostToDevice, s));
 
-    if (n_fast) {
-        // persistent warps; one boundary buffer of (wmax + 1) x 32 lanes per warp
-        const int bps = band_fast_blocks_per_sm(h->strip_rows);
+    CU(h, cudaEventRecord(ev[1], s));
+    // packed int16 launches: the R-row class, then the 8-row class; persistent
+    // warps, one boundary buffer of (wmax + 1) x 32 lanes per warp, shared by
+    // the two launches (same stream)
+    for (int pass = 0; pass < 2; pass++) {
+        const uint32_t nj = pass == 0 ? n_fast : n_fast8;
+        if (nj == 0) continue;
+        const int rows = pass == 0 ? h->strip_rows : kStripRowsMin;
+        const int bps = band_fast_blocks_per_sm(rows);
         const unsigned grid = (unsigned)(h->sm_count * bps);
         const uint64_t warps = (uint64_t)grid * 256 / 32;
         const uint32_t stride = (uint32_t)(wmax_fast + 1);
@@ -317,9 +348,9 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.prof_mpad = qs.prof_mpad.as<uint32_t>();
         a.qoffs = qs.offsets.as<uint64_t>();
         a.jobs = d_jobs;
-        a.order = order;
-        a.counts = counts;
-        a.wt_counter = counts + 6;
+        a.order = order + (pass == 0 ? 0 : n_fast);
+        a.n_ptr = counts + (pass == 0 ? 0 : 7);
+        a.wt_counter = counts + (pass == 0 ? 6 : 8);
         a.bufs = h->bufs.as<uint2>();
         a.buf_stride = stride;
         a.go = sch.go;
@@ -327,15 +358,11 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.scores = d_scores;
         a.rescue = h->list.as<uint32_t>();
         a.rescue_count = counts + 5;
-        a.strip_rows = h->strip_rows;
-        CU(h, cudaEventRecord(ev[1], s));
+        a.strip_rows = rows;
         CU(h, launch_band_fast(grid, s, a));
-        CU(h, cudaEventRecord(ev[2], s));
         local.kernel_launches++;
-    } else {
-        CU(h, cudaEventRecord(ev[1], s));
-        CU(h, cudaEventRecord(ev[2], s));
     }
+    CU(h, cudaEventRecord(ev[2], s));
     {
         // int32 kernel over narrow bands and rescued jobs (count read on the device)
         const unsigned T = 128;
