@@ -139,6 +139,85 @@ int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m,
                             const int32_t* matrix576, int32_t gap_open, int32_t gap_extend,
                             int32_t* scores);
 
+/* ---- banded traceback ---------------------------------------------------- */
+
+/* One banded alignment job: window of the loaded database, band relative to
+ * the window, and stop_at (rows after the first whose best cell reaches it
+ * are not computed; INT32_MAX = none).  The arguments of banded_align_until
+ * (src/algorithm/banded.rs:472-521) per job. */
+typedef struct {
+    uint32_t query;
+    uint32_t subject;   /* informational */
+    uint64_t win_begin;
+    uint32_t win_len;
+    int32_t band_lo, band_hi;
+    int32_t stop_at;
+} saber_align_job;
+
+/* Result of one alignment (LocalAlignment, banded.rs:101-113, plus status).
+ * Coordinates are 0-based half-open in window coordinates; the operations are
+ * n_ops run-length words at ops[ops_offset..]: (run length << 8) | op with op
+ * the ASCII 'M', 'I' (query residue vs gap) or 'D' (subject residue vs gap). */
+typedef struct {
+    int32_t status;  /* banded_align: 1 alignment, 0 none (best 0), SABER_ERR_CAP over
+                        the byte cap; traceback: 1 exact, 2 inexact (band capped), 0 none */
+    int32_t score;
+    uint32_t q_start, q_end, s_start, s_end;
+    uint32_t n_ops, ops_offset;
+    uint64_t cells;
+} saber_alignment;
+
+/* Banded SW with traceback for every job (banded_align_until,
+ * banded.rs:472-521, with walk banded.rs:336-403); a job whose direction
+ * matrix (m x band width bytes) exceeds max_dir_bytes gets status
+ * SABER_ERR_CAP, as the reference returns Err(bytes). */
+int saber_gpu_banded_align(saber_gpu* h, const saber_align_job* jobs, uint64_t njobs,
+                           uint64_t max_dir_bytes, saber_alignment* out, uint32_t* ops,
+                           uint64_t ops_cap);
+
+/* banded_align_until for one query / subject pair given as host arrays, with
+ * the handle's scheme (parity mirror of banded.rs:472). */
+int saber_gpu_banded_align_one(saber_gpu* h, const uint8_t* query, uint32_t m,
+                               const int8_t* bias, const uint8_t* subject, uint32_t n,
+                               int64_t band_lo, int64_t band_hi, uint64_t max_dir_bytes,
+                               int32_t stop_at, saber_alignment* out, uint32_t* ops,
+                               uint64_t ops_cap);
+
+/* One region to trace back (the arguments of Engine::traceback,
+ * src/search/engine.rs:1328-1337): its diagonals relative to the window
+ * start (region d_min - lo, d_max - lo), the exact score of the window
+ * (want) and the scoring band of its plan (limit, flags bit 1).  flags bit 0:
+ * full band (exhaustive search or a region with best == 0). */
+typedef struct {
+    uint32_t query;
+    uint32_t subject;   /* informational */
+    uint64_t win_begin;
+    uint32_t win_len;
+    int32_t d_min, d_max;
+    int32_t limit_lo, limit_hi;
+    int32_t want;
+    uint32_t flags;
+    uint32_t reserved;  /* 0; pads the struct to 48 bytes */
+} saber_traceback_job;
+
+typedef struct {
+    uint64_t tracebacks;      /* banded_align calls (Counters::tracebacks) */
+    uint64_t band_widenings;  /* Counters::band_widenings */
+    uint64_t end_anchored;    /* Counters::end_anchored_tracebacks */
+    uint64_t band_capped;     /* Counters::band_capped */
+    uint64_t banded_cells;    /* cells of all passes */
+    uint64_t launches;        /* widening rounds (one launch each) */
+} saber_traceback_stats;
+
+/* The widening band traceback that reproduces the window score
+ * (Engine::traceback + traceback_from_end, src/search/engine.rs:1328-1445),
+ * batched: band = region diagonals +- pad, pad = max(band_pad, 4) doubling,
+ * clipped to the limit, until the score reaches want or the band covers; a
+ * band over the byte cap falls back to the end-anchored search. */
+int saber_gpu_traceback(saber_gpu* h, const saber_traceback_job* jobs, uint64_t njobs,
+                        int32_t band_pad, uint64_t max_dir_bytes, saber_alignment* out,
+                        uint32_t* ops, uint64_t ops_cap, saber_traceback_stats* stats);
+
 /* Tuning: rows per strip of the packed int16 scoring kernel (8 or 16,
  * default 16).  Results do not depend on it.  No reference counterpart (the
  * reference's AVX2 kernels have fixed vector widths). */

@@ -55,6 +55,8 @@ struct DevBuf {
 struct QuerySet {
     uint32_t nq = 0;
     std::vector<uint64_t> offs;  // host copy
+    std::vector<uint64_t> poff;  // host copy of the profile offsets
+    std::vector<uint32_t> pmpad; // host copy of the profile row strides
     DevBuf codes, offsets, bias, prof, prof_off, prof_mpad;
     bool has = false;
     bool has_bias = false;
@@ -93,6 +95,8 @@ struct saber_gpu {
     // per-call scratch
     saber::DevBuf keys_in, keys_out, vals_in, vals_out, counts, stats, cub_tmp, bufs, slabs, list, jobs_dev,
         scores_dev;
+    // traceback scratch
+    saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
 };
 
 namespace saber {
@@ -424,6 +428,8 @@ static int load_queries(saber_gpu* h, const Scheme& sch, QuerySet& q, const uint
     q.has = false;
     q.nq = nq;
     q.offs.assign(offsets, offsets + nq + 1);
+    q.poff.clear();
+    q.pmpad.clear();
     std::vector<uint64_t> poff(nq ? nq : 1, 0);
     std::vector<uint32_t> pm(nq ? nq : 1, kStripRows);
     uint64_t acc = 0;
@@ -452,6 +458,8 @@ static int load_queries(saber_gpu* h, const Scheme& sch, QuerySet& q, const uint
         CU(h, cudaMemcpyAsync(q.bias.p, bias, total, cudaMemcpyHostToDevice, s));
     }
     CU(h, cudaStreamSynchronize(s));
+    q.poff.assign(poff.begin(), poff.begin() + nq);
+    q.pmpad.assign(pm.begin(), pm.begin() + nq);
     q.has = true;
     return build_profiles(h, sch, q);
 }
@@ -541,6 +549,381 @@ static int one_query_jobs(saber_gpu* h, const Scheme& sch, const uint8_t* query,
     if (rc != SABER_OK) return rc;
     CU(h, cudaMemcpyAsync(scores, h->scores_dev.p, njobs * 4, cudaMemcpyDeviceToHost, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
+    return SABER_OK;
+}
+
+// ---------------------------------------------------------------------------
+// banded traceback: batched banded_align_until and the widening driver
+// ---------------------------------------------------------------------------
+struct AlignReq {
+    const uint8_t* win;
+    const int16_t* prof;
+    uint64_t dir_off;
+    uint64_t ops_off;
+    int32_t m, n, lo, w;
+    int32_t mpad;
+    int32_t stop_at;
+    int32_t want_dir;
+    int32_t pad_;
+};
+struct AlignOut {
+    int32_t status;
+    int32_t score;
+    uint32_t q_start, q_end, s_start, s_end;
+    uint32_t n_ops;
+    uint32_t pad_;
+    uint64_t cells;
+};
+cudaError_t launch_band_align(unsigned grid, cudaStream_t s, const AlignReq* reqs, uint32_t nreq, uint8_t* dir_pool,
+                              uint8_t* opbytes, uint32_t* runs, int32_t* slabs, uint32_t slab_stride, int go, int ge,
+                              AlignOut* outs);
+
+__global__ void k_pack_runs(const uint32_t* __restrict__ runs, const uint64_t* __restrict__ src_off,
+                            const uint64_t* __restrict__ dst_off, const uint32_t* __restrict__ counts, uint32_t n,
+                            uint32_t* __restrict__ packed) {
+    for (uint32_t t = blockIdx.x; t < n; t += gridDim.x)
+        for (uint32_t k = threadIdx.x; k < counts[t]; k += blockDim.x) packed[dst_off[t] + k] = runs[src_off[t] + k];
+}
+
+struct AlignHostReq {
+    uint32_t query;
+    uint64_t win_begin;
+    uint32_t win_len;
+    int64_t lo, hi;  // band (unclipped)
+    int32_t stop_at;
+    bool want_dir;
+};
+struct AlignResult {
+    int status = 0;  // 1 alignment, 0 none, SABER_ERR_CAP over the direction-byte cap
+    int32_t score = 0;
+    uint32_t q_start = 0, q_end = 0, s_start = 0, s_end = 0;
+    uint64_t cells = 0;
+    std::vector<uint32_t> runs;  // (len << 8) | op
+};
+
+// Budget of the direction-byte pool per launch (larger batches are split).
+constexpr uint64_t kDirPoolBudget = 2ull << 30;
+constexpr uint64_t kAlignSlabBudget = 512ull << 20;
+
+static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const std::vector<AlignHostReq>& in,
+                       uint64_t max_dir_bytes, std::vector<AlignResult>& out) {
+    if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (!ds.has_db || !ds.qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
+    const QuerySet& qs = ds.qs;
+    out.assign(in.size(), AlignResult());
+    std::vector<size_t> todo;
+    todo.reserve(in.size());
+    for (size_t t = 0; t < in.size(); t++) {
+        const AlignHostReq& r = in[t];
+        if (r.query >= qs.nq || r.win_begin + r.win_len > ds.n_res)
+            return fail(h, SABER_ERR_ARG, "traceback job %zu references data outside the loaded set", t);
+        int64_t m = (int64_t)(qs.offs[r.query + 1] - qs.offs[r.query]);
+        int64_t lo = r.lo, hi = r.hi;
+        int64_t w = clip_band(m, r.win_len, lo, hi);
+        if (w == 0) continue;  // Ok(None)
+        if (r.want_dir && (uint64_t)m * (uint64_t)w > max_dir_bytes) {
+            out[t].status = SABER_ERR_CAP;
+            continue;
+        }
+        todo.push_back(t);
+    }
+    cudaStream_t s = h->stream;
+    size_t pos = 0;
+    while (pos < todo.size()) {
+        // one launch: as many jobs as fit the pool budget
+        std::vector<AlignReq> reqs;
+        std::vector<size_t> idx;
+        uint64_t dir_tot = 0, ops_tot = 0;
+        int64_t wmax = 1;
+        while (pos < todo.size()) {
+            const AlignHostReq& r = in[todo[pos]];
+            int64_t m = (int64_t)(qs.offs[r.query + 1] - qs.offs[r.query]);
+            int64_t lo = r.lo, hi = r.hi;
+            int64_t w = clip_band(m, r.win_len, lo, hi);
+            uint64_t dbytes = r.want_dir ? (uint64_t)m * (uint64_t)w : 0;
+            if (!reqs.empty() && dir_tot + dbytes > kDirPoolBudget) break;
+            AlignReq q;
+            q.win = ds.res.as<uint8_t>() + r.win_begin;
+            q.prof = qs.prof.as<int16_t>() + qs.poff[r.query];
+            q.dir_off = dir_tot;
+            q.ops_off = ops_tot;
+            q.m = (int32_t)m;
+            q.n = (int32_t)r.win_len;
+            q.lo = (int32_t)lo;
+            q.w = (int32_t)w;
+            q.mpad = (int32_t)qs.pmpad[r.query];
+            q.stop_at = r.stop_at;
+            q.want_dir = r.want_dir ? 1 : 0;
+            q.pad_ = 0;
+            dir_tot += (dbytes + 15) / 16 * 16;
+            if (r.want_dir) ops_tot += (uint64_t)m + r.win_len + 2;
+            wmax = std::max(wmax, w);
+            reqs.push_back(q);
+            idx.push_back(todo[pos]);
+            pos++;
+        }
+        const uint32_t nreq = (uint32_t)reqs.size();
+        const uint32_t stride = (uint32_t)(wmax + 1);
+        uint64_t thr = kAlignSlabBudget / ((uint64_t)stride * 16);
+        if (thr < 128) thr = 128;
+        uint64_t want_thr = ((uint64_t)nreq + 127) / 128 * 128;
+        thr = std::min<uint64_t>(std::min<uint64_t>(thr, want_thr), (uint64_t)h->sm_count * 8 * 128);
+        thr = thr / 128 * 128;
+        const unsigned grid = (unsigned)(thr / 128);
+        CUALLOC(h, h->al_reqs, nreq * sizeof(AlignReq));
+        CUALLOC(h, h->al_outs, nreq * sizeof(AlignOut));
+        CUALLOC(h, h->al_dir, dir_tot + 16);
+        CUALLOC(h, h->al_opbytes, ops_tot + 16);
+        CUALLOC(h, h->al_runs, (ops_tot + 16) * 4);
+        CUALLOC(h, h->al_slabs, thr * stride * 16);
+        CU(h, cudaMemcpyAsync(h->al_reqs.p, reqs.data(), nreq * sizeof(AlignReq), cudaMemcpyHostToDevice, s));
+        CU(h, launch_band_align(grid, s, h->al_reqs.as<AlignReq>(), nreq, h->al_dir.as<uint8_t>(),
+                                h->al_opbytes.as<uint8_t>(), h->al_runs.as<uint32_t>(), h->al_slabs.as<int32_t>(),
+                                stride, sch.go, sch.ge, h->al_outs.as<AlignOut>()));
+        std::vector<AlignOut> outs(nreq);
+        CU(h, cudaMemcpyAsync(outs.data(), h->al_outs.p, nreq * sizeof(AlignOut), cudaMemcpyDeviceToHost, s));
+        CU(h, cudaStreamSynchronize(s));
+        // gather the op runs of the alignments into one packed copy
+        std::vector<uint64_t> src(nreq), dst(nreq);
+        std::vector<uint32_t> cnt(nreq);
+        uint64_t packed = 0;
+        for (uint32_t t = 0; t < nreq; t++) {
+            src[t] = reqs[t].ops_off;
+            dst[t] = packed;
+            cnt[t] = outs[t].n_ops;
+            packed += outs[t].n_ops;
+        }
+        std::vector<uint32_t> hostruns(packed);
+        if (packed) {
+            CUALLOC(h, h->al_pack_off, (uint64_t)nreq * 20 + 64);
+            uint64_t* d_src = h->al_pack_off.as<uint64_t>();
+            uint64_t* d_dst = d_src + nreq;
+            uint32_t* d_cnt = reinterpret_cast<uint32_t*>(d_dst + nreq);
+            CUALLOC(h, h->al_packed, packed * 4);
+            CU(h, cudaMemcpyAsync(d_src, src.data(), nreq * 8, cudaMemcpyHostToDevice, s));
+            CU(h, cudaMemcpyAsync(d_dst, dst.data(), nreq * 8, cudaMemcpyHostToDevice, s));
+            CU(h, cudaMemcpyAsync(d_cnt, cnt.data(), nreq * 4, cudaMemcpyHostToDevice, s));
+            k_pack_runs<<<std::min<uint32_t>(nreq, 4096), 32, 0, s>>>(h->al_runs.as<uint32_t>(), d_src, d_dst, d_cnt,
+                                                                      nreq, h->al_packed.as<uint32_t>());
+            CU(h, cudaGetLastError());
+            CU(h, cudaMemcpyAsync(hostruns.data(), h->al_packed.p, packed * 4, cudaMemcpyDeviceToHost, s));
+            CU(h, cudaStreamSynchronize(s));
+        }
+        for (uint32_t t = 0; t < nreq; t++) {
+            AlignResult& r = out[idx[t]];
+            const AlignOut& o = outs[t];
+            r.status = o.status;
+            r.score = o.score;
+            r.q_start = o.q_start;
+            r.q_end = o.q_end;
+            r.s_start = o.s_start;
+            r.s_end = o.s_end;
+            r.cells = o.cells;
+            r.runs.assign(hostruns.begin() + dst[t], hostruns.begin() + dst[t] + cnt[t]);
+        }
+    }
+    return SABER_OK;
+}
+
+static void put_alignment(const AlignResult& r, int status, saber_alignment* o, uint32_t* ops, uint64_t ops_cap,
+                          uint64_t& ops_used, bool& overflow) {
+    o->status = status;
+    o->score = r.score;
+    o->q_start = r.q_start;
+    o->q_end = r.q_end;
+    o->s_start = r.s_start;
+    o->s_end = r.s_end;
+    o->cells = r.cells;
+    o->n_ops = (uint32_t)r.runs.size();
+    o->ops_offset = (uint32_t)ops_used;
+    if (ops_used + r.runs.size() > ops_cap) {
+        overflow = true;
+    } else if (!r.runs.empty()) {
+        memcpy(ops + ops_used, r.runs.data(), r.runs.size() * 4);
+    }
+    ops_used += r.runs.size();
+}
+
+// Engine::traceback (src/search/engine.rs:1328-1393) and traceback_from_end
+// (engine.rs:1403-1445) for a batch of regions: each widening round of every
+// unresolved region is one align_batch launch.
+struct TbState {
+    int phase = 0;        // 0 region band, 1 end-anchored, 2 done
+    int64_t pad = 16;
+    bool has_best = false;
+    AlignResult best;
+    int64_t d_end = 0, target = 0;
+    int64_t slo = 0, shi = 0;  // scope of the end-anchored search
+    int status = 0;       // final: 1 exact, 2 inexact, 0 none
+};
+
+static int traceback_driver(saber_gpu* h, const saber_traceback_job* jobs, uint64_t n, int32_t band_pad,
+                            uint64_t max_dir_bytes, saber_alignment* out, uint32_t* ops, uint64_t ops_cap,
+                            saber_traceback_stats* st) {
+    const Dataset& ds = h->main;
+    const QuerySet& qs = ds.qs;
+    if (!ds.qs.has || !ds.has_db) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
+    saber_traceback_stats local{};
+    std::vector<TbState> S(n);
+    const int64_t pad0 = band_pad > 4 ? band_pad : 4;
+    for (uint64_t t = 0; t < n; t++) {
+        if (jobs[t].query >= qs.nq) return fail(h, SABER_ERR_ARG, "traceback job %llu: bad query", (unsigned long long)t);
+        S[t].pad = pad0;
+    }
+    auto mlen = [&](uint64_t t) { return (int64_t)(qs.offs[jobs[t].query + 1] - qs.offs[jobs[t].query]); };
+    std::vector<AlignResult> res;
+    for (int round = 0; round < 64; round++) {
+        std::vector<AlignHostReq> reqs;
+        std::vector<uint64_t> who;
+        std::vector<int> kind;  // 0 region band, 1 end-anchored band, 2 end-finding score pass
+        std::vector<char> covers;
+        for (uint64_t t = 0; t < n; t++) {
+            TbState& x = S[t];
+            if (x.phase == 2) continue;
+            const saber_traceback_job& j = jobs[t];
+            const int64_t m = mlen(t), nn = j.win_len;
+            AlignHostReq r;
+            r.query = j.query;
+            r.win_begin = j.win_begin;
+            r.win_len = j.win_len;
+            r.want_dir = true;
+            if (x.phase == 0) {
+                // engine.rs:1342-1356
+                const bool full = (j.flags & 1u) != 0;
+                int64_t lo = full ? -m : (int64_t)j.d_min - x.pad;
+                int64_t hi = full ? nn : (int64_t)j.d_max + x.pad;
+                bool cov = lo <= -(m - 1) && hi >= nn - 1;
+                if (j.flags & 2u) {
+                    lo = std::max<int64_t>(lo, j.limit_lo);
+                    hi = std::min<int64_t>(hi, j.limit_hi);
+                    cov = cov || (lo <= j.limit_lo && hi >= j.limit_hi);
+                }
+                r.lo = lo;
+                r.hi = hi;
+                r.stop_at = j.want;
+                reqs.push_back(r);
+                who.push_back(t);
+                kind.push_back(0);
+                covers.push_back(cov);
+            } else if (x.phase == 3) {
+                // engine.rs:1412-1414: score pass over the scope for the end cell
+                r.lo = x.slo;
+                r.hi = x.shi;
+                r.stop_at = INT32_MAX;
+                r.want_dir = false;
+                reqs.push_back(r);
+                who.push_back(t);
+                kind.push_back(2);
+                covers.push_back(1);
+            } else {
+                // engine.rs:1422-1427
+                int64_t lo = std::max<int64_t>(x.d_end - x.pad, x.slo);
+                int64_t hi = std::min<int64_t>(x.d_end + x.pad, x.shi);
+                reqs.push_back(AlignHostReq{j.query, j.win_begin, j.win_len, lo, hi, (int32_t)x.target, true});
+                who.push_back(t);
+                kind.push_back(1);
+                covers.push_back(lo <= x.slo && hi >= x.shi);
+            }
+        }
+        if (reqs.empty()) break;
+        int rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res);
+        if (rc != SABER_OK) return rc;
+        local.launches++;
+        for (size_t k = 0; k < reqs.size(); k++) {
+            const uint64_t t = who[k];
+            TbState& x = S[t];
+            const saber_traceback_job& j = jobs[t];
+            AlignResult& r = res[k];
+            const bool cov = covers[k] != 0;
+            if (kind[k] != 2) local.tracebacks++;
+            // the reference adds the cells of an alignment pass only when it
+            // returns an alignment, and those of the score pass always
+            if (kind[k] == 2 || r.status == 1) local.banded_cells += r.cells;
+            if (kind[k] == 0) {
+                if (r.status == 1) {
+                    bool done = r.score >= j.want || cov;
+                    x.best = r;
+                    x.has_best = true;
+                    if (done) {
+                        x.status = r.score >= j.want ? 1 : 2;
+                        x.phase = 2;
+                        continue;
+                    }
+                } else if (r.status == 0) {
+                    if (cov) {
+                        x.status = 0;
+                        x.phase = 2;
+                        continue;
+                    }
+                } else {  // over the cap: traceback_from_end
+                    const int64_t m = mlen(t);
+                    if (j.flags & 2u) {
+                        x.slo = j.limit_lo;
+                        x.shi = j.limit_hi;
+                    } else {
+                        x.slo = -m;
+                        x.shi = j.win_len;
+                    }
+                    x.phase = 3;
+                    continue;
+                }
+                local.band_widenings++;
+                x.pad *= 2;
+            } else if (kind[k] == 2) {
+                if (r.status != 1 || r.score <= 0) {
+                    // no end cell: report the best so far, flagged (engine.rs:1384-1387)
+                    local.band_capped++;
+                    x.status = x.has_best ? 2 : 0;
+                    x.phase = 2;
+                    continue;
+                }
+                local.end_anchored++;
+                x.target = std::max<int64_t>(r.score, j.want);
+                x.d_end = (int64_t)r.s_end - (int64_t)r.q_end;
+                x.pad = pad0;
+                x.phase = 1;
+            } else {
+                if (r.status == 1) {
+                    if (r.score >= x.target || cov) {
+                        x.best = r;
+                        x.has_best = true;
+                        x.status = r.score >= j.want ? 1 : 2;
+                        x.phase = 2;
+                        continue;
+                    }
+                } else if (r.status == 0) {
+                    if (cov) {
+                        local.band_capped++;
+                        x.status = x.has_best ? 2 : 0;
+                        x.phase = 2;
+                        continue;
+                    }
+                } else {
+                    local.band_capped++;
+                    x.status = x.has_best ? 2 : 0;
+                    x.phase = 2;
+                    continue;
+                }
+                local.band_widenings++;
+                x.pad *= 2;
+            }
+        }
+    }
+    uint64_t used = 0;
+    bool overflow = false;
+    for (uint64_t t = 0; t < n; t++) {
+        const TbState& x = S[t];
+        if (x.phase != 2) return fail(h, SABER_ERR_DEVICE, "traceback of job %llu did not converge",
+                                      (unsigned long long)t);
+        if (x.status == 0 || !x.has_best) {
+            memset(&out[t], 0, sizeof(out[t]));
+            out[t].ops_offset = (uint32_t)used;
+            continue;
+        }
+        put_alignment(x.best, x.status, &out[t], ops, ops_cap, used, overflow);
+    }
+    if (st) *st = local;
+    if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
     return SABER_OK;
 }
 
@@ -703,6 +1086,62 @@ int saber_gpu_set_strip_rows(saber_gpu* h, int32_t strip_rows) {
 }
 
 int32_t saber_gpu_get_strip_rows(saber_gpu* h) { return h ? h->strip_rows : 0; }
+
+int saber_gpu_banded_align(saber_gpu* h, const saber_align_job* jobs, uint64_t njobs, uint64_t max_dir_bytes,
+                           saber_alignment* out, uint32_t* ops, uint64_t ops_cap) {
+    ENTER(h);
+    if (njobs && (!jobs || !out)) return fail(h, SABER_ERR_ARG, "null argument");
+    std::vector<AlignHostReq> reqs(njobs);
+    for (uint64_t t = 0; t < njobs; t++)
+        reqs[t] = AlignHostReq{jobs[t].query, jobs[t].win_begin, jobs[t].win_len, jobs[t].band_lo, jobs[t].band_hi,
+                               jobs[t].stop_at, true};
+    std::vector<AlignResult> res;
+    int rc = align_batch(h, h->scheme, h->main, reqs, max_dir_bytes, res);
+    if (rc != SABER_OK) return rc;
+    uint64_t used = 0;
+    bool overflow = false;
+    for (uint64_t t = 0; t < njobs; t++) put_alignment(res[t], res[t].status, &out[t], ops, ops_cap, used, overflow);
+    if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
+    return SABER_OK;
+}
+
+int saber_gpu_banded_align_one(saber_gpu* h, const uint8_t* query, uint32_t m, const int8_t* bias,
+                               const uint8_t* subject, uint32_t n, int64_t band_lo, int64_t band_hi,
+                               uint64_t max_dir_bytes, int32_t stop_at, saber_alignment* out, uint32_t* ops,
+                               uint64_t ops_cap) {
+    ENTER(h);
+    if (!out) return fail(h, SABER_ERR_ARG, "null argument");
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    memset(out, 0, sizeof(*out));
+    if (m == 0 || n == 0 || band_hi < band_lo) return SABER_OK;
+    Dataset& ds = h->eph;
+    uint64_t offs[2] = {0, n};
+    int rc = load_db(h, ds, subject, n, offs, 1);
+    if (rc != SABER_OK) return rc;
+    uint64_t qoff[2] = {0, m};
+    rc = load_queries(h, h->scheme, ds.qs, query, qoff, bias, 1);
+    if (rc != SABER_OK) return rc;
+    int64_t lo = std::max<int64_t>(band_lo, -(int64_t)m - 1), hi = std::min<int64_t>(band_hi, (int64_t)n + 1);
+    if (hi < lo) return SABER_OK;
+    std::vector<AlignHostReq> reqs(1, AlignHostReq{0, 0, n, lo, hi, stop_at, true});
+    std::vector<AlignResult> res;
+    rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res);
+    if (rc != SABER_OK) return rc;
+    uint64_t used = 0;
+    bool overflow = false;
+    put_alignment(res[0], res[0].status, out, ops, ops_cap, used, overflow);
+    if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
+    return SABER_OK;
+}
+
+int saber_gpu_traceback(saber_gpu* h, const saber_traceback_job* jobs, uint64_t njobs, int32_t band_pad,
+                        uint64_t max_dir_bytes, saber_alignment* out, uint32_t* ops, uint64_t ops_cap,
+                        saber_traceback_stats* stats) {
+    ENTER(h);
+    if (njobs && (!jobs || !out)) return fail(h, SABER_ERR_ARG, "null argument");
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    return traceback_driver(h, jobs, njobs, band_pad, max_dir_bytes, out, ops, ops_cap, stats);
+}
 
 uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi) {
     int64_t lo = band_lo, hi = band_hi;

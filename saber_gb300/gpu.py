@@ -31,6 +31,36 @@ class SaberGpuError(RuntimeError):
     """A call of the C ABI returned an error status."""
 
 
+ALIGN_JOB_DTYPE = np.dtype([
+    ("query", "<u4"), ("subject", "<u4"), ("win_begin", "<u8"), ("win_len", "<u4"),
+    ("band_lo", "<i4"), ("band_hi", "<i4"), ("stop_at", "<i4")])
+TB_JOB_DTYPE = np.dtype([
+    ("query", "<u4"), ("subject", "<u4"), ("win_begin", "<u8"), ("win_len", "<u4"),
+    ("d_min", "<i4"), ("d_max", "<i4"), ("limit_lo", "<i4"), ("limit_hi", "<i4"), ("want", "<i4"),
+    ("flags", "<u4"), ("reserved", "<u4")])
+assert ALIGN_JOB_DTYPE.itemsize == 32 and TB_JOB_DTYPE.itemsize == 48
+
+
+class Alignment(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("score", ctypes.c_int32), ("q_start", ctypes.c_uint32),
+                ("q_end", ctypes.c_uint32), ("s_start", ctypes.c_uint32), ("s_end", ctypes.c_uint32),
+                ("n_ops", ctypes.c_uint32), ("ops_offset", ctypes.c_uint32), ("cells", ctypes.c_uint64)]
+
+
+class TracebackStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("tracebacks", "band_widenings", "end_anchored", "band_capped",
+                                                 "banded_cells", "launches")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+def _alignment_dict(a, ops):
+    runs = [(chr(ops[a.ops_offset + k] & 0xFF), int(ops[a.ops_offset + k] >> 8)) for k in range(a.n_ops)]
+    return dict(status=int(a.status), score=int(a.score), q_start=int(a.q_start), q_end=int(a.q_end),
+                s_start=int(a.s_start), s_end=int(a.s_end), cells=int(a.cells), ops=runs)
+
+
 class ScoreStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "jobs", "banded_cells", "fast_cells", "fast_jobs", "generic_jobs", "i16_rescored", "empty_jobs",
@@ -72,6 +102,9 @@ def load_library():
         "saber_band_cells": (U64, [U64, U64, I64, I64]),
         "saber_gpu_probe_int_peak": (ctypes.c_int, [P, P, P]),
         "saber_gpu_set_strip_rows": (ctypes.c_int, [P, I32]),
+        "saber_gpu_banded_align": (ctypes.c_int, [P, P, U64, U64, P, P, U64]),
+        "saber_gpu_banded_align_one": (ctypes.c_int, [P, P, U32, P, P, U32, I64, I64, U64, I32, P, P, U64]),
+        "saber_gpu_traceback": (ctypes.c_int, [P, P, U64, I32, U64, P, P, U64, P]),
         "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
@@ -184,6 +217,49 @@ class Device:
         self._check(self.lib.saber_gpu_score_band_jobs_noalloc(self.h, ctypes.c_void_p(d_jobs_ptr), int(njobs),
                                                                int(max_band_width), ctypes.c_void_p(d_scores_ptr)),
                     "score_band_jobs_noalloc")
+
+    def banded_align_one(self, query, bias, subject, lo, hi, max_dir_bytes=1 << 62, stop_at=2 ** 31 - 1):
+        """banded_align_until for one pair -> dict (status 1), None (status 0) or MemoryError (cap)."""
+        q = np.ascontiguousarray(query, dtype=np.uint8)
+        sj = np.ascontiguousarray(subject, dtype=np.uint8)
+        b = None if bias is None else np.ascontiguousarray(bias, dtype=np.int8)
+        cap = q.size + sj.size + 2
+        ops = np.zeros(cap, np.uint32)
+        out = Alignment()
+        self._check(self.lib.saber_gpu_banded_align_one(
+            self.h, _ptr(q) if q.size else None, q.size, _ptr(b), _ptr(sj) if sj.size else None, sj.size, int(lo),
+            int(hi), int(max_dir_bytes), int(stop_at), ctypes.byref(out), _ptr(ops), cap), "banded_align_one")
+        if out.status == -5:
+            raise MemoryError("direction matrix over the cap")
+        if out.status == 0:
+            return None
+        return _alignment_dict(out, ops)
+
+    def banded_align(self, jobs, max_dir_bytes=1 << 62):
+        """Batched banded_align_until over ALIGN_JOB_DTYPE jobs -> list of dicts / None / 'cap'."""
+        jobs = np.ascontiguousarray(jobs, dtype=ALIGN_JOB_DTYPE)
+        out = (Alignment * max(1, jobs.size))()
+        cap = int(np.sum(jobs["win_len"].astype(np.int64))) + 64 * jobs.size + 64
+        ops = np.zeros(cap, np.uint32)
+        self._check(self.lib.saber_gpu_banded_align(self.h, _ptr(jobs), jobs.size, int(max_dir_bytes), out,
+                                                    _ptr(ops), cap), "banded_align")
+        res = []
+        for t in range(jobs.size):
+            a = out[t]
+            res.append("cap" if a.status == -5 else None if a.status == 0 else _alignment_dict(a, ops))
+        return res
+
+    def traceback(self, jobs, band_pad=16, max_dir_bytes=32 << 20):
+        """Widening band traceback of TB_JOB_DTYPE regions -> (list of dicts or None, stats)."""
+        jobs = np.ascontiguousarray(jobs, dtype=TB_JOB_DTYPE)
+        out = (Alignment * max(1, jobs.size))()
+        cap = int(np.sum(jobs["win_len"].astype(np.int64))) + 4096 * jobs.size + 64
+        ops = np.zeros(cap, np.uint32)
+        st = TracebackStats()
+        self._check(self.lib.saber_gpu_traceback(self.h, _ptr(jobs), jobs.size, int(band_pad), int(max_dir_bytes),
+                                                 out, _ptr(ops), cap, ctypes.byref(st)), "traceback")
+        res = [None if out[t].status == 0 else _alignment_dict(out[t], ops) for t in range(jobs.size)]
+        return res, st.as_dict()
 
     @property
     def strip_rows(self):
