@@ -139,6 +139,63 @@ int saber_gpu_score_windows(saber_gpu* h, const uint8_t* query, uint32_t m,
                             const int32_t* matrix576, int32_t gap_open, int32_t gap_extend,
                             int32_t* scores);
 
+/* ---- scan schedule: seeds, hits, window filter, X-drop, regions ------------ */
+
+/* Seeding scheme and heuristics of the scan schedule (ScanSeeds,
+ * src/search/engine/scan.rs:28-33, and the SearchParams fields it reads,
+ * src/search/engine.rs:60-159).  Shapes are given by their care offsets. */
+typedef struct {
+    uint8_t alpha_map[24];         /* reduced letter per residue code, 255 = not seedable */
+    uint32_t alpha_size;           /* letters of the seed alphabet */
+    uint32_t nshapes;              /* <= 32 */
+    uint32_t shape_span[32];
+    uint32_t shape_weight[32];     /* <= 16 */
+    uint16_t shape_off[32][16];    /* care offsets of every shape */
+    uint32_t hit_filter_min_ids;   /* window filter threshold, 0 = off */
+    uint32_t hit_filter_exact_weight;
+    int32_t hsp_threshold;         /* minimum ungapped HSP score */
+    int32_t x_drop;                /* ungapped X-drop */
+    int32_t window_slack;          /* HSPs within 2 x slack diagonals form one region */
+    uint32_t max_regions_per_subject;
+    uint32_t max_candidates;       /* regions kept per query */
+    uint64_t seed_max_occ;         /* 0 = automatic frequent-seed cap */
+    uint64_t ref_db_residues;      /* reference database size of the automatic cap */
+    uint64_t db_length;            /* database residues of the statistics */
+} saber_scan_params;
+
+/* A candidate region: subject, diagonal range d = j - i, best HSP score
+ * (Region, src/search/engine.rs:467-473). */
+typedef struct {
+    uint32_t query;
+    uint32_t subject;
+    int32_t d_min, d_max;
+    int32_t best;
+} saber_region;
+
+/* Work counters of one scan (names of Counters, src/search/engine.rs:205-282). */
+typedef struct {
+    uint64_t seed_positions, seeds_frequent_skipped, hits, hits_filtered, ungapped_extensions,
+        extensions_avoided, xdrop_steps, hsps, regions, regions_weak_dropped, regions_dropped_by_cap;
+    double t_tables_ms, t_scan_ms, t_visit_ms, t_regions_ms;
+} saber_scan_stats;
+
+/* Database seed mask: one byte per residue of the loaded database, nonzero =
+ * masked from seeding (the tantan runs of the index, index.rs mask_runs;
+ * scan.rs:123-141 applies them).  NULL clears the mask. */
+int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residues);
+
+/* Engine::search_scan's candidate regions for the loaded query set against
+ * the loaded database (scan.rs:1261-1497 up to the per-query candidate cap):
+ * seed tables of the batch, database scan with the window filter,
+ * per-diagonal coverage and ungapped X-drop, region clustering, per-subject
+ * and per-query caps.  q_mask: one byte per query residue, nonzero = masked
+ * from seeding (NULL = none); region_thr: the per-query region threshold
+ * (Engine::hsp_threshold_for, engine.rs:729-736; NULL = hsp_threshold).
+ * Regions are written ordered by query, then region_order (engine.rs:493). */
+int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask,
+                   const int32_t* region_thr, saber_region* out, uint64_t out_cap,
+                   uint64_t* n_out, saber_scan_stats* stats);
+
 /* ---- banded traceback ---------------------------------------------------- */
 
 /* One banded alignment job: window of the loaded database, band relative to

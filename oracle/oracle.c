@@ -431,3 +431,314 @@ int orc_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
     if (cells_out) *cells_out = c.cells;
     return 0;
 }
+
+/* ======================================================================== */
+/* scan schedule                                                             */
+/* ======================================================================== */
+#include <math.h>
+
+#define NONSEED 0x7F
+#define MASKED 0x80
+
+uint64_t orc_auto_occ_cap(uint64_t total, uint64_t ncodes, uint64_t db_residues, uint64_t ref_residues) {
+    /* index.rs:329-336 */
+    uint64_t floor_ = 256;
+    if (ref_residues > 0 && db_residues > ref_residues)
+        floor_ = (uint64_t)ceil(256.0 * (double)db_residues / (double)ref_residues);
+    uint64_t c = (uint64_t)ceil((double)total / (double)(ncodes > 0 ? ncodes : 1) * 64.0);
+    return c > floor_ ? c : floor_;
+}
+
+typedef struct { uint32_t code; uint32_t q; uint32_t p; } seed_t;
+typedef struct { uint32_t subject, query, qp, sp, shape; } surv_t;
+typedef struct { int64_t diag; uint32_t q_lo, q_hi; int32_t score; } hsp_t;
+
+static int cmp_seed(const void* a, const void* b) {
+    const seed_t* x = (const seed_t*)a; const seed_t* y = (const seed_t*)b;
+    if (x->code != y->code) return x->code < y->code ? -1 : 1;
+    if (x->q != y->q) return x->q < y->q ? -1 : 1;
+    return x->p < y->p ? -1 : (x->p > y->p);
+}
+/* (subject, query) groups in order; within a pair (qp, shape, sp):
+ * scan.rs:2158-2170 (survivors in (shape, position) order, stable by position) */
+static int cmp_surv(const void* a, const void* b) {
+    const surv_t* x = (const surv_t*)a; const surv_t* y = (const surv_t*)b;
+    if (x->subject != y->subject) return x->subject < y->subject ? -1 : 1;
+    if (x->query != y->query) return x->query < y->query ? -1 : 1;
+    if (x->qp != y->qp) return x->qp < y->qp ? -1 : 1;
+    if (x->shape != y->shape) return x->shape < y->shape ? -1 : 1;
+    return x->sp < y->sp ? -1 : (x->sp > y->sp);
+}
+static int cmp_hsp(const void* a, const void* b) {
+    const hsp_t* x = (const hsp_t*)a; const hsp_t* y = (const hsp_t*)b;
+    return x->diag < y->diag ? -1 : (x->diag > y->diag);
+}
+/* region_order, engine.rs:493-495 (within one query) */
+static int cmp_region(const void* a, const void* b) {
+    const orc_region* x = (const orc_region*)a; const orc_region* y = (const orc_region*)b;
+    if (x->query != y->query) return x->query < y->query ? -1 : 1;
+    if (x->best != y->best) return x->best > y->best ? -1 : 1;
+    if (x->subject != y->subject) return x->subject < y->subject ? -1 : 1;
+    if (x->d_min != y->d_min) return x->d_min < y->d_min ? -1 : 1;
+    return x->d_max < y->d_max ? -1 : (x->d_max > y->d_max);
+}
+
+/* seed code of the care positions (scan.rs:841-856): -1 when invalid */
+static int64_t code_at(const uint8_t* sr, const uint16_t* offs, uint32_t w, uint32_t asize) {
+    uint32_t c = 0;
+    for (uint32_t i = 0; i < w; i++) {
+        uint8_t r = sr[offs[i]];
+        if (r >= asize) return -1;
+        c = c * asize + r;
+    }
+    return c;
+}
+
+int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsub, const uint8_t* db_mask,
+                         const uint8_t* qcodes, const uint64_t* qoffs, uint32_t nq, const int8_t* qbias,
+                         const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
+                         const orc_scan_params* P, orc_region* out, uint64_t out_cap,
+                         orc_scan_counters* ctr) {
+    memset(ctr, 0, sizeof(*ctr));
+    const uint64_t N = soffs[nsub];
+    const uint32_t asize = P->alpha_size;
+    /* database seed bytes (scan.rs:123-141, seed_map at 1072-1077) */
+    uint8_t* sb = (uint8_t*)malloc(N + 1);
+    for (uint64_t r = 0; r < N; r++) {
+        uint8_t c = res[r];
+        uint8_t v = (c < 24 && P->alpha_map[c] != 255) ? P->alpha_map[c] : NONSEED;
+        if (v != NONSEED && db_mask && db_mask[r]) v |= MASKED;
+        sb[r] = v;
+    }
+    /* query reduced bytes and window bytes (build_batch, scan.rs:1514-1530) */
+    const uint64_t QN = qoffs[nq];
+    uint8_t* qred = (uint8_t*)malloc(QN + 1); /* reduced letter or 0xFE */
+    uint8_t* qfull = (uint8_t*)malloc(QN + 1); /* alignment code or 0xFE */
+    for (uint64_t i = 0; i < QN; i++) {
+        uint8_t c = qcodes[i];
+        uint8_t r = P->alpha_map[c < 24 ? c : 23];
+        int ok = !(q_mask && q_mask[i]) && r != 255;
+        qred[i] = ok ? r : 0xFE;
+        qfull[i] = ok ? c : 0xFE;
+    }
+    uint32_t cmin = 1u << 30;
+    for (uint32_t s = 0; s < P->nshapes; s++) if (P->shape_span[s] < cmin) cmin = P->shape_span[s];
+    const int64_t cfil = cmin / 2;
+
+    size_t ns_cap = 1024, ns = 0;
+    surv_t* sv = (surv_t*)malloc(ns_cap * sizeof(surv_t));
+    for (uint32_t si = 0; si < P->nshapes; si++) {
+        const uint32_t span = P->shape_span[si], w = P->shape_weight[si];
+        const uint16_t* offs = P->shape_off[si];
+        uint64_t ncodes = 1;
+        for (uint32_t k = 0; k < w; k++) ncodes *= asize;
+        /* frequent codes (scan.rs:1184-1238) */
+        uint32_t* cnt = (uint32_t*)calloc(ncodes, sizeof(uint32_t));
+        uint64_t total = 0;
+        for (uint64_t s = 0; s < nsub; s++) {
+            uint64_t b = soffs[s], e = soffs[s + 1];
+            if (e - b < span) continue;
+            for (uint64_t p = b; p + span <= e; p++) {
+                int64_t c = code_at(sb + p, offs, w, asize);
+                if (c >= 0) { cnt[c]++; total++; }
+            }
+        }
+        uint64_t cap = P->seed_max_occ > 0 ? P->seed_max_occ
+                                           : orc_auto_occ_cap(total, ncodes, P->db_length, P->ref_db_residues);
+        uint8_t* freq = (uint8_t*)calloc(ncodes, 1);
+        if (total > cap)
+            for (uint64_t c = 0; c < ncodes; c++) freq[c] = cnt[c] > cap;
+        free(cnt);
+        /* query seeds (scan.rs:1541-1562) */
+        size_t nseed = 0, seed_cap = 1024;
+        seed_t* seeds = (seed_t*)malloc(seed_cap * sizeof(seed_t));
+        for (uint32_t q = 0; q < nq; q++) {
+            uint64_t b = qoffs[q], e = qoffs[q + 1];
+            if (e - b < span) continue;
+            for (uint64_t p = b; p + span <= e; p++) {
+                int64_t c = code_at(qred + p, offs, w, asize);
+                if (c < 0) continue;
+                if (freq[c]) { ctr->seeds_frequent_skipped++; continue; }
+                if (nseed == seed_cap) { seed_cap *= 2; seeds = (seed_t*)realloc(seeds, seed_cap * sizeof(seed_t)); }
+                seeds[nseed].code = (uint32_t)c; seeds[nseed].q = q; seeds[nseed].p = (uint32_t)(p - b);
+                nseed++;
+            }
+        }
+        free(freq);
+        ctr->seed_positions += nseed;
+        qsort(seeds, nseed, sizeof(seed_t), cmp_seed);
+        /* database positions: hits and window filter (scan.rs:1603-1856) */
+        for (uint64_t s = 0; s < nsub && nseed; s++) {
+            uint64_t b = soffs[s], e = soffs[s + 1];
+            const int64_t sl = (int64_t)(e - b);
+            if ((uint64_t)sl < span) continue;
+            for (int64_t p = 0; p + span <= (uint64_t)sl; p++) {
+                int64_t c = code_at(sb + b + p, offs, w, asize);
+                if (c < 0) continue;
+                /* entries of code c */
+                size_t lo = 0, hi = nseed;
+                while (lo < hi) { size_t mid = (lo + hi) / 2; if (seeds[mid].code < (uint32_t)c) lo = mid + 1; else hi = mid; }
+                for (size_t k = lo; k < nseed && seeds[k].code == (uint32_t)c; k++) {
+                    const uint32_t q = seeds[k].q, qp = seeds[k].p;
+                    ctr->hits++;
+                    if (P->hit_filter_min_ids > 0) {
+                        const int64_t ss = p + cfil - 16;
+                        const int64_t qs = (int64_t)qp + cfil - 16;
+                        const int64_t qlen = (int64_t)(qoffs[q + 1] - qoffs[q]);
+                        uint32_t r = 0, ex = 0;
+                        for (int t = 0; t < 32; t++) {
+                            int64_t j = ss + t, i = qs + t;
+                            if (j < 0 || j >= sl) continue;
+                            if (i < 0 || i >= qlen) continue;
+                            uint8_t qr = qred[qoffs[q] + i];
+                            if (qr != 0xFE && qr == (sb[b + j] & 0x7F)) {
+                                r++;
+                                if (P->hit_filter_exact_weight > 0 && qfull[qoffs[q] + i] == res[b + j]) ex++;
+                            }
+                        }
+                        if (r + P->hit_filter_exact_weight * ex < P->hit_filter_min_ids) {
+                            ctr->hits_filtered++;
+                            continue;
+                        }
+                    }
+                    if (ns == ns_cap) { ns_cap *= 2; sv = (surv_t*)realloc(sv, ns_cap * sizeof(surv_t)); }
+                    sv[ns].subject = (uint32_t)s; sv[ns].query = q; sv[ns].qp = qp; sv[ns].sp = (uint32_t)p;
+                    sv[ns].shape = si;
+                    ns++;
+                }
+            }
+        }
+        free(seeds);
+    }
+    free(sb);
+    free(qred);
+    free(qfull);
+    qsort(sv, ns, sizeof(surv_t), cmp_surv);
+
+    /* visit every (subject, query) pair: coverage + X-drop -> HSPs -> regions */
+    size_t nr = 0, r_cap = 1024;
+    orc_region* regs_all = (orc_region*)malloc(r_cap * sizeof(orc_region));
+    size_t i = 0;
+    while (i < ns) {
+        size_t j = i + 1;
+        while (j < ns && sv[j].subject == sv[i].subject && sv[j].query == sv[i].query) j++;
+        const uint32_t q = sv[i].query, s = sv[i].subject;
+        const uint8_t* qc = qcodes + qoffs[q];
+        const int8_t* qb = qbias ? qbias + qoffs[q] : NULL;
+        const uint64_t qlen = qoffs[q + 1] - qoffs[q];
+        const uint8_t* sc = res + soffs[s];
+        const uint64_t sl = soffs[s + 1] - soffs[s];
+        uint32_t* cover = (uint32_t*)calloc(qlen + sl + 1, sizeof(uint32_t));
+        size_t nh = 0;
+        hsp_t* hs = (hsp_t*)malloc((j - i) * sizeof(hsp_t));
+        for (size_t k = i; k < j; k++) {
+            const uint32_t qp = sv[k].qp, sp = sv[k].sp;
+            const int64_t d = (int64_t)sp - (int64_t)qp;
+            const size_t di = (size_t)(d + (int64_t)qlen);
+            if (qp < cover[di]) { ctr->extensions_avoided++; continue; }
+            ctr->ungapped_extensions++;
+            uint64_t lo, hi;
+            int32_t score = orc_ungapped_xdrop(qc, qlen, sc, sl, qp, sp, matrix, qb, P->x_drop, &lo, &hi);
+            /* steps of xdrop_cat (scan.rs:904): right steps + left steps */
+            {
+                /* recount the steps the way xdrop_cat counts them */
+                uint64_t nrt = qlen - qp < sl - sp ? qlen - qp : sl - sp;
+                uint64_t nlt = qp < sp ? qp : sp;
+                int32_t best = 0, cur = 0; uint64_t tr = 0;
+                while (tr < nrt) {
+                    cur += matrix[(qc[qp + tr] < 24 ? qc[qp + tr] : 22) * 24 + (sc[sp + tr] < 24 ? sc[sp + tr] : 22)] + (qb ? qb[qp + tr] : 0);
+                    tr++;
+                    if (cur > best) best = cur;
+                    if (cur < best - P->x_drop) break;
+                }
+                int32_t bl = 0, cl = 0; uint64_t tl = 1;
+                if (nlt > 0) {
+                    for (;;) {
+                        cl += matrix[(qc[qp - tl] < 24 ? qc[qp - tl] : 22) * 24 + (sc[sp - tl] < 24 ? sc[sp - tl] : 22)] + (qb ? qb[qp - tl] : 0);
+                        if (cl > bl) bl = cl;
+                        tl++;
+                        if (!(tl <= nlt && cl >= bl - P->x_drop)) break;
+                    }
+                }
+                ctr->xdrop_steps += tr + tl - 1;
+            }
+            cover[di] = (uint32_t)hi;
+            if (score >= P->hsp_threshold) {
+                hs[nh].diag = d; hs[nh].q_lo = (uint32_t)lo; hs[nh].q_hi = (uint32_t)hi; hs[nh].score = score;
+                nh++;
+            }
+        }
+        free(cover);
+        if (nh) {
+            /* finish_subject_into (scan.rs:2437-2474) */
+            ctr->hsps += nh;
+            qsort(hs, nh, sizeof(hsp_t), cmp_hsp);
+            const int64_t join = 2 * (int64_t)P->window_slack;
+            orc_region* rg = (orc_region*)malloc(nh * sizeof(orc_region));
+            uint32_t* ev_n = (uint32_t*)malloc(nh * sizeof(uint32_t));
+            int32_t* ev_s = (int32_t*)malloc(nh * sizeof(int32_t));
+            size_t ng = 0;
+            for (size_t k = 0; k < nh; k++) {
+                if (ng > 0 && hs[k].diag - rg[ng - 1].d_max <= join) {
+                    if (hs[k].diag > rg[ng - 1].d_max) rg[ng - 1].d_max = (int32_t)hs[k].diag;
+                    if (hs[k].score > rg[ng - 1].best) rg[ng - 1].best = hs[k].score;
+                    ev_n[ng - 1]++;
+                    int64_t sum = (int64_t)ev_s[ng - 1] + hs[k].score;
+                    ev_s[ng - 1] = sum > INT32_MAX ? INT32_MAX : (sum < INT32_MIN ? INT32_MIN : (int32_t)sum);
+                } else {
+                    rg[ng].query = q; rg[ng].subject = s;
+                    rg[ng].d_min = rg[ng].d_max = (int32_t)hs[k].diag; rg[ng].best = hs[k].score;
+                    ev_n[ng] = 1; ev_s[ng] = hs[k].score;
+                    ng++;
+                }
+            }
+            const int32_t thr = region_thr ? region_thr[q] : P->hsp_threshold;
+            size_t kept = ng;
+            if (thr > P->hsp_threshold) {
+                kept = 0;
+                for (size_t k = 0; k < ng; k++)
+                    if (rg[k].best >= thr || (ev_n[k] >= 2 && ev_s[k] >= thr)) rg[kept++] = rg[k];
+                ctr->regions_weak_dropped += ng - kept;
+            }
+            /* sort by (best desc, d_min asc), keep max_regions_per_subject */
+            for (size_t a = 1; a < kept; a++) {
+                orc_region x = rg[a];
+                size_t b2 = a;
+                while (b2 > 0 && (rg[b2 - 1].best < x.best || (rg[b2 - 1].best == x.best && rg[b2 - 1].d_min > x.d_min))) {
+                    rg[b2] = rg[b2 - 1];
+                    b2--;
+                }
+                rg[b2] = x;
+            }
+            size_t keep = kept < P->max_regions_per_subject ? kept : (P->max_regions_per_subject ? P->max_regions_per_subject : 1);
+            if (keep > kept) keep = kept;
+            for (size_t k = 0; k < keep; k++) {
+                if (nr == r_cap) { r_cap *= 2; regs_all = (orc_region*)realloc(regs_all, r_cap * sizeof(orc_region)); }
+                regs_all[nr++] = rg[k];
+            }
+            free(rg); free(ev_n); free(ev_s);
+        }
+        free(hs);
+        i = j;
+    }
+    free(sv);
+    /* per query: region_order, cap at max_candidates */
+    qsort(regs_all, nr, sizeof(orc_region), cmp_region);
+    uint64_t w = 0;
+    size_t a = 0;
+    const uint64_t cap = P->max_candidates ? P->max_candidates : 1;
+    while (a < nr) {
+        size_t b2 = a;
+        while (b2 < nr && regs_all[b2].query == regs_all[a].query) b2++;
+        size_t take = (b2 - a) > cap ? cap : (b2 - a);
+        ctr->regions_dropped_by_cap += (b2 - a) - take;
+        for (size_t k = 0; k < take; k++) {
+            if (w >= out_cap) { free(regs_all); return -1; }
+            out[w++] = regs_all[a + k];
+        }
+        a = b2;
+    }
+    ctr->regions = w;
+    free(regs_all);
+    return (int64_t)w;
+}

@@ -117,6 +117,54 @@ int orc_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
                         const int32_t* matrix, int32_t gap_open, int32_t gap_extend,
                         int32_t* scores, int threads, uint64_t* cells_out);
 
+
+/* ---- scan schedule: seeds -> hits -> window filter -> X-drop -> regions ----
+ * Restates Engine::search_scan for one query batch (src/search/engine/scan.rs:
+ * build_scan_db 1066-1257, build_batch 1500-1596, scan_hits 1603-1804,
+ * filter_scalar 1809-1856, visit_chunk_inner 2084-2225, visit_scan 2384-2431,
+ * finish_subject_into 2437-2474; index.rs:329-336 auto_occ_cap; the per-query
+ * candidate cap under region_order, engine.rs:493-495). */
+typedef struct {
+    uint8_t alpha_map[24];      /* reduced letter per code, 255 = not seedable */
+    uint32_t alpha_size;
+    uint32_t nshapes;
+    uint32_t shape_span[32];
+    uint32_t shape_weight[32];
+    uint16_t shape_off[32][16];
+    uint32_t hit_filter_min_ids; /* 0 = no window filter */
+    uint32_t hit_filter_exact_weight;
+    int32_t hsp_threshold;
+    int32_t x_drop;
+    int32_t window_slack;
+    uint32_t max_regions_per_subject;
+    uint32_t max_candidates;
+    uint64_t seed_max_occ;       /* 0 = automatic cap */
+    uint64_t ref_db_residues;
+    uint64_t db_length;          /* database residues of the statistics */
+} orc_scan_params;
+
+typedef struct {
+    uint32_t query, subject;
+    int32_t d_min, d_max, best;
+} orc_region;
+
+typedef struct {
+    uint64_t seed_positions, seeds_frequent_skipped, hits, hits_filtered, ungapped_extensions,
+        extensions_avoided, xdrop_steps, hsps, regions, regions_weak_dropped, regions_dropped_by_cap;
+} orc_scan_counters;
+
+/* Returns the number of regions written to `out` (capacity out_cap; -1 when
+ * too small), ordered by query, then region_order.  db_mask / q_mask: one
+ * byte per residue, nonzero = masked from seeding (NULL = none). */
+int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsub, const uint8_t* db_mask,
+                         const uint8_t* qcodes, const uint64_t* qoffs, uint32_t nq, const int8_t* qbias,
+                         const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
+                         const orc_scan_params* p, orc_region* out, uint64_t out_cap,
+                         orc_scan_counters* ctr);
+
+/* auto_occ_cap (src/search/index.rs:329-336). */
+uint64_t orc_auto_occ_cap(uint64_t total, uint64_t ncodes, uint64_t db_residues, uint64_t ref_residues);
+
 #ifdef __cplusplus
 }
 #endif

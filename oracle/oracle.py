@@ -157,3 +157,78 @@ def score_band_jobs(residues, qcodes, qoffs, qbias, jobs, matrix, go, ge, thread
     lib().orc_score_band_jobs(_p(res), _p(qc), _p(qo), _p(qb) if qb is not None else None, _p(jb), jb.size, _p(m),
                               int(go), int(ge), _p(out), int(threads), ctypes.byref(cells))
     return out, int(cells.value)
+
+
+class ScanParams(ctypes.Structure):
+    _fields_ = [("alpha_map", ctypes.c_uint8 * 24), ("alpha_size", ctypes.c_uint32), ("nshapes", ctypes.c_uint32),
+                ("shape_span", ctypes.c_uint32 * 32), ("shape_weight", ctypes.c_uint32 * 32),
+                ("shape_off", (ctypes.c_uint16 * 16) * 32), ("hit_filter_min_ids", ctypes.c_uint32),
+                ("hit_filter_exact_weight", ctypes.c_uint32), ("hsp_threshold", ctypes.c_int32),
+                ("x_drop", ctypes.c_int32), ("window_slack", ctypes.c_int32),
+                ("max_regions_per_subject", ctypes.c_uint32), ("max_candidates", ctypes.c_uint32),
+                ("seed_max_occ", ctypes.c_uint64), ("ref_db_residues", ctypes.c_uint64), ("db_length", ctypes.c_uint64)]
+
+
+class ScanCounters(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "seed_positions", "seeds_frequent_skipped", "hits", "hits_filtered", "ungapped_extensions",
+        "extensions_avoided", "xdrop_steps", "hsps", "regions", "regions_weak_dropped", "regions_dropped_by_cap")]
+
+
+REGION_DTYPE = np.dtype([("query", "<u4"), ("subject", "<u4"), ("d_min", "<i4"), ("d_max", "<i4"), ("best", "<i4")])
+
+
+def make_scan_params(alpha_map, alpha_size, shapes, min_ids=27, exact_weight=2, hsp_threshold=40, x_drop=20,
+                     window_slack=64, max_regions_per_subject=4, max_candidates=5000, seed_max_occ=0,
+                     ref_db_residues=40_000_000, db_length=0):
+    p = ScanParams()
+    for i in range(24):
+        p.alpha_map[i] = int(alpha_map[i])
+    p.alpha_size = int(alpha_size)
+    p.nshapes = len(shapes)
+    for si, sh in enumerate(shapes):
+        offs = [i for i, ch in enumerate(sh) if ch == "1"]
+        p.shape_span[si] = len(sh)
+        p.shape_weight[si] = len(offs)
+        for k, o in enumerate(offs):
+            p.shape_off[si][k] = o
+    p.hit_filter_min_ids = min_ids
+    p.hit_filter_exact_weight = exact_weight
+    p.hsp_threshold = hsp_threshold
+    p.x_drop = x_drop
+    p.window_slack = window_slack
+    p.max_regions_per_subject = max_regions_per_subject
+    p.max_candidates = max_candidates
+    p.seed_max_occ = seed_max_occ
+    p.ref_db_residues = ref_db_residues
+    p.db_length = db_length
+    return p
+
+
+def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, matrix, params, out_cap=None):
+    """Engine::search_scan's candidate regions for one batch -> (REGION_DTYPE array, counters dict)."""
+    L = lib()
+    f = L.orc_scan_regions
+    f.restype = ctypes.c_int64
+    P = ctypes.c_void_p
+    f.argtypes = [P, P, ctypes.c_uint64, P, P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_uint64, P]
+    res = _a(res, np.uint8)
+    so = _a(soffs, np.uint64)
+    dm = None if db_mask is None else _a(db_mask, np.uint8)
+    qc = _a(qcodes, np.uint8)
+    qo = _a(qoffs, np.uint64)
+    qb = None if qbias is None else _a(qbias, np.int8)
+    qm = None if q_mask is None else _a(q_mask, np.uint8)
+    rt = None if region_thr is None else _a(region_thr, np.int32)
+    m = _a(np.asarray(matrix).reshape(576), np.int32)
+    cap = out_cap or max(1024, (qo.size - 1) * params.max_candidates)
+    out = np.zeros(cap, REGION_DTYPE)
+    ctr = ScanCounters()
+    n = f(_p(res), so.size - 1 if so.size else 0, None, None, None, None, 0, None, None, None, None, None, None, 0,
+          None) if False else f(_p(res), _p(so), so.size - 1, _p(dm) if dm is not None else None, _p(qc), _p(qo),
+                                qo.size - 1, _p(qb) if qb is not None else None, _p(qm) if qm is not None else None,
+                                _p(rt) if rt is not None else None, _p(m), ctypes.byref(params), _p(out), cap,
+                                ctypes.byref(ctr))
+    if n < 0:
+        raise MemoryError("region buffer too small")
+    return out[:n].copy(), {k: int(getattr(ctr, k)) for k, _ in ctr._fields_}

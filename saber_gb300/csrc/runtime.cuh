@@ -1,0 +1,145 @@
+// Internal runtime types shared by the library's translation units: device
+// buffers, datasets, schemes, the handle and the error helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "band_common.cuh"
+#include "saber_gpu.h"
+
+namespace saber {
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    // grow-only; contents are not preserved
+    cudaError_t reserve(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = bytes < 256 ? 256 : bytes;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+struct QuerySet {
+    uint32_t nq = 0;
+    std::vector<uint64_t> offs;  // host copy
+    std::vector<uint64_t> poff;  // host copy of the profile offsets
+    std::vector<uint32_t> pmpad; // host copy of the profile row strides
+    DevBuf codes, offsets, bias, prof, prof_off, prof_mpad;
+    bool has = false;
+    bool has_bias = false;
+};
+
+// Residues + subject offsets + a query set with profiles for one scheme.
+struct Dataset {
+    DevBuf res, soff;
+    uint64_t n_res = 0, nsub = 0;
+    bool has_db = false;
+    QuerySet qs;
+};
+
+struct Scheme {
+    int32_t matrix[576];
+    int32_t go = 11, ge = 1;
+    bool has = false;
+    DevBuf d_matrix;
+};
+
+}  // namespace saber
+
+struct saber_gpu {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+    int sm_count = 0;
+    int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
+    // the handle's scheme and dataset (set_scheme / load_db / load_queries)
+    saber::Scheme scheme;
+    saber::Dataset main;
+    // per-call scheme and dataset of the one-query entry points
+    saber::Scheme eph_scheme;
+    saber::Dataset eph;
+    // per-call scratch
+    saber::DevBuf keys_in, keys_out, vals_in, vals_out, counts, stats, cub_tmp, bufs, slabs, list, jobs_dev,
+        scores_dev;
+    // scan state: per-residue seed bytes / distances of the database, the
+    // database mask, per-shape frequent-code bitmaps, and per-call buffers
+    saber::DevBuf db_mask, sc_sb, sc_rem, sc_dst, sc_freq, sc_counts, sc_qsb, sc_qfull, sc_qrem, sc_qdst,
+        sc_qcnt, sc_qoff, sc_qent, sc_qpres, sc_surv, sc_key1, sc_key2, sc_val, sc_key1o, sc_key2o, sc_valo,
+        sc_chains, sc_hsp, sc_hkey, sc_hkeyo, sc_hval, sc_hvalo, sc_pairs, sc_regions, sc_rthr, sc_ctr, sc_tmp,
+        sc_flags;
+    bool has_db_mask = false;
+    uint64_t sc_key = 0;            // fingerprint of the database state built
+    std::vector<uint64_t> sc_caps;  // per shape
+    std::vector<uint64_t> sc_freq_off;
+    // traceback scratch
+    saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
+};
+
+namespace saber {
+
+static int fail(saber_gpu* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    h->err = buf;
+    return code;
+}
+
+#define CU(h, call)                                                                       \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return ::saber::fail((h), SABER_ERR_CUDA, "%s: %s (%s:%d)", #call,            \
+                                 cudaGetErrorString(e_), __FILE__, __LINE__);             \
+    } while (0)
+#define CUALLOC(h, buf, bytes)                                                            \
+    do {                                                                                  \
+        cudaError_t e_ = (buf).reserve(bytes);                                            \
+        if (e_ != cudaSuccess)                                                            \
+            return ::saber::fail((h), SABER_ERR_NOMEM, "device allocation of %zu bytes: %s", \
+                                 (size_t)(bytes), cudaGetErrorString(e_));                \
+    } while (0)
+
+
+int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st);
+
+static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
+    uint64_t b = (n + t - 1) / t;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+
+}  // namespace saber

@@ -18,113 +18,9 @@
 #include "band_common.cuh"
 #include "saber_gpu.h"
 
-namespace saber {
-
-// ---------------------------------------------------------------------------
-// device buffers
-// ---------------------------------------------------------------------------
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    // grow-only; contents are not preserved
-    cudaError_t reserve(size_t bytes) {
-        if (bytes <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = bytes < 256 ? 256 : bytes;
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    template <class T>
-    T* as() const {
-        return reinterpret_cast<T*>(p);
-    }
-};
-
-struct QuerySet {
-    uint32_t nq = 0;
-    std::vector<uint64_t> offs;  // host copy
-    std::vector<uint64_t> poff;  // host copy of the profile offsets
-    std::vector<uint32_t> pmpad; // host copy of the profile row strides
-    DevBuf codes, offsets, bias, prof, prof_off, prof_mpad;
-    bool has = false;
-    bool has_bias = false;
-};
-
-// Residues + subject offsets + a query set with profiles for one scheme.
-struct Dataset {
-    DevBuf res, soff;
-    uint64_t n_res = 0, nsub = 0;
-    bool has_db = false;
-    QuerySet qs;
-};
-
-struct Scheme {
-    int32_t matrix[576];
-    int32_t go = 11, ge = 1;
-    bool has = false;
-    DevBuf d_matrix;
-};
-
-}  // namespace saber
-
-struct saber_gpu {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::mutex mu;
-    std::string err;
-    int sm_count = 0;
-    int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
-    // the handle's scheme and dataset (set_scheme / load_db / load_queries)
-    saber::Scheme scheme;
-    saber::Dataset main;
-    // per-call scheme and dataset of the one-query entry points
-    saber::Scheme eph_scheme;
-    saber::Dataset eph;
-    // per-call scratch
-    saber::DevBuf keys_in, keys_out, vals_in, vals_out, counts, stats, cub_tmp, bufs, slabs, list, jobs_dev,
-        scores_dev;
-    // traceback scratch
-    saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
-};
+#include "runtime.cuh"
 
 namespace saber {
-
-static int fail(saber_gpu* h, int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    h->err = buf;
-    return code;
-}
-
-#define CU(h, call)                                                                       \
-    do {                                                                                  \
-        cudaError_t e_ = (call);                                                          \
-        if (e_ != cudaSuccess)                                                            \
-            return ::saber::fail((h), SABER_ERR_CUDA, "%s: %s (%s:%d)", #call,            \
-                                 cudaGetErrorString(e_), __FILE__, __LINE__);             \
-    } while (0)
-#define CUALLOC(h, buf, bytes)                                                            \
-    do {                                                                                  \
-        cudaError_t e_ = (buf).reserve(bytes);                                            \
-        if (e_ != cudaSuccess)                                                            \
-            return ::saber::fail((h), SABER_ERR_NOMEM, "device allocation of %zu bytes: %s", \
-                                 (size_t)(bytes), cudaGetErrorString(e_));                \
-    } while (0)
 
 // ---------------------------------------------------------------------------
 // small kernels
@@ -243,12 +139,6 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
     atomicMax(&stats[5], w1);
 }
 
-static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
-    uint64_t b = (n + t - 1) / t;
-    if (b < 1) b = 1;
-    if (b > cap) b = cap;
-    return (unsigned)b;
-}
 
 // ---------------------------------------------------------------------------
 // the scoring pipeline (device-resident jobs and scores)
@@ -486,6 +376,10 @@ static int load_db(saber_gpu* h, Dataset& ds, const uint8_t* residues, uint64_t 
     ds.n_res = n_res;
     ds.nsub = nsub;
     ds.has_db = true;
+    if (&ds == &h->main) {
+        h->sc_key = 0;
+        h->has_db_mask = false;
+    }
     return SABER_OK;
 }
 
@@ -1141,6 +1035,29 @@ int saber_gpu_traceback(saber_gpu* h, const saber_traceback_job* jobs, uint64_t 
     if (njobs && (!jobs || !out)) return fail(h, SABER_ERR_ARG, "null argument");
     if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
     return traceback_driver(h, jobs, njobs, band_pad, max_dir_bytes, out, ops, ops_cap, stats);
+}
+
+int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residues) {
+    ENTER(h);
+    h->sc_key = 0;  // the scan's database state depends on the mask
+    if (!mask) {
+        h->has_db_mask = false;
+        return SABER_OK;
+    }
+    if (!h->main.has_db || n_residues != h->main.n_res)
+        return fail(h, SABER_ERR_ARG, "mask length must equal the loaded database's residues");
+    CUALLOC(h, h->db_mask, n_residues + 64);
+    if (n_residues) CU(h, cudaMemcpyAsync(h->db_mask.p, mask, n_residues, cudaMemcpyHostToDevice, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    h->has_db_mask = true;
+    return SABER_OK;
+}
+
+int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask, const int32_t* region_thr,
+                   saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* stats) {
+    ENTER(h);
+    if (!params || (out_cap && !out)) return fail(h, SABER_ERR_ARG, "null argument");
+    return scan_regions(h, params, q_mask, region_thr, out, out_cap, n_out, stats);
 }
 
 uint64_t saber_band_cells(uint64_t m, uint64_t n, int64_t band_lo, int64_t band_hi) {

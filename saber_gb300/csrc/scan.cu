@@ -1,0 +1,853 @@
+// Scan schedule on the GPU: the seed scan of the database against a query
+// batch's seed tables, the window filter, per-diagonal coverage with ungapped
+// X-drop, and region clustering — Engine::search_scan up to the per-query
+// candidate cap (src/search/engine/scan.rs:1261-1497).
+//
+// Database state (built once per database, seed alphabet and shape set):
+//   sb[r]   seed byte of residue r: reduced letter, | 0x80 when masked from
+//           seeding, 0x7F when not in the seed alphabet (scan.rs:123-141)
+//   rem[r]  min(255, residues from r to the end of its subject)
+//   dst[r]  min(255, residues from the start of its subject to r)
+//   per shape: the bitmap of codes occurring more than the cap in the
+//           database (scan.rs:1184-1238, cap = index.rs:329-336)
+// Per call:
+//   per shape: dense code -> batch-position table of the unmasked, not
+//   frequent query seeds (count, scan, scatter; a presence bitmap in front),
+//   then one thread per database position computes its seed code, looks it
+//   up and runs the window filter on every hit; survivors (position, batch
+//   position, shape) are appended to a device list.
+//   Survivors are sorted into chains of one (subject, query, diagonal) in
+//   (query position, shape) order — the order in which the reference visits
+//   the hits of a pair (scan.rs:2158-2170) restricted to one diagonal, which
+//   is all the coverage rule couples (scan.rs:2398-2425) — and one thread per
+//   chain runs the coverage test and the X-drop extensions.  HSPs are sorted
+//   by (subject, query, diagonal) and one thread per pair forms its regions
+//   (scan.rs:2437-2474).  The per-query order and cap are applied on the host.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+
+#include "runtime.cuh"
+
+namespace saber {
+
+constexpr uint8_t kNonSeed = 0x7F;
+constexpr uint8_t kMasked = 0x80;
+constexpr uint8_t kQSent = 0xFE;
+constexpr int kDBias = 1 << 19;  // diagonal offset in the chain keys
+
+struct AlphaMap {
+    uint8_t m[24];
+};
+struct ShapeDev {
+    uint16_t off[16];
+    uint32_t w, span;
+};
+
+// ---- database state --------------------------------------------------------
+__global__ void k_seed_bytes(const uint8_t* __restrict__ res, const uint8_t* __restrict__ mask, uint64_t N,
+                             AlphaMap am, uint8_t* __restrict__ sb) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (uint64_t)gridDim.x * blockDim.x) {
+        const uint8_t c = res[r];
+        uint8_t v = (c < 24 && am.m[c] != 255) ? am.m[c] : kNonSeed;
+        if (v != kNonSeed && mask && mask[r]) v |= kMasked;
+        sb[r] = v;
+    }
+}
+
+// distances to the end / from the start of the sequence holding position r
+__global__ void k_dists(const uint64_t* __restrict__ offs, uint64_t nseq, uint64_t N, uint8_t* __restrict__ rem,
+                        uint8_t* __restrict__ dst) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t lo = 0, hi = nseq;  // last s with offs[s] <= r
+        while (hi - lo > 1) {
+            uint64_t mid = (lo + hi) >> 1;
+            if (offs[mid] <= r) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t a = r - offs[lo], b = offs[lo + 1] - r;
+        rem[r] = (uint8_t)(b < 255 ? b : 255);
+        dst[r] = (uint8_t)(a < 255 ? a : 255);
+    }
+}
+
+__device__ __forceinline__ int64_t seed_code(const uint8_t* __restrict__ sr, const ShapeDev& sh, uint32_t asize) {
+    uint32_t c = 0;
+    for (uint32_t i = 0; i < sh.w; i++) {
+        const uint8_t r = sr[sh.off[i]];
+        if (r >= asize) return -1;
+        c = c * asize + r;
+    }
+    return c;
+}
+
+__global__ void k_db_counts(const uint8_t* __restrict__ sb, const uint8_t* __restrict__ rem, uint64_t N, ShapeDev sh,
+                            uint32_t asize, uint32_t* __restrict__ counts, unsigned long long* __restrict__ total) {
+    unsigned long long t = 0;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (uint64_t)gridDim.x * blockDim.x) {
+        if (rem[r] < sh.span) continue;
+        const int64_t c = seed_code(sb + r, sh, asize);
+        if (c < 0) continue;
+        atomicAdd(&counts[c], 1u);
+        t++;
+    }
+    atomicAdd(total, t);
+}
+
+__global__ void k_freq_bits(const uint32_t* __restrict__ counts, uint64_t ncodes, uint64_t cap,
+                            unsigned long long* __restrict__ bits) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncodes; c += (uint64_t)gridDim.x * blockDim.x)
+        if (counts[c] > cap) atomicOr(&bits[c >> 6], 1ull << (c & 63));
+}
+
+// ---- query tables ------------------------------------------------------------
+__global__ void k_query_bytes(const uint8_t* __restrict__ qcodes, const uint8_t* __restrict__ qmask, uint64_t QN,
+                              AlphaMap am, uint8_t* __restrict__ qsb, uint8_t* __restrict__ qfull) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < QN; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint8_t c = qcodes[i];
+        const uint8_t r = am.m[c < 24 ? c : 23];
+        const bool ok = !(qmask && qmask[i]) && r != 255;
+        qsb[i] = ok ? r : kQSent;
+        qfull[i] = ok ? c : kQSent;
+    }
+}
+
+__device__ __forceinline__ bool is_frequent(const unsigned long long* freq, uint32_t c) {
+    return freq && ((freq[c >> 6] >> (c & 63)) & 1ull);
+}
+
+// pass 0: count per code; pass 1: scatter batch positions (cnt = cursors)
+template <int PASS>
+__global__ void k_query_seeds(const uint8_t* __restrict__ qsb, const uint8_t* __restrict__ qrem, uint64_t QN,
+                              ShapeDev sh, uint32_t asize, const unsigned long long* __restrict__ freq,
+                              uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off, uint32_t* __restrict__ ent,
+                              unsigned long long* __restrict__ ctr) {
+    unsigned long long kept = 0, skipped = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < QN; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (qrem[i] < sh.span) continue;
+        const int64_t c = seed_code(qsb + i, sh, asize);
+        if (c < 0) continue;
+        if (is_frequent(freq, (uint32_t)c)) {
+            skipped++;
+            continue;
+        }
+        if (PASS == 0) {
+            atomicAdd(&cnt[c], 1u);
+            kept++;
+        } else {
+            const uint32_t slot = atomicAdd(&cnt[c], 1u);
+            ent[off[c] + slot] = (uint32_t)i;
+        }
+    }
+    if (PASS == 0) {
+        atomicAdd(&ctr[0], kept);
+        atomicAdd(&ctr[1], skipped);
+    }
+}
+
+__global__ void k_presence(const uint32_t* __restrict__ cnt, uint64_t ncodes, unsigned long long* __restrict__ bits) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncodes; c += (uint64_t)gridDim.x * blockDim.x)
+        if (cnt[c]) atomicOr(&bits[c >> 6], 1ull << (c & 63));
+}
+
+// ---- database scan with the window filter ---------------------------------------
+struct ScanArgs {
+    const uint8_t *sb, *res, *rem, *dst;
+    uint64_t N;
+    const unsigned long long* pres;
+    const uint32_t *qoff, *qent;
+    const uint8_t *qsb, *qfull, *qrem, *qdst;
+    int cfil;
+    uint32_t min_ids, kx;
+    uint32_t shape;
+    uint2* surv;
+    unsigned long long* nsurv;  // counter (may exceed cap: overflow)
+    uint64_t cap;
+    unsigned long long* ctr;    // [2] hits, [3] filtered
+};
+
+__global__ void k_scan(ScanArgs a, ShapeDev sh, uint32_t asize) {
+    unsigned long long hits = 0, filtered = 0;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.N; r += (uint64_t)gridDim.x * blockDim.x) {
+        if (a.rem[r] < sh.span) continue;
+        const int64_t c = seed_code(a.sb + r, sh, asize);
+        if (c < 0) continue;
+        if (!((a.pres[c >> 6] >> (c & 63)) & 1ull)) continue;
+        const uint32_t e0 = a.qoff[c], e1 = a.qoff[c + 1];
+        // subject lanes of the 32-residue window starting at r + c - 16 (filter_scalar, scan.rs:1829-1833)
+        const int sdst = a.dst[r], srem = a.rem[r];
+        const int s_lo = max(0, 16 - a.cfil - sdst);
+        const int s_hi = min(32, srem + 16 - a.cfil);
+        for (uint32_t e = e0; e < e1; e++) {
+            const uint32_t g = a.qent[e];
+            hits++;
+            if (a.min_ids > 0) {
+                const int t_lo = max(s_lo, 16 - a.cfil - (int)a.qdst[g]);
+                const int t_hi = min(s_hi, (int)a.qrem[g] + 16 - a.cfil);
+                uint32_t ids = 0, ex = 0;
+                const int64_t so = (int64_t)r + a.cfil - 16, qo = (int64_t)g + a.cfil - 16;
+                for (int t = t_lo; t < t_hi; t++) {
+                    const uint8_t qr = a.qsb[qo + t];
+                    if (qr != kQSent && qr == (a.sb[so + t] & 0x7F)) {
+                        ids++;
+                        if (a.kx && a.qfull[qo + t] == a.res[so + t]) ex++;
+                    }
+                }
+                if (ids + a.kx * ex < a.min_ids) {
+                    filtered++;
+                    continue;
+                }
+            }
+            const unsigned long long slot = atomicAdd(a.nsurv, 1ull);
+            if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)r, g | (a.shape << 27));
+        }
+    }
+    atomicAdd(&a.ctr[2], hits);
+    atomicAdd(&a.ctr[3], filtered);
+}
+
+// ---- chains ------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t upper_idx(const uint64_t* offs, uint64_t n, uint64_t x) {
+    uint64_t lo = 0, hi = n;  // last k with offs[k] <= x
+    while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_surv_keys(const uint2* __restrict__ surv, uint32_t n, const uint64_t* __restrict__ soffs,
+                            uint64_t nsub, const uint64_t* __restrict__ qoffs, uint32_t nq,
+                            unsigned long long* __restrict__ key1, uint32_t* __restrict__ key2,
+                            uint32_t* __restrict__ val) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint2 v = surv[i];
+        const uint32_t g = v.y & ((1u << 27) - 1), shape = v.y >> 27;
+        const uint64_t s = upper_idx(soffs, nsub, v.x);
+        const uint64_t q = upper_idx(qoffs, nq, g);
+        const int64_t qp = (int64_t)g - (int64_t)qoffs[q], sp = (int64_t)v.x - (int64_t)soffs[s];
+        const int64_t d = sp - qp;
+        key1[i] = ((unsigned long long)s << 40) | ((unsigned long long)q << 20) | (unsigned long long)(d + kDBias);
+        key2[i] = ((uint32_t)qp << 5) | shape;
+        val[i] = i;
+    }
+}
+
+__global__ void k_gather_key1(const unsigned long long* __restrict__ key1, const uint32_t* __restrict__ val,
+                              uint32_t n, unsigned long long* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = key1[val[i]];
+}
+
+__global__ void k_run_flags(const unsigned long long* __restrict__ key, uint32_t n, int shift,
+                            uint8_t* __restrict__ flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flag[i] = i == 0 || (key[i] >> shift) != (key[i - 1] >> shift);
+}
+
+struct ChainArgs {
+    const uint2* surv;
+    const uint32_t* order;            // survivors in chain order
+    const unsigned long long* key1s;  // sorted chain keys
+    const uint32_t* starts;           // chain starts
+    const uint32_t* nchains;
+    uint32_t nsurv;
+    const uint64_t *soffs, *qoffs;
+    const uint8_t* res;               // canonical residues
+    const int16_t* prof;              // query profiles (S + bias), rows c, stride mpad
+    const uint64_t* prof_off;
+    const uint32_t* prof_mpad;
+    int thr, x;
+    uint4* hsp;                       // (lo, hi, score, chain)
+    unsigned long long* hkey;
+    uint32_t* hval;
+    unsigned long long* nhsp;
+    uint64_t hcap;
+    unsigned long long* ctr;          // [4] extensions, [5] avoided, [6] steps
+};
+
+// Ungapped X-drop through (qp, sp) (ungapped_xdrop, engine.rs:2460-2494, with
+// the step count of xdrop_cat, scan.rs:859-904).
+__device__ __forceinline__ int xdrop(const int16_t* P, int mpad, const uint8_t* s, int64_t qlen, int64_t sl,
+                                     int64_t qp, int64_t sp, int x, int64_t& lo, int64_t& hi, uint64_t& steps) {
+    const int64_t nr = min(qlen - qp, sl - sp), nl = min(qp, sp);
+    int best_r = 0, cur = 0;
+    int64_t tr = 0, end_t = 0;
+    while (tr < nr) {
+        cur += P[(size_t)s[sp + tr] * mpad + qp + tr];
+        tr++;
+        if (cur > best_r) {
+            best_r = cur;
+            end_t = tr;
+        }
+        if (cur < best_r - x) break;
+    }
+    int best_l = 0;
+    cur = 0;
+    int64_t tl = 1, st_t = 0;
+    if (nl > 0) {
+        for (;;) {
+            cur += P[(size_t)s[sp - tl] * mpad + qp - tl];
+            if (cur > best_l) {
+                best_l = cur;
+                st_t = tl;
+            }
+            tl++;
+            if (!(tl <= nl && cur >= best_l - x)) break;
+        }
+    }
+    steps += (uint64_t)(tr + tl - 1);
+    lo = qp - st_t;
+    hi = qp + end_t;
+    return best_r + best_l;
+}
+
+__global__ void k_chains(ChainArgs a) {
+    unsigned long long ext = 0, avoided = 0;
+    uint64_t steps = 0;
+    const uint32_t nch = *a.nchains;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nch; c += gridDim.x * blockDim.x) {
+        const uint32_t b = a.starts[c];
+        const uint32_t e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
+        const unsigned long long key = a.key1s[b];
+        const uint64_t s = key >> 40, q = (key >> 20) & 0xFFFFF;
+        const int64_t qlen = (int64_t)(a.qoffs[q + 1] - a.qoffs[q]);
+        const int64_t sl = (int64_t)(a.soffs[s + 1] - a.soffs[s]);
+        const int16_t* P = a.prof + a.prof_off[q];
+        const int mpad = (int)a.prof_mpad[q];
+        const uint8_t* subj = a.res + a.soffs[s];
+        int64_t cover = 0;
+        for (uint32_t i = b; i < e; i++) {
+            const uint2 v = a.surv[a.order[i]];
+            const uint32_t g = v.y & ((1u << 27) - 1);
+            const int64_t qp = (int64_t)g - (int64_t)a.qoffs[q];
+            const int64_t sp = (int64_t)v.x - (int64_t)a.soffs[s];
+            if (qp < cover) {
+                avoided++;
+                continue;
+            }
+            ext++;
+            int64_t lo, hi;
+            const int score = xdrop(P, mpad, subj, qlen, sl, qp, sp, a.x, lo, hi, steps);
+            cover = hi;
+            if (score >= a.thr) {
+                const unsigned long long slot = atomicAdd(a.nhsp, 1ull);
+                if (slot < a.hcap) {
+                    a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, c);
+                    a.hkey[slot] = key;
+                    a.hval[slot] = (uint32_t)slot;
+                }
+            }
+        }
+    }
+    atomicAdd(&a.ctr[4], ext);
+    atomicAdd(&a.ctr[5], avoided);
+    atomicAdd(&a.ctr[6], (unsigned long long)steps);
+}
+
+// ---- regions (finish_subject_into, scan.rs:2437-2474) --------------------------
+struct RegionArgs {
+    const uint4* hsp;
+    const uint32_t* order;            // HSPs sorted by (subject, query, diagonal)
+    const unsigned long long* hkeys;  // sorted keys
+    const uint32_t* starts;           // pair starts
+    const uint32_t* npairs;
+    uint32_t nhsp;
+    const int32_t* region_thr;        // per query (NULL: hsp_threshold)
+    int hsp_thr;
+    int64_t join;
+    uint32_t kmax;                    // max_regions_per_subject (<= 64)
+    saber_region* out;
+    unsigned long long* nout;
+    uint64_t cap;
+    unsigned long long* ctr;          // [7] hsps, [8] weak dropped
+};
+
+__global__ void k_regions(RegionArgs a) {
+    unsigned long long hsps = 0, weak = 0;
+    const uint32_t np = *a.npairs;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const uint32_t b = a.starts[p];
+        const uint32_t e = p + 1 < np ? a.starts[p + 1] : a.nhsp;
+        const unsigned long long key = a.hkeys[b];
+        const uint32_t s = (uint32_t)(key >> 40), q = (uint32_t)((key >> 20) & 0xFFFFF);
+        const int thr = a.region_thr ? a.region_thr[q] : a.hsp_thr;
+        hsps += e - b;
+        // top kmax regions by (best desc, d_min asc)
+        saber_region top[64];
+        uint32_t ntop = 0;
+        int64_t dmin = 0, dmax = 0;
+        int best = 0;
+        uint32_t evn = 0;
+        int32_t evs = 0;
+        bool open = false;
+        auto close = [&]() {
+            if (thr > a.hsp_thr && !(best >= thr || (evn >= 2 && evs >= thr))) {
+                weak++;
+                return;
+            }
+            saber_region r;
+            r.query = q;
+            r.subject = s;
+            r.d_min = (int32_t)dmin;
+            r.d_max = (int32_t)dmax;
+            r.best = best;
+            // insert into the top list
+            uint32_t pos = ntop;
+            while (pos > 0 && (top[pos - 1].best < r.best || (top[pos - 1].best == r.best && top[pos - 1].d_min > r.d_min)))
+                pos--;
+            if (pos >= a.kmax) return;
+            uint32_t last = ntop < a.kmax ? ntop : a.kmax - 1;
+            for (uint32_t k = last; k > pos; k--) top[k] = top[k - 1];
+            top[pos] = r;
+            if (ntop < a.kmax) ntop++;
+        };
+        for (uint32_t i = b; i < e; i++) {
+            const uint4 h = a.hsp[a.order[i]];
+            const int64_t d = (int64_t)(a.hkeys[i] & 0xFFFFF) - kDBias;
+            const int score = (int)h.z;
+            if (open && d - dmax <= a.join) {
+                if (d > dmax) dmax = d;
+                if (score > best) best = score;
+                evn++;
+                const int64_t sum = (int64_t)evs + score;
+                evs = sum > INT32_MAX ? INT32_MAX : (int32_t)sum;
+            } else {
+                if (open) close();
+                open = true;
+                dmin = dmax = d;
+                best = score;
+                evn = 1;
+                evs = score;
+            }
+        }
+        if (open) close();
+        if (ntop) {
+            const unsigned long long base = atomicAdd(a.nout, (unsigned long long)ntop);
+            for (uint32_t k = 0; k < ntop; k++)
+                if (base + k < a.cap) a.out[base + k] = top[k];
+        }
+    }
+    atomicAdd(&a.ctr[7], hsps);
+    atomicAdd(&a.ctr[8], weak);
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+static uint64_t ncodes_of(const saber_scan_params* p, uint32_t si) {
+    uint64_t n = 1;
+    for (uint32_t k = 0; k < p->shape_weight[si]; k++) n *= p->alpha_size;
+    return n;
+}
+
+static ShapeDev shape_dev(const saber_scan_params* p, uint32_t si) {
+    ShapeDev sh;
+    memset(&sh, 0, sizeof(sh));
+    for (uint32_t k = 0; k < p->shape_weight[si]; k++) sh.off[k] = p->shape_off[si][k];
+    sh.w = p->shape_weight[si];
+    sh.span = p->shape_span[si];
+    return sh;
+}
+
+// auto_occ_cap (index.rs:329-336), host f64 as the reference computes it
+static uint64_t auto_cap(uint64_t total, uint64_t ncodes, uint64_t db, uint64_t ref) {
+    uint64_t fl = 256;
+    if (ref > 0 && db > ref) fl = (uint64_t)std::ceil(256.0 * (double)db / (double)ref);
+    uint64_t c = (uint64_t)std::ceil((double)total / (double)(ncodes ? ncodes : 1) * 64.0);
+    return std::max(c, fl);
+}
+
+static uint64_t fingerprint(const saber_gpu* h, const saber_scan_params* p) {
+    uint64_t f = 1469598103934665603ull;
+    auto mix = [&](const void* d, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(d);
+        for (size_t i = 0; i < n; i++) f = (f ^ b[i]) * 1099511628211ull;
+    };
+    mix(p->alpha_map, 24);
+    mix(&p->alpha_size, 4);
+    mix(&p->nshapes, 4);
+    mix(p->shape_span, 4 * p->nshapes);
+    mix(p->shape_weight, 4 * p->nshapes);
+    mix(p->shape_off, sizeof(p->shape_off[0]) * p->nshapes);
+    mix(&p->seed_max_occ, 8);
+    mix(&p->ref_db_residues, 8);
+    mix(&p->db_length, 8);
+    mix(&h->main.n_res, 8);
+    mix(&h->main.nsub, 8);
+    const void* rp = h->main.res.p;
+    mix(&rp, sizeof(rp));
+    mix(&h->has_db_mask, 1);
+    return f;
+}
+
+int scan_build_db(saber_gpu* h, const saber_scan_params* p) {
+    const Dataset& ds = h->main;
+    cudaStream_t s = h->stream;
+    const uint64_t N = ds.n_res;
+    AlphaMap am;
+    memcpy(am.m, p->alpha_map, 24);
+    CUALLOC(h, h->sc_sb, N + 64);
+    CUALLOC(h, h->sc_rem, N + 64);
+    CUALLOC(h, h->sc_dst, N + 64);
+    CU(h, cudaMemsetAsync(h->sc_sb.p, kNonSeed, N + 64, s));
+    CU(h, cudaMemsetAsync(h->sc_rem.p, 0, N + 64, s));
+    CU(h, cudaMemsetAsync(h->sc_dst.p, 0, N + 64, s));
+    if (N) {
+        k_seed_bytes<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(
+            ds.res.as<uint8_t>(), h->has_db_mask ? h->db_mask.as<uint8_t>() : nullptr, N, am, h->sc_sb.as<uint8_t>());
+        k_dists<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(ds.soff.as<uint64_t>(), ds.nsub, N,
+                                                                   h->sc_rem.as<uint8_t>(), h->sc_dst.as<uint8_t>());
+        CU(h, cudaGetLastError());
+    }
+    // frequent codes per shape
+    h->sc_caps.assign(p->nshapes, 0);
+    h->sc_freq_off.assign(p->nshapes + 1, 0);
+    uint64_t words = 0;
+    for (uint32_t si = 0; si < p->nshapes; si++) {
+        h->sc_freq_off[si] = words;
+        words += (ncodes_of(p, si) + 63) / 64;
+    }
+    h->sc_freq_off[p->nshapes] = words;
+    CUALLOC(h, h->sc_freq, words * 8 + 8);
+    CU(h, cudaMemsetAsync(h->sc_freq.p, 0, words * 8 + 8, s));
+    CUALLOC(h, h->sc_ctr, 32 * 8);
+    for (uint32_t si = 0; si < p->nshapes; si++) {
+        const uint64_t nc = ncodes_of(p, si);
+        CUALLOC(h, h->sc_counts, nc * 4);
+        CU(h, cudaMemsetAsync(h->sc_counts.p, 0, nc * 4, s));
+        CU(h, cudaMemsetAsync(h->sc_ctr.p, 0, 8, s));
+        if (N)
+            k_db_counts<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(
+                h->sc_sb.as<uint8_t>(), h->sc_rem.as<uint8_t>(), N, shape_dev(p, si), p->alpha_size,
+                h->sc_counts.as<uint32_t>(), h->sc_ctr.as<unsigned long long>());
+        CU(h, cudaGetLastError());
+        unsigned long long total = 0;
+        CU(h, cudaMemcpyAsync(&total, h->sc_ctr.p, 8, cudaMemcpyDeviceToHost, s));
+        CU(h, cudaStreamSynchronize(s));
+        const uint64_t cap = p->seed_max_occ > 0 ? p->seed_max_occ
+                                                 : auto_cap(total, nc, p->db_length, p->ref_db_residues);
+        h->sc_caps[si] = cap;
+        if (total > cap)
+            k_freq_bits<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(
+                h->sc_counts.as<uint32_t>(), nc, cap,
+                h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si]);
+        CU(h, cudaGetLastError());
+    }
+    CU(h, cudaStreamSynchronize(s));
+    h->sc_key = fingerprint(h, p);
+    return SABER_OK;
+}
+
+static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st) {
+    const Dataset& ds = h->main;
+    const QuerySet& qs = ds.qs;
+    if (!ds.has_db || !qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (!p || p->nshapes == 0 || p->nshapes > 32 || p->alpha_size == 0 || p->alpha_size > 127)
+        return fail(h, SABER_ERR_ARG, "invalid scan parameters");
+    uint32_t minspan = 1u << 30;
+    for (uint32_t si = 0; si < p->nshapes; si++) {
+        if (p->shape_weight[si] < 1 || p->shape_weight[si] > 16 || p->shape_span[si] > 64 ||
+            p->shape_span[si] < p->shape_weight[si])
+            return fail(h, SABER_ERR_ARG, "invalid shape %u", si);
+        if (ncodes_of(p, si) > (1ull << 31)) return fail(h, SABER_ERR_ARG, "shape %u has too many codes", si);
+        minspan = std::min(minspan, p->shape_span[si]);
+    }
+    if (p->max_regions_per_subject > 64) return fail(h, SABER_ERR_ARG, "max_regions_per_subject must be <= 64");
+    if (ds.nsub >= (1ull << 24) || qs.nq >= (1u << 20) || qs.offs[qs.nq] >= (1ull << 27))
+        return fail(h, SABER_ERR_ARG, "scan batch too large (subjects < 2^24, queries < 2^20, residues < 2^27)");
+    for (uint32_t q = 0; q < qs.nq; q++)
+        if (qs.offs[q + 1] - qs.offs[q] >= (uint64_t)kDBias) return fail(h, SABER_ERR_ARG, "query too long");
+    cudaStream_t s = h->stream;
+    if (h->sc_key != fingerprint(h, p)) {
+        int rc = scan_build_db(h, p);
+        if (rc != SABER_OK) return rc;
+    }
+    saber_scan_stats local{};
+    cudaEvent_t ev[5];
+    for (int i = 0; i < 5; i++) CU(h, cudaEventCreate(&ev[i]));
+    struct G {
+        cudaEvent_t* e;
+        ~G() {
+            for (int i = 0; i < 5; i++) cudaEventDestroy(e[i]);
+        }
+    } g_{ev};
+    CU(h, cudaEventRecord(ev[0], s));
+    const uint64_t N = ds.n_res, QN = qs.offs[qs.nq];
+    AlphaMap am;
+    memcpy(am.m, p->alpha_map, 24);
+    // query bytes and distances
+    CUALLOC(h, h->sc_qsb, QN + 64);
+    CUALLOC(h, h->sc_qfull, QN + 64);
+    CUALLOC(h, h->sc_qrem, QN + 64);
+    CUALLOC(h, h->sc_qdst, QN + 64);
+    CUALLOC(h, h->sc_tmp, QN + 64);
+    if (q_mask) CU(h, cudaMemcpyAsync(h->sc_tmp.p, q_mask, QN, cudaMemcpyHostToDevice, s));
+    CU(h, cudaMemsetAsync(h->sc_qsb.p, kQSent, QN + 64, s));
+    if (QN) {
+        k_query_bytes<<<nblocks(QN, 256), 256, 0, s>>>(qs.codes.as<uint8_t>(), q_mask ? h->sc_tmp.as<uint8_t>() : nullptr,
+                                                       QN, am, h->sc_qsb.as<uint8_t>(), h->sc_qfull.as<uint8_t>());
+        k_dists<<<nblocks(QN, 256), 256, 0, s>>>(qs.offsets.as<uint64_t>(), qs.nq, QN, h->sc_qrem.as<uint8_t>(),
+                                                 h->sc_qdst.as<uint8_t>());
+        CU(h, cudaGetLastError());
+    }
+    if (region_thr) {
+        CUALLOC(h, h->sc_rthr, (uint64_t)qs.nq * 4 + 4);
+        CU(h, cudaMemcpyAsync(h->sc_rthr.p, region_thr, (uint64_t)qs.nq * 4, cudaMemcpyHostToDevice, s));
+    }
+    CUALLOC(h, h->sc_ctr, 32 * 8);
+    unsigned long long* ctr = h->sc_ctr.as<unsigned long long>();
+    CU(h, cudaMemsetAsync(ctr, 0, 32 * 8, s));
+    // survivors buffer (grown and the scan redone on overflow)
+    uint64_t scap = std::max<uint64_t>(1 << 20, h->sc_surv.cap / 8);
+    uint64_t nsurv = 0;
+    const int cfil = (int)(minspan / 2);
+    CU(h, cudaEventRecord(ev[1], s));
+    for (int attempt = 0; attempt < 8; attempt++) {
+        CUALLOC(h, h->sc_surv, scap * 8);
+        CU(h, cudaMemsetAsync(ctr, 0, 32 * 8, s));
+        for (uint32_t si = 0; si < p->nshapes; si++) {
+            const uint64_t nc = ncodes_of(p, si);
+            const ShapeDev sh = shape_dev(p, si);
+            const unsigned long long* freq = h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si];
+            CUALLOC(h, h->sc_qcnt, (nc + 1) * 4);
+            CUALLOC(h, h->sc_qoff, (nc + 1) * 4);
+            CUALLOC(h, h->sc_qpres, ((nc + 63) / 64) * 8 + 8);
+            CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, (nc + 1) * 4, s));
+            CU(h, cudaMemsetAsync(h->sc_qpres.p, 0, ((nc + 63) / 64) * 8 + 8, s));
+            if (QN)
+                k_query_seeds<0><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
+                                                                  sh, p->alpha_size, freq, h->sc_qcnt.as<uint32_t>(),
+                                                                  nullptr, nullptr, ctr);
+            size_t tb = 0;
+            CU(h, cub::DeviceScan::ExclusiveSum(nullptr, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
+                                                (int)(nc + 1), s));
+            CUALLOC(h, h->cub_tmp, tb);
+            tb = h->cub_tmp.cap;
+            CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
+                                                (int)(nc + 1), s));
+            k_presence<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(h->sc_qcnt.as<uint32_t>(), nc,
+                                                                           h->sc_qpres.as<unsigned long long>());
+            uint32_t nseed = 0;
+            CU(h, cudaMemcpyAsync(&nseed, h->sc_qoff.as<uint32_t>() + nc, 4, cudaMemcpyDeviceToHost, s));
+            CU(h, cudaStreamSynchronize(s));
+            CUALLOC(h, h->sc_qent, (uint64_t)nseed * 4 + 4);
+            CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, (nc + 1) * 4, s));
+            if (QN && nseed)
+                k_query_seeds<1><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
+                                                                  sh, p->alpha_size, freq, h->sc_qcnt.as<uint32_t>(),
+                                                                  h->sc_qoff.as<uint32_t>(), h->sc_qent.as<uint32_t>(),
+                                                                  ctr);
+            if (!nseed || !N) continue;
+            ScanArgs a;
+            a.sb = h->sc_sb.as<uint8_t>();
+            a.res = ds.res.as<uint8_t>();
+            a.rem = h->sc_rem.as<uint8_t>();
+            a.dst = h->sc_dst.as<uint8_t>();
+            a.N = N;
+            a.pres = h->sc_qpres.as<unsigned long long>();
+            a.qoff = h->sc_qoff.as<uint32_t>();
+            a.qent = h->sc_qent.as<uint32_t>();
+            a.qsb = h->sc_qsb.as<uint8_t>();
+            a.qfull = h->sc_qfull.as<uint8_t>();
+            a.qrem = h->sc_qrem.as<uint8_t>();
+            a.qdst = h->sc_qdst.as<uint8_t>();
+            a.cfil = cfil;
+            a.min_ids = p->hit_filter_min_ids;
+            a.kx = p->hit_filter_exact_weight;
+            a.shape = si;
+            a.surv = h->sc_surv.as<uint2>();
+            a.nsurv = ctr + 10;
+            a.cap = scap;
+            a.ctr = ctr;
+            k_scan<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(a, sh, p->alpha_size);
+            CU(h, cudaGetLastError());
+        }
+        unsigned long long hc[16];
+        CU(h, cudaMemcpyAsync(hc, ctr, 16 * 8, cudaMemcpyDeviceToHost, s));
+        CU(h, cudaStreamSynchronize(s));
+        nsurv = hc[10];
+        local.seed_positions = hc[0];
+        local.seeds_frequent_skipped = hc[1];
+        local.hits = hc[2];
+        local.hits_filtered = hc[3];
+        if (nsurv <= scap) break;
+        scap = nsurv + nsurv / 4 + 1024;
+        if (attempt == 7) return fail(h, SABER_ERR_NOMEM, "survivor buffer did not converge");
+    }
+    if (nsurv >= (1ull << 31)) return fail(h, SABER_ERR_ARG, "too many survivors in one batch");
+    const uint32_t ns = (uint32_t)nsurv;
+    CU(h, cudaEventRecord(ev[2], s));
+    uint64_t nregions = 0;
+    std::vector<saber_region> regs;
+    if (ns) {
+        CUALLOC(h, h->sc_key1, (uint64_t)ns * 8);
+        CUALLOC(h, h->sc_key1o, (uint64_t)ns * 8);
+        CUALLOC(h, h->sc_key2, (uint64_t)ns * 4);
+        CUALLOC(h, h->sc_key2o, (uint64_t)ns * 4);
+        CUALLOC(h, h->sc_val, (uint64_t)ns * 4);
+        CUALLOC(h, h->sc_valo, (uint64_t)ns * 4);
+        CUALLOC(h, h->sc_flags, (uint64_t)ns + 8);
+        CUALLOC(h, h->sc_chains, (uint64_t)ns * 4 + 8);
+        k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(), ds.nsub,
+                                                     qs.offsets.as<uint64_t>(), qs.nq, h->sc_key1.as<unsigned long long>(),
+                                                     h->sc_key2.as<uint32_t>(), h->sc_val.as<uint32_t>());
+        // stable two-key order: by (query position, shape), then by (subject, query, diagonal)
+        size_t t1 = 0, t2 = 0, t3 = 0;
+        CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t1, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
+                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, 32, s));
+        CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t2, h->sc_key1o.as<unsigned long long>(),
+                                              h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
+                                              h->sc_val.as<uint32_t>(), (int)ns, 0, 64, s));
+        CU(h, cub::DeviceSelect::Flagged(nullptr, t3, thrust::counting_iterator<uint32_t>(0), h->sc_flags.as<uint8_t>(),
+                                         h->sc_chains.as<uint32_t>(), h->sc_ctr.as<uint32_t>() + 40, (int)ns, s));
+        CUALLOC(h, h->cub_tmp, std::max(t1, std::max(t2, t3)));
+        size_t tb = h->cub_tmp.cap;
+        CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
+                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, 32, s));
+        k_gather_key1<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(), ns,
+                                                       h->sc_key1o.as<unsigned long long>());
+        CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key1o.as<unsigned long long>(),
+                                              h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
+                                              h->sc_val.as<uint32_t>(), (int)ns, 0, 64, s));
+        // chains: runs of one (subject, query, diagonal)
+        k_run_flags<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), ns, 0, h->sc_flags.as<uint8_t>());
+        uint32_t* nchains = h->sc_ctr.as<uint32_t>() + 40;
+        CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
+                                         h->sc_flags.as<uint8_t>(), h->sc_chains.as<uint32_t>(), nchains, (int)ns, s));
+        uint64_t hcap = std::max<uint64_t>(1024, ns);
+        CUALLOC(h, h->sc_hsp, hcap * 16);
+        CUALLOC(h, h->sc_hkey, hcap * 8);
+        CUALLOC(h, h->sc_hkeyo, hcap * 8);
+        CUALLOC(h, h->sc_hval, hcap * 4);
+        CUALLOC(h, h->sc_hvalo, hcap * 4);
+        ChainArgs c;
+        c.surv = h->sc_surv.as<uint2>();
+        c.order = h->sc_val.as<uint32_t>();
+        c.key1s = h->sc_key1.as<unsigned long long>();
+        c.starts = h->sc_chains.as<uint32_t>();
+        c.nchains = nchains;
+        c.nsurv = ns;
+        c.soffs = ds.soff.as<uint64_t>();
+        c.qoffs = qs.offsets.as<uint64_t>();
+        c.res = ds.res.as<uint8_t>();
+        c.prof = qs.prof.as<int16_t>();
+        c.prof_off = qs.prof_off.as<uint64_t>();
+        c.prof_mpad = qs.prof_mpad.as<uint32_t>();
+        c.thr = p->hsp_threshold;
+        c.x = p->x_drop;
+        c.hsp = h->sc_hsp.as<uint4>();
+        c.hkey = h->sc_hkey.as<unsigned long long>();
+        c.hval = h->sc_hval.as<uint32_t>();
+        c.nhsp = ctr + 11;
+        c.hcap = hcap;
+        c.ctr = ctr;
+        k_chains<<<nblocks(ns, 128), 128, 0, s>>>(c);
+        CU(h, cudaGetLastError());
+        unsigned long long nh = 0;
+        CU(h, cudaMemcpyAsync(&nh, ctr + 11, 8, cudaMemcpyDeviceToHost, s));
+        CU(h, cudaStreamSynchronize(s));
+        if (nh > hcap) return fail(h, SABER_ERR_DEVICE, "HSP buffer overflow");
+        CU(h, cudaEventRecord(ev[3], s));
+        const uint32_t nhsp = (uint32_t)nh;
+        if (nhsp) {
+            size_t t4 = 0;
+            CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t4, h->sc_hkey.as<unsigned long long>(),
+                                                  h->sc_hkeyo.as<unsigned long long>(), h->sc_hval.as<uint32_t>(),
+                                                  h->sc_hvalo.as<uint32_t>(), (int)nhsp, 0, 64, s));
+            CUALLOC(h, h->cub_tmp, t4);
+            tb = h->cub_tmp.cap;
+            CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_hkey.as<unsigned long long>(),
+                                                  h->sc_hkeyo.as<unsigned long long>(), h->sc_hval.as<uint32_t>(),
+                                                  h->sc_hvalo.as<uint32_t>(), (int)nhsp, 0, 64, s));
+            CUALLOC(h, h->sc_pairs, (uint64_t)nhsp * 4 + 8);
+            k_run_flags<<<nblocks(nhsp, 256), 256, 0, s>>>(h->sc_hkeyo.as<unsigned long long>(), nhsp, 20,
+                                                           h->sc_flags.as<uint8_t>());
+            uint32_t* npairs = h->sc_ctr.as<uint32_t>() + 42;
+            CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
+                                             h->sc_flags.as<uint8_t>(), h->sc_pairs.as<uint32_t>(), npairs, (int)nhsp, s));
+            uint64_t rcap = (uint64_t)nhsp + 16;
+            CUALLOC(h, h->sc_regions, rcap * sizeof(saber_region));
+            RegionArgs r;
+            r.hsp = h->sc_hsp.as<uint4>();
+            r.order = h->sc_hvalo.as<uint32_t>();
+            r.hkeys = h->sc_hkeyo.as<unsigned long long>();
+            r.starts = h->sc_pairs.as<uint32_t>();
+            r.npairs = npairs;
+            r.nhsp = nhsp;
+            r.region_thr = region_thr ? h->sc_rthr.as<int32_t>() : nullptr;
+            r.hsp_thr = p->hsp_threshold;
+            r.join = 2 * (int64_t)p->window_slack;
+            r.kmax = std::max<uint32_t>(1, p->max_regions_per_subject);
+            r.out = h->sc_regions.as<saber_region>();
+            r.nout = ctr + 12;
+            r.cap = rcap;
+            r.ctr = ctr;
+            k_regions<<<nblocks(nhsp, 128), 128, 0, s>>>(r);
+            CU(h, cudaGetLastError());
+            unsigned long long nr = 0;
+            CU(h, cudaMemcpyAsync(&nr, ctr + 12, 8, cudaMemcpyDeviceToHost, s));
+            CU(h, cudaStreamSynchronize(s));
+            nregions = std::min<uint64_t>(nr, rcap);
+            regs.resize(nregions);
+            if (nregions)
+                CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions.p, nregions * sizeof(saber_region), cudaMemcpyDeviceToHost,
+                                      s));
+        }
+    } else {
+        CU(h, cudaEventRecord(ev[3], s));
+    }
+    CU(h, cudaEventRecord(ev[4], s));
+    unsigned long long hc[16];
+    CU(h, cudaMemcpyAsync(hc, ctr, 16 * 8, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaStreamSynchronize(s));
+    local.ungapped_extensions = hc[4];
+    local.extensions_avoided = hc[5];
+    local.xdrop_steps = hc[6];
+    local.hsps = hc[7];
+    local.regions_weak_dropped = hc[8];
+    // per query: region_order (engine.rs:493-495), cap at max_candidates
+    std::sort(regs.begin(), regs.end(), [](const saber_region& a, const saber_region& b) {
+        if (a.query != b.query) return a.query < b.query;
+        if (a.best != b.best) return a.best > b.best;
+        if (a.subject != b.subject) return a.subject < b.subject;
+        if (a.d_min != b.d_min) return a.d_min < b.d_min;
+        return a.d_max < b.d_max;
+    });
+    const uint64_t cap = std::max<uint32_t>(1, p->max_candidates);
+    uint64_t w = 0;
+    size_t i = 0;
+    bool overflow = false;
+    while (i < regs.size()) {
+        size_t j = i;
+        while (j < regs.size() && regs[j].query == regs[i].query) j++;
+        const uint64_t take = std::min<uint64_t>(j - i, cap);
+        local.regions_dropped_by_cap += (j - i) - take;
+        for (uint64_t k = 0; k < take; k++) {
+            if (w < out_cap) out[w] = regs[i + k];
+            else overflow = true;
+            w++;
+        }
+        i = j;
+    }
+    local.regions = w;
+    local.t_tables_ms = 0;
+    local.t_scan_ms = ev_ms(ev[1], ev[2]);
+    local.t_visit_ms = ev_ms(ev[2], ev[3]);
+    local.t_regions_ms = ev_ms(ev[3], ev[4]);
+    if (n_out) *n_out = w;
+    if (st) *st = local;
+    if (overflow) return fail(h, SABER_ERR_ARG, "region buffer too small: %llu regions", (unsigned long long)w);
+    return SABER_OK;
+}
+
+}  // namespace saber

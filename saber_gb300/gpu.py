@@ -61,6 +61,58 @@ def _alignment_dict(a, ops):
                 s_start=int(a.s_start), s_end=int(a.s_end), cells=int(a.cells), ops=runs)
 
 
+class ScanParams(ctypes.Structure):
+    """saber_scan_params (include/saber_gpu.h)."""
+    _fields_ = [("alpha_map", ctypes.c_uint8 * 24), ("alpha_size", ctypes.c_uint32), ("nshapes", ctypes.c_uint32),
+                ("shape_span", ctypes.c_uint32 * 32), ("shape_weight", ctypes.c_uint32 * 32),
+                ("shape_off", (ctypes.c_uint16 * 16) * 32), ("hit_filter_min_ids", ctypes.c_uint32),
+                ("hit_filter_exact_weight", ctypes.c_uint32), ("hsp_threshold", ctypes.c_int32),
+                ("x_drop", ctypes.c_int32), ("window_slack", ctypes.c_int32),
+                ("max_regions_per_subject", ctypes.c_uint32), ("max_candidates", ctypes.c_uint32),
+                ("seed_max_occ", ctypes.c_uint64), ("ref_db_residues", ctypes.c_uint64), ("db_length", ctypes.c_uint64)]
+
+
+class ScanStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "seed_positions", "seeds_frequent_skipped", "hits", "hits_filtered", "ungapped_extensions",
+        "extensions_avoided", "xdrop_steps", "hsps", "regions", "regions_weak_dropped", "regions_dropped_by_cap")] + [
+        (n, ctypes.c_double) for n in ("t_tables_ms", "t_scan_ms", "t_visit_ms", "t_regions_ms")]
+
+    def as_dict(self):
+        return {n: (float(getattr(self, n)) if n.startswith("t_") else int(getattr(self, n))) for n, _ in self._fields_}
+
+
+REGION_DTYPE = np.dtype([("query", "<u4"), ("subject", "<u4"), ("d_min", "<i4"), ("d_max", "<i4"), ("best", "<i4")])
+
+
+def scan_params(alpha_map, alpha_size, shapes, min_ids=27, exact_weight=2, hsp_threshold=40, x_drop=20,
+                window_slack=64, max_regions_per_subject=4, max_candidates=5000, seed_max_occ=0,
+                ref_db_residues=40_000_000, db_length=0):
+    """Fill saber_scan_params from shape patterns ("11110111", ...)."""
+    p = ScanParams()
+    for i in range(24):
+        p.alpha_map[i] = int(alpha_map[i])
+    p.alpha_size = int(alpha_size)
+    p.nshapes = len(shapes)
+    for si, sh in enumerate(shapes):
+        offs = [i for i, ch in enumerate(sh) if ch == "1"]
+        p.shape_span[si] = len(sh)
+        p.shape_weight[si] = len(offs)
+        for k, o in enumerate(offs):
+            p.shape_off[si][k] = o
+    p.hit_filter_min_ids = min_ids
+    p.hit_filter_exact_weight = exact_weight
+    p.hsp_threshold = hsp_threshold
+    p.x_drop = x_drop
+    p.window_slack = window_slack
+    p.max_regions_per_subject = max_regions_per_subject
+    p.max_candidates = max_candidates
+    p.seed_max_occ = seed_max_occ
+    p.ref_db_residues = ref_db_residues
+    p.db_length = db_length
+    return p
+
+
 class ScoreStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "jobs", "banded_cells", "fast_cells", "fast_jobs", "generic_jobs", "i16_rescored", "empty_jobs",
@@ -105,6 +157,8 @@ def load_library():
         "saber_gpu_banded_align": (ctypes.c_int, [P, P, U64, U64, P, P, U64]),
         "saber_gpu_banded_align_one": (ctypes.c_int, [P, P, U32, P, P, U32, I64, I64, U64, I32, P, P, U64]),
         "saber_gpu_traceback": (ctypes.c_int, [P, P, U64, I32, U64, P, P, U64, P]),
+        "saber_gpu_load_db_mask": (ctypes.c_int, [P, P, U64]),
+        "saber_gpu_scan": (ctypes.c_int, [P, P, P, P, P, U64, P, P]),
         "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
@@ -260,6 +314,29 @@ class Device:
                                                  out, _ptr(ops), cap, ctypes.byref(st)), "traceback")
         res = [None if out[t].status == 0 else _alignment_dict(out[t], ops) for t in range(jobs.size)]
         return res, st.as_dict()
+
+    def load_db_mask(self, mask):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        self._check(self.lib.saber_gpu_load_db_mask(self.h, _ptr(m), 0 if m is None else m.size), "load_db_mask")
+
+    def scan(self, params, q_mask=None, region_thr=None, out_cap=None):
+        """Candidate regions of the loaded query set (REGION_DTYPE, ordered by query and region order)."""
+        qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+        rt = None if region_thr is None else np.ascontiguousarray(region_thr, dtype=np.int32)
+        cap = out_cap or 1 << 20
+        for _ in range(4):
+            out = np.zeros(cap, REGION_DTYPE)
+            n = ctypes.c_uint64()
+            st = ScanStats()
+            rc = self.lib.saber_gpu_scan(self.h, ctypes.byref(params), _ptr(qm), _ptr(rt), _ptr(out), cap,
+                                         ctypes.byref(n), ctypes.byref(st))
+            if rc == 0:
+                return out[:n.value].copy(), st.as_dict()
+            if n.value > cap:
+                cap = int(n.value)
+                continue
+            self._check(rc, "scan")
+        self._check(rc, "scan")
 
     @property
     def strip_rows(self):

@@ -1,0 +1,62 @@
+"""GPU parity of the scan schedule (seed tables, database scan, window filter,
+coverage + X-drop, regions, caps): the candidate regions and the work
+counters equal the oracle's restatement of Engine::search_scan."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from saber_gb300 import presets, synth
+from saber_gb300.gpu import scan_params
+from saber_gb300.scoring import matrix
+
+pytestmark = pytest.mark.gpu
+B62 = matrix("BLOSUM62")
+COUNTERS = ("seed_positions", "seeds_frequent_skipped", "hits", "hits_filtered", "ungapped_extensions",
+            "extensions_avoided", "xdrop_steps", "hsps", "regions", "regions_weak_dropped", "regions_dropped_by_cap")
+
+
+def _run(dev, qs, ss, bias, db_mask, q_mask, region_thr, shapes, alpha, **kw):
+    amap, asz = alpha
+    gp = scan_params(amap, asz, shapes, db_length=int(ss.codes.size), **kw)
+    op = orc.make_scan_params(amap, asz, shapes, db_length=int(ss.codes.size), **kw)
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_db_mask(db_mask)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    got, gst = dev.scan(gp, q_mask, region_thr)
+    want, ost = orc.scan_regions(ss.codes, ss.offsets, db_mask, qs.codes, qs.offsets, bias, q_mask, region_thr, B62, op)
+    return got, gst, want, ost
+
+
+def _check(got, gst, want, ost):
+    assert got.size == want.size, (got.size, want.size)
+    for f in ("query", "subject", "d_min", "d_max", "best"):
+        assert np.array_equal(got[f], want[f]), f
+    for k in COUNTERS:
+        assert gst[k] == ost[k], (k, gst[k], ost[k])
+
+
+@pytest.mark.parametrize("preset", ["default", "very-fast", "sensitive"])
+def test_scan_regions_match_oracle(dev, preset):
+    qs, ss, planted = synth.protein_db(7, 16, 1500)
+    bias = synth.query_bias(8, qs)
+    rng = np.random.default_rng(9)
+    q_mask = (rng.random(qs.codes.size) < 0.05).astype(np.uint8)
+    db_mask = (rng.random(ss.codes.size) < 0.03).astype(np.uint8)
+    region_thr = rng.integers(40, 70, size=len(qs)).astype(np.int32)
+    _, shapes, ids, kx, thr, cand, _, _, _, _ = presets.PRESETS[preset]
+    got, gst, want, ost = _run(dev, qs, ss, bias, db_mask, q_mask, region_thr, shapes, presets.alphabet_map(),
+                               min_ids=ids, exact_weight=kx, hsp_threshold=thr, max_candidates=cand)
+    assert want.size > 0
+    _check(got, gst, want, ost)
+
+
+def test_scan_caps_and_no_filter(dev):
+    """Small frequent-seed cap, no window filter, tiny per-subject and
+    per-query region caps, full 20-letter alphabet with contiguous seeds."""
+    qs, ss, planted = synth.protein_db(17, 10, 800)
+    got, gst, want, ost = _run(dev, qs, ss, None, None, None, None, ["1111", "11011"], presets.full_alphabet(),
+                               min_ids=0, exact_weight=0, seed_max_occ=6, max_regions_per_subject=2,
+                               max_candidates=7)
+    assert ost["seeds_frequent_skipped"] > 0 and ost["regions_dropped_by_cap"] > 0
+    _check(got, gst, want, ost)
