@@ -2,6 +2,8 @@
 has the reference tree; the fixtures are committed and the tests only read
 them).
 
+* saber_gb300/data/karlin.json — the NCBI blast_stat.c gapped
+  Karlin-Altschul tables as listed in src/scoring/stats.rs.
 * matrices.json — the substitution tables of src/scoring/matrices.rs (the
   public NCBI BLOSUM/PAM tables in NCBI order ARNDCQEGHILKMFPSTWYVBZX*),
   parsed from the reference source; also copied to saber_gb300/data/.
@@ -43,6 +45,27 @@ def parse_matrices(ref_root):
         mat = [[int(v) for v in r.split(",") if v.strip()] for r in rows]
         assert len(mat) == 24 and all(len(r) == 24 for r in mat), name
         out[name] = mat
+    return out
+
+
+def parse_karlin(ref_root):
+    """The NCBI blast_stat.c Karlin-Altschul tables of src/scoring/stats.rs:
+    rows (existence, extension, lambda, K, H, alpha, beta)."""
+    src = open(os.path.join(ref_root, "src/scoring/stats.rs")).read()
+    row = r"Row\(\s*(-?\d+),\s*(-?\d+),\s*([-\d.eE]+),\s*([-\d.eE]+),\s*([-\d.eE]+),\s*([-\d.eE]+),\s*([-\d.eE]+)\)"
+    out = {"protein": {}, "nucleotide": []}
+    for name in NAMES.values():
+        u = re.search(r"const UNGAPPED_%s: Row = %s;" % (name, row), src)
+        t = re.search(r"const %s: &\[Row\] = &\[(.*?)\];" % name, src, re.S)
+        rows = [[int(m[0]), int(m[1])] + [float(x) for x in m[2:]] for m in re.findall(row, t.group(1))]
+        out["protein"][name] = {"ungapped": [int(u.group(1)), int(u.group(2))] + [float(u.group(k)) for k in range(3, 8)],
+                                "gapped": rows}
+    nt = re.search(r"const NT_TABLES: &\[NtTable\] = &\[(.*?)\n\];", src, re.S).group(1)
+    for m in re.finditer(r"NtTable \{ reward: (-?\d+), penalty: (-?\d+), even_only: (true|false), rows: &\[(.*?)\] \}",
+                         nt, re.S):
+        rows = [[int(x[0]), int(x[1])] + [float(y) for y in x[2:]] for x in re.findall(row, m.group(4))]
+        out["nucleotide"].append({"reward": int(m.group(1)), "penalty": int(m.group(2)),
+                                  "even_only": m.group(3) == "true", "rows": rows})
     return out
 
 
@@ -136,6 +159,8 @@ def main():
     data_dir = os.path.join(REPO, "saber_gb300", "data")
     os.makedirs(data_dir, exist_ok=True)
     shutil.copy(os.path.join(HERE, "matrices.json"), os.path.join(data_dir, "matrices.json"))
+    with open(os.path.join(data_dir, "karlin.json"), "w") as f:
+        json.dump(parse_karlin(a.ref_root), f)
 
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref",
                            "REF_ROOT=%s" % a.ref_root])
