@@ -4,6 +4,9 @@ them).
 
 * saber_gb300/data/karlin.json — the NCBI blast_stat.c gapped
   Karlin-Altschul tables as listed in src/scoring/stats.rs.
+* defects.json — the reference's defect-reproduction inputs
+  (bench/defects/*.fa) and the outputs its v1.2.0 binary recorded for them
+  (bench/results/v1.2.0/defects.json).
 * matrices.json — the substitution tables of src/scoring/matrices.rs (the
   public NCBI BLOSUM/PAM tables in NCBI order ARNDCQEGHILKMFPSTWYVBZX*),
   parsed from the reference source; also copied to saber_gb300/data/.
@@ -66,6 +69,34 @@ def parse_karlin(ref_root):
         rows = [[int(x[0]), int(x[1])] + [float(y) for y in x[2:]] for x in re.findall(row, m.group(4))]
         out["nucleotide"].append({"reward": int(m.group(1)), "penalty": int(m.group(2)),
                                   "even_only": m.group(3) == "true", "rows": rows})
+    return out
+
+
+def read_fasta(path):
+    recs, name, seq = [], None, []
+    for line in open(path):
+        line = line.strip()
+        if line.startswith(">"):
+            if name is not None:
+                recs.append((name, "".join(seq)))
+            name, seq = line[1:].split()[0], []
+        elif line:
+            seq.append(line)
+    if name is not None:
+        recs.append((name, "".join(seq)))
+    return recs
+
+
+def defect_cases(ref_root):
+    """bench/defects/*.fa with the outputs the reference binary (v1.2.0)
+    recorded for them in bench/results/v1.2.0/defects.json."""
+    rec = json.load(open(os.path.join(ref_root, "bench/results/v1.2.0/defects.json")))
+    out = []
+    for name in ("gap", "amb", "amb2", "long", "sat"):
+        q = read_fasta(os.path.join(ref_root, "bench/defects/%s_q.fa" % name))
+        d = read_fasta(os.path.join(ref_root, "bench/defects/%s_db.fa" % name))
+        runs = {k: v for k, v in rec[name].items() if k.startswith("v1.2.0") and "score" in v}
+        out.append({"name": name, "query": q, "db": d, "recorded": runs})
     return out
 
 
@@ -161,6 +192,10 @@ def main():
     shutil.copy(os.path.join(HERE, "matrices.json"), os.path.join(data_dir, "matrices.json"))
     with open(os.path.join(data_dir, "karlin.json"), "w") as f:
         json.dump(parse_karlin(a.ref_root), f)
+
+    with open(os.path.join(HERE, "defects.json"), "w") as f:
+        json.dump({"source": "bench/defects/*.fa and bench/results/v1.2.0/defects.json", "cases": defect_cases(a.ref_root)},
+                  f, indent=0)
 
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref",
                            "REF_ROOT=%s" % a.ref_root])
