@@ -51,7 +51,11 @@ def test_gpu_search_reproduces_recorded_hit(dev, case, run, want):
     from saber_gb300.search import Searcher, SearchParams
     q = encode_protein(case["query"][0][1])
     s = encode_protein(case["db"][0][1])
-    P = SearchParams("default", comp_bias="--comp-bias off" not in run)
+    # sat (4000 W): every Murphy-10 seed of the run has the same code, which
+    # the 1.4 frequent-seed cap drops (v1.2.0 seeded differently); the
+    # exhaustive preset scores the pair without seeding
+    preset = "exhaustive" if case["name"] == "sat" else "default"
+    P = SearchParams(preset, comp_bias="--comp-bias off" not in run)
     se = Searcher(dev, s, np.array([0, len(s)], np.uint64), P)
     hits = se.search(q, np.array([0, len(q)], np.uint64))[0]
     assert len(hits) == 1
