@@ -60,22 +60,28 @@ struct PackedConsts {
     uint32_t ngo2, nge2, neg2;
 };
 
-// One cell pair of one row: updates E (row state), computes F and H.
-__device__ __forceinline__ void cell(uint32_t& E, uint32_t Hleft, uint32_t Hup, uint32_t Fup,
+// One cell pair of one row.  E and F are carried shifted by the gap-open
+// cost, X = E + go and Y = F + go, so that each updates with one fused DPX op:
+//   X(i,j) = max(X(i,j-1) - ge, H(i,j-1))
+//   Y(i,j) = max(Y(i-1,j) - ge, H(i-1,j))
+//   H(i,j) = max(max(X, Y) - go, H(i-1,j-1) + S, 0)
+// X and Y never fall below kNeg16 (H >= kNeg16 everywhere), and where the
+// reference holds E or F at its NEG sentinel (the band's first cell, row 0)
+// these hold values <= 0, which no H can tell apart (H is clamped at 0).
+__device__ __forceinline__ void cell(uint32_t& X, uint32_t Hleft, uint32_t Hup, uint32_t Yup,
                                      uint32_t diag, uint32_t sub, const PackedConsts& c,
-                                     uint32_t& H, uint32_t& F) {
-    uint32_t ee = __viaddmax_s16x2(E, c.nge2, c.neg2);      // max(E - ge, NEG)
-    E = __viaddmax_s16x2(Hleft, c.ngo2, ee);                // max(H(i,j-1) - go, ...)
-    uint32_t fe = __viaddmax_s16x2(Fup, c.nge2, c.neg2);
-    F = __viaddmax_s16x2(Hup, c.ngo2, fe);                  // max(H(i-1,j) - go, ...)
-    uint32_t ef = __vimax_s16x2_relu(E, F);                 // max(E, F, 0)
-    H = __viaddmax_s16x2_relu(diag, sub, ef);               // max(diag + S, E, F, 0)
+                                     uint32_t& H, uint32_t& Y) {
+    X = __viaddmax_s16x2(X, c.nge2, Hleft);
+    Y = __viaddmax_s16x2(Yup, c.nge2, Hup);
+    const uint32_t z = __vimax_s16x2_relu(X, Y);
+    const uint32_t ds = __viaddmax_s16x2(diag, sub, c.neg2);
+    H = __viaddmax_s16x2_relu(z, c.ngo2, ds);
 }
 
 template <int R>
 struct StripState {
     uint32_t Hd[R];  // H(row r, previous column)
-    uint32_t E[R];   // E(row r, previous column)
+    uint32_t X[R];   // E(row r, previous column) + go
 };
 
 // One job of a half: its window, clipped band and rows.
@@ -128,7 +134,7 @@ template <int R>
 struct StepLoads {
     uint4 a[R / 8];
     uint4 b[R / 8];
-    uint2 top;  // (H, F) of the row above at band offset u + 1
+    uint2 top;  // (H, F + go) of the row above at band offset u + 1
 };
 
 template <int R>
@@ -169,27 +175,31 @@ template <int R, int MODE, int U>
 __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, uint2* __restrict__ buf, int u,
                                            const StepLoads<R>& L, const PackedConsts& c, uint32_t& best,
                                            int thr_a, int thr_b) {
-    uint32_t Hup = L.top.x, Fup = L.top.y;
+    uint32_t Hup = L.top.x, Yup = L.top.y;
     uint32_t diag = diag0;
     diag0 = L.top.x;
+    uint32_t hprev = 0;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (MODE == 0 && r > U) break;
-        uint32_t H, F;
+        uint32_t H, Y;
         uint32_t hold = st.Hd[r];
-        cell(st.E[r], hold, Hup, Fup, diag, sub_of<R>(L, r), c, H, F);
+        cell(st.X[r], hold, Hup, Yup, diag, sub_of<R>(L, r), c, H, Y);
         if (MODE == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
             H = (H & mk) | (c.neg2 & ~mk);
-            F = (F & mk) | (c.neg2 & ~mk);
+            Y = (Y & mk) | (c.neg2 & ~mk);
         }
         diag = hold;
         st.Hd[r] = H;
         Hup = H;
-        Fup = F;
-        best = __vimax_s16x2_relu(best, H);
+        Yup = Y;
+        // running best over row pairs: one three-input max per two rows
+        if (r & 1) best = __vimax3_s16x2_relu(best, hprev, H);
+        else if (r == R - 1 || (MODE == 0 && r == U)) best = __vimax_s16x2_relu(best, H);
+        else hprev = H;
     }
-    if (MODE != 0 || U == R - 1) __stcg(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Fup));
+    if (MODE != 0 || U == R - 1) __stcg(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Yup));
 }
 
 // The pipelined column loop state of one strip: the loads of step u + 1 and
@@ -290,8 +300,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         if (!has_b) B.w = wmin;
 
         // Boundary of the row above each job's first strip: H = 0 (the
-        // reference's hd = 0 on row 0), F unreachable; position wmax lies
-        // outside every band.
+        // reference's hd = 0 on row 0), F + go unreachable; position wmax
+        // lies outside every band.
         for (int k = 0; k < wmax; k++) __stcg(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
         __stcg(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
 
@@ -302,7 +312,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 st.Hd[r] = c.neg2;
-                st.E[r] = c.neg2;
+                st.X[r] = c.neg2;
             }
             uint32_t diag0 = __ldcg(mybuf).x;
             Pipe<R> p;

@@ -127,16 +127,53 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
             }
         }
     }
-    atomicAdd(&counts[0], c0);
-    atomicAdd(&counts[7], c1);
-    atomicAdd(&counts[1], c2);
-    atomicAdd(&counts[4], c3);
-    atomicAdd(&stats[0], (unsigned long long)cells);
-    atomicMax(&stats[1], w0);
-    atomicMax(&stats[2], w2);
-    atomicAdd(&stats[3], (unsigned long long)bad);
-    atomicAdd(&stats[4], (unsigned long long)fcells);
-    atomicMax(&stats[5], w1);
+    // block totals in shared memory, then one global atomic per counter and block
+    __shared__ unsigned long long b_sum[4];  // cells, bad, fast cells, unused
+    __shared__ unsigned long long b_max[3];  // w0, w2, w1
+    __shared__ uint32_t b_cnt[4];            // c0, c1, c2, c3
+    if (threadIdx.x < 4) {
+        b_sum[threadIdx.x] = 0;
+        b_cnt[threadIdx.x] = 0;
+        if (threadIdx.x < 3) b_max[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    c0 = __reduce_add_sync(0xffffffffu, c0);
+    c1 = __reduce_add_sync(0xffffffffu, c1);
+    c2 = __reduce_add_sync(0xffffffffu, c2);
+    c3 = __reduce_add_sync(0xffffffffu, c3);
+    bad = __reduce_add_sync(0xffffffffu, bad);
+    for (int o = 16; o > 0; o >>= 1) {
+        cells += __shfl_xor_sync(0xffffffffu, cells, o);
+        fcells += __shfl_xor_sync(0xffffffffu, fcells, o);
+        w0 = max(w0, __shfl_xor_sync(0xffffffffu, w0, o));
+        w1 = max(w1, __shfl_xor_sync(0xffffffffu, w1, o));
+        w2 = max(w2, __shfl_xor_sync(0xffffffffu, w2, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&b_cnt[0], c0);
+        atomicAdd(&b_cnt[1], c1);
+        atomicAdd(&b_cnt[2], c2);
+        atomicAdd(&b_cnt[3], c3);
+        atomicAdd(&b_sum[0], (unsigned long long)cells);
+        atomicAdd(&b_sum[1], (unsigned long long)bad);
+        atomicAdd(&b_sum[2], (unsigned long long)fcells);
+        atomicMax(&b_max[0], w0);
+        atomicMax(&b_max[1], w2);
+        atomicMax(&b_max[2], w1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(&counts[0], b_cnt[0]);
+        atomicAdd(&counts[7], b_cnt[1]);
+        atomicAdd(&counts[1], b_cnt[2]);
+        atomicAdd(&counts[4], b_cnt[3]);
+        atomicAdd(&stats[0], b_sum[0]);
+        atomicMax(&stats[1], b_max[0]);
+        atomicMax(&stats[2], b_max[1]);
+        atomicAdd(&stats[3], b_sum[1]);
+        atomicAdd(&stats[4], b_sum[2]);
+        atomicMax(&stats[5], b_max[2]);
+    }
 }
 
 
