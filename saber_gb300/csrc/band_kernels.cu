@@ -45,8 +45,8 @@ __device__ __forceinline__ int lo16(uint32_t v) { return (int)(int16_t)(v & 0xFF
 __device__ __forceinline__ int hi16(uint32_t v) { return (int)(int16_t)(v >> 16); }
 
 // R int16 sentinel profile entries: the profile of a half whose job has no
-// strip left (16-byte aligned for the vector loads).
-__device__ __align__(16) int16_t g_sent_profile[64] = {
+// strip left (32-byte aligned for the vector loads).
+__device__ __align__(32) int16_t g_sent_profile[64] = {
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
@@ -124,9 +124,29 @@ __device__ __forceinline__ HalfStrip half_strip(const HalfJob& h, int t, int R) 
     return v;
 }
 
-__device__ __forceinline__ int load_code(const HalfStrip& h, int u) {
-    int col = h.col0 + u;
-    return ((unsigned)col < (unsigned)h.n) ? (int)__ldg(h.win + col) : kSentCode;
+// Residue codes of steps u .. u + 3 of a strip (window columns col0 + u ..),
+// one byte each, the sentinel code outside the window.  Interior groups take
+// one or two aligned 32-bit loads; the residue buffer is padded past its end,
+// so the second word never leaves the allocation.
+__device__ __forceinline__ uint32_t code_word(const HalfStrip& h, int u) {
+    const int c = h.col0 + u;
+    if (c >= 0 && c + 4 <= h.n) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(h.win + c);
+        const uint32_t* p = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+        const uint32_t sh = (uint32_t)(a & 3u) * 8u;
+        const uint32_t w0 = __ldg(p);
+        const uint32_t w1 = sh ? __ldg(p + 1) : 0u;
+        return __funnelshift_r(w0, w1, sh);
+    }
+    if (c + 4 <= 0 || c >= h.n) return 0x01010101u * kSentCode;
+    uint32_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int col = c + i;
+        const uint32_t b = ((unsigned)col < (unsigned)h.n) ? (uint32_t)__ldg(h.win + col) : (uint32_t)kSentCode;
+        r |= b << (8 * i);
+    }
+    return r;
 }
 
 // Raw profile vectors of one step for both halves (R/8 x 16 bytes each).
@@ -137,15 +157,26 @@ struct StepLoads {
     uint2 top;  // (H, F + go) of the row above at band offset u + 1
 };
 
+// 32-byte read-only load (sm_100 and later): one request per lane for the
+// 16 profile rows of a step.
+__device__ __forceinline__ void ld256(uint4& lo, uint4& hi, const void* p) {
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(lo.x), "=r"(lo.y), "=r"(lo.z), "=r"(lo.w), "=r"(hi.x), "=r"(hi.y), "=r"(hi.z), "=r"(hi.w)
+        : "l"(p));
+}
+
 template <int R>
 __device__ __forceinline__ void fetch_step(StepLoads<R>& L, const HalfStrip& ha, const HalfStrip& hb, int ca,
                                            int cb, const uint2* __restrict__ buf, int kin) {
-    const uint4* pa = reinterpret_cast<const uint4*>(ha.rows + (size_t)ca * ha.mpad);
-    const uint4* pb = reinterpret_cast<const uint4*>(hb.rows + (size_t)cb * hb.mpad);
-#pragma unroll
-    for (int g = 0; g < R / 8; g++) {
-        L.a[g] = __ldg(pa + g);
-        L.b[g] = __ldg(pb + g);
+    const int16_t* pa = ha.rows + (size_t)ca * ha.mpad;
+    const int16_t* pb = hb.rows + (size_t)cb * hb.mpad;
+    if constexpr (R == 16) {
+        ld256(L.a[0], L.a[1], pa);
+        ld256(L.b[0], L.b[1], pb);
+    } else {
+        static_assert(R == 8, "strip rows are 8 or 16");
+        L.a[0] = __ldg(reinterpret_cast<const uint4*>(pa));
+        L.b[0] = __ldg(reinterpret_cast<const uint4*>(pb));
     }
     L.top = __ldcg(buf + (size_t)kin * 32);  // boundary rows live in L2, not L1
 }
@@ -202,23 +233,34 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
     if (MODE != 0 || U == R - 1) __stcg(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Yup));
 }
 
-// The pipelined column loop state of one strip: the loads of step u + 1 and
-// the residue codes of step u + 2 are in flight while step u computes.
+// The pipelined column loop state of one strip: the loads of step u + 1 are
+// in flight while step u computes; the residue codes come four steps to a
+// word, the word of the next group loaded a group ahead.
 template <int R>
 struct Pipe {
     StepLoads<R> cur, nxt;
-    int ca2, cb2;  // codes of step u + 2
+    uint32_t wa, wb;    // codes of the group of step u + 1 (byte i: step 4g + i)
+    uint32_t wa2, wb2;  // codes of the group after it
 };
 
-template <int R>
+// Called before computing step u: cur <- nxt (step u), issue step u + 1.
+// K = (u + 1) & 3 when known at compile time, else -1.
+template <int R, int K>
 __device__ __forceinline__ void pipe_advance(Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
                                              const uint2* buf, int u, int wmax) {
-    // called before computing step u: cur <- nxt (step u), issue step u + 1
     p.cur = p.nxt;
-    int k1 = u + 2 <= wmax ? u + 2 : wmax;
-    fetch_step<R>(p.nxt, ha, hb, p.ca2, p.cb2, buf, k1);
-    p.ca2 = load_code(ha, u + 2);
-    p.cb2 = load_code(hb, u + 2);
+    const int v = u + 1;
+    const int k = K >= 0 ? K : (v & 3);
+    if (k == 0) {
+        p.wa = p.wa2;
+        p.wb = p.wb2;
+        p.wa2 = code_word(ha, v + 4);
+        p.wb2 = code_word(hb, v + 4);
+    }
+    const uint32_t sel = 0x4440u | (uint32_t)k;
+    const int ca = (int)__byte_perm(p.wa, 0u, sel), cb = (int)__byte_perm(p.wb, 0u, sel);
+    const int k1 = u + 2 <= wmax ? u + 2 : wmax;
+    fetch_step<R>(p.nxt, ha, hb, ca, cb, buf, k1);
 }
 
 template <int R, int U>
@@ -227,7 +269,7 @@ struct LeftTriangle {
                                                Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
                                                const PackedConsts& c, uint32_t& best) {
         LeftTriangle<R, U - 1>::run(st, diag0, buf, wmax, p, ha, hb, c, best);
-        pipe_advance<R>(p, ha, hb, buf, U, wmax);
+        pipe_advance<R, (U + 1) & 3>(p, ha, hb, buf, U, wmax);
         strip_step<R, 0, U>(st, diag0, buf, U, p.cur, c, best, 0, 0);
     }
 };
@@ -317,21 +359,30 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
             uint32_t diag0 = __ldcg(mybuf).x;
             Pipe<R> p;
             {
-                int ca0 = load_code(ha, 0), cb0 = load_code(hb, 0);
-                fetch_step<R>(p.nxt, ha, hb, ca0, cb0, mybuf, 1);
-                p.ca2 = load_code(ha, 1);
-                p.cb2 = load_code(hb, 1);
+                p.wa = code_word(ha, 0);
+                p.wb = code_word(hb, 0);
+                p.wa2 = code_word(ha, 4);
+                p.wb2 = code_word(hb, 4);
+                fetch_step<R>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf, 1);
             }
             LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
+            // middle steps (every row in band for every half), four at a time
+            // so that the code bytes are selected at compile time
             int u = R;
-#pragma unroll 2
-            for (; u < wmin; u++) {
-                pipe_advance<R>(p, ha, hb, mybuf, u, wmax);
+            for (; u + 4 <= wmin; u += 4) {
+                pipe_advance<R, 1>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
+                pipe_advance<R, 2>(p, ha, hb, mybuf, u + 1, wmax);
+                strip_step<R, 1, 0>(st, diag0, mybuf, u + 1, p.cur, c, best, 0, 0);
+                pipe_advance<R, 3>(p, ha, hb, mybuf, u + 2, wmax);
+                strip_step<R, 1, 0>(st, diag0, mybuf, u + 2, p.cur, c, best, 0, 0);
+                pipe_advance<R, 0>(p, ha, hb, mybuf, u + 3, wmax);
+                strip_step<R, 1, 0>(st, diag0, mybuf, u + 3, p.cur, c, best, 0, 0);
             }
+            // the rest, with the right-edge masks (all ones while u < wmin)
             const int uend = wmax + R - 1;
             for (; u < uend; u++) {
-                pipe_advance<R>(p, ha, hb, mybuf, u, wmax);
+                pipe_advance<R, -1>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);
             }
         }
