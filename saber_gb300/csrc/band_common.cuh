@@ -12,6 +12,12 @@ namespace saber {
 // (tuning); query profiles are padded to the largest.
 constexpr int kStripRows = 16;
 constexpr int kStripRowsMin = 8;
+// Query profiles are padded to a multiple of the paired kernel's super-strip
+// (2 x 16 rows).
+constexpr int kProfPad = 32;
+// Default pairing threshold: a job whose R-row sweep takes more than this
+// many column steps (strips x (width + R - 1)) is swept as paired strips.
+constexpr uint32_t kPairStepsDefault = 8192;
 // Residue code used for positions outside a window or a query: its profile
 // entries are kSent, so such cells never beat a real cell (banded.rs:123-131
 // excludes them; the kernels compute them harmlessly instead of branching).
@@ -66,6 +72,7 @@ struct FastArgs {
     const saber_band_job* jobs;
     const uint32_t* order;  // sorted job indices of this launch's class
     const uint32_t* n_ptr;  // device count of those jobs
+    const uint32_t* np_ptr; // device count of the paired jobs among them (at the end), or null
     uint32_t* wt_counter;
     uint2* bufs;
     uint32_t buf_stride;

@@ -279,6 +279,100 @@ struct LeftTriangle<R, -1> {
                                                const HalfStrip&, const PackedConsts&, uint32_t&) {}
 };
 
+// ---- paired strips (one job per lane) --------------------------------------
+// A job whose sweep as R-row strips would be long takes a whole lane: the
+// lane sweeps super-strips of 2R rows, rows 0 .. R-1 in the low halves and
+// rows R .. 2R-1 in the high halves one column behind, so the high half's row
+// above (the low half's last row) comes from the previous step's registers
+// and its residue code is the low half's code of the previous step.  The
+// boundary buffer then carries one job per lane: 32-bit words H | (F + go) << 16
+// of the super-strip's last row.  A warp task is 32 such jobs; the job's
+// critical path is about half of its R-row sweep.
+template <int R>
+struct PairPipe {
+    StepLoads<R> cur, nxt;  // top.x: boundary word of the low half's row above
+    uint32_t w, w2;         // code words of the low half: group of step g + 1, next group
+    int cprev;              // low half's code at step g (the high half's at step g + 1)
+};
+
+// Called before computing step g: cur <- nxt (step g), issue step g + 1.
+template <int R, int K>
+__device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha, const int16_t* hb_rows,
+                                             const uint32_t* pbuf, int g, int wmax) {
+    p.cur = p.nxt;
+    const int v = g + 1;
+    const int k = K >= 0 ? K : (v & 3);
+    if (k == 0) {
+        p.w = p.w2;
+        p.w2 = code_word(ha, v + 4);
+    }
+    const int ca = (int)__byte_perm(p.w, 0u, 0x4440u | (uint32_t)k);
+    const int cb = p.cprev;
+    p.cprev = ca;
+    const int kin = g + 2 <= wmax ? g + 2 : wmax;
+    ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca * ha.mpad);
+    ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb * ha.mpad);
+    p.nxt.top.x = __ldcg(pbuf + (size_t)kin * 32);
+}
+
+// One step g of a super-strip.  PH 0: compile-time step G <= 2R (low rows
+// r > G not yet in band, high rows r > G - R - 1 not yet in band); PH 1: every
+// row of both halves in band; PH 2: right-edge masks from the thresholds.
+template <int R, int PH, int G>
+__device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, uint32_t& lastH, uint32_t& lastY,
+                                          uint32_t* __restrict__ pbuf, int g, const StepLoads<R>& L,
+                                          const PackedConsts& c, uint32_t& best, int thr_a, int thr_b) {
+    const uint32_t top = L.top.x;
+    uint32_t Hup = __byte_perm(top, lastH, 0x5410);
+    uint32_t Yup = __byte_perm(top, lastY, 0x5432);
+    uint32_t diag = diag0;
+    diag0 = Hup;
+    uint32_t hprev = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        if (PH == 0 && r > G) break;
+        uint32_t H, Y;
+        uint32_t hold = st.Hd[r];
+        cell(st.X[r], hold, Hup, Yup, diag, sub_of<R>(L, r), c, H, Y);
+        if (PH == 0 && r > G - R - 1) {
+            H = (H & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
+            Y = (Y & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
+        }
+        if (PH == 2) {
+            uint32_t mk = ragged_mask(r, thr_a, thr_b);
+            H = (H & mk) | (c.neg2 & ~mk);
+            Y = (Y & mk) | (c.neg2 & ~mk);
+        }
+        diag = hold;
+        st.Hd[r] = H;
+        Hup = H;
+        Yup = Y;
+        if (r & 1) best = __vimax3_s16x2_relu(best, hprev, H);
+        else if (r == R - 1 || (PH == 0 && r == G)) best = __vimax_s16x2_relu(best, H);
+        else hprev = H;
+    }
+    lastH = Hup;
+    lastY = Yup;
+    if (g >= 2 * R) __stcg(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Hup, Yup, 0x7632));
+}
+
+template <int R, int G>
+struct PairTriangle {
+    __device__ __forceinline__ static void run(PairPipe<R>& p, StripState<R>& st, uint32_t& diag0, uint32_t& lastH,
+                                               uint32_t& lastY, uint32_t* pbuf, int wmax, const HalfStrip& ha,
+                                               const int16_t* hb_rows, const PackedConsts& c, uint32_t& best) {
+        PairTriangle<R, G - 1>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
+        pair_advance<R, (G + 1) & 3>(p, ha, hb_rows, pbuf, G, wmax);
+        pair_step<R, 0, G>(st, diag0, lastH, lastY, pbuf, G, p.cur, c, best, 0, 0);
+    }
+};
+template <int R>
+struct PairTriangle<R, -1> {
+    __device__ __forceinline__ static void run(PairPipe<R>&, StripState<R>&, uint32_t&, uint32_t&, uint32_t&,
+                                               uint32_t*, int, const HalfStrip&, const int16_t*,
+                                               const PackedConsts&, uint32_t&) {}
+};
+
 __device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, const int16_t* prof,
                                           const uint64_t* prof_off, const uint32_t* prof_mpad,
                                           const uint64_t* qoffs, const uint8_t* res, int R) {
@@ -299,6 +393,78 @@ __device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, c
     h.ns = (int)(last / R - first / R + 1);
 }
 
+// One paired task: sorted positions [32t, 32t + 32) of the paired range,
+// lane l takes position 32t + l.
+template <int R>
+__device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
+                                       const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
+                                       const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
+                                       const uint32_t* __restrict__ porder, uint32_t n_pair, uint32_t task, int lane,
+                                       uint32_t* __restrict__ pbuf, const PackedConsts& c,
+                                       int32_t* __restrict__ scores, uint32_t* __restrict__ rescue,
+                                       uint32_t* __restrict__ rescue_count) {
+    const uint32_t pos = task * 32 + lane;
+    const bool has = pos < n_pair;
+    const uint32_t jidx = has ? porder[pos] : 0u;
+    HalfJob J{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0};
+    if (has) load_half(J, jobs[jidx], prof, prof_off, prof_mpad, qoffs, res, 2 * R);
+    const int big = 1 << 30;
+    const int wmin = __reduce_min_sync(0xffffffffu, has ? J.w : big);
+    const int wmax = __reduce_max_sync(0xffffffffu, has ? J.w : 0);
+    const int nsmax = __reduce_max_sync(0xffffffffu, J.ns);
+    if (!has) J.w = wmin;
+    const uint32_t top0 = (uint32_t)(uint16_t)kNeg16 << 16;  // H = 0, F + go unreachable
+    for (int k = 0; k < wmax; k++) __stcg(pbuf + (size_t)k * 32, top0);
+    __stcg(pbuf + (size_t)wmax * 32, c.neg2);
+
+    uint32_t best = 0;
+    const int gend = wmax + 2 * R;
+    for (int t = 0; t < nsmax; t++) {
+        const HalfStrip ha = half_strip(J, t, 2 * R);
+        const int16_t* hb_rows = ha.rows + R;
+        StripState<R> st;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            st.Hd[r] = c.neg2;
+            st.X[r] = c.neg2;
+        }
+        uint32_t diag0 = __byte_perm(__ldcg(pbuf), c.neg2, 0x5410);
+        uint32_t lastH = c.neg2, lastY = c.neg2;
+        PairPipe<R> p;
+        {
+            p.w = code_word(ha, 0);
+            p.w2 = code_word(ha, 4);
+            const int ca0 = (int)(p.w & 0xFFu);
+            ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
+            ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)kSentCode * ha.mpad);
+            p.nxt.top.x = __ldcg(pbuf + 32);
+            p.cprev = ca0;
+        }
+        PairTriangle<R, 2 * R>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
+        int g = 2 * R + 1;
+        // (g + 1) & 3 runs 2, 3, 0, 1 from g = 2R + 1 (R a multiple of 4)
+        for (; g + 4 <= wmin; g += 4) {
+            pair_advance<R, 2>(p, ha, hb_rows, pbuf, g, wmax);
+            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g, p.cur, c, best, 0, 0);
+            pair_advance<R, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
+            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 1, p.cur, c, best, 0, 0);
+            pair_advance<R, 0>(p, ha, hb_rows, pbuf, g + 2, wmax);
+            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 2, p.cur, c, best, 0, 0);
+            pair_advance<R, 1>(p, ha, hb_rows, pbuf, g + 3, wmax);
+            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 3, p.cur, c, best, 0, 0);
+        }
+        for (; g < gend; g++) {
+            pair_advance<R, -1>(p, ha, hb_rows, pbuf, g, wmax);
+            pair_step<R, 2, 0>(st, diag0, lastH, lastY, pbuf, g, p.cur, c, best, g - J.w + 1, g - R - J.w);
+        }
+    }
+    const int sc = max(lo16(best), hi16(best));
+    if (has) {
+        if (sc >= kLimit16) rescue[atomicAdd(rescue_count, 1u)] = jidx;
+        else scores[jidx] = sc;
+    }
+}
+
 // Persistent warps over warp tasks: task t = sorted positions [64t, 64t + 64)
 // of the fast class, taken largest first; lane l takes positions 64t + 2l
 // (low half) and 64t + 2l + 1 (high half).
@@ -307,13 +473,18 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
     const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
     const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
-    const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_ptr,
+    const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_ptr, const uint32_t* __restrict__ np_ptr,
     uint32_t* __restrict__ wt_counter, uint2* __restrict__ bufs, uint32_t buf_stride, int go, int ge,
     int32_t* __restrict__ scores, uint32_t* __restrict__ rescue, uint32_t* __restrict__ rescue_count) {
     const int lane = threadIdx.x & 31;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint2* mybuf = bufs + (size_t)gwarp * buf_stride * 32 + lane;
-    const uint32_t n_fast = *n_ptr;
+    // sorted positions [0, n_fast - n_pair): R-row strips, two jobs per lane;
+    // [n_fast - n_pair, n_fast): paired strips, one job per lane
+    const uint32_t n_all = *n_ptr;
+    const uint32_t n_pair = (R == 16 && np_ptr) ? *np_ptr : 0u;
+    const uint32_t n_fast = n_all - n_pair;
+    const uint32_t n_ptasks = (n_pair + 31) / 32;
     const uint32_t n_wtasks = (n_fast + 63) / 64;
     PackedConsts c;
     c.ngo2 = pk2(-go);
@@ -324,9 +495,19 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         uint32_t wt = 0;
         if (lane == 0) wt = atomicAdd(wt_counter, 1u);
         wt = __shfl_sync(0xffffffffu, wt, 0);
-        if (wt >= n_wtasks) break;
-        // largest tasks first: the sort order is ascending in strips and width
-        const uint32_t task = n_wtasks - 1 - wt;
+        if (wt >= n_ptasks + n_wtasks) break;
+        // largest tasks first: paired tasks, then R-row tasks; each sorted
+        // range is ascending in strips and width
+        bool paired = false;
+        if constexpr (R == 16) paired = wt < n_ptasks;
+        if (paired) {
+            if constexpr (R == 16)
+                pair_task<R>(res, prof, prof_off, prof_mpad, qoffs, jobs, order + n_fast, n_pair, n_ptasks - 1 - wt,
+                             lane, reinterpret_cast<uint32_t*>(bufs + (size_t)gwarp * buf_stride * 32) + lane, c,
+                             scores, rescue, rescue_count);
+            continue;
+        }
+        const uint32_t task = n_wtasks - 1 - (wt - n_ptasks);
         const uint32_t pa = task * 64 + 2 * lane, pb = pa + 1;
         const bool has_a = pa < n_fast, has_b = pb < n_fast;
         const uint32_t ja_idx = has_a ? order[pa] : 0u;
@@ -503,11 +684,11 @@ int band_fast_blocks_per_sm(int strip_rows) {
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a) {
     if (a.strip_rows == 8)
         k_band_fast<8><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                            a.n_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                            a.n_ptr, a.np_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                             a.rescue, a.rescue_count);
     else
         k_band_fast<16><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                             a.n_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                             a.n_ptr, a.np_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                              a.rescue, a.rescue_count);
     return cudaGetLastError();
 }

@@ -81,6 +81,7 @@ struct saber_gpu {
     std::string err;
     int sm_count = 0;
     int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
+    uint32_t pair_steps = saber::kPairStepsDefault;  // tuning: paired-strip threshold
     // the handle's scheme and dataset (set_scheme / load_db / load_queries)
     saber::Scheme scheme;
     saber::Dataset main;

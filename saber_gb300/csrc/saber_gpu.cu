@@ -62,9 +62,10 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
 // stats layout (uint64): 0 cells, 1 wmax of the R-row class, 2 wmax of the
 //   int32 class, 3 bad job count, 4 cells of the packed classes, 5 wmax of
 //   the 8-row class
-// counts layout (uint32): 0 jobs in the R-row class, 1 int32 class, 4 empty,
-//   5 int32 list length (class + rescued), 6 task counter of the R-row launch,
-//   7 jobs in the 8-row class, 8 task counter of the 8-row launch
+// counts layout (uint32): 0 jobs in the R-row class (paired ones included),
+//   1 int32 class, 4 empty, 5 int32 list length (class + rescued), 6 task
+//   counter of the R-row launch, 7 jobs in the 8-row class, 8 task counter of
+//   the 8-row launch, 9 paired jobs of the R-row class
 //
 // Classes (the top two key bits, so the sort makes them contiguous):
 //   0: width >= R (R = the handle's strip rows), packed int16 kernel with R rows
@@ -72,15 +73,16 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
 //   2: narrower bands and out-of-range sizes, int32 kernel
 //   3: empty jobs (score 0, written here)
 // Packed-class keys order jobs by (strips, width, query) so that the 64
-// consecutive jobs of a warp task share their loop counts and widths.
-__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, int R,
+// consecutive jobs of a warp task share their loop counts and widths; within
+// class 0 the paired jobs (bit 61; their strips counted in 2R rows) sort last.
+__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, int R, uint32_t pair_steps,
                            const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
                            uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                            int32_t* __restrict__ scores, uint32_t* __restrict__ counts,
                            unsigned long long* __restrict__ stats) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t cells = 0, fcells = 0;
-    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, bad = 0;
+    uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, cp = 0, bad = 0;
     unsigned long long w0 = 0, w1 = 0, w2 = 0;
     for (; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
         saber_band_job j = jobs[t];
@@ -109,14 +111,22 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
             cls = 1;
             rows = kStripRowsMin;
         }
-        const int64_t ns = last / rows - first / rows + 1;
-        if (cls != 2 && (w >= (1 << 16) || ns >= (1 << 14))) cls = 2;
+        int64_t ns = last / rows - first / rows + 1;
+        // long R-row sweeps go to paired strips (one job per lane, 2R rows)
+        uint64_t pair = 0;
+        if (cls == 0 && R == kStripRows && w >= 2 * R + 1 && (uint64_t)ns * (uint64_t)(w + R - 1) > pair_steps) {
+            pair = 1;
+            ns = last / (2 * R) - first / (2 * R) + 1;
+        }
+        if (cls != 2 && (w >= (1 << 16) || ns >= (1 << 13))) cls = 2;
         if (cls == 2) {
             keys[t] = (2ull << 62) | t;
             c2++;
             w2 = max(w2, (unsigned long long)w);
         } else {
-            keys[t] = ((uint64_t)cls << 62) | ((uint64_t)ns << 48) | ((uint64_t)w << 32) | (uint64_t)j.query;
+            keys[t] = ((uint64_t)cls << 62) | (pair << 61) | ((uint64_t)ns << 48) | ((uint64_t)w << 32) |
+                      (uint64_t)j.query;
+            cp += (uint32_t)pair;
             fcells += jc;
             if (cls == 0) {
                 c0++;
@@ -130,10 +140,10 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
     // block totals in shared memory, then one global atomic per counter and block
     __shared__ unsigned long long b_sum[4];  // cells, bad, fast cells, unused
     __shared__ unsigned long long b_max[3];  // w0, w2, w1
-    __shared__ uint32_t b_cnt[4];            // c0, c1, c2, c3
+    __shared__ uint32_t b_cnt[5];            // c0, c1, c2, c3, paired
+    if (threadIdx.x < 5) b_cnt[threadIdx.x] = 0;
     if (threadIdx.x < 4) {
         b_sum[threadIdx.x] = 0;
-        b_cnt[threadIdx.x] = 0;
         if (threadIdx.x < 3) b_max[threadIdx.x] = 0;
     }
     __syncthreads();
@@ -141,6 +151,7 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
     c1 = __reduce_add_sync(0xffffffffu, c1);
     c2 = __reduce_add_sync(0xffffffffu, c2);
     c3 = __reduce_add_sync(0xffffffffu, c3);
+    cp = __reduce_add_sync(0xffffffffu, cp);
     bad = __reduce_add_sync(0xffffffffu, bad);
     for (int o = 16; o > 0; o >>= 1) {
         cells += __shfl_xor_sync(0xffffffffu, cells, o);
@@ -154,6 +165,7 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
         atomicAdd(&b_cnt[1], c1);
         atomicAdd(&b_cnt[2], c2);
         atomicAdd(&b_cnt[3], c3);
+        atomicAdd(&b_cnt[4], cp);
         atomicAdd(&b_sum[0], (unsigned long long)cells);
         atomicAdd(&b_sum[1], (unsigned long long)bad);
         atomicAdd(&b_sum[2], (unsigned long long)fcells);
@@ -167,6 +179,7 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
         atomicAdd(&counts[7], b_cnt[1]);
         atomicAdd(&counts[1], b_cnt[2]);
         atomicAdd(&counts[4], b_cnt[3]);
+        atomicAdd(&counts[9], b_cnt[4]);
         atomicAdd(&stats[0], b_sum[0]);
         atomicMax(&stats[1], b_max[0]);
         atomicMax(&stats[2], b_max[1]);
@@ -217,7 +230,8 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, h->strip_rows, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res, h->keys_in.as<uint64_t>(),
+        d_jobs, njobs, h->strip_rows, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
+        h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
     CU(h, cudaGetLastError());
     local.kernel_launches++;
@@ -281,6 +295,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.jobs = d_jobs;
         a.order = order + (pass == 0 ? 0 : n_fast);
         a.n_ptr = counts + (pass == 0 ? 0 : 7);
+        a.np_ptr = pass == 0 ? counts + 9 : nullptr;
         a.wt_counter = counts + (pass == 0 ? 6 : 8);
         a.bufs = h->bufs.as<uint2>();
         a.buf_stride = stride;
@@ -362,8 +377,8 @@ static int load_queries(saber_gpu* h, const Scheme& sch, QuerySet& q, const uint
     uint64_t acc = 0;
     for (uint32_t i = 0; i < nq; i++) {
         uint64_t m = offsets[i + 1] - offsets[i];
-        uint64_t mpad = (m + kStripRows - 1) / kStripRows * kStripRows;
-        if (mpad == 0) mpad = kStripRows;
+        uint64_t mpad = (m + kProfPad - 1) / kProfPad * kProfPad;
+        if (mpad == 0) mpad = kProfPad;
         if (mpad > (1ull << 30)) return fail(h, SABER_ERR_ARG, "query %u too long", i);
         poff[i] = acc;
         pm[i] = (uint32_t)mpad;
@@ -1017,6 +1032,14 @@ int saber_gpu_set_strip_rows(saber_gpu* h, int32_t strip_rows) {
 }
 
 int32_t saber_gpu_get_strip_rows(saber_gpu* h) { return h ? h->strip_rows : 0; }
+
+int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps) {
+    ENTER(h);
+    h->pair_steps = steps;
+    return SABER_OK;
+}
+
+uint32_t saber_gpu_get_pair_steps(saber_gpu* h) { return h ? h->pair_steps : 0u; }
 
 int saber_gpu_banded_align(saber_gpu* h, const saber_align_job* jobs, uint64_t njobs, uint64_t max_dir_bytes,
                            saber_alignment* out, uint32_t* ops, uint64_t ops_cap) {

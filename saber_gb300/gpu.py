@@ -160,6 +160,8 @@ def load_library():
         "saber_gpu_load_db_mask": (ctypes.c_int, [P, P, U64]),
         "saber_gpu_scan": (ctypes.c_int, [P, P, P, P, P, U64, P, P]),
         "saber_gpu_get_strip_rows": (I32, [P]),
+        "saber_gpu_set_pair_steps": (ctypes.c_int, [P, U32]),
+        "saber_gpu_get_pair_steps": (U32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
     for name, (res, args) in sig.items():
@@ -345,6 +347,15 @@ class Device:
     @strip_rows.setter
     def strip_rows(self, r):
         self._check(self.lib.saber_gpu_set_strip_rows(self.h, int(r)), "set_strip_rows")
+
+    @property
+    def pair_steps(self):
+        """Paired-strip threshold in column steps (0xFFFFFFFF: never pair)."""
+        return int(self.lib.saber_gpu_get_pair_steps(self.h))
+
+    @pair_steps.setter
+    def pair_steps(self, v):
+        self._check(self.lib.saber_gpu_set_pair_steps(self.h, int(v) & 0xFFFFFFFF), "set_pair_steps")
 
     def probe_int_peak(self):
         """(DPX s16x2 lane-instructions/s, int32 max lane-instructions/s) of this GPU."""

@@ -47,14 +47,30 @@ def test_golden_vectors_through_score_backend():
         assert list(got) == c["expected"], c["matrix"]
 
 
-@pytest.mark.parametrize("strip_rows", [8, 16])
+PAIR_DEFAULT = 8192
+PAIR_NEVER = 0xFFFFFFFF
+
+# (strip rows, paired-strip threshold): 8-row strips; 16-row strips with the
+# default threshold; every job of width > 32 as paired strips; no pairing
+KERNEL_MODES = [(8, PAIR_DEFAULT), (16, PAIR_DEFAULT), (16, 0), (16, PAIR_NEVER)]
+
+
+@pytest.fixture
+def tuned(dev):
+    yield dev
+    dev.strip_rows = 16
+    dev.pair_steps = PAIR_DEFAULT
+
+
+@pytest.mark.parametrize("mode", KERNEL_MODES)
 @pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8)])
-def test_random_band_jobs_match_oracle(dev, gaps, strip_rows):
+def test_random_band_jobs_match_oracle(tuned, gaps, mode):
+    dev = tuned
     go, ge = gaps
     qs, ss, planted = synth.protein_db(100 + go, 40, 3000)
     bias = synth.query_bias(7, qs)
     jobs = synth.band_jobs(200 + ge, qs, ss, planted, 6000, half_min=1, half_max=140)
-    dev.strip_rows = strip_rows
+    dev.strip_rows, dev.pair_steps = mode
     dev.set_scheme(B62, go, ge)
     dev.load_db(ss.codes, ss.offsets)
     dev.load_queries(qs.codes, qs.offsets, bias)
@@ -83,9 +99,12 @@ def test_device_resident_path_matches_host_path(dev):
     assert np.array_equal(host, want), _report(host, want, jobs)
 
 
-def test_int16_overflow_is_rescored_exactly(dev):
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+def test_int16_overflow_is_rescored_exactly(tuned, mode):
     """Scores above the int16 range: W x 4000 (44 000, banded.rs:716-731) and
     300 W (3300, band_simd8.rs:454-468) next to ordinary jobs."""
+    dev = tuned
+    dev.strip_rows, dev.pair_steps = mode
     w4000 = np.full(4000, 17, np.uint8)
     w300 = np.full(300, 17, np.uint8)
     other = encode_protein("MKVLAAGIVGKLLA")
@@ -98,9 +117,12 @@ def test_int16_overflow_is_rescored_exactly(dev):
     assert got[0] == 44000
 
 
-def test_score_banded_many_reference_cases(dev):
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+def test_score_banded_many_reference_cases(tuned, mode):
     """band_simd8.rs:403-451 cases (same LCG): BLOSUM62/PAM30/BLOSUM45, gaps
     11/1 and 7/2, bands up to 200 wide, with and without bias."""
+    dev = tuned
+    dev.strip_rows, dev.pair_steps = mode
     for sysname in ("BLOSUM62", "PAM30", "BLOSUM45"):
         mx = matrix(sysname)
         r = Lcg(7)
@@ -132,9 +154,12 @@ def test_score_banded_many_reference_cases(dev):
                 assert list(got) == want, (sysname, trial, go, ge)
 
 
-def test_edge_cases(dev):
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+def test_edge_cases(tuned, mode):
     """Empty windows and queries, bands outside the rectangle, one-residue
     queries, bands wider than the rectangle, codes >= 24 (scored as X)."""
+    dev = tuned
+    dev.strip_rows, dev.pair_steps = mode
     rng = np.random.default_rng(5)
     q = rng.integers(0, 24, 37).astype(np.uint8)
     cases = [
@@ -159,13 +184,16 @@ def test_edge_cases(dev):
     assert list(got1) == [orc.banded_score(one, q, None, B62, 11, 1, -3, 40)[0], 11]
 
 
-def test_wide_full_window_bands(dev):
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+def test_wide_full_window_bands(tuned, mode):
     """Full-rectangle plans (band covers the window) of long pairs."""
+    dev = tuned
+    dev.strip_rows, dev.pair_steps = mode
     qs, ss, planted = synth.protein_db(31, 6, 40, max_len=1500)
     dev.set_scheme(B62, 11, 1)
     for qi in range(len(qs)):
         q = qs.seq(qi)
         subs = [ss.seq(k) for k in range(len(ss))]
-        got = CudaBackend(0).score_windows(q, None, subs, B62, (11, 1))
+        got = dev.score_windows(q, None, subs, B62, 11, 1)
         want = [orc.banded_score(q, s, None, B62, 11, 1, -q.size, s.size)[0] for s in subs]
         assert list(got) == want
