@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample size (seconds of work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--strip-rows", type=int, default=16, help="rows per strip of the int16 kernel (8 or 16)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep --strip-rows and the default pairing")
     return ap.parse_args()
 
 
@@ -57,8 +58,7 @@ def config_dict(a, world):
     return {"workload": "sw-scoring-microbench: %d banded regions, %d queries x %d subjects, half-widths 8-128, "
                         "BLOSUM62 11/1, query bias" % (a.jobs, a.queries, a.subjects),
             "jobs_per_gpu": a.jobs, "queries": a.queries, "subjects": a.subjects, "seed": a.seed,
-            "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world,
-            "strip_rows": a.strip_rows}
+            "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas x%d" % world}
 
 
 class Clocks:
@@ -189,6 +189,11 @@ def run_ours(a, rank, world, local_rank):
     for _ in range(a.warmup):
         step_dev()
     torch.cuda.synchronize()
+    tuned = None
+    if not a.no_autotune:
+        from saber_gb300.tune import autotune_scoring
+        tuned = autotune_scoring(dev, d_jobs, d_scores)
+    torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clocks = Clocks(local_rank)
@@ -244,10 +249,15 @@ def run_ours(a, rank, world, local_rank):
     fast_s = fast_ms * 1e-3
     achieved = fast_cells * ALGO_OPS_PER_CELL / fast_s / 1e12 if fast_s > 0 else None
     peak = dpx_peak * 2 / 1e12
+    cfg = config_dict(a, world)
+    cfg["strip_rows"] = dev.strip_rows
+    cfg["pair_steps"] = dev.pair_steps
+    if tuned is not None:
+        cfg["autotune"] = tuned["candidates"]
     out = {"metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": a.steps,
            "warmup": a.warmup, "ms_per_step": round(tot_ms / a.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int16 (int32 rescore)", "data": "synthetic",
-           "config": config_dict(a, world),
+           "config": cfg,
            "e2e": {"value": round(e2e, 2), "unit": "GCUPS", "h2d_bytes_per_step": int(jobs.nbytes),
                    "d2h_bytes_per_step": int(jobs.size * 4), "matches_device_path": same},
            "roofline": {"bound": "int", "kernel": "k_band_fast",

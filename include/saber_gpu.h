@@ -284,7 +284,7 @@ int32_t saber_gpu_get_strip_rows(saber_gpu* h);
 /* Tuning: with 16-row strips, a job of width > 32 whose sweep as 16-row
  * strips takes more than `steps` column steps (strips x (width + 15)) is
  * swept by a whole lane as paired strips (32 rows, half the critical path);
- * 0xFFFFFFFF disables pairing.  Default 8192.  Results do not depend on it.
+ * 0xFFFFFFFF disables pairing.  Default 2048.  Results do not depend on it.
  * No reference counterpart. */
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h);

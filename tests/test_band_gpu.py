@@ -47,7 +47,7 @@ def test_golden_vectors_through_score_backend():
         assert list(got) == c["expected"], c["matrix"]
 
 
-PAIR_DEFAULT = 8192
+PAIR_DEFAULT = 2048
 PAIR_NEVER = 0xFFFFFFFF
 
 # (strip rows, paired-strip threshold): 8-row strips; 16-row strips with the
