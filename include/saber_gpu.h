@@ -275,6 +275,76 @@ int saber_gpu_traceback(saber_gpu* h, const saber_traceback_job* jobs, uint64_t 
                         int32_t band_pad, uint64_t max_dir_bytes, saber_alignment* out,
                         uint32_t* ops, uint64_t ops_cap, saber_traceback_stats* stats);
 
+/* ---- the batch search (host engine over the device stages) ---------------
+ *
+ * saber_gpu_search runs Engine::search_scan for one query batch end to end
+ * (src/search/engine/scan.rs:1261-1497 with the shared Engine stages of
+ * src/search/engine.rs): query preparation (composition bias, statistics,
+ * floors, engine.rs:714-786), the scan (saber_gpu_scan), window plans
+ * (engine.rs:1223-1324), two-stage banded scoring of the whole batch
+ * (engine.rs:1021-1099), finish with E-values, ordering, per-subject and
+ * per-query caps and the widening traceback (engine.rs:1127-1221,1328-1445),
+ * and make_hit (engine.rs:1447-1530).  The f64 statistics run on the host
+ * in the operation order of src/scoring/stats.rs. */
+typedef struct {
+    /* SearchParams (engine.rs:60-201) */
+    double evalue;                 /* -E; <= 0 or inf: no cut */
+    double min_bitscore;           /* NaN: none */
+    uint32_t max_target_seqs, max_hsps;
+    double min_identity, min_query_cover, min_subject_cover;
+    int32_t hsp_threshold;
+    double hsp_floor_fraction;
+    int32_t band_pad, window_slack, score_band, score_prefilter_band;
+    double score_prefilter_frac;
+    uint32_t comp_bias;            /* 1: composition-bias correction (protein) */
+    uint32_t exhaustive;           /* --preset exhaustive: every subject, full rectangle */
+    uint64_t traceback_max_bytes;
+    uint64_t ref_db_residues;
+    uint32_t evalue_model;         /* 0 per-subject, 1 database */
+    uint32_t is_protein;
+    /* gapped Karlin-Altschul parameters of the scheme (stats.rs:277-310) */
+    double lambda, k, h, alpha, beta;
+    uint32_t even_scores_only;
+    uint32_t pad_;
+    /* the scan (its db_length must be the database residues) */
+    saber_scan_params scan;
+} saber_search_params;
+
+/* One reported alignment (Hit, engine.rs:310-357): 1-based inclusive
+ * coordinates; n_ops run-length words (len << 8 | op) at ops[ops_offset..]. */
+typedef struct {
+    uint32_t query, subject;
+    int32_t score;
+    uint32_t exact;
+    double evalue, bitscore;
+    uint32_t q_start, q_end, s_start, s_end;
+    uint32_t columns, matches, mismatches, positives, gap_opens, gap_columns;
+    uint32_t q_len, s_len;
+    uint32_t n_ops, pad_;
+    uint64_t ops_offset;
+} saber_hit;
+
+typedef struct {
+    saber_scan_stats scan;
+    saber_traceback_stats traceback;
+    uint64_t regions;             /* candidate regions after the per-query caps */
+    uint64_t band_scored_regions, band_rescored, banded_cells, score_launches;
+    uint64_t alignments;
+    double t_prep_ms, t_scan_ms, t_plan_ms, t_score_ms, t_finish_ms, t_total_ms;  /* host wall clock */
+} saber_search_stats;
+
+/* Hits of every query of the batch, ordered by query, then (E-value, score
+ * desc, subject, s_start) as the reference reports them.  db_res / db_offsets:
+ * the host copy of the loaded database (make_hit reads residues); q_mask:
+ * one byte per query residue masked from seeding (NULL = none).  Returns
+ * SABER_ERR_CAP with *n_hits / *n_ops set when hits_cap or ops_cap is too
+ * small (nothing else is written then). */
+int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint8_t* db_res,
+                     const uint64_t* db_offsets, uint64_t nsub, const uint8_t* q_codes,
+                     const uint64_t* q_offsets, uint32_t nq, const uint8_t* q_mask, saber_hit* hits,
+                     uint64_t hits_cap, uint64_t* n_hits, uint32_t* ops, uint64_t ops_cap, uint64_t* n_ops,
+                     saber_search_stats* stats);
+
 /* Tuning: rows per strip of the packed int16 scoring kernel (8 or 16,
  * default 16).  Results do not depend on it.  No reference counterpart (the
  * reference's AVX2 kernels have fixed vector widths). */

@@ -10,7 +10,9 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libsaber_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["saber_gpu.cu", "band_kernels.cu", "probe.cu", "noalloc.cu", "traceback.cu", "scan.cu"]
+SOURCES = ["saber_gpu.cu", "band_kernels.cu", "probe.cu", "noalloc.cu", "traceback.cu", "scan.cu", "engine.cpp"]
+# host C++ of the search engine: f64 statistics must round like the reference's (no fused multiply-add)
+HOST_FLAGS = {"engine.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc():
@@ -28,8 +30,8 @@ def build_library(verbose=False):
               "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
 
     def compile_one(src):
-        obj = os.path.join(LIBDIR, "obj", src.replace(".cu", ".o"))
-        cmd = [nvcc] + common + ["-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(LIBDIR, "obj", os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc] + common + HOST_FLAGS.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))

@@ -1,0 +1,851 @@
+// Host engine of the batch search: Engine::search_scan for one query batch
+// (src/search/engine/scan.rs:1261-1497) with the shared Engine stages of
+// src/search/engine.rs, over the device stages of this library (scan,
+// banded scoring, widening traceback).  The host keeps what the reference
+// keeps on its host: query preparation, window plans, the two-stage scoring
+// bookkeeping, the f64 Karlin-Altschul statistics (in the operation order of
+// src/scoring/stats.rs, glibc libm, no contraction: this file is compiled
+// with -ffp-contract=off), finish and make_hit.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <unordered_map>
+#include <vector>
+
+#include "saber_gpu.h"
+
+namespace {
+
+constexpr double kRegionFloorEvalue = 10.0;     // engine.rs:518
+constexpr int64_t kBandScoreMinCells = 1 << 20;  // engine.rs:401
+constexpr int64_t kBandCostRatio = 12;           // engine.rs:402
+constexpr int64_t kBandBridge = 1024;            // engine.rs:404
+constexpr int64_t kI32Max = 2147483647;
+constexpr int64_t kI64Max = std::numeric_limits<int64_t>::max();
+const double kLn2 = std::log(2.0);
+const double kInf = std::numeric_limits<double>::infinity();
+
+// Robinson & Robinson background frequencies per 1000 (src/scoring/bias.rs:32-53)
+constexpr double kRobinson[20] = {78.05, 51.29, 44.87, 53.64, 19.25, 42.64, 62.95, 73.77, 21.99, 51.42,
+                                  90.19, 57.44, 22.43, 38.56, 52.03, 71.20, 58.41, 13.30, 32.16, 64.41};
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ---- statistics (src/scoring/stats.rs) ------------------------------------
+
+// BLAST_ComputeLengthAdjustment (stats.rs:458-520)
+int64_t length_adjustment(double k, double log_k, double adl, double beta, int64_t query_length, int64_t db_length,
+                          int64_t db_num_seqs) {
+    const double m = (double)query_length, n = (double)db_length, nn = (double)db_num_seqs;
+    double ell_min = 0.0, ell_next = 0.0;
+    bool converged = false;
+    const double a = nn;
+    const double mb = m * nn + n;
+    const double c = n * m - std::max(m, n) / k;
+    if (c < 0.0) return 0;
+    double ell_max = 2.0 * c / (mb + std::sqrt(mb * mb - 4.0 * a * c));
+    for (int i = 1; i <= 20; i++) {
+        const double ell = ell_next;
+        const double ss = (m - ell) * (n - nn * ell);
+        const double ell_bar = adl * (log_k + std::log(ss)) + beta;
+        if (ell_bar >= ell) {
+            ell_min = ell;
+            if (ell_bar - ell_min <= 1.0) {
+                converged = true;
+                break;
+            }
+            if (ell_min == ell_max) break;
+        } else {
+            ell_max = ell;
+        }
+        if (ell_min <= ell_bar && ell_bar <= ell_max) ell_next = ell_bar;
+        else ell_next = i == 1 ? ell_max : (ell_min + ell_max) / 2.0;
+    }
+    if (converged) {
+        int64_t adj = (int64_t)ell_min;
+        const double ell = std::ceil(ell_min);
+        if (ell <= ell_max) {
+            const double ss = (m - ell) * (n - nn * ell);
+            if (adl * (log_k + std::log(ss)) + beta >= ell) adj = (int64_t)ell;
+        }
+        return adj;
+    }
+    return (int64_t)ell_min;
+}
+
+struct Karlin {
+    double lambda, k, log_k, adl, beta;
+    bool even;
+};
+
+// QueryStatistics (stats.rs:646-760)
+struct QStats {
+    Karlin p;
+    bool database_model;
+    int64_t query_len;
+    double num_seqs, search_space;
+
+    double adj_score(int64_t raw) const { return (double)(p.even && raw % 2 != 0 ? raw - 1 : raw); }
+    double space_for(int64_t subject_len) const {
+        if (database_model) return search_space;
+        const int64_t m = std::max<int64_t>(query_len, 1), n = std::max<int64_t>(subject_len, 1);
+        int64_t adj = length_adjustment(p.k, p.log_k, p.adl, p.beta, m, n, 1);
+        const int64_t min_l = (int64_t)std::ceil(1.0 / p.k);
+        adj = std::max<int64_t>(std::min(std::min(adj, std::max<int64_t>(m - min_l, 0)), std::max<int64_t>(n - min_l, 0)),
+                                0);
+        return num_seqs * (double)std::max<int64_t>(m - adj, 1) * (double)std::max<int64_t>(n - adj, 1);
+    }
+    double space_lower_bound(int64_t subject_len) const {
+        if (database_model) return search_space;
+        const double m = (double)std::max<int64_t>(query_len, 1), n = (double)std::max<int64_t>(subject_len, 1);
+        const double up = std::ceil(std::max(p.adl * (p.log_k + std::log(m * n)) + p.beta, 0.0));
+        return num_seqs * std::max(m - up, 1.0) * std::max(n - up, 1.0);
+    }
+    double floor_lower_bound(double evalue_cut, bool has_bits, double min_bits, int64_t subject_len,
+                             int64_t db_floor) const {
+        if (database_model) return (double)db_floor;
+        double f = 1.0;
+        if (evalue_cut > 0.0 && std::isfinite(evalue_cut))
+            f = std::max(f, std::log(p.k * space_lower_bound(subject_len) / evalue_cut) / p.lambda);
+        if (has_bits) f = std::max(f, (min_bits * kLn2 + p.log_k) / p.lambda);
+        if (p.even) f -= 1.0;
+        return f;
+    }
+    double evalue_in(int64_t raw, double space) const {
+        if (raw <= 0) return kInf;
+        const double s = adj_score(raw);
+        const double e = p.k * space * std::exp(-p.lambda * s);
+        return e == 0.0 ? 2.2250738585072014e-308 : e;
+    }
+    double evalue_for(int64_t raw, int64_t subject_len) const { return evalue_in(raw, space_for(subject_len)); }
+    double evalue(int64_t raw) const {
+        if (raw <= 0) return kInf;
+        const double s = adj_score(raw);
+        const double e = p.k * search_space * std::exp(-p.lambda * s);
+        return e == 0.0 ? 2.2250738585072014e-308 : e;
+    }
+    double bitscore(int64_t raw) const {
+        if (raw <= 0) return 0.0;
+        return (p.lambda * adj_score(raw) - p.log_k) / kLn2;
+    }
+    bool passes(int64_t s, double ecut, bool has_bits, double bits) const {
+        return evalue(s) <= ecut && (!has_bits || bitscore(s) >= bits);
+    }
+    int64_t min_score(double ecut, bool has_bits, double bits) const {
+        double floor = 1.0;
+        if (ecut > 0.0 && std::isfinite(ecut)) floor = std::max(floor, std::log((p.k * search_space) / ecut) / p.lambda);
+        if (has_bits) floor = std::max(floor, (bits * kLn2 + p.log_k) / p.lambda);
+        if (!std::isfinite(floor)) return 1;
+        int64_t s = (int64_t)std::max(std::ceil(floor), 1.0);
+        while (s > 1 && passes(s - 1, ecut, has_bits, bits)) s--;
+        while (!passes(s, ecut, has_bits, bits) && s < kI64Max / 2) s++;
+        return s;
+    }
+};
+
+// SearchStatistics::for_query (stats.rs:581-645)
+QStats for_query(const Karlin& kp, bool database_model, int64_t db_length, int64_t db_num_seqs, int64_t qlen) {
+    const int64_t dbl = std::max<int64_t>(db_length, 1), dbn = std::max<int64_t>(db_num_seqs, 1);
+    const int64_t m = std::max<int64_t>(qlen, 1);
+    int64_t adj = length_adjustment(kp.k, kp.log_k, kp.adl, kp.beta, m, dbl, dbn);
+    const int64_t min_q = (int64_t)std::ceil(1.0 / kp.k);
+    if (m - adj < min_q) adj = std::max<int64_t>(m - min_q, 0);
+    const double eff_q = std::max((double)(m - adj), 1.0);
+    const double eff_db = std::max((double)dbl - (double)dbn * (double)adj, 1.0);
+    QStats q;
+    q.p = kp;
+    q.database_model = database_model;
+    q.query_len = m;
+    q.num_seqs = (double)dbn;
+    q.search_space = eff_q * eff_db;
+    return q;
+}
+
+// ---- composition bias (src/scoring/bias.rs:64-122) -------------------------
+void composition_bias(const uint8_t* q, int64_t n, const int32_t* mat, int8_t* out) {
+    std::fill(out, out + n, (int8_t)0);
+    if (n < 2) return;
+    double s = 0.0;
+    for (int a = 0; a < 20; a++) s += kRobinson[a];
+    double p[20], bg[20];
+    for (int a = 0; a < 20; a++) p[a] = kRobinson[a] / s;
+    for (int r = 0; r < 20; r++) {
+        double acc = 0.0;
+        for (int a = 0; a < 20; a++) acc += p[a] * (double)mat[r * 24 + a];
+        bg[r] = acc;
+    }
+    // prefix sums of S(r, q_j) for r < 20 (codes >= 24 index column 23)
+    std::vector<int64_t> csum((size_t)20 * (n + 1), 0);
+    for (int r = 0; r < 20; r++) {
+        int64_t* c = &csum[(size_t)r * (n + 1)];
+        for (int64_t j = 0; j < n; j++) c[j + 1] = c[j] + mat[r * 24 + std::min<int>(q[j], 23)];
+    }
+    const int64_t half = 20;
+    for (int64_t i = 0; i < n; i++) {
+        const int r = q[i];
+        if (r >= 20) continue;
+        const int64_t hi = std::min(i + half + 1, n), lo = std::max<int64_t>(i - half, 0);
+        const int64_t w = hi - lo;
+        if (w < 2) continue;
+        const int64_t* c = &csum[(size_t)r * (n + 1)];
+        const int64_t acc = c[hi] - c[lo];
+        const int64_t own = mat[r * 24 + r];
+        const double neigh = (double)(acc - own) / (double)(w - 1);
+        const double f = bg[r] - neigh;
+        const int64_t v = f < 0.0 ? (int64_t)(f - 0.5) : (int64_t)(f + 0.5);
+        out[i] = (int8_t)std::max<int64_t>(-127, std::min<int64_t>(127, v));
+    }
+}
+
+// ---- the batch ----------------------------------------------------------------
+struct Region {
+    uint32_t subject;
+    int64_t dmin, dmax, best;
+};
+struct Plan {
+    int64_t lo, hi;
+    bool band;
+    int64_t blo, bhi;
+};
+struct Prep {
+    QStats qs;
+    int64_t floor, region_floor, region_thr;
+};
+struct Aln {
+    bool present = false;
+    int32_t status = 0, score = 0;
+    uint32_t q_start = 0, q_end = 0, s_start = 0, s_end = 0;
+    std::vector<uint32_t> runs;
+};
+struct HitRec {
+    saber_hit h;
+    std::vector<uint32_t> runs;
+};
+
+inline void band_clip(int64_t& lo, int64_t& hi, int64_t m, int64_t n) {
+    lo = std::max(lo, -(m - 1));
+    hi = std::min(hi, n - 1);
+}
+inline bool band_covers(int64_t lo, int64_t hi, int64_t m, int64_t n) { return lo <= -(m - 1) && hi >= n - 1; }
+inline int64_t band_width(int64_t lo, int64_t hi) { return std::max<int64_t>(hi - lo + 1, 0); }
+
+struct Engine {
+    saber_gpu* h;
+    const saber_search_params& P;
+    const uint8_t* db;
+    const uint64_t* soff;
+    uint64_t nsub;
+    int32_t mat[576];
+    Karlin kp;
+    bool has_bits;
+    saber_search_stats st{};
+
+    Engine(saber_gpu* h_, const saber_search_params& p, const uint8_t* db_, const uint64_t* soff_, uint64_t nsub_,
+           const int32_t* m)
+        : h(h_), P(p), db(db_), soff(soff_), nsub(nsub_) {
+        std::memcpy(mat, m, sizeof(mat));
+        kp.lambda = p.lambda;
+        kp.k = p.k;
+        kp.log_k = std::log(p.k);
+        kp.adl = p.alpha / p.lambda;
+        kp.beta = p.beta;
+        kp.even = p.even_scores_only != 0;
+        has_bits = !std::isnan(p.min_bitscore);
+    }
+
+    int64_t slen(uint32_t s) const { return (int64_t)(soff[s + 1] - soff[s]); }
+
+    double region_evalue() const {
+        const double e = std::max(P.evalue, kRegionFloorEvalue);
+        const double r = (double)P.ref_db_residues;
+        const double dbl = (double)std::max<uint64_t>(P.scan.db_length, 1);
+        if (P.ref_db_residues > 0 && dbl > r) return e * (dbl / r);
+        return e;
+    }
+
+    // engine.rs:759-786
+    Prep prepare(int64_t qlen) const {
+        Prep pr;
+        pr.qs = for_query(kp, P.evalue_model == 1, (int64_t)P.scan.db_length, (int64_t)nsub, std::max<int64_t>(qlen, 1));
+        pr.floor = pr.qs.min_score(P.evalue, has_bits, P.min_bitscore);
+        const double re = region_evalue();
+        if (re == P.evalue && !has_bits) pr.region_floor = pr.floor;
+        else pr.region_floor = pr.qs.min_score(re, false, 0.0);
+        const double f = P.hsp_floor_fraction;
+        if (f > 0.0 && pr.region_floor > 0) {
+            const double v = std::min(std::ceil((double)pr.region_floor * f), (double)kI32Max);
+            pr.region_thr = std::max<int64_t>(P.hsp_threshold, (int64_t)v);
+        } else {
+            pr.region_thr = P.hsp_threshold;
+        }
+        return pr;
+    }
+
+    // engine.rs:1223-1234
+    void window(int64_t dmin, int64_t dmax, uint32_t s, int64_t qlen, int64_t& lo, int64_t& hi) const {
+        const int64_t sl = slen(s), slack = P.window_slack;
+        lo = std::min(std::max<int64_t>(dmin - slack, 0), sl);
+        hi = std::max(std::min(qlen + dmax + slack, sl), lo);
+        if ((hi - lo) * 4 >= sl * 3) {
+            lo = 0;
+            hi = sl;
+        }
+    }
+
+    // engine.rs:1247-1324
+    std::vector<Plan> plan_windows(const std::vector<Region>& regs, int64_t qlen) const {
+        const size_t n = regs.size();
+        std::vector<int64_t> span_lo(n), span_hi(n);
+        for (size_t i = 0; i < n; i++) {
+            span_lo[i] = regs[i].dmin;
+            span_hi[i] = regs[i].dmax;
+        }
+        // group by subject
+        std::vector<size_t> by(n);
+        for (size_t i = 0; i < n; i++) by[i] = i;
+        std::stable_sort(by.begin(), by.end(), [&](size_t a, size_t b) { return regs[a].subject < regs[b].subject; });
+        std::vector<size_t> idx;
+        for (size_t a = 0; a < n;) {
+            size_t b = a;
+            while (b < n && regs[by[b]].subject == regs[by[a]].subject) b++;
+            int64_t top = std::numeric_limits<int64_t>::min();
+            for (size_t t = a; t < b; t++) top = std::max(top, regs[by[t]].best);
+            const int64_t strong = std::max<int64_t>(2 * (int64_t)P.hsp_threshold, top / 4);
+            idx.clear();
+            for (size_t t = a; t < b; t++)
+                if (regs[by[t]].best >= strong) idx.push_back(by[t]);
+            std::sort(idx.begin(), idx.end(), [&](size_t x, size_t y) {
+                if (regs[x].dmin != regs[y].dmin) return regs[x].dmin < regs[y].dmin;
+                if (regs[x].dmax != regs[y].dmax) return regs[x].dmax < regs[y].dmax;
+                return x < y;
+            });
+            size_t start = 0;
+            while (start < idx.size()) {
+                int64_t lo = regs[idx[start]].dmin, hi = regs[idx[start]].dmax;
+                size_t end = start + 1;
+                while (end < idx.size() && regs[idx[end]].dmin - hi <= kBandBridge) {
+                    hi = std::max(hi, regs[idx[end]].dmax);
+                    end++;
+                }
+                for (size_t t = start; t < end; t++) {
+                    span_lo[idx[t]] = lo;
+                    span_hi[idx[t]] = hi;
+                }
+                start = end;
+            }
+            a = b;
+        }
+        std::vector<Plan> plans(n);
+        for (size_t ri = 0; ri < n; ri++) {
+            const Region& r = regs[ri];
+            int64_t lo, hi;
+            window(r.dmin, r.dmax, r.subject, qlen, lo, hi);
+            Plan own{lo, hi, false, 0, 0};
+            if (P.exhaustive || r.best == 0 || (int64_t)P.window_slack >= kI64Max / 8) {
+                plans[ri] = own;
+                continue;
+            }
+            if (P.score_band > 0) {
+                const int64_t w = P.score_band, dmin = span_lo[ri], dmax = span_hi[ri], sl = slen(r.subject);
+                const int64_t lo2 = std::min(std::max<int64_t>(dmin - w, 0), sl);
+                const int64_t hi2 = std::max(std::min(qlen + dmax + w, sl), lo2);
+                const int64_t nn = hi2 - lo2;
+                int64_t blo = dmin - w - lo2, bhi = dmax + w - lo2;
+                band_clip(blo, bhi, qlen, nn);
+                if (nn == 0 || band_covers(blo, bhi, qlen, nn)) plans[ri] = Plan{lo2, hi2, false, 0, 0};
+                else plans[ri] = Plan{lo2, hi2, true, blo, bhi};
+                continue;
+            }
+            if (qlen * (hi - lo) < kBandScoreMinCells) {
+                plans[ri] = own;
+                continue;
+            }
+            int64_t ulo, uhi;
+            window(span_lo[ri], span_hi[ri], r.subject, qlen, ulo, uhi);
+            const int64_t nn = uhi - ulo;
+            int64_t blo = span_lo[ri] - ulo - P.window_slack, bhi = span_hi[ri] - ulo + P.window_slack;
+            band_clip(blo, bhi, qlen, nn);
+            if (band_covers(blo, bhi, qlen, nn)) {
+                plans[ri] = own;
+                continue;
+            }
+            const int64_t rows = std::min(qlen, nn + band_width(blo, bhi));
+            const int64_t rect = qlen * nn;
+            if (band_width(blo, bhi) * rows * kBandCostRatio < rect) plans[ri] = Plan{ulo, uhi, true, blo, bhi};
+            else plans[ri] = own;
+        }
+        return plans;
+    }
+
+    saber_band_job job(uint32_t qi, uint32_t s, int64_t lo, int64_t hi, int64_t blo, int64_t bhi) const {
+        saber_band_job j{};
+        j.query = qi;
+        j.subject = s;
+        j.win_begin = soff[s] + (uint64_t)lo;
+        j.win_len = (uint32_t)(hi - lo);
+        j.band_lo = (int32_t)std::max<int64_t>(std::min(blo, kI32Max), -kI32Max - 1);
+        j.band_hi = (int32_t)std::max<int64_t>(std::min(bhi, kI32Max), -kI32Max - 1);
+        j.flags = 0;
+        return j;
+    }
+
+    int score(const std::vector<saber_band_job>& jobs, std::vector<int32_t>& out) {
+        out.assign(jobs.size(), 0);
+        if (jobs.empty()) return SABER_OK;
+        saber_score_stats ss{};
+        int rc = saber_gpu_score_band_jobs(h, jobs.data(), jobs.size(), out.data(), &ss);
+        if (rc != SABER_OK) return rc;
+        st.banded_cells += ss.banded_cells;
+        st.score_launches += 1;
+        return SABER_OK;
+    }
+
+    // engine.rs:1021-1099, batched over the queries
+    int score_windows(const std::vector<Prep>& preps, const std::vector<std::vector<Region>>& per_q,
+                      const std::vector<std::vector<Plan>>& plans, const std::vector<int64_t>& qlens,
+                      std::vector<std::vector<int64_t>>& scores) {
+        const int64_t wn = P.score_prefilter_band, full_band = P.score_band;
+        std::vector<saber_band_job> s1;
+        struct Ref {
+            uint32_t qi, ri;
+            int kind;  // 0 full, 1 narrow, 2 band
+        };
+        std::vector<Ref> r1;
+        scores.resize(per_q.size());
+        for (uint32_t qi = 0; qi < per_q.size(); qi++) {
+            scores[qi].assign(per_q[qi].size(), 0);
+            const int64_t m = qlens[qi];
+            for (uint32_t ri = 0; ri < per_q[qi].size(); ri++) {
+                const Region& r = per_q[qi][ri];
+                const Plan& pl = plans[qi][ri];
+                const int64_t n = pl.hi - pl.lo;
+                if (!pl.band) {
+                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, -m, n));
+                    r1.push_back({qi, ri, 0});
+                } else if (0 < wn && wn < full_band) {
+                    int64_t blo = r.dmin - wn - pl.lo, bhi = r.dmax + wn - pl.lo;
+                    band_clip(blo, bhi, m, n);
+                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, blo, bhi));
+                    r1.push_back({qi, ri, 1});
+                } else {
+                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
+                    r1.push_back({qi, ri, 2});
+                }
+            }
+        }
+        std::vector<int32_t> sc1;
+        int rc = score(s1, sc1);
+        if (rc != SABER_OK) return rc;
+        std::vector<saber_band_job> s2;
+        std::vector<Ref> r2;
+        const double re = region_evalue();
+        for (size_t k = 0; k < r1.size(); k++) {
+            const Ref& x = r1[k];
+            if (x.kind != 1) {
+                scores[x.qi][x.ri] = sc1[k];
+                st.band_scored_regions += x.kind == 2;
+                continue;
+            }
+            st.band_scored_regions++;
+            const Region& r = per_q[x.qi][x.ri];
+            const Prep& pr = preps[x.qi];
+            const double thr =
+                P.score_prefilter_frac * pr.qs.floor_lower_bound(re, false, 0.0, slen(r.subject), pr.region_floor);
+            if ((double)sc1[k] >= thr) {
+                const Plan& pl = plans[x.qi][x.ri];
+                s2.push_back(job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
+                r2.push_back(x);
+            } else {
+                scores[x.qi][x.ri] = sc1[k];
+            }
+        }
+        std::vector<int32_t> sc2;
+        rc = score(s2, sc2);
+        if (rc != SABER_OK) return rc;
+        for (size_t k = 0; k < r2.size(); k++) scores[r2[k].qi][r2[k].ri] = sc2[k];
+        st.band_rescored += s2.size();
+        return SABER_OK;
+    }
+
+    // engine.rs:1447-1530
+    HitRec make_hit(const uint8_t* q, int64_t qlen, uint32_t subject, int64_t s_off, const Aln& al,
+                    const QStats& qs) const {
+        const uint8_t* s_full = db + soff[subject];
+        const int64_t s_len = slen(subject);
+        const uint8_t* s = s_full + s_off;
+        int64_t i = al.q_start, j = al.s_start;
+        uint64_t matches = 0, mism = 0, pos = 0, gopen = 0, gcols = 0, cols = 0;
+        const int lim = P.is_protein ? 20 : 4;
+        for (uint32_t run : al.runs) {
+            const char op = (char)(run & 0xFF);
+            const int64_t l = run >> 8;
+            cols += l;
+            if (op == 'M') {
+                for (int64_t t = 0; t < l; t++) {
+                    const int a = q[i + t], b = s[j + t];
+                    const bool ident = a == b && a < lim;
+                    const int sc = mat[(a < 24 ? a : 22) * 24 + (b < 24 ? b : 22)];
+                    matches += ident;
+                    pos += ident || sc > 0;
+                }
+                mism += l;
+                i += l;
+                j += l;
+            } else if (op == 'I') {
+                gopen++;
+                gcols += l;
+                i += l;
+            } else {
+                gopen++;
+                gcols += l;
+                j += l;
+            }
+        }
+        mism -= matches;
+        HitRec r;
+        saber_hit& x = r.h;
+        std::memset(&x, 0, sizeof(x));
+        x.subject = subject;
+        x.score = al.score;
+        x.exact = al.status == 1;
+        x.bitscore = qs.bitscore(al.score);
+        x.evalue = qs.evalue_for(al.score, s_len);
+        x.q_start = al.q_start + 1;
+        x.q_end = al.q_end;
+        x.s_start = (uint32_t)(al.s_start + s_off + 1);
+        x.s_end = (uint32_t)(al.s_end + s_off);
+        x.columns = (uint32_t)cols;
+        x.matches = (uint32_t)matches;
+        x.mismatches = (uint32_t)mism;
+        x.positives = (uint32_t)pos;
+        x.gap_opens = (uint32_t)gopen;
+        x.gap_columns = (uint32_t)gcols;
+        x.q_len = (uint32_t)qlen;
+        x.s_len = (uint32_t)s_len;
+        r.runs = al.runs;
+        return r;
+    }
+
+    static double identity(const saber_hit& x) { return x.columns == 0 ? 0.0 : 100.0 * x.matches / x.columns; }
+    static double query_cover(const saber_hit& x) {
+        return x.q_len == 0 ? 0.0 : 100.0 * ((double)x.q_end + 1 - x.q_start) / x.q_len;
+    }
+    static double subject_cover(const saber_hit& x) {
+        return x.s_len == 0 ? 0.0 : 100.0 * ((double)x.s_end + 1 - x.s_start) / x.s_len;
+    }
+    // engine.rs:2415-2417
+    static bool overlaps(const saber_hit& a, const saber_hit& b) {
+        return a.q_start <= b.q_end && b.q_start <= a.q_end && a.s_start <= b.s_end && b.s_start <= a.s_end;
+    }
+
+    struct QState {
+        size_t pos = 0;
+        std::vector<HitRec> out;
+        std::unordered_map<uint32_t, uint32_t> per_subject;
+        uint32_t reported = 0;
+        bool done = false;
+    };
+
+    static uint64_t key(uint32_t qi, uint32_t ri) { return ((uint64_t)qi << 32) | ri; }
+
+    // engine.rs:1127-1221: E-value cut and order, then speculative batched
+    // tracebacks (a traceback depends only on its region) for the next chunk
+    // of candidates of every unfinished query, and the reporting steps
+    int finish(const uint8_t* q_codes, const uint64_t* q_offsets, const std::vector<Prep>& preps,
+               const std::vector<std::vector<Region>>& per_q, const std::vector<std::vector<Plan>>& plans,
+               const std::vector<std::vector<int64_t>>& scores, std::vector<std::vector<HitRec>>& result) {
+        const double ecut = (P.evalue > 0.0 && std::isfinite(P.evalue)) ? P.evalue : kInf;
+        const size_t nq = per_q.size();
+        std::vector<std::vector<std::pair<double, uint32_t>>> orders(nq);
+        for (size_t qi = 0; qi < nq; qi++) {
+            const QStats& qs = preps[qi].qs;
+            auto& order = orders[qi];
+            const auto& regs = per_q[qi];
+            for (uint32_t i = 0; i < regs.size(); i++) {
+                const int64_t sc = scores[qi][i];
+                if (qs.database_model) {
+                    if (sc >= preps[qi].floor) order.push_back({qs.evalue(sc), i});
+                    continue;
+                }
+                if (sc <= 0 || (has_bits && qs.bitscore(sc) < P.min_bitscore)) continue;
+                const int64_t n = slen(regs[i].subject);
+                if (qs.evalue_in(sc, qs.space_lower_bound(n)) > ecut) continue;
+                const double e = qs.evalue_for(sc, n);
+                if (e <= ecut) order.push_back({e, i});
+            }
+            const auto& sc_ = scores[qi];
+            std::stable_sort(order.begin(), order.end(), [&](const std::pair<double, uint32_t>& a,
+                                                             const std::pair<double, uint32_t>& b) {
+                if (a.first != b.first) return a.first < b.first;
+                const int64_t sa = sc_[a.second], sb = sc_[b.second];
+                if (sa != sb) return sa > sb;
+                const Region& x = regs[a.second];
+                const Region& y = regs[b.second];
+                if (x.best != y.best) return x.best > y.best;
+                if (x.subject != y.subject) return x.subject < y.subject;
+                if (x.dmin != y.dmin) return x.dmin < y.dmin;
+                return x.dmax < y.dmax;
+            });
+        }
+        std::unordered_map<uint64_t, Aln> tb;
+        std::vector<QState> state(nq);
+        for (size_t qi = 0; qi < nq; qi++) state[qi].done = orders[qi].empty();
+        const size_t chunk = std::max<size_t>(4, 2 * (size_t)P.max_target_seqs * P.max_hsps);
+        for (;;) {
+            std::vector<std::pair<uint32_t, uint32_t>> need;
+            for (uint32_t qi = 0; qi < nq; qi++) {
+                if (state[qi].done) continue;
+                const size_t k = state[qi].pos;
+                for (size_t t = k; t < std::min(orders[qi].size(), k + chunk); t++) {
+                    const uint32_t ri = orders[qi][t].second;
+                    if (!tb.count(key(qi, ri))) need.push_back({qi, ri});
+                }
+            }
+            if (!need.empty()) {
+                int rc = traceback(need, per_q, plans, scores, q_offsets, tb);
+                if (rc != SABER_OK) return rc;
+            }
+            bool progress = false;
+            for (uint32_t qi = 0; qi < nq; qi++) {
+                if (state[qi].done) continue;
+                progress |= finish_steps(qi, state[qi], orders[qi], per_q[qi], plans[qi], tb, preps[qi],
+                                         q_codes + q_offsets[qi], (int64_t)(q_offsets[qi + 1] - q_offsets[qi]), ecut);
+            }
+            bool all = true;
+            for (const QState& s : state) all &= s.done;
+            if (all) break;
+            if (need.empty() && !progress) break;
+        }
+        result.assign(nq, {});
+        for (uint32_t qi = 0; qi < nq; qi++) {
+            auto& hits = state[qi].out;
+            std::stable_sort(hits.begin(), hits.end(), [](const HitRec& a, const HitRec& b) {
+                if (a.h.evalue != b.h.evalue) return a.h.evalue < b.h.evalue;
+                if (a.h.score != b.h.score) return a.h.score > b.h.score;
+                if (a.h.subject != b.h.subject) return a.h.subject < b.h.subject;
+                return a.h.s_start < b.h.s_start;
+            });
+            for (auto& x : hits) x.h.query = qi;
+            st.alignments += hits.size();
+            result[qi] = std::move(hits);
+        }
+        return SABER_OK;
+    }
+
+    bool finish_steps(uint32_t qi, QState& stt, const std::vector<std::pair<double, uint32_t>>& order,
+                      const std::vector<Region>& regs, const std::vector<Plan>& plans,
+                      const std::unordered_map<uint64_t, Aln>& tb, const Prep& prep, const uint8_t* q, int64_t qlen,
+                      double ecut) {
+        bool moved = false;
+        while (stt.pos < order.size()) {
+            const uint32_t ri = order[stt.pos].second;
+            const uint32_t s = regs[ri].subject;
+            auto it = stt.per_subject.find(s);
+            if (stt.reported >= P.max_target_seqs && it == stt.per_subject.end()) {
+                stt.done = true;
+                return true;
+            }
+            const uint32_t cnt = it == stt.per_subject.end() ? 0 : it->second;
+            if (cnt >= P.max_hsps) {
+                stt.pos++;
+                moved = true;
+                continue;
+            }
+            auto t = tb.find(key(qi, ri));
+            if (t == tb.end()) return moved;
+            stt.pos++;
+            moved = true;
+            const Aln& al = t->second;
+            if (!al.present) continue;
+            HitRec hit = make_hit(q, qlen, s, plans[ri].lo, al, prep.qs);
+            if (cnt > 0) {
+                bool dup = false;
+                for (const HitRec& o : stt.out)
+                    if (o.h.subject == hit.h.subject && overlaps(o.h, hit.h)) {
+                        dup = true;
+                        break;
+                    }
+                if (dup) continue;
+            }
+            bool passes;
+            if (prep.qs.database_model) passes = hit.h.score >= prep.floor;
+            else passes = hit.h.evalue <= ecut && (!has_bits || hit.h.bitscore >= P.min_bitscore);
+            if (identity(hit.h) < P.min_identity || query_cover(hit.h) < P.min_query_cover ||
+                subject_cover(hit.h) < P.min_subject_cover || !passes)
+                continue;
+            if (cnt == 0) stt.reported++;
+            stt.per_subject[s] = cnt + 1;
+            stt.out.push_back(std::move(hit));
+        }
+        stt.done = true;
+        return true;
+    }
+
+    // engine.rs:1328-1445 through the batched widening traceback
+    int traceback(const std::vector<std::pair<uint32_t, uint32_t>>& need, const std::vector<std::vector<Region>>& per_q,
+                  const std::vector<std::vector<Plan>>& plans, const std::vector<std::vector<int64_t>>& scores,
+                  const uint64_t* q_offsets, std::unordered_map<uint64_t, Aln>& tb) {
+        std::vector<saber_traceback_job> jobs(need.size());
+        uint64_t cap = 64;
+        for (size_t k = 0; k < need.size(); k++) {
+            const uint32_t qi = need[k].first, ri = need[k].second;
+            const Region& r = per_q[qi][ri];
+            const Plan& pl = plans[qi][ri];
+            const bool full = P.exhaustive || r.best == 0;
+            saber_traceback_job& j = jobs[k];
+            std::memset(&j, 0, sizeof(j));
+            j.query = qi;
+            j.subject = r.subject;
+            j.win_begin = soff[r.subject] + (uint64_t)pl.lo;
+            j.win_len = (uint32_t)(pl.hi - pl.lo);
+            j.d_min = (int32_t)(r.dmin - pl.lo);
+            j.d_max = (int32_t)(r.dmax - pl.lo);
+            j.limit_lo = pl.band ? (int32_t)pl.blo : 0;
+            j.limit_hi = pl.band ? (int32_t)pl.bhi : 0;
+            j.want = (int32_t)scores[qi][ri];
+            j.flags = (full ? 1u : 0u) | (pl.band ? 2u : 0u);
+            cap += (uint64_t)j.win_len + (q_offsets[qi + 1] - q_offsets[qi]) + 2;
+        }
+        std::vector<saber_alignment> out(need.size());
+        std::vector<uint32_t> ops(cap);
+        saber_traceback_stats ts{};
+        int rc = saber_gpu_traceback(h, jobs.data(), jobs.size(), P.band_pad, P.traceback_max_bytes, out.data(),
+                                     ops.data(), cap, &ts);
+        if (rc != SABER_OK) return rc;
+        st.traceback.tracebacks += ts.tracebacks;
+        st.traceback.band_widenings += ts.band_widenings;
+        st.traceback.end_anchored += ts.end_anchored;
+        st.traceback.band_capped += ts.band_capped;
+        st.traceback.banded_cells += ts.banded_cells;
+        st.traceback.launches += ts.launches;
+        for (size_t k = 0; k < need.size(); k++) {
+            Aln a;
+            const saber_alignment& o = out[k];
+            a.present = o.status != 0;
+            a.status = o.status;
+            a.score = o.score;
+            a.q_start = o.q_start;
+            a.q_end = o.q_end;
+            a.s_start = o.s_start;
+            a.s_end = o.s_end;
+            if (a.present) a.runs.assign(ops.begin() + o.ops_offset, ops.begin() + o.ops_offset + o.n_ops);
+            tb[key(need[k].first, need[k].second)] = std::move(a);
+        }
+        return SABER_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint8_t* db_res,
+                                const uint64_t* db_offsets, uint64_t nsub, const uint8_t* q_codes,
+                                const uint64_t* q_offsets, uint32_t nq, const uint8_t* q_mask, saber_hit* hits,
+                                uint64_t hits_cap, uint64_t* n_hits, uint32_t* ops, uint64_t ops_cap, uint64_t* n_ops,
+                                saber_search_stats* stats);
+
+namespace saber {
+int scheme_matrix(saber_gpu* h, int32_t* out576);  // saber_gpu.cu
+}
+
+extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint8_t* db_res,
+                                const uint64_t* db_offsets, uint64_t nsub, const uint8_t* q_codes,
+                                const uint64_t* q_offsets, uint32_t nq, const uint8_t* q_mask, saber_hit* hits,
+                                uint64_t hits_cap, uint64_t* n_hits, uint32_t* ops, uint64_t ops_cap, uint64_t* n_ops,
+                                saber_search_stats* stats) {
+    if (!h || !params || !db_offsets || (nq && (!q_codes || !q_offsets)) || !n_hits || !n_ops) return SABER_ERR_ARG;
+    if (nsub && !db_res) return SABER_ERR_ARG;
+    const double t0 = now_ms();
+    int32_t mat[576];
+    int rc = saber::scheme_matrix(h, mat);
+    if (rc != SABER_OK) return rc;
+    Engine E(h, *params, db_res, db_offsets, nsub, mat);
+    const saber_search_params& P = *params;
+
+    // query preparation (engine.rs:759-786)
+    std::vector<int64_t> qlens(nq);
+    std::vector<Prep> preps(nq);
+    std::vector<int8_t> bias(nq ? q_offsets[nq] : 0, 0);
+    for (uint32_t qi = 0; qi < nq; qi++) {
+        qlens[qi] = (int64_t)(q_offsets[qi + 1] - q_offsets[qi]);
+        if (P.comp_bias && P.is_protein)
+            composition_bias(q_codes + q_offsets[qi], qlens[qi], mat, bias.data() + q_offsets[qi]);
+        preps[qi] = E.prepare(qlens[qi]);
+    }
+    rc = saber_gpu_load_queries(h, q_codes, q_offsets, bias.data(), nq);
+    if (rc != SABER_OK) return rc;
+    const double t1 = now_ms();
+
+    // candidate regions
+    std::vector<std::vector<Region>> per_q(nq);
+    if (P.exhaustive) {
+        for (uint32_t qi = 0; qi < nq; qi++)
+            if (qlens[qi] > 0)
+                for (uint32_t s = 0; s < nsub; s++) per_q[qi].push_back({s, -qlens[qi], E.slen(s), 0});
+    } else if (nq && nsub) {
+        std::vector<int32_t> thr(nq);
+        for (uint32_t qi = 0; qi < nq; qi++) thr[qi] = (int32_t)preps[qi].region_thr;
+        uint64_t cap = 1 << 20, n = 0;
+        std::vector<saber_region> regs;
+        for (int attempt = 0; attempt < 4; attempt++) {
+            regs.resize(cap);
+            rc = saber_gpu_scan(h, &P.scan, q_mask, thr.data(), regs.data(), cap, &n, &E.st.scan);
+            if (rc == SABER_OK || n <= cap) break;
+            cap = n;
+        }
+        if (rc != SABER_OK) return rc;
+        for (uint64_t t = 0; t < n; t++) {
+            const saber_region& r = regs[t];
+            per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best});
+        }
+    }
+    for (uint32_t qi = 0; qi < nq; qi++) {
+        if (qlens[qi] == 0) per_q[qi].clear();
+        E.st.regions += per_q[qi].size();
+    }
+    const double t2 = now_ms();
+
+    std::vector<std::vector<Plan>> plans(nq);
+    for (uint32_t qi = 0; qi < nq; qi++) plans[qi] = E.plan_windows(per_q[qi], qlens[qi]);
+    const double t3 = now_ms();
+    std::vector<std::vector<int64_t>> scores;
+    rc = E.score_windows(preps, per_q, plans, qlens, scores);
+    if (rc != SABER_OK) return rc;
+    const double t4 = now_ms();
+    std::vector<std::vector<HitRec>> result;
+    rc = E.finish(q_codes, q_offsets, preps, per_q, plans, scores, result);
+    if (rc != SABER_OK) return rc;
+    const double t5 = now_ms();
+
+    uint64_t nh = 0, no = 0;
+    for (const auto& v : result)
+        for (const HitRec& x : v) {
+            nh++;
+            no += x.runs.size();
+        }
+    *n_hits = nh;
+    *n_ops = no;
+    E.st.t_prep_ms = t1 - t0;
+    E.st.t_scan_ms = t2 - t1;
+    E.st.t_plan_ms = t3 - t2;
+    E.st.t_score_ms = t4 - t3;
+    E.st.t_finish_ms = t5 - t4;
+    E.st.t_total_ms = t5 - t0;
+    if (stats) *stats = E.st;
+    if (nh > hits_cap || no > ops_cap || (nh && !hits) || (no && !ops)) return SABER_ERR_CAP;
+    uint64_t k = 0, o = 0;
+    for (const auto& v : result)
+        for (const HitRec& x : v) {
+            hits[k] = x.h;
+            hits[k].ops_offset = o;
+            hits[k].n_ops = (uint32_t)x.runs.size();
+            std::copy(x.runs.begin(), x.runs.end(), ops + o);
+            o += x.runs.size();
+            k++;
+        }
+    return SABER_OK;
+}

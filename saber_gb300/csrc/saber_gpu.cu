@@ -888,6 +888,16 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
     cudaSetDevice((h)->device);           \
     (h)->err.clear()
 
+namespace saber {
+// The handle's scoring matrix, for the host engine (engine.cpp).
+int scheme_matrix(saber_gpu* h, int32_t* out576) {
+    ENTER(h);
+    if (!h->scheme.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    std::memcpy(out576, h->scheme.matrix, sizeof(int32_t) * 576);
+    return SABER_OK;
+}
+}  // namespace saber
+
 extern "C" {
 
 int saber_gpu_open(int device, saber_gpu** out) {

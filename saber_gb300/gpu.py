@@ -82,6 +82,50 @@ class ScanStats(ctypes.Structure):
         return {n: (float(getattr(self, n)) if n.startswith("t_") else int(getattr(self, n))) for n, _ in self._fields_}
 
 
+class SearchParamsC(ctypes.Structure):
+    """saber_search_params (include/saber_gpu.h)."""
+    _fields_ = [("evalue", ctypes.c_double), ("min_bitscore", ctypes.c_double),
+                ("max_target_seqs", ctypes.c_uint32), ("max_hsps", ctypes.c_uint32),
+                ("min_identity", ctypes.c_double), ("min_query_cover", ctypes.c_double),
+                ("min_subject_cover", ctypes.c_double), ("hsp_threshold", ctypes.c_int32),
+                ("hsp_floor_fraction", ctypes.c_double), ("band_pad", ctypes.c_int32),
+                ("window_slack", ctypes.c_int32), ("score_band", ctypes.c_int32),
+                ("score_prefilter_band", ctypes.c_int32), ("score_prefilter_frac", ctypes.c_double),
+                ("comp_bias", ctypes.c_uint32), ("exhaustive", ctypes.c_uint32),
+                ("traceback_max_bytes", ctypes.c_uint64), ("ref_db_residues", ctypes.c_uint64),
+                ("evalue_model", ctypes.c_uint32), ("is_protein", ctypes.c_uint32),
+                ("lambda_", ctypes.c_double), ("k", ctypes.c_double), ("h", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("even_scores_only", ctypes.c_uint32), ("pad_", ctypes.c_uint32), ("scan", ScanParams)]
+
+
+class SearchStats(ctypes.Structure):
+    """saber_search_stats (include/saber_gpu.h)."""
+    _fields_ = [("scan", ScanStats), ("traceback", TracebackStats)] + [
+        (n, ctypes.c_uint64) for n in ("regions", "band_scored_regions", "band_rescored", "banded_cells",
+                                       "score_launches", "alignments")] + [
+        (n, ctypes.c_double) for n in ("t_prep_ms", "t_scan_ms", "t_plan_ms", "t_score_ms", "t_finish_ms",
+                                       "t_total_ms")]
+
+    def as_dict(self):
+        d = {}
+        d.update(self.scan.as_dict())
+        d.update({"tb_" + k: v for k, v in self.traceback.as_dict().items()})
+        for n, t in self._fields_[2:]:
+            v = getattr(self, n)
+            d[n] = float(v) if n.startswith("t_") else int(v)
+        return d
+
+
+# saber_hit
+HIT_DTYPE = np.dtype([("query", "<u4"), ("subject", "<u4"), ("score", "<i4"), ("exact", "<u4"),
+                      ("evalue", "<f8"), ("bitscore", "<f8"), ("q_start", "<u4"), ("q_end", "<u4"),
+                      ("s_start", "<u4"), ("s_end", "<u4"), ("columns", "<u4"), ("matches", "<u4"),
+                      ("mismatches", "<u4"), ("positives", "<u4"), ("gap_opens", "<u4"), ("gap_columns", "<u4"),
+                      ("q_len", "<u4"), ("s_len", "<u4"), ("n_ops", "<u4"), ("pad_", "<u4"), ("ops_offset", "<u8")])
+assert HIT_DTYPE.itemsize == 96
+
+
 REGION_DTYPE = np.dtype([("query", "<u4"), ("subject", "<u4"), ("d_min", "<i4"), ("d_max", "<i4"), ("best", "<i4")])
 
 
@@ -161,6 +205,7 @@ def load_library():
         "saber_gpu_scan": (ctypes.c_int, [P, P, P, P, P, U64, P, P]),
         "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_set_pair_steps": (ctypes.c_int, [P, U32]),
+        "saber_gpu_search": (ctypes.c_int, [P, P, P, P, U64, P, P, U32, P, P, U64, P, P, U64, P, P]),
         "saber_gpu_get_pair_steps": (U32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
@@ -339,6 +384,30 @@ class Device:
                 continue
             self._check(rc, "scan")
         self._check(rc, "scan")
+
+    def search(self, cparams, db_codes, db_offsets, q_codes, q_offsets, q_mask=None):
+        """saber_gpu_search: (HIT_DTYPE array ordered by query, ops uint32 array, stats dict)."""
+        db = np.ascontiguousarray(db_codes, dtype=np.uint8)
+        do = np.ascontiguousarray(db_offsets, dtype=np.uint64)
+        qc = np.ascontiguousarray(q_codes, dtype=np.uint8)
+        qo = np.ascontiguousarray(q_offsets, dtype=np.uint64)
+        qm = None if q_mask is None else np.ascontiguousarray(q_mask, dtype=np.uint8)
+        hcap, ocap = 1 << 16, 1 << 20
+        for _ in range(3):
+            hits = np.zeros(hcap, HIT_DTYPE)
+            ops = np.zeros(ocap, np.uint32)
+            nh, no = ctypes.c_uint64(), ctypes.c_uint64()
+            st = SearchStats()
+            rc = self.lib.saber_gpu_search(self.h, ctypes.byref(cparams), _ptr(db), _ptr(do), do.size - 1, _ptr(qc),
+                                           _ptr(qo), qo.size - 1, _ptr(qm), _ptr(hits), hcap, ctypes.byref(nh),
+                                           _ptr(ops), ocap, ctypes.byref(no), ctypes.byref(st))
+            if rc == 0:
+                return hits[:nh.value].copy(), ops[:no.value].copy(), st.as_dict()
+            if rc == -5 and (nh.value > hcap or no.value > ocap):  # SABER_ERR_CAP
+                hcap, ocap = max(hcap, int(nh.value)), max(ocap, int(no.value))
+                continue
+            self._check(rc, "search")
+        self._check(rc, "search")
 
     @property
     def strip_rows(self):

@@ -19,7 +19,7 @@ import numpy as np
 
 from . import presets as _presets
 from .bias import composition_bias
-from .gpu import JOB_DTYPE, TB_JOB_DTYPE, scan_params
+from .gpu import JOB_DTYPE, TB_JOB_DTYPE, SearchParamsC, scan_params
 from .scoring import ALPHABET, matrix as _matrix, nucleotide as _nt_matrix
 from .stats import SearchStatistics, gapped_nucleotide, gapped_protein
 
@@ -144,6 +144,7 @@ class Searcher:
         self.slen = np.diff(self.db_offsets.astype(np.int64))
         kp = gapped_protein(matrix_name, gap_open, gap_extend) if self.is_protein else \
             gapped_nucleotide(nucleotide[0], nucleotide[1], gap_open, gap_extend)
+        self.karlin = kp
         self.stats = SearchStatistics(kp, int(self.db_codes.size), self.nsub, self.p.evalue_model)
         dev.set_scheme(self.matrix, gap_open, gap_extend)
         dev.load_db(self.db_codes, self.db_offsets)
@@ -261,8 +262,51 @@ class Searcher:
                 plans.append(own)
         return plans
 
-    # ---- the batch ----
+    # ---- the batch, through the library's host engine (saber_gpu_search) ----
+    def cparams(self):
+        """saber_search_params of this configuration."""
+        p, kp = self.p, self.karlin
+        c = SearchParamsC()
+        c.evalue = p.evalue
+        c.min_bitscore = math.nan if p.min_bitscore is None else p.min_bitscore
+        c.max_target_seqs, c.max_hsps = p.max_target_seqs, p.max_hsps
+        c.min_identity, c.min_query_cover, c.min_subject_cover = p.min_identity, p.min_query_cover, \
+            p.min_subject_cover
+        c.hsp_threshold, c.hsp_floor_fraction = p.hsp_threshold, p.hsp_floor_fraction
+        c.band_pad, c.window_slack = p.band_pad, min(p.window_slack, I32_MAX)
+        c.score_band, c.score_prefilter_band = p.score_band, p.score_prefilter_band
+        c.score_prefilter_frac = p.score_prefilter_frac
+        c.comp_bias, c.exhaustive = int(bool(p.comp_bias)), int(bool(p.exhaustive))
+        c.traceback_max_bytes, c.ref_db_residues = p.traceback_max_bytes, p.ref_db_residues
+        c.evalue_model = 1 if p.evalue_model == "database" else 0
+        c.is_protein = int(self.is_protein)
+        c.lambda_, c.k, c.h, c.alpha, c.beta = kp.lambda_, kp.k, kp.h, kp.alpha, kp.beta
+        c.even_scores_only = int(bool(kp.even_scores_only))
+        c.scan = self.scan_params
+        return c
+
     def search(self, q_codes, q_offsets, q_mask=None):
+        """Hits of every query of the batch: list (per query) of Hit, in report order."""
+        q_offsets = np.ascontiguousarray(q_offsets, dtype=np.uint64)
+        nq = q_offsets.size - 1
+        hits, ops, st = self.dev.search(self.cparams(), self.db_codes, self.db_offsets, q_codes, q_offsets, q_mask)
+        out = [[] for _ in range(nq)]
+        for r in hits:
+            o, n = int(r["ops_offset"]), int(r["n_ops"])
+            runs = [(chr(int(w) & 0xFF), int(w) >> 8) for w in ops[o:o + n]]
+            out[int(r["query"])].append(Hit(
+                subject=int(r["subject"]), score=int(r["score"]), bitscore=float(r["bitscore"]),
+                evalue=float(r["evalue"]), q_start=int(r["q_start"]), q_end=int(r["q_end"]),
+                s_start=int(r["s_start"]), s_end=int(r["s_end"]), columns=int(r["columns"]),
+                matches=int(r["matches"]), mismatches=int(r["mismatches"]), positives=int(r["positives"]),
+                gap_opens=int(r["gap_opens"]), gap_columns=int(r["gap_columns"]), q_len=int(r["q_len"]),
+                s_len=int(r["s_len"]), ops=runs, exact=bool(r["exact"])))
+        st["queries"] = nq
+        self.counters = st
+        return out
+
+    # ---- the same batch with the engine steps in Python (cross-check) ----
+    def search_py(self, q_codes, q_offsets, q_mask=None):
         """Hits of every query of the batch: list (per query) of Hit, in report order."""
         q_codes = np.ascontiguousarray(q_codes, dtype=np.uint8)
         q_offsets = np.ascontiguousarray(q_offsets, dtype=np.uint64)

@@ -32,6 +32,7 @@ class KarlinParams:
         self.k = k
         self.log_k = math.log(k)
         self.h = h
+        self.alpha = alpha
         self.alpha_d_lambda = alpha / lam
         self.beta = beta
         self.calibrated = calibrated

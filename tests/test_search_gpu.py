@@ -50,3 +50,17 @@ def test_search_variants_match_oracle(dev):
     _compare(got, want)
     got, want, _ = _case(dev, "default", 6, 8, 500, evalue_model="database", evalue=1e-3)
     _compare(got, want)
+
+
+@pytest.mark.parametrize("preset,kw", [("default", {}), ("fast", {}), ("sensitive", {"max_target_seqs": 25}),
+                                       ("exhaustive", {}), ("default", {"comp_bias": False, "min_bitscore": 30.0}),
+                                       ("default", {"min_identity": 35.0, "max_hsps": 3})])
+def test_native_engine_matches_python_engine(dev, preset, kw):
+    """The library's host engine (saber_gpu_search) against the same stages
+    written in Python over the same device calls: identical hits and m8 rows."""
+    qs, ss, planted = synth.protein_db(77, 16 if preset == "exhaustive" else 30, 500 if preset == "exhaustive" else 1500)
+    se = Searcher(dev, ss.codes, ss.offsets, SearchParams(preset, **kw))
+    got = se.search(qs.codes, qs.offsets)
+    want = se.search_py(qs.codes, qs.offsets)
+    assert sum(len(h) for h in want) > 0
+    _compare(got, want)
