@@ -11,7 +11,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <atomic>
 #include <limits>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -31,6 +33,30 @@ const double kInf = std::numeric_limits<double>::infinity();
 // Robinson & Robinson background frequencies per 1000 (src/scoring/bias.rs:32-53)
 constexpr double kRobinson[20] = {78.05, 51.29, 44.87, 53.64, 19.25, 42.64, 62.95, 73.77, 21.99, 51.42,
                                   90.19, 57.44, 22.43, 38.56, 52.03, 71.20, 58.41, 13.30, 32.16, 64.41};
+
+// Runs f(i) for i in [0, n) on the host cores (chunks taken from an atomic
+// counter); the per-query stages of the engine are independent.
+template <class F>
+void parallel_for(size_t n, F f) {
+    unsigned hw = std::thread::hardware_concurrency();
+    size_t nt = std::min<size_t>(hw ? hw : 1, (n + 7) / 8);
+    if (nt <= 1) {
+        for (size_t i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const size_t b = next.fetch_add(8);
+            if (b >= n) return;
+            for (size_t i = b; i < std::min(n, b + 8); i++) f(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; t++) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+}
 
 double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -410,59 +436,70 @@ struct Engine {
                       const std::vector<std::vector<Plan>>& plans, const std::vector<int64_t>& qlens,
                       std::vector<std::vector<int64_t>>& scores) {
         const int64_t wn = P.score_prefilter_band, full_band = P.score_band;
-        std::vector<saber_band_job> s1;
         struct Ref {
             uint32_t qi, ri;
             int kind;  // 0 full, 1 narrow, 2 band
         };
-        std::vector<Ref> r1;
-        scores.resize(per_q.size());
-        for (uint32_t qi = 0; qi < per_q.size(); qi++) {
+        const size_t nq = per_q.size();
+        scores.resize(nq);
+        std::vector<size_t> base(nq + 1, 0);
+        for (size_t qi = 0; qi < nq; qi++) base[qi + 1] = base[qi] + per_q[qi].size();
+        std::vector<saber_band_job> s1(base[nq]);
+        std::vector<Ref> r1(base[nq]);
+        parallel_for(nq, [&](size_t q) {
+            const uint32_t qi = (uint32_t)q;
             scores[qi].assign(per_q[qi].size(), 0);
             const int64_t m = qlens[qi];
             for (uint32_t ri = 0; ri < per_q[qi].size(); ri++) {
                 const Region& r = per_q[qi][ri];
                 const Plan& pl = plans[qi][ri];
                 const int64_t n = pl.hi - pl.lo;
+                const size_t k = base[qi] + ri;
                 if (!pl.band) {
-                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, -m, n));
-                    r1.push_back({qi, ri, 0});
+                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, -m, n);
+                    r1[k] = {qi, ri, 0};
                 } else if (0 < wn && wn < full_band) {
                     int64_t blo = r.dmin - wn - pl.lo, bhi = r.dmax + wn - pl.lo;
                     band_clip(blo, bhi, m, n);
-                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, blo, bhi));
-                    r1.push_back({qi, ri, 1});
+                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, blo, bhi);
+                    r1[k] = {qi, ri, 1};
                 } else {
-                    s1.push_back(job(qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
-                    r1.push_back({qi, ri, 2});
+                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi);
+                    r1[k] = {qi, ri, 2};
                 }
             }
-        }
+        });
         std::vector<int32_t> sc1;
         int rc = score(s1, sc1);
         if (rc != SABER_OK) return rc;
+        // stage-2 decision per region (f64 threshold of the region's subject length)
+        const double re = region_evalue();
+        std::vector<uint8_t> again(r1.size(), 0);
+        parallel_for(nq, [&](size_t q) {
+            for (size_t k = base[q]; k < base[q + 1]; k++) {
+                const Ref& x = r1[k];
+                if (x.kind != 1) {
+                    scores[x.qi][x.ri] = sc1[k];
+                    continue;
+                }
+                const Region& r = per_q[x.qi][x.ri];
+                const Prep& pr = preps[x.qi];
+                const double thr = P.score_prefilter_frac *
+                                   pr.qs.floor_lower_bound(re, false, 0.0, slen(r.subject), pr.region_floor);
+                if ((double)sc1[k] >= thr) again[k] = 1;
+                else scores[x.qi][x.ri] = sc1[k];
+            }
+        });
         std::vector<saber_band_job> s2;
         std::vector<Ref> r2;
-        const double re = region_evalue();
         for (size_t k = 0; k < r1.size(); k++) {
             const Ref& x = r1[k];
-            if (x.kind != 1) {
-                scores[x.qi][x.ri] = sc1[k];
-                st.band_scored_regions += x.kind == 2;
-                continue;
-            }
-            st.band_scored_regions++;
+            st.band_scored_regions += x.kind != 0;
+            if (!again[k]) continue;
             const Region& r = per_q[x.qi][x.ri];
-            const Prep& pr = preps[x.qi];
-            const double thr =
-                P.score_prefilter_frac * pr.qs.floor_lower_bound(re, false, 0.0, slen(r.subject), pr.region_floor);
-            if ((double)sc1[k] >= thr) {
-                const Plan& pl = plans[x.qi][x.ri];
-                s2.push_back(job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
-                r2.push_back(x);
-            } else {
-                scores[x.qi][x.ri] = sc1[k];
-            }
+            const Plan& pl = plans[x.qi][x.ri];
+            s2.push_back(job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
+            r2.push_back(x);
         }
         std::vector<int32_t> sc2;
         rc = score(s2, sc2);
@@ -562,7 +599,7 @@ struct Engine {
         const double ecut = (P.evalue > 0.0 && std::isfinite(P.evalue)) ? P.evalue : kInf;
         const size_t nq = per_q.size();
         std::vector<std::vector<std::pair<double, uint32_t>>> orders(nq);
-        for (size_t qi = 0; qi < nq; qi++) {
+        parallel_for(nq, [&](size_t qi) {
             const QStats& qs = preps[qi].qs;
             auto& order = orders[qi];
             const auto& regs = per_q[qi];
@@ -591,7 +628,7 @@ struct Engine {
                 if (x.dmin != y.dmin) return x.dmin < y.dmin;
                 return x.dmax < y.dmax;
             });
-        }
+        });
         std::unordered_map<uint64_t, Aln> tb;
         std::vector<QState> state(nq);
         for (size_t qi = 0; qi < nq; qi++) state[qi].done = orders[qi].empty();
@@ -610,12 +647,15 @@ struct Engine {
                 int rc = traceback(need, per_q, plans, scores, q_offsets, tb);
                 if (rc != SABER_OK) return rc;
             }
-            bool progress = false;
-            for (uint32_t qi = 0; qi < nq; qi++) {
-                if (state[qi].done) continue;
-                progress |= finish_steps(qi, state[qi], orders[qi], per_q[qi], plans[qi], tb, preps[qi],
+            std::vector<uint8_t> moved(nq, 0);
+            parallel_for(nq, [&](size_t q) {
+                const uint32_t qi = (uint32_t)q;
+                if (state[qi].done) return;
+                moved[qi] = finish_steps(qi, state[qi], orders[qi], per_q[qi], plans[qi], tb, preps[qi],
                                          q_codes + q_offsets[qi], (int64_t)(q_offsets[qi + 1] - q_offsets[qi]), ecut);
-            }
+            });
+            bool progress = false;
+            for (uint8_t v : moved) progress |= v != 0;
             bool all = true;
             for (const QState& s : state) all &= s.done;
             if (all) break;
@@ -750,6 +790,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
 
 namespace saber {
 int scheme_matrix(saber_gpu* h, int32_t* out576);  // saber_gpu.cu
+int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                     std::vector<saber_region>& out, saber_scan_stats* st);  // saber_gpu.cu
 }
 
 extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint8_t* db_res,
@@ -770,12 +812,12 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     std::vector<int64_t> qlens(nq);
     std::vector<Prep> preps(nq);
     std::vector<int8_t> bias(nq ? q_offsets[nq] : 0, 0);
-    for (uint32_t qi = 0; qi < nq; qi++) {
+    parallel_for(nq, [&](size_t qi) {
         qlens[qi] = (int64_t)(q_offsets[qi + 1] - q_offsets[qi]);
         if (P.comp_bias && P.is_protein)
             composition_bias(q_codes + q_offsets[qi], qlens[qi], mat, bias.data() + q_offsets[qi]);
         preps[qi] = E.prepare(qlens[qi]);
-    }
+    });
     rc = saber_gpu_load_queries(h, q_codes, q_offsets, bias.data(), nq);
     if (rc != SABER_OK) return rc;
     const double t1 = now_ms();
@@ -789,19 +831,14 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     } else if (nq && nsub) {
         std::vector<int32_t> thr(nq);
         for (uint32_t qi = 0; qi < nq; qi++) thr[qi] = (int32_t)preps[qi].region_thr;
-        uint64_t cap = 1 << 20, n = 0;
         std::vector<saber_region> regs;
-        for (int attempt = 0; attempt < 4; attempt++) {
-            regs.resize(cap);
-            rc = saber_gpu_scan(h, &P.scan, q_mask, thr.data(), regs.data(), cap, &n, &E.st.scan);
-            if (rc == SABER_OK || n <= cap) break;
-            cap = n;
-        }
+        rc = saber::scan_regions_all(h, &P.scan, q_mask, thr.data(), regs, &E.st.scan);
         if (rc != SABER_OK) return rc;
-        for (uint64_t t = 0; t < n; t++) {
-            const saber_region& r = regs[t];
-            per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best});
-        }
+        // regions arrive grouped by query
+        std::vector<size_t> cnt(nq + 1, 0);
+        for (const saber_region& r : regs) cnt[r.query + 1]++;
+        for (uint32_t qi = 0; qi < nq; qi++) per_q[qi].reserve(cnt[qi + 1]);
+        for (const saber_region& r : regs) per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best});
     }
     for (uint32_t qi = 0; qi < nq; qi++) {
         if (qlens[qi] == 0) per_q[qi].clear();
@@ -810,7 +847,7 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     const double t2 = now_ms();
 
     std::vector<std::vector<Plan>> plans(nq);
-    for (uint32_t qi = 0; qi < nq; qi++) plans[qi] = E.plan_windows(per_q[qi], qlens[qi]);
+    parallel_for(nq, [&](size_t qi) { plans[qi] = E.plan_windows(per_q[qi], qlens[qi]); });
     const double t3 = now_ms();
     std::vector<std::vector<int64_t>> scores;
     rc = E.score_windows(preps, per_q, plans, qlens, scores);

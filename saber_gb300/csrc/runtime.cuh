@@ -96,6 +96,7 @@ struct saber_gpu {
     saber::DevBuf db_mask, sc_sb, sc_rem, sc_dst, sc_freq, sc_counts, sc_qsb, sc_qfull, sc_qrem, sc_qdst,
         sc_qcnt, sc_qoff, sc_qent, sc_qpres, sc_surv, sc_key1, sc_key2, sc_val, sc_key1o, sc_key2o, sc_valo,
         sc_chains, sc_hsp, sc_hkey, sc_hkeyo, sc_hval, sc_hvalo, sc_pairs, sc_regions, sc_rthr, sc_ctr, sc_tmp,
+        sc_rk64a, sc_rk64b, sc_rk64c, sc_rk32a, sc_rk32b, sc_ridxa, sc_ridxb, sc_regions2,
         sc_flags;
     bool has_db_mask = false;
     uint64_t sc_key = 0;            // fingerprint of the database state built
@@ -134,7 +135,8 @@ static int fail(saber_gpu* h, int code, const char* fmt, ...) {
 
 
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st);
+                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
+                 std::vector<saber_region>* all = nullptr);
 
 static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
     uint64_t b = (n + t - 1) / t;

@@ -889,6 +889,14 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
     (h)->err.clear()
 
 namespace saber {
+// Every region of the scan into a host vector, for the host engine (engine.cpp).
+int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                     std::vector<saber_region>& out, saber_scan_stats* st) {
+    ENTER(h);
+    uint64_t n = 0;
+    return scan_regions(h, p, q_mask, region_thr, nullptr, 0, &n, st, &out);
+}
+
 // The handle's scoring matrix, for the host engine (engine.cpp).
 int scheme_matrix(saber_gpu* h, int32_t* out576) {
     ENTER(h);
@@ -1125,6 +1133,7 @@ int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residue
 
 int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask, const int32_t* region_thr,
                    saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* stats) {
+    // (the batch engine, engine.cpp, takes every region through scan_regions_all)
     ENTER(h);
     if (!params || (out_cap && !out)) return fail(h, SABER_ERR_ARG, "null argument");
     return scan_regions(h, params, q_mask, region_thr, out, out_cap, n_out, stats);

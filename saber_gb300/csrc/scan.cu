@@ -74,7 +74,10 @@ __global__ void k_dists(const uint64_t* __restrict__ offs, uint64_t nseq, uint64
 
 __device__ __forceinline__ int64_t seed_code(const uint8_t* __restrict__ sr, const ShapeDev& sh, uint32_t asize) {
     uint32_t c = 0;
-    for (uint32_t i = 0; i < sh.w; i++) {
+    // unrolled to the largest weight so that the offsets stay in registers
+#pragma unroll
+    for (uint32_t i = 0; i < 16; i++) {
+        if (i >= sh.w) break;
         const uint8_t r = sr[sh.off[i]];
         if (r >= asize) return -1;
         c = c * asize + r;
@@ -167,44 +170,161 @@ struct ScanArgs {
     unsigned long long* ctr;    // [2] hits, [3] filtered
 };
 
-__global__ void k_scan(ScanArgs a, ShapeDev sh, uint32_t asize) {
+// 32-lane mask of byte equality between q[0..32) and s[0..32) & smask, from
+// aligned 32-bit words (the caller guarantees q - 3 .. q + 36 and s - 3 ..
+// s + 36 are readable).
+__device__ __forceinline__ uint32_t eq_lanes(const uint8_t* q, const uint8_t* s, uint32_t smask) {
+    const uint32_t* qa = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(q) & ~(uintptr_t)3);
+    const uint32_t* sa = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(s) & ~(uintptr_t)3);
+    const uint32_t qs = (uint32_t)(reinterpret_cast<uintptr_t>(q) & 3u) * 8u;
+    const uint32_t ss = (uint32_t)(reinterpret_cast<uintptr_t>(s) & 3u) * 8u;
+    uint32_t E = 0, qn = __ldg(qa), sn = __ldg(sa);
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+        const uint32_t q0 = qn, s0 = sn;
+        qn = __ldg(qa + w + 1);
+        sn = __ldg(sa + w + 1);
+        const uint32_t x = __funnelshift_r(q0, qn, qs) ^ (__funnelshift_r(s0, sn, ss) & smask);
+        // 0x80 in every zero byte of x (no carries between bytes), then the
+        // four flags gathered into bits 28..31
+        const uint32_t z = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+        E |= (((z >> 7) * 0x10204080u) >> 28) << (4 * w);
+    }
+    return E;
+}
+
+// Lanes [lo, hi) of a 32-lane mask (0 <= lo, hi <= 32).
+__device__ __forceinline__ uint32_t lane_range(int lo, int hi) {
+    if (hi <= lo) return 0u;
+    return (uint32_t)(((1ull << hi) - 1ull) & ~((1ull << lo) - 1ull));
+}
+
+// One seed hit through the window filter (filter_scalar, scan.rs:1809-1856):
+// the 32-residue windows starting at r + cfil - 16 (subject) and g + cfil - 16
+// (query batch), restricted to lanes inside both sequences; reduced-letter
+// identities (query positions masked from seeding never count, the subject's
+// masked residues do) plus kx x exact identities must reach min_ids.
+__device__ __forceinline__ bool window_passes(const ScanArgs& a, uint64_t r, uint32_t g) {
+    const int sdst = a.dst[r], srem = a.rem[r];
+    const int t_lo = max(max(0, 16 - a.cfil - sdst), 16 - a.cfil - (int)a.qdst[g]);
+    const int t_hi = min(min(32, srem + 16 - a.cfil), (int)a.qrem[g] + 16 - a.cfil);
+    const int64_t so = (int64_t)r + a.cfil - 16, qo = (int64_t)g + a.cfil - 16;
+    uint32_t ids = 0, ex = 0;
+    if (so >= 4 && qo >= 4) {
+        const uint32_t L = lane_range(t_lo, t_hi);
+        const uint32_t E = eq_lanes(a.qsb + qo, a.sb + so, 0x7F7F7F7Fu) & L;
+        ids = __popc(E);
+        if (ids >= a.min_ids) return true;
+        if (a.kx == 0 || ids * (1 + a.kx) < a.min_ids) return false;
+        ex = __popc(E & eq_lanes(a.qfull + qo, a.res + so, 0xFFFFFFFFu));
+    } else {
+        for (int t = t_lo; t < t_hi; t++) {
+            const uint8_t qr = a.qsb[qo + t];
+            if (qr != kQSent && qr == (a.sb[so + t] & 0x7F)) {
+                ids++;
+                if (a.kx && a.qfull[qo + t] == a.res[so + t]) ex++;
+            }
+        }
+    }
+    return ids + a.kx * ex >= a.min_ids;
+}
+
+// One shape over the database.  Each warp takes 32 consecutive positions,
+// computes their seed codes and presence, then works through all their hits
+// (one batch position each) as a warp queue, one hit per lane per round, so
+// that a position with many hits does not stall the other lanes; survivors
+// are appended with one atomic per warp round.  (A query byte of QSENT never
+// equals a masked-off subject byte, which is below 0x80.)
+__global__ void __launch_bounds__(256) k_scan(ScanArgs a, ShapeDev sh, uint32_t asize) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long hits = 0, filtered = 0;
-    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < a.N; r += (uint64_t)gridDim.x * blockDim.x) {
-        if (a.rem[r] < sh.span) continue;
-        const int64_t c = seed_code(a.sb + r, sh, asize);
-        if (c < 0) continue;
-        if (!((a.pres[c >> 6] >> (c & 63)) & 1ull)) continue;
-        const uint32_t e0 = a.qoff[c], e1 = a.qoff[c + 1];
-        // subject lanes of the 32-residue window starting at r + c - 16 (filter_scalar, scan.rs:1829-1833)
-        const int sdst = a.dst[r], srem = a.rem[r];
-        const int s_lo = max(0, 16 - a.cfil - sdst);
-        const int s_hi = min(32, srem + 16 - a.cfil);
-        for (uint32_t e = e0; e < e1; e++) {
-            const uint32_t g = a.qent[e];
-            hits++;
-            if (a.min_ids > 0) {
-                const int t_lo = max(s_lo, 16 - a.cfil - (int)a.qdst[g]);
-                const int t_hi = min(s_hi, (int)a.qrem[g] + 16 - a.cfil);
-                uint32_t ids = 0, ex = 0;
-                const int64_t so = (int64_t)r + a.cfil - 16, qo = (int64_t)g + a.cfil - 16;
-                for (int t = t_lo; t < t_hi; t++) {
-                    const uint8_t qr = a.qsb[qo + t];
-                    if (qr != kQSent && qr == (a.sb[so + t] & 0x7F)) {
-                        ids++;
-                        if (a.kx && a.qfull[qo + t] == a.res[so + t]) ex++;
-                    }
-                }
-                if (ids + a.kx * ex < a.min_ids) {
-                    filtered++;
-                    continue;
+    for (uint64_t base = warp0 * 32; base < a.N; base += nwarps * 32) {
+        const uint64_t r = base + lane;
+        uint32_t n = 0, e0 = 0;
+        if (r < a.N && a.rem[r] >= sh.span) {
+            const int64_t c = seed_code(a.sb + r, sh, asize);
+            if (c >= 0 && ((a.pres[c >> 6] >> (c & 63)) & 1ull)) {
+                e0 = a.qoff[c];
+                n = a.qoff[c + 1] - e0;
+            }
+        }
+        // exclusive prefix of the lanes' hit counts
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t start = incl - n;
+        if (lane == 0) hits += total;
+        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            // owner lane: the last lane whose start is <= k
+            int lo = 0, hi = 32;
+#pragma unroll
+            for (int it = 0; it < 5; it++) {
+                const int mid = (lo + hi) >> 1;
+                if (__shfl_sync(0xffffffffu, start, mid) <= k) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t ostart = __shfl_sync(0xffffffffu, start, lo);
+            const uint32_t oe0 = __shfl_sync(0xffffffffu, e0, lo);
+            const uint64_t orr = __shfl_sync(0xffffffffu, r, lo);
+            bool pass = false;
+            if (k < total) {
+                const uint32_t g = a.qent[oe0 + (k - ostart)];
+                pass = a.min_ids == 0 || window_passes(a, orr, g);
+                if (!pass) filtered++;
+                const uint32_t bal = __ballot_sync(__activemask(), pass);
+                if (pass) {
+                    const uint32_t gg = g;
+                    // one atomic per round, from the lowest passing lane
+                    const uint32_t mine = __popc(bal & ((1u << lane) - 1u));
+                    unsigned long long slot0 = 0;
+                    const int leader = __ffs(bal) - 1;
+                    if (lane == leader) slot0 = atomicAdd(a.nsurv, (unsigned long long)__popc(bal));
+                    slot0 = __shfl_sync(bal, slot0, leader);
+                    const unsigned long long slot = slot0 + mine;
+                    if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)orr, gg | (a.shape << 27));
                 }
             }
-            const unsigned long long slot = atomicAdd(a.nsurv, 1ull);
-            if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)r, g | (a.shape << 27));
         }
     }
     atomicAdd(&a.ctr[2], hits);
     atomicAdd(&a.ctr[3], filtered);
+}
+
+// Keys of the per-query region order (region_order, engine.rs:493-495:
+// query, best descending, subject, d_min, d_max) for three stable radix
+// passes, least significant first.
+__global__ void k_region_keys(const saber_region* __restrict__ regs, uint32_t n, unsigned long long* __restrict__ k_lo,
+                              uint32_t* __restrict__ k_sub, unsigned long long* __restrict__ k_hi,
+                              uint32_t* __restrict__ idx) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const saber_region r = regs[i];
+        k_lo[i] = ((unsigned long long)((uint32_t)r.d_min ^ 0x80000000u) << 32) | ((uint32_t)r.d_max ^ 0x80000000u);
+        k_sub[i] = r.subject;
+        k_hi[i] = ((unsigned long long)r.query << 32) | (0xFFFFFFFFu - ((uint32_t)r.best ^ 0x80000000u));
+        idx[i] = i;
+    }
+}
+
+__global__ void k_gather_u32_by(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n,
+                                uint32_t* __restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
+}
+
+__global__ void k_gather_u64_by(const unsigned long long* __restrict__ src, const uint32_t* __restrict__ idx,
+                                uint32_t n, unsigned long long* __restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
+}
+
+__global__ void k_gather_regions(const saber_region* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n,
+                                 saber_region* __restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
 }
 
 // ---- chains ------------------------------------------------------------------------
@@ -547,7 +667,8 @@ static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
 }
 
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st) {
+                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
+                 std::vector<saber_region>* all) {
     const Dataset& ds = h->main;
     const QuerySet& qs = ds.qs;
     if (!ds.has_db || !qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
@@ -799,9 +920,43 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             CU(h, cudaStreamSynchronize(s));
             nregions = std::min<uint64_t>(nr, rcap);
             regs.resize(nregions);
-            if (nregions)
-                CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions.p, nregions * sizeof(saber_region), cudaMemcpyDeviceToHost,
-                                      s));
+            if (nregions) {
+                // region_order on the device: stable passes by (d_min, d_max), subject, (query, best desc)
+                const uint32_t nrg = (uint32_t)nregions;
+                CUALLOC(h, h->sc_rk64a, (uint64_t)nrg * 8);
+                CUALLOC(h, h->sc_rk64b, (uint64_t)nrg * 8);
+                CUALLOC(h, h->sc_rk64c, (uint64_t)nrg * 8);
+                CUALLOC(h, h->sc_rk32a, (uint64_t)nrg * 4);
+                CUALLOC(h, h->sc_rk32b, (uint64_t)nrg * 4);
+                CUALLOC(h, h->sc_ridxa, (uint64_t)nrg * 4);
+                CUALLOC(h, h->sc_ridxb, (uint64_t)nrg * 4);
+                CUALLOC(h, h->sc_regions2, (uint64_t)nrg * sizeof(saber_region));
+                unsigned long long* klo = h->sc_rk64a.as<unsigned long long>();
+                unsigned long long* khi = h->sc_rk64c.as<unsigned long long>();
+                unsigned long long* k64o = h->sc_rk64b.as<unsigned long long>();
+                uint32_t* ksub = h->sc_rk32a.as<uint32_t>();
+                uint32_t* k32o = h->sc_rk32b.as<uint32_t>();
+                uint32_t* ia = h->sc_ridxa.as<uint32_t>();
+                uint32_t* ib = h->sc_ridxb.as<uint32_t>();
+                k_region_keys<<<nblocks(nrg, 256), 256, 0, s>>>(h->sc_regions.as<saber_region>(), nrg, klo, ksub, khi, ia);
+                size_t r1 = 0, r2 = 0;
+                CU(h, cub::DeviceRadixSort::SortPairs(nullptr, r1, klo, k64o, ia, ib, (int)nrg, 0, 64, s));
+                CU(h, cub::DeviceRadixSort::SortPairs(nullptr, r2, ksub, k32o, ia, ib, (int)nrg, 0, 32, s));
+                CUALLOC(h, h->cub_tmp, std::max(r1, r2));
+                size_t rb = h->cub_tmp.cap;
+                // pass 1: (d_min, d_max); ib = order
+                CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, rb, klo, k64o, ia, ib, (int)nrg, 0, 64, s));
+                // pass 2: subject, stable
+                k_gather_u32_by<<<nblocks(nrg, 256), 256, 0, s>>>(ksub, ib, nrg, k32o);
+                CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, rb, k32o, ksub, ib, ia, (int)nrg, 0, 32, s));
+                // pass 3: (query, best desc), stable
+                k_gather_u64_by<<<nblocks(nrg, 256), 256, 0, s>>>(khi, ia, nrg, k64o);
+                CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, rb, k64o, klo, ia, ib, (int)nrg, 0, 64, s));
+                k_gather_regions<<<nblocks(nrg, 256), 256, 0, s>>>(h->sc_regions.as<saber_region>(), ib, nrg,
+                                                                   h->sc_regions2.as<saber_region>());
+                CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions2.p, nregions * sizeof(saber_region),
+                                      cudaMemcpyDeviceToHost, s));
+            }
         }
     } else {
         CU(h, cudaEventRecord(ev[3], s));
@@ -815,32 +970,27 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     local.xdrop_steps = hc[6];
     local.hsps = hc[7];
     local.regions_weak_dropped = hc[8];
-    // per query: region_order (engine.rs:493-495), cap at max_candidates
-    std::sort(regs.begin(), regs.end(), [](const saber_region& a, const saber_region& b) {
-        if (a.query != b.query) return a.query < b.query;
-        if (a.best != b.best) return a.best > b.best;
-        if (a.subject != b.subject) return a.subject < b.subject;
-        if (a.d_min != b.d_min) return a.d_min < b.d_min;
-        return a.d_max < b.d_max;
-    });
+    // per query in region_order (sorted on the device above), cap at max_candidates
     const uint64_t cap = std::max<uint32_t>(1, p->max_candidates);
     uint64_t w = 0;
     size_t i = 0;
     bool overflow = false;
+    if (all) all->clear();
     while (i < regs.size()) {
         size_t j = i;
         while (j < regs.size() && regs[j].query == regs[i].query) j++;
         const uint64_t take = std::min<uint64_t>(j - i, cap);
         local.regions_dropped_by_cap += (j - i) - take;
         for (uint64_t k = 0; k < take; k++) {
-            if (w < out_cap) out[w] = regs[i + k];
+            if (all) all->push_back(regs[i + k]);
+            else if (w < out_cap) out[w] = regs[i + k];
             else overflow = true;
             w++;
         }
         i = j;
     }
     local.regions = w;
-    local.t_tables_ms = 0;
+    local.t_tables_ms = ev_ms(ev[0], ev[1]);
     local.t_scan_ms = ev_ms(ev[1], ev[2]);
     local.t_visit_ms = ev_ms(ev[2], ev[3]);
     local.t_regions_ms = ev_ms(ev[3], ev[4]);

@@ -109,7 +109,7 @@ class SearchStats(ctypes.Structure):
 
     def as_dict(self):
         d = {}
-        d.update(self.scan.as_dict())
+        d.update({("scan_" + k if k.startswith("t_") else k): v for k, v in self.scan.as_dict().items()})
         d.update({"tb_" + k: v for k, v in self.traceback.as_dict().items()})
         for n, t in self._fields_[2:]:
             v = getattr(self, n)
