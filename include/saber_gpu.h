@@ -328,9 +328,10 @@ typedef struct {
     saber_scan_stats scan;
     saber_traceback_stats traceback;
     uint64_t regions;             /* candidate regions after the per-query caps */
+    uint64_t triage_dropped;      /* regions dropped by the learned triage */
     uint64_t band_scored_regions, band_rescored, banded_cells, score_launches;
     uint64_t alignments;
-    double t_prep_ms, t_scan_ms, t_plan_ms, t_score_ms, t_finish_ms, t_total_ms;  /* host wall clock */
+    double t_prep_ms, t_scan_ms, t_triage_ms, t_plan_ms, t_score_ms, t_finish_ms, t_total_ms;  /* host wall clock */
 } saber_search_stats;
 
 /* Hits of every query of the batch, ordered by query, then (E-value, score
@@ -344,6 +345,57 @@ int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint
                      const uint64_t* q_offsets, uint32_t nq, const uint8_t* q_mask, saber_hit* hits,
                      uint64_t hits_cap, uint64_t* n_hits, uint32_t* ops, uint64_t ops_cap, uint64_t* n_ops,
                      saber_search_stats* stats);
+
+/* ---- learned triage of candidate regions ------------------------------------
+ *
+ * A 3-layer MLP (24 region features -> 256 -> 256 -> 1 logit, ReLU) with
+ * bf16 weights and fp32 accumulation, trained on the GPU by this library's
+ * own forward / backward / Adam kernels, on labels that the plain search
+ * produces (the region yields a reported hit).  Installed on a handle, the
+ * batch engine (saber_gpu_search) drops the candidate regions whose logit is
+ * below the threshold before window planning and banded scoring; every
+ * surviving region is still scored exactly.  No reference counterpart.
+ *
+ * Model: SABER_TRIAGE_MODEL_FLOATS floats: W1[32][256] (input-major; rows
+ * 24..31 unused), b1[256], W2[256][256], b2[256], W3[256], b3, mu[32],
+ * isd[32] (input normalisation x' = (x - mu) * isd, not trained).  Feature
+ * rows are 32 floats (24 used). */
+#define SABER_TRIAGE_MODEL_FLOATS 74561
+#define SABER_TRIAGE_ROW_FLOATS 32
+
+typedef struct {
+    uint32_t epochs, batch;
+    float lr, pos_weight, weight_decay;
+    uint32_t pad_;
+    uint64_t seed;
+} saber_triage_train_cfg;
+
+typedef struct {
+    uint64_t steps;
+    double final_loss;   /* mean batch loss of the last epoch */
+} saber_triage_train_stats;
+
+/* One forward + backward pass over n rows: gradients of the mean weighted
+ * binary cross-entropy (positives weighted by pos_weight) in the model
+ * layout (zeros for mu / isd), and the loss. */
+int saber_gpu_triage_grads(saber_gpu* h, const float* model, const float* rows, const uint8_t* labels, uint32_t n,
+                           float pos_weight, float* grads, double* loss);
+/* Adam training (seeded shuffles, mini-batches) starting from and
+ * overwriting model. */
+int saber_gpu_triage_train(saber_gpu* h, float* model, const float* rows, const uint8_t* labels, uint64_t n,
+                           const saber_triage_train_cfg* cfg, saber_triage_train_stats* stats);
+/* Logits of n feature rows (the inference kernel the engine runs). */
+int saber_gpu_triage_predict(saber_gpu* h, const float* model, const float* rows, uint64_t n, float* logits);
+/* Install (model != NULL) or remove the triage model of the batch engine:
+ * regions with logit < threshold are dropped. */
+int saber_gpu_set_triage(saber_gpu* h, const float* model, float threshold);
+/* Collect, on the next saber_gpu_search calls, every candidate region's
+ * feature row and label (1 = it produced a reported hit), regions in the
+ * engine's order (query, then region order); with triage installed, the
+ * rows of the regions kept and the logits of all.  collect = 0 stops. */
+int saber_gpu_collect_regions(saber_gpu* h, int32_t collect);
+int saber_gpu_collected_regions(saber_gpu* h, float* rows, uint8_t* labels, float* logits, uint64_t cap,
+                                uint64_t* n);
 
 /* Tuning: rows per strip of the packed int16 scoring kernel (8 or 16,
  * default 16).  Results do not depend on it.  No reference counterpart (the

@@ -17,6 +17,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_runtime.h>  // float4, uint4
+
 #include "saber_gpu.h"
 
 namespace {
@@ -232,6 +234,7 @@ void composition_bias(const uint8_t* q, int64_t n, const int32_t* mat, int8_t* o
 struct Region {
     uint32_t subject;
     int64_t dmin, dmax, best;
+    uint64_t src;  // index among the scan's regions of the batch
 };
 struct Plan {
     int64_t lo, hi;
@@ -583,6 +586,7 @@ struct Engine {
     struct QState {
         size_t pos = 0;
         std::vector<HitRec> out;
+        std::vector<uint64_t> hit_src;
         std::unordered_map<uint32_t, uint32_t> per_subject;
         uint32_t reported = 0;
         bool done = false;
@@ -595,7 +599,8 @@ struct Engine {
     // of candidates of every unfinished query, and the reporting steps
     int finish(const uint8_t* q_codes, const uint64_t* q_offsets, const std::vector<Prep>& preps,
                const std::vector<std::vector<Region>>& per_q, const std::vector<std::vector<Plan>>& plans,
-               const std::vector<std::vector<int64_t>>& scores, std::vector<std::vector<HitRec>>& result) {
+               const std::vector<std::vector<int64_t>>& scores, std::vector<std::vector<HitRec>>& result,
+               std::vector<uint64_t>* hit_src) {
         const double ecut = (P.evalue > 0.0 && std::isfinite(P.evalue)) ? P.evalue : kInf;
         const size_t nq = per_q.size();
         std::vector<std::vector<std::pair<double, uint32_t>>> orders(nq);
@@ -671,6 +676,7 @@ struct Engine {
                 return a.h.s_start < b.h.s_start;
             });
             for (auto& x : hits) x.h.query = qi;
+            if (hit_src) hit_src->insert(hit_src->end(), state[qi].hit_src.begin(), state[qi].hit_src.end());
             st.alignments += hits.size();
             result[qi] = std::move(hits);
         }
@@ -721,6 +727,7 @@ struct Engine {
             if (cnt == 0) stt.reported++;
             stt.per_subject[s] = cnt + 1;
             stt.out.push_back(std::move(hit));
+            stt.hit_src.push_back(regs[ri].src);
         }
         stt.done = true;
         return true;
@@ -791,7 +798,12 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
 namespace saber {
 int scheme_matrix(saber_gpu* h, int32_t* out576);  // saber_gpu.cu
 int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                     std::vector<saber_region>& out, saber_scan_stats* st);  // saber_gpu.cu
+                     std::vector<saber_region>& out, std::vector<uint4>& rstat, saber_scan_stats* st);
+int triage_regions(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
+                   const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
+                   const std::vector<float4>& qinfo, float lambda, float logk, std::vector<uint8_t>& keep,
+                   bool* active);
+void triage_set_labels(saber_gpu* h, const std::vector<uint64_t>& hit_regions);
 }
 
 extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params, const uint8_t* db_res,
@@ -824,27 +836,56 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
 
     // candidate regions
     std::vector<std::vector<Region>> per_q(nq);
+    double t_scan_end = 0;
+    bool collecting = false;
     if (P.exhaustive) {
         for (uint32_t qi = 0; qi < nq; qi++)
             if (qlens[qi] > 0)
-                for (uint32_t s = 0; s < nsub; s++) per_q[qi].push_back({s, -qlens[qi], E.slen(s), 0});
+                for (uint32_t s = 0; s < nsub; s++) per_q[qi].push_back({s, -qlens[qi], E.slen(s), 0, 0});
     } else if (nq && nsub) {
         std::vector<int32_t> thr(nq);
         for (uint32_t qi = 0; qi < nq; qi++) thr[qi] = (int32_t)preps[qi].region_thr;
         std::vector<saber_region> regs;
-        rc = saber::scan_regions_all(h, &P.scan, q_mask, thr.data(), regs, &E.st.scan);
+        std::vector<uint4> rstat;
+        rc = saber::scan_regions_all(h, &P.scan, q_mask, thr.data(), regs, rstat, &E.st.scan);
         if (rc != SABER_OK) return rc;
-        // regions arrive grouped by query
+        t_scan_end = now_ms();
+        // learned triage (a no-op without a model or collection): regions
+        // arrive grouped by query in region order
+        const uint64_t nr = regs.size();
+        std::vector<uint32_t> rq(nr), rrank(nr);
+        std::vector<float4> qinfo(nq, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (uint32_t qi = 0; qi < nq; qi++) qinfo[qi] = make_float4((float)qlens[qi], (float)preps[qi].region_thr, 0.f, 0.f);
+        for (uint64_t t = 0; t < nr; t++) {
+            const uint32_t q = regs[t].query;
+            rq[t] = q;
+            rrank[t] = (uint32_t)qinfo[q].w;
+            if (qinfo[q].w == 0.f) qinfo[q].z = (float)regs[t].best;
+            qinfo[q].w += 1.f;
+        }
+        std::vector<uint8_t> keep;
+        bool tri = false;
+        rc = saber::triage_regions(h, regs, rstat, rq, rrank, qinfo, (float)P.lambda, (float)std::log(P.k), keep, &tri);
+        if (rc != SABER_OK) return rc;
+        collecting = tri;
         std::vector<size_t> cnt(nq + 1, 0);
         for (const saber_region& r : regs) cnt[r.query + 1]++;
         for (uint32_t qi = 0; qi < nq; qi++) per_q[qi].reserve(cnt[qi + 1]);
-        for (const saber_region& r : regs) per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best});
+        for (uint64_t t = 0; t < nr; t++) {
+            const saber_region& r = regs[t];
+            if (!keep[t]) {
+                E.st.triage_dropped++;
+                continue;
+            }
+            per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best, t});
+        }
     }
     for (uint32_t qi = 0; qi < nq; qi++) {
         if (qlens[qi] == 0) per_q[qi].clear();
         E.st.regions += per_q[qi].size();
     }
     const double t2 = now_ms();
+    if (t_scan_end == 0) t_scan_end = t2;
 
     std::vector<std::vector<Plan>> plans(nq);
     parallel_for(nq, [&](size_t qi) { plans[qi] = E.plan_windows(per_q[qi], qlens[qi]); });
@@ -854,8 +895,10 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     if (rc != SABER_OK) return rc;
     const double t4 = now_ms();
     std::vector<std::vector<HitRec>> result;
-    rc = E.finish(q_codes, q_offsets, preps, per_q, plans, scores, result);
+    std::vector<uint64_t> hit_src;
+    rc = E.finish(q_codes, q_offsets, preps, per_q, plans, scores, result, collecting ? &hit_src : nullptr);
     if (rc != SABER_OK) return rc;
+    if (collecting) saber::triage_set_labels(h, hit_src);
     const double t5 = now_ms();
 
     uint64_t nh = 0, no = 0;
@@ -867,7 +910,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     *n_hits = nh;
     *n_ops = no;
     E.st.t_prep_ms = t1 - t0;
-    E.st.t_scan_ms = t2 - t1;
+    E.st.t_scan_ms = t_scan_end - t1;
+    E.st.t_triage_ms = t2 - t_scan_end;
     E.st.t_plan_ms = t3 - t2;
     E.st.t_score_ms = t4 - t3;
     E.st.t_finish_ms = t5 - t4;

@@ -96,9 +96,17 @@ struct saber_gpu {
     saber::DevBuf db_mask, sc_sb, sc_rem, sc_dst, sc_freq, sc_counts, sc_qsb, sc_qfull, sc_qrem, sc_qdst,
         sc_qcnt, sc_qoff, sc_qent, sc_qpres, sc_surv, sc_key1, sc_key2, sc_val, sc_key1o, sc_key2o, sc_valo,
         sc_chains, sc_hsp, sc_hkey, sc_hkeyo, sc_hval, sc_hvalo, sc_pairs, sc_regions, sc_rthr, sc_ctr, sc_tmp,
-        sc_rk64a, sc_rk64b, sc_rk64c, sc_rk32a, sc_rk32b, sc_ridxa, sc_ridxb, sc_regions2,
+        sc_rk64a, sc_rk64b, sc_rk64c, sc_rk32a, sc_rk32b, sc_ridxa, sc_ridxb, sc_regions2, sc_rstat, sc_rstat2,
         sc_flags;
     bool has_db_mask = false;
+    // learned triage: installed model, per-call feature buffers, collection
+    saber::DevBuf tr_model, tr_wb, tr_sfeat, tr_qfeat, tr_reg, tr_rstat, tr_rq, tr_rrank, tr_qinfo, tr_X, tr_logit;
+    bool tr_on = false, tr_sfeat_ok = false;
+    uint64_t tr_sfeat_key = 0;
+    float tr_threshold = 0.f;
+    bool tr_collect = false;
+    std::vector<float> tr_rows, tr_logits;
+    std::vector<uint8_t> tr_labels;
     uint64_t sc_key = 0;            // fingerprint of the database state built
     std::vector<uint64_t> sc_caps;  // per shape
     std::vector<uint64_t> sc_freq_off;
@@ -136,7 +144,7 @@ static int fail(saber_gpu* h, int code, const char* fmt, ...) {
 
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
                  saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
-                 std::vector<saber_region>* all = nullptr);
+                 std::vector<saber_region>* all = nullptr, std::vector<uint4>* rstats = nullptr);
 
 static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
     uint64_t b = (n + t - 1) / t;

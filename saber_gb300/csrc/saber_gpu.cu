@@ -891,10 +891,67 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
 namespace saber {
 // Every region of the scan into a host vector, for the host engine (engine.cpp).
 int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                     std::vector<saber_region>& out, saber_scan_stats* st) {
+                     std::vector<saber_region>& out, std::vector<uint4>& rstat, saber_scan_stats* st) {
     ENTER(h);
     uint64_t n = 0;
-    return scan_regions(h, p, q_mask, region_thr, nullptr, 0, &n, st, &out);
+    return scan_regions(h, p, q_mask, region_thr, nullptr, 0, &n, st, &out, &rstat);
+}
+
+int triage_grads(saber_gpu* h, const float* model, const float* X, const uint8_t* y, uint32_t n, float pos_weight,
+                 float* grads, double* loss);
+int triage_train(saber_gpu* h, float* model, const float* X, const uint8_t* y, uint64_t n,
+                 const saber_triage_train_cfg* cfg, saber_triage_train_stats* st);
+int triage_predict_host(saber_gpu* h, const float* model, const float* X, uint64_t n, float* logits);
+int triage_predict(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* d_X, uint64_t n, float* d_logit);
+int triage_region_features(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
+                           const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
+                           const std::vector<float4>& qinfo, float lambda, float logk);
+int triage_upload_model(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* host_model);
+
+// Triage of the batch's candidate regions for the host engine (engine.cpp):
+// keep[i] = 0 drops region i.  Without a model and without collection it
+// does nothing (the plain path); with collection it keeps the feature rows
+// (and logits) on the handle for saber_gpu_collected_regions.
+int triage_regions(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
+                   const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
+                   const std::vector<float4>& qinfo, float lambda, float logk, std::vector<uint8_t>& keep,
+                   bool* active) {
+    ENTER(h);
+    keep.assign(regs.size(), 1);
+    *active = h->tr_on || h->tr_collect;
+    if (!*active) return SABER_OK;
+    int rc = triage_region_features(h, regs, rstat, rquery, rrank, qinfo, lambda, logk);
+    if (rc != SABER_OK) return rc;
+    const uint64_t n = regs.size();
+    cudaStream_t s = h->stream;
+    if (h->tr_on) {
+        rc = triage_predict(h, h->tr_model, h->tr_wb, h->tr_X.as<float>(), n, h->tr_logit.as<float>());
+        if (rc != SABER_OK) return rc;
+    }
+    std::vector<float> logits(h->tr_on ? n : 0);
+    if (h->tr_on && n) CU(h, cudaMemcpyAsync(logits.data(), h->tr_logit.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (h->tr_collect) {
+        h->tr_rows.resize(n * SABER_TRIAGE_ROW_FLOATS);
+        if (n) CU(h, cudaMemcpyAsync(h->tr_rows.data(), h->tr_X.p, n * SABER_TRIAGE_ROW_FLOATS * 4,
+                                     cudaMemcpyDeviceToHost, s));
+    }
+    CU(h, cudaStreamSynchronize(s));
+    if (h->tr_on)
+        for (uint64_t i = 0; i < n; i++) keep[i] = logits[i] >= h->tr_threshold;
+    if (h->tr_collect) {
+        h->tr_logits = logits;
+        h->tr_logits.resize(n, 0.f);
+        h->tr_labels.assign(n, 0);
+    }
+    return SABER_OK;
+}
+
+// Labels of the collected regions (1 = produced a reported hit).
+void triage_set_labels(saber_gpu* h, const std::vector<uint64_t>& hit_regions) {
+    std::lock_guard<std::mutex> g_(h->mu);
+    if (!h->tr_collect) return;
+    for (uint64_t i : hit_regions)
+        if (i < h->tr_labels.size()) h->tr_labels[i] = 1;
 }
 
 // The handle's scoring matrix, for the host engine (engine.cpp).
@@ -1050,6 +1107,61 @@ int saber_gpu_set_strip_rows(saber_gpu* h, int32_t strip_rows) {
 }
 
 int32_t saber_gpu_get_strip_rows(saber_gpu* h) { return h ? h->strip_rows : 0; }
+
+int saber_gpu_triage_grads(saber_gpu* h, const float* model, const float* rows, const uint8_t* labels, uint32_t n,
+                           float pos_weight, float* grads, double* loss) {
+    ENTER(h);
+    if (!model || !grads || (n && (!rows || !labels))) return fail(h, SABER_ERR_ARG, "null argument");
+    return triage_grads(h, model, rows, labels, n, pos_weight, grads, loss);
+}
+
+int saber_gpu_triage_train(saber_gpu* h, float* model, const float* rows, const uint8_t* labels, uint64_t n,
+                           const saber_triage_train_cfg* cfg, saber_triage_train_stats* stats) {
+    ENTER(h);
+    if (!model || !cfg || (n && (!rows || !labels))) return fail(h, SABER_ERR_ARG, "null argument");
+    return triage_train(h, model, rows, labels, n, cfg, stats);
+}
+
+int saber_gpu_triage_predict(saber_gpu* h, const float* model, const float* rows, uint64_t n, float* logits) {
+    ENTER(h);
+    if (!model || (n && (!rows || !logits))) return fail(h, SABER_ERR_ARG, "null argument");
+    return triage_predict_host(h, model, rows, n, logits);
+}
+
+int saber_gpu_set_triage(saber_gpu* h, const float* model, float threshold) {
+    ENTER(h);
+    if (!model) {
+        h->tr_on = false;
+        return SABER_OK;
+    }
+    int rc = triage_upload_model(h, h->tr_model, h->tr_wb, model);
+    if (rc != SABER_OK) return rc;
+    CU(h, cudaStreamSynchronize(h->stream));
+    h->tr_threshold = threshold;
+    h->tr_on = true;
+    return SABER_OK;
+}
+
+int saber_gpu_collect_regions(saber_gpu* h, int32_t collect) {
+    ENTER(h);
+    h->tr_collect = collect != 0;
+    h->tr_rows.clear();
+    h->tr_labels.clear();
+    h->tr_logits.clear();
+    return SABER_OK;
+}
+
+int saber_gpu_collected_regions(saber_gpu* h, float* rows, uint8_t* labels, float* logits, uint64_t cap,
+                                uint64_t* n) {
+    ENTER(h);
+    const uint64_t m = h->tr_labels.size();
+    if (n) *n = m;
+    if (m > cap) return fail(h, SABER_ERR_CAP, "%llu collected regions", (unsigned long long)m);
+    if (rows) std::memcpy(rows, h->tr_rows.data(), m * SABER_TRIAGE_ROW_FLOATS * 4);
+    if (labels) std::memcpy(labels, h->tr_labels.data(), m);
+    if (logits) std::memcpy(logits, h->tr_logits.data(), m * 4);
+    return SABER_OK;
+}
 
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps) {
     ENTER(h);

@@ -322,6 +322,11 @@ __global__ void k_gather_u64_by(const unsigned long long* __restrict__ src, cons
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
 }
 
+__global__ void k_gather_uint4(const uint4* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n,
+                               uint4* __restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
+}
+
 __global__ void k_gather_regions(const saber_region* __restrict__ src, const uint32_t* __restrict__ idx, uint32_t n,
                                  saber_region* __restrict__ dst) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[idx[i]];
@@ -379,7 +384,7 @@ struct ChainArgs {
     const uint64_t* prof_off;
     const uint32_t* prof_mpad;
     int thr, x;
-    uint4* hsp;                       // (lo, hi, score, chain)
+    uint4* hsp;                       // (lo, hi, score, seed hits)
     unsigned long long* hkey;
     uint32_t* hval;
     unsigned long long* nhsp;
@@ -452,9 +457,17 @@ __global__ void k_chains(ChainArgs a) {
             const int score = xdrop(P, mpad, subj, qlen, sl, qp, sp, a.x, lo, hi, steps);
             cover = hi;
             if (score >= a.thr) {
+                // seed hits of the HSP: this one and the later hits of the
+                // chain that its extension covers (query positions below hi)
+                uint32_t nhits = 1;
+                for (uint32_t j = i + 1; j < e; j++) {
+                    const uint32_t gj = a.surv[a.order[j]].y & ((1u << 27) - 1);
+                    if ((int64_t)gj - (int64_t)a.qoffs[q] >= hi) break;
+                    nhits++;
+                }
                 const unsigned long long slot = atomicAdd(a.nhsp, 1ull);
                 if (slot < a.hcap) {
-                    a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, c);
+                    a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, nhits);
                     a.hkey[slot] = key;
                     a.hval[slot] = (uint32_t)slot;
                 }
@@ -479,6 +492,7 @@ struct RegionArgs {
     int64_t join;
     uint32_t kmax;                    // max_regions_per_subject (<= 64)
     saber_region* out;
+    uint4* rstat;                     // per region: HSPs, score sum, seed hits, 0
     unsigned long long* nout;
     uint64_t cap;
     unsigned long long* ctr;          // [7] hsps, [8] weak dropped
@@ -496,10 +510,11 @@ __global__ void k_regions(RegionArgs a) {
         hsps += e - b;
         // top kmax regions by (best desc, d_min asc)
         saber_region top[64];
+        uint4 tst[64];
         uint32_t ntop = 0;
         int64_t dmin = 0, dmax = 0;
         int best = 0;
-        uint32_t evn = 0;
+        uint32_t evn = 0, evh = 0;
         int32_t evs = 0;
         bool open = false;
         auto close = [&]() {
@@ -519,8 +534,12 @@ __global__ void k_regions(RegionArgs a) {
                 pos--;
             if (pos >= a.kmax) return;
             uint32_t last = ntop < a.kmax ? ntop : a.kmax - 1;
-            for (uint32_t k = last; k > pos; k--) top[k] = top[k - 1];
+            for (uint32_t k = last; k > pos; k--) {
+                top[k] = top[k - 1];
+                tst[k] = tst[k - 1];
+            }
             top[pos] = r;
+            tst[pos] = make_uint4(evn, (uint32_t)evs, evh, 0u);
             if (ntop < a.kmax) ntop++;
         };
         for (uint32_t i = b; i < e; i++) {
@@ -531,6 +550,7 @@ __global__ void k_regions(RegionArgs a) {
                 if (d > dmax) dmax = d;
                 if (score > best) best = score;
                 evn++;
+                evh += h.w;
                 const int64_t sum = (int64_t)evs + score;
                 evs = sum > INT32_MAX ? INT32_MAX : (int32_t)sum;
             } else {
@@ -539,6 +559,7 @@ __global__ void k_regions(RegionArgs a) {
                 dmin = dmax = d;
                 best = score;
                 evn = 1;
+                evh = h.w;
                 evs = score;
             }
         }
@@ -546,7 +567,10 @@ __global__ void k_regions(RegionArgs a) {
         if (ntop) {
             const unsigned long long base = atomicAdd(a.nout, (unsigned long long)ntop);
             for (uint32_t k = 0; k < ntop; k++)
-                if (base + k < a.cap) a.out[base + k] = top[k];
+                if (base + k < a.cap) {
+                    a.out[base + k] = top[k];
+                    a.rstat[base + k] = tst[k];
+                }
         }
     }
     atomicAdd(&a.ctr[7], hsps);
@@ -668,7 +692,7 @@ static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
 
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
                  saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
-                 std::vector<saber_region>* all) {
+                 std::vector<saber_region>* all, std::vector<uint4>* rstats) {
     const Dataset& ds = h->main;
     const QuerySet& qs = ds.qs;
     if (!ds.has_db || !qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
@@ -810,6 +834,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     CU(h, cudaEventRecord(ev[2], s));
     uint64_t nregions = 0;
     std::vector<saber_region> regs;
+    std::vector<uint4> rstat_all;
     if (ns) {
         CUALLOC(h, h->sc_key1, (uint64_t)ns * 8);
         CUALLOC(h, h->sc_key1o, (uint64_t)ns * 8);
@@ -898,6 +923,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                                              h->sc_flags.as<uint8_t>(), h->sc_pairs.as<uint32_t>(), npairs, (int)nhsp, s));
             uint64_t rcap = (uint64_t)nhsp + 16;
             CUALLOC(h, h->sc_regions, rcap * sizeof(saber_region));
+            CUALLOC(h, h->sc_rstat, rcap * sizeof(uint4));
             RegionArgs r;
             r.hsp = h->sc_hsp.as<uint4>();
             r.order = h->sc_hvalo.as<uint32_t>();
@@ -910,6 +936,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             r.join = 2 * (int64_t)p->window_slack;
             r.kmax = std::max<uint32_t>(1, p->max_regions_per_subject);
             r.out = h->sc_regions.as<saber_region>();
+            r.rstat = h->sc_rstat.as<uint4>();
             r.nout = ctr + 12;
             r.cap = rcap;
             r.ctr = ctr;
@@ -956,6 +983,14 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                                                                    h->sc_regions2.as<saber_region>());
                 CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions2.p, nregions * sizeof(saber_region),
                                       cudaMemcpyDeviceToHost, s));
+                if (rstats) {
+                    CUALLOC(h, h->sc_rstat2, (uint64_t)nrg * sizeof(uint4));
+                    k_gather_uint4<<<nblocks(nrg, 256), 256, 0, s>>>(h->sc_rstat.as<uint4>(), ib, nrg,
+                                                                     h->sc_rstat2.as<uint4>());
+                    rstat_all.resize(nregions);
+                    CU(h, cudaMemcpyAsync(rstat_all.data(), h->sc_rstat2.p, nregions * sizeof(uint4),
+                                          cudaMemcpyDeviceToHost, s));
+                }
             }
         }
     } else {
@@ -976,6 +1011,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     size_t i = 0;
     bool overflow = false;
     if (all) all->clear();
+    if (rstats) rstats->clear();
     while (i < regs.size()) {
         size_t j = i;
         while (j < regs.size() && regs[j].query == regs[i].query) j++;
@@ -983,6 +1019,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         local.regions_dropped_by_cap += (j - i) - take;
         for (uint64_t k = 0; k < take; k++) {
             if (all) all->push_back(regs[i + k]);
+            if (rstats) rstats->push_back(rstat_all.empty() ? make_uint4(0, 0, 0, 0) : rstat_all[i + k]);
             else if (w < out_cap) out[w] = regs[i + k];
             else overflow = true;
             w++;

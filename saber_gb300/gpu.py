@@ -102,10 +102,10 @@ class SearchParamsC(ctypes.Structure):
 class SearchStats(ctypes.Structure):
     """saber_search_stats (include/saber_gpu.h)."""
     _fields_ = [("scan", ScanStats), ("traceback", TracebackStats)] + [
-        (n, ctypes.c_uint64) for n in ("regions", "band_scored_regions", "band_rescored", "banded_cells",
-                                       "score_launches", "alignments")] + [
-        (n, ctypes.c_double) for n in ("t_prep_ms", "t_scan_ms", "t_plan_ms", "t_score_ms", "t_finish_ms",
-                                       "t_total_ms")]
+        (n, ctypes.c_uint64) for n in ("regions", "triage_dropped", "band_scored_regions", "band_rescored",
+                                       "banded_cells", "score_launches", "alignments")] + [
+        (n, ctypes.c_double) for n in ("t_prep_ms", "t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms",
+                                       "t_finish_ms", "t_total_ms")]
 
     def as_dict(self):
         d = {}
@@ -116,6 +116,20 @@ class SearchStats(ctypes.Structure):
             d[n] = float(v) if n.startswith("t_") else int(v)
         return d
 
+
+class TriageTrainCfg(ctypes.Structure):
+    """saber_triage_train_cfg (include/saber_gpu.h)."""
+    _fields_ = [("epochs", ctypes.c_uint32), ("batch", ctypes.c_uint32), ("lr", ctypes.c_float),
+                ("pos_weight", ctypes.c_float), ("weight_decay", ctypes.c_float), ("pad_", ctypes.c_uint32),
+                ("seed", ctypes.c_uint64)]
+
+
+class TriageTrainStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_uint64), ("final_loss", ctypes.c_double)]
+
+
+TRIAGE_MODEL_FLOATS = 74561
+TRIAGE_ROW_FLOATS = 32
 
 # saber_hit
 HIT_DTYPE = np.dtype([("query", "<u4"), ("subject", "<u4"), ("score", "<i4"), ("exact", "<u4"),
@@ -206,6 +220,12 @@ def load_library():
         "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_set_pair_steps": (ctypes.c_int, [P, U32]),
         "saber_gpu_search": (ctypes.c_int, [P, P, P, P, U64, P, P, U32, P, P, U64, P, P, U64, P, P]),
+        "saber_gpu_triage_grads": (ctypes.c_int, [P, P, P, P, U32, ctypes.c_float, P, P]),
+        "saber_gpu_triage_train": (ctypes.c_int, [P, P, P, P, U64, P, P]),
+        "saber_gpu_triage_predict": (ctypes.c_int, [P, P, P, U64, P]),
+        "saber_gpu_set_triage": (ctypes.c_int, [P, P, ctypes.c_float]),
+        "saber_gpu_collect_regions": (ctypes.c_int, [P, I32]),
+        "saber_gpu_collected_regions": (ctypes.c_int, [P, P, P, P, U64, P]),
         "saber_gpu_get_pair_steps": (U32, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
@@ -408,6 +428,58 @@ class Device:
                 continue
             self._check(rc, "search")
         self._check(rc, "search")
+
+    # ---- learned triage ----
+    def triage_grads(self, model, rows, labels, pos_weight=1.0):
+        """(gradients in the model layout, loss) of one forward + backward pass."""
+        m = np.ascontiguousarray(model, dtype=np.float32)
+        x = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, TRIAGE_ROW_FLOATS)
+        y = np.ascontiguousarray(labels, dtype=np.uint8)
+        g = np.zeros(TRIAGE_MODEL_FLOATS, np.float32)
+        loss = ctypes.c_double()
+        self._check(self.lib.saber_gpu_triage_grads(self.h, _ptr(m), _ptr(x), _ptr(y), x.shape[0],
+                                                    float(pos_weight), _ptr(g), ctypes.byref(loss)), "triage_grads")
+        return g, loss.value
+
+    def triage_train(self, model, rows, labels, epochs=8, batch=1024, lr=1e-3, pos_weight=1.0, weight_decay=0.0,
+                     seed=0):
+        """Adam training on the GPU; returns (trained model, stats)."""
+        m = np.ascontiguousarray(model, dtype=np.float32).copy()
+        x = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, TRIAGE_ROW_FLOATS)
+        y = np.ascontiguousarray(labels, dtype=np.uint8)
+        cfg = TriageTrainCfg(epochs=epochs, batch=batch, lr=lr, pos_weight=pos_weight, weight_decay=weight_decay,
+                             seed=seed)
+        st = TriageTrainStats()
+        self._check(self.lib.saber_gpu_triage_train(self.h, _ptr(m), _ptr(x), _ptr(y), x.shape[0], ctypes.byref(cfg),
+                                                    ctypes.byref(st)), "triage_train")
+        return m, {"steps": int(st.steps), "final_loss": float(st.final_loss)}
+
+    def triage_predict(self, model, rows):
+        m = np.ascontiguousarray(model, dtype=np.float32)
+        x = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, TRIAGE_ROW_FLOATS)
+        out = np.zeros(x.shape[0], np.float32)
+        self._check(self.lib.saber_gpu_triage_predict(self.h, _ptr(m), _ptr(x), x.shape[0], _ptr(out)),
+                    "triage_predict")
+        return out
+
+    def set_triage(self, model, threshold=0.0):
+        m = None if model is None else np.ascontiguousarray(model, dtype=np.float32)
+        self._check(self.lib.saber_gpu_set_triage(self.h, _ptr(m), float(threshold)), "set_triage")
+
+    def collect_regions(self, on=True):
+        self._check(self.lib.saber_gpu_collect_regions(self.h, 1 if on else 0), "collect_regions")
+
+    def collected_regions(self):
+        """(feature rows n x 32, labels, logits) of the regions of the last search."""
+        n = ctypes.c_uint64()
+        self.lib.saber_gpu_collected_regions(self.h, None, None, None, 0, ctypes.byref(n))
+        k = int(n.value)
+        rows = np.zeros((k, TRIAGE_ROW_FLOATS), np.float32)
+        y = np.zeros(k, np.uint8)
+        z = np.zeros(k, np.float32)
+        self._check(self.lib.saber_gpu_collected_regions(self.h, _ptr(rows), _ptr(y), _ptr(z), k, ctypes.byref(n)),
+                    "collected_regions")
+        return rows, y, z
 
     @property
     def strip_rows(self):
