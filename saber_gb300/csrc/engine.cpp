@@ -853,32 +853,40 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
         // learned triage (a no-op without a model or collection): regions
         // arrive grouped by query in region order
         const uint64_t nr = regs.size();
+        std::vector<uint64_t> qstart(nq + 1, 0);
+        for (const saber_region& r : regs) qstart[r.query + 1]++;
+        for (uint32_t qi = 0; qi < nq; qi++) qstart[qi + 1] += qstart[qi];
         std::vector<uint32_t> rq(nr), rrank(nr);
-        std::vector<float4> qinfo(nq, make_float4(0.f, 0.f, 0.f, 0.f));
-        for (uint32_t qi = 0; qi < nq; qi++) qinfo[qi] = make_float4((float)qlens[qi], (float)preps[qi].region_thr, 0.f, 0.f);
-        for (uint64_t t = 0; t < nr; t++) {
-            const uint32_t q = regs[t].query;
-            rq[t] = q;
-            rrank[t] = (uint32_t)qinfo[q].w;
-            if (qinfo[q].w == 0.f) qinfo[q].z = (float)regs[t].best;
-            qinfo[q].w += 1.f;
-        }
+        std::vector<float4> qinfo(nq);
+        parallel_for(nq, [&](size_t qi) {
+            const uint64_t b = qstart[qi], e = qstart[qi + 1];
+            for (uint64_t t = b; t < e; t++) {
+                rq[t] = (uint32_t)qi;
+                rrank[t] = (uint32_t)(t - b);
+            }
+            qinfo[qi] = make_float4((float)qlens[qi], (float)preps[qi].region_thr, e > b ? (float)regs[b].best : 0.f,
+                                    (float)(e - b));
+        });
         std::vector<uint8_t> keep;
         bool tri = false;
         rc = saber::triage_regions(h, regs, rstat, rq, rrank, qinfo, (float)P.lambda, (float)std::log(P.k), keep, &tri);
         if (rc != SABER_OK) return rc;
         collecting = tri;
-        std::vector<size_t> cnt(nq + 1, 0);
-        for (const saber_region& r : regs) cnt[r.query + 1]++;
-        for (uint32_t qi = 0; qi < nq; qi++) per_q[qi].reserve(cnt[qi + 1]);
-        for (uint64_t t = 0; t < nr; t++) {
-            const saber_region& r = regs[t];
-            if (!keep[t]) {
-                E.st.triage_dropped++;
-                continue;
+        std::vector<uint64_t> dropped(nq, 0);
+        parallel_for(nq, [&](size_t qi) {
+            const uint64_t b = qstart[qi], e = qstart[qi + 1];
+            auto& v = per_q[qi];
+            v.reserve(e - b);
+            for (uint64_t t = b; t < e; t++) {
+                if (!keep[t]) {
+                    dropped[qi]++;
+                    continue;
+                }
+                const saber_region& r = regs[t];
+                v.push_back({r.subject, r.d_min, r.d_max, r.best, t});
             }
-            per_q[r.query].push_back({r.subject, r.d_min, r.d_max, r.best, t});
-        }
+        });
+        for (uint64_t d : dropped) E.st.triage_dropped += d;
     }
     for (uint32_t qi = 0; qi < nq; qi++) {
         if (qlens[qi] == 0) per_q[qi].clear();

@@ -392,94 +392,133 @@ struct ChainArgs {
     unsigned long long* ctr;          // [4] extensions, [5] avoided, [6] steps
 };
 
-// Ungapped X-drop through (qp, sp) (ungapped_xdrop, engine.rs:2460-2494, with
-// the step count of xdrop_cat, scan.rs:859-904).
-__device__ __forceinline__ int xdrop(const int16_t* P, int mpad, const uint8_t* s, int64_t qlen, int64_t sl,
-                                     int64_t qp, int64_t sp, int x, int64_t& lo, int64_t& hi, uint64_t& steps) {
-    const int64_t nr = min(qlen - qp, sl - sp), nl = min(qp, sp);
-    int best_r = 0, cur = 0;
-    int64_t tr = 0, end_t = 0;
-    while (tr < nr) {
-        cur += P[(size_t)s[sp + tr] * mpad + qp + tr];
-        tr++;
-        if (cur > best_r) {
-            best_r = cur;
-            end_t = tr;
+// One direction of the ungapped X-drop (ungapped_xdrop, engine.rs:2460-2494,
+// step count of xdrop_cat, scan.rs:859-904), 32 positions per warp round:
+// position t (0-based) scores P[s[sp + dir (t + off)]][qp + dir (t + off)]
+// with off = 0 rightwards (dir = +1) and 1 leftwards (dir = -1).  The
+// running sum, the running best (starting at 0) and the first position where
+// the sum falls more than x below the best come from warp scans; as in the
+// scalar loops, the stop position is evaluated, later ones are not, and the
+// extent is the first position of the best sum (strictly greater than every
+// earlier one).  Returns the best; *ext = extent (0 if the best is 0),
+// *evaluated = positions evaluated.
+__device__ __forceinline__ int xdrop_dir(const int16_t* __restrict__ P, int mpad, const uint8_t* __restrict__ s,
+                                         int64_t qp, int64_t sp, int64_t n, int dir, int x, int lane, int64_t* ext,
+                                         int64_t* evaluated) {
+    const int off = dir > 0 ? 0 : 1;
+    int best = 0, cur = 0;
+    int64_t e = 0, done = 0;
+    for (int64_t base = 0; base < n; base += 32) {
+        const int64_t t = base + lane;
+        const bool valid = t < n;
+        int v = 0;
+        if (valid) {
+            const int64_t d = dir * (t + off);
+            v = P[(size_t)s[sp + d] * mpad + qp + d];
         }
-        if (cur < best_r - x) break;
-    }
-    int best_l = 0;
-    cur = 0;
-    int64_t tl = 1, st_t = 0;
-    if (nl > 0) {
-        for (;;) {
-            cur += P[(size_t)s[sp - tl] * mpad + qp - tl];
-            if (cur > best_l) {
-                best_l = cur;
-                st_t = tl;
-            }
-            tl++;
-            if (!(tl <= nl && cur >= best_l - x)) break;
+        int c = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, c, o);
+            if (lane >= o) c += u;
         }
+        c += cur;
+        int m = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, m, o);
+            if (lane >= o) m = max(m, u);
+        }
+        m = max(m, best);
+        const int prev = __shfl_up_sync(0xffffffffu, m, 1);
+        const int excl = lane == 0 ? best : prev;
+        const unsigned viol = __ballot_sync(0xffffffffu, valid && c < m - x);
+        const int64_t left = n - 1 - base;
+        int limit = left < 31 ? (int)left : 31;
+        if (viol) limit = min(limit, __ffs(viol) - 1);
+        const unsigned upto = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
+        const unsigned rec = __ballot_sync(0xffffffffu, valid && c > excl) & upto;
+        if (rec) e = base + (31 - __clz(rec)) + 1;
+        best = __shfl_sync(0xffffffffu, m, limit);
+        cur = __shfl_sync(0xffffffffu, c, limit);
+        done = base + limit + 1;
+        if (viol) break;
     }
-    steps += (uint64_t)(tr + tl - 1);
-    lo = qp - st_t;
-    hi = qp + end_t;
-    return best_r + best_l;
+    *ext = e;
+    *evaluated = done;
+    return best;
 }
 
-__global__ void k_chains(ChainArgs a) {
-    unsigned long long ext = 0, avoided = 0;
-    uint64_t steps = 0;
+// One warp per chain (one subject, query and diagonal; hits in (query
+// position, shape) order): the coverage test and the X-drop extensions of
+// visit_scan (scan.rs:2384-2431), HSPs of at least thr appended with the
+// number of the chain's seed hits they cover.
+__global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long ext = 0, avoided = 0, steps = 0;
     const uint32_t nch = *a.nchains;
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nch; c += gridDim.x * blockDim.x) {
+    for (uint32_t c = warp0; c < nch; c += nwarps) {
         const uint32_t b = a.starts[c];
         const uint32_t e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
         const unsigned long long key = a.key1s[b];
         const uint64_t s = key >> 40, q = (key >> 20) & 0xFFFFF;
-        const int64_t qlen = (int64_t)(a.qoffs[q + 1] - a.qoffs[q]);
-        const int64_t sl = (int64_t)(a.soffs[s + 1] - a.soffs[s]);
+        const int64_t q0 = (int64_t)a.qoffs[q], s0 = (int64_t)a.soffs[s];
+        const int64_t qlen = (int64_t)a.qoffs[q + 1] - q0;
+        const int64_t sl = (int64_t)a.soffs[s + 1] - s0;
         const int16_t* P = a.prof + a.prof_off[q];
         const int mpad = (int)a.prof_mpad[q];
-        const uint8_t* subj = a.res + a.soffs[s];
+        const uint8_t* subj = a.res + s0;
         int64_t cover = 0;
         for (uint32_t i = b; i < e; i++) {
             const uint2 v = a.surv[a.order[i]];
-            const uint32_t g = v.y & ((1u << 27) - 1);
-            const int64_t qp = (int64_t)g - (int64_t)a.qoffs[q];
-            const int64_t sp = (int64_t)v.x - (int64_t)a.soffs[s];
+            const int64_t qp = (int64_t)(v.y & ((1u << 27) - 1)) - q0;
+            const int64_t sp = (int64_t)v.x - s0;
             if (qp < cover) {
                 avoided++;
                 continue;
             }
             ext++;
-            int64_t lo, hi;
-            const int score = xdrop(P, mpad, subj, qlen, sl, qp, sp, a.x, lo, hi, steps);
+            int64_t end_t, st_t, nr_done, nl_done;
+            const int64_t nr = qlen - qp < sl - sp ? qlen - qp : sl - sp;
+            const int64_t nl = qp < sp ? qp : sp;
+            const int br = xdrop_dir(P, mpad, subj, qp, sp, nr, 1, a.x, lane, &end_t, &nr_done);
+            const int bl = xdrop_dir(P, mpad, subj, qp, sp, nl, -1, a.x, lane, &st_t, &nl_done);
+            steps += (uint64_t)(nr_done + nl_done);
+            const int64_t hi = qp + end_t, lo = qp - st_t;
             cover = hi;
+            const int score = br + bl;
             if (score >= a.thr) {
-                // seed hits of the HSP: this one and the later hits of the
-                // chain that its extension covers (query positions below hi)
+                // seed hits of the HSP: this one and the chain's later hits
+                // below hi (query positions ascend along the chain)
                 uint32_t nhits = 1;
-                for (uint32_t j = i + 1; j < e; j++) {
-                    const uint32_t gj = a.surv[a.order[j]].y & ((1u << 27) - 1);
-                    if ((int64_t)gj - (int64_t)a.qoffs[q] >= hi) break;
-                    nhits++;
+                for (uint32_t j0 = i + 1; j0 < e; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    const bool in = j < e && (int64_t)(a.surv[a.order[j]].y & ((1u << 27) - 1)) - q0 < hi;
+                    const unsigned bal = __ballot_sync(0xffffffffu, in);
+                    const unsigned run = ~bal ? (unsigned)__ffs(~bal) - 1u : 32u;
+                    nhits += run;
+                    if (run < 32) break;
                 }
-                const unsigned long long slot = atomicAdd(a.nhsp, 1ull);
-                if (slot < a.hcap) {
-                    a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, nhits);
-                    a.hkey[slot] = key;
-                    a.hval[slot] = (uint32_t)slot;
+                if (lane == 0) {
+                    const unsigned long long slot = atomicAdd(a.nhsp, 1ull);
+                    if (slot < a.hcap) {
+                        a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, nhits);
+                        a.hkey[slot] = key;
+                        a.hval[slot] = (uint32_t)slot;
+                    }
                 }
             }
         }
     }
-    atomicAdd(&a.ctr[4], ext);
-    atomicAdd(&a.ctr[5], avoided);
-    atomicAdd(&a.ctr[6], (unsigned long long)steps);
+    if (lane == 0) {
+        atomicAdd(&a.ctr[4], ext);
+        atomicAdd(&a.ctr[5], avoided);
+        atomicAdd(&a.ctr[6], steps);
+    }
 }
 
-// ---- regions (finish_subject_into, scan.rs:2437-2474) --------------------------
 struct RegionArgs {
     const uint4* hsp;
     const uint32_t* order;            // HSPs sorted by (subject, query, diagonal)
@@ -897,7 +936,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         c.nhsp = ctr + 11;
         c.hcap = hcap;
         c.ctr = ctr;
-        k_chains<<<nblocks(ns, 128), 128, 0, s>>>(c);
+        k_chains<<<h->sm_count * 8, 256, 0, s>>>(c);
         CU(h, cudaGetLastError());
         unsigned long long nh = 0;
         CU(h, cudaMemcpyAsync(&nh, ctr + 11, 8, cudaMemcpyDeviceToHost, s));

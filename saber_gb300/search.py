@@ -69,6 +69,24 @@ class SearchParams:
                 raise AttributeError(k)
             setattr(self, k, v)
 
+    @classmethod
+    def nucleotide(cls, k=11, **kw):
+        """blastn (nn) mode (src/bin/main.rs:473-545, driver.rs:111-129,
+        344-360): one contiguous k-mer shape over ACGT, no window filter, no
+        composition bias, the default preset's other settings.  Use with
+        Searcher(..., nucleotide=(2, -3), gap_open=7, gap_extend=2)."""
+        p = cls("default")
+        p.preset = "nn"
+        p.alphabet = "acgt"
+        p.shapes = ["1" * k]
+        p.hit_filter_min_ids = 0
+        p.comp_bias = False
+        for key, v in kw.items():
+            if not hasattr(p, key):
+                raise AttributeError(key)
+            setattr(p, key, v)
+        return p
+
 
 class Hit(dict):
     """One reported alignment (Hit, engine.rs:310-357), 1-based inclusive coordinates."""

@@ -184,3 +184,47 @@ def band_jobs(seed, queries, subjects, planted, n_jobs, half_min=8, half_max=128
     jobs["band_hi"] = d0 + h - wlo
     perm = rng.permutation(n_jobs)
     return jobs[perm]
+
+
+def dna_db(seed, n_queries, n_subjects, qlen=(1000, 10000), slen=(1000, 10000), planted_frac=0.10,
+           identity_range=(0.80, 0.95), indel_rate=0.01):
+    """Nucleotide queries and subjects, codes 0..3 = A, C, G, T, uniform
+    (GC 0.5); a fraction of subjects are planted homologs of a random query
+    (substitutions and indels at the given rates, embedded in background)."""
+    rng = np.random.default_rng(seed)
+    ql = rng.integers(qlen[0], qlen[1] + 1, size=n_queries)
+    qs = [rng.integers(0, 4, size=int(l)).astype(np.uint8) for l in ql]
+    sl = rng.integers(slen[0], slen[1] + 1, size=n_subjects)
+    planted = np.full(n_subjects, -1, dtype=np.int64)
+    n_pl = int(round(planted_frac * n_subjects))
+    pl_idx = rng.choice(n_subjects, size=n_pl, replace=False) if n_pl else np.zeros(0, np.int64)
+    planted[pl_idx] = rng.integers(0, n_queries, size=n_pl)
+    subs = []
+    for s in range(n_subjects):
+        q = planted[s]
+        bg = rng.integers(0, 4, size=int(sl[s])).astype(np.uint8)
+        if q >= 0:
+            src = qs[q]
+            a = int(rng.integers(0, max(1, src.size // 2)))
+            b = int(rng.integers(a + min(200, src.size - a), src.size + 1))
+            seg = src[a:b].copy()
+            ident = rng.uniform(*identity_range)
+            sub = rng.random(seg.size) > ident
+            seg[sub] = (seg[sub] + rng.integers(1, 4, size=int(sub.sum()))) % 4
+            out = []
+            i = 0
+            while i < seg.size:
+                if rng.random() < indel_rate:
+                    k = int(rng.geometric(1.0 / 3.0))
+                    if rng.random() < 0.5:
+                        i += k
+                    else:
+                        out.append(rng.integers(0, 4, size=k).astype(np.uint8))
+                    continue
+                out.append(seg[i:i + 1])
+                i += 1
+            body = np.concatenate(out) if out else np.zeros(0, np.uint8)
+            cut = int(rng.integers(0, bg.size + 1))
+            bg = np.concatenate([bg[:cut], body, bg[cut:]]).astype(np.uint8)
+        subs.append(bg)
+    return _concat(qs), _concat(subs), planted

@@ -64,3 +64,19 @@ def test_native_engine_matches_python_engine(dev, preset, kw):
     want = se.search_py(qs.codes, qs.offsets)
     assert sum(len(h) for h in want) > 0
     _compare(got, want)
+
+
+def test_nucleotide_search_matches_oracle(dev):
+    """blastn (nn) mode: contiguous 11-mers over ACGT, +2/-3 with SABER gaps
+    7/2 (BLAST 5/2), even-score E-values; hits and m8 rows identical to the
+    oracle pipeline on planted 80-95 % identity homologs."""
+    from saber_gb300.stats import gapped_nucleotide
+    qs, ss, planted = synth.dna_db(71, 10, 120, qlen=(800, 3000), slen=(1000, 5000))
+    P = SearchParams.nucleotide()
+    se = Searcher(dev, ss.codes, ss.offsets, P, gap_open=7, gap_extend=2, nucleotide=(2, -3))
+    got = se.search(qs.codes, qs.offsets)
+    want = oeng.search_batch(ss.codes, ss.offsets, qs.codes, qs.offsets, P, se.matrix, 7, 2,
+                             gapped_nucleotide(2, -3, 7, 2), se.scan_params, None, None, is_protein=False)
+    assert sum(len(h) for h in want) >= 5
+    _compare(got, want)
+    assert [len(h) for h in got] == [len(h) for h in se.search_py(qs.codes, qs.offsets)]
