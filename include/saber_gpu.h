@@ -411,6 +411,18 @@ int32_t saber_gpu_get_strip_rows(saber_gpu* h);
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
 
+/* Captured scoring graphs (default on): saber_gpu_score_band_jobs (and so
+ * the batch engine's scoring stages) runs classify -> radix sort -> int16
+ * kernels -> int32 kernel as one CUDA graph with every count kept on the
+ * device, job count padded to a power of two and scratch sized for the
+ * widest band rounded up to a power of two; a graph is captured once per
+ * size bucket and buffer set and replayed.  Off: the step-by-step launches
+ * (which also report per-stage device times).  Results do not depend on it.
+ * saber_gpu_graph_captures counts the captures of the handle. */
+int saber_gpu_set_graphs(saber_gpu* h, int32_t on);
+int32_t saber_gpu_get_graphs(saber_gpu* h);
+uint64_t saber_gpu_graph_captures(saber_gpu* h);
+
 /* Allocation-free variant of saber_gpu_score_band_jobs_dev.  No counterpart
  * in the reference: it exists for callers that cannot allocate GPU memory at
  * scoring time — code between the nodes of a CUDA graph being captured, a

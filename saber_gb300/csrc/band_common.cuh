@@ -73,6 +73,7 @@ struct FastArgs {
     const uint32_t* order;  // sorted job indices of this launch's class
     const uint32_t* n_ptr;  // device count of those jobs
     const uint32_t* np_ptr; // device count of the paired jobs among them (at the end), or null
+    const uint32_t* order_skip;  // device count of leading entries of order to skip, or null
     uint32_t* wt_counter;
     uint2* bufs;
     uint32_t buf_stride;

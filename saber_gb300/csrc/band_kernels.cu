@@ -474,8 +474,10 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
     const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
     const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_ptr, const uint32_t* __restrict__ np_ptr,
-    uint32_t* __restrict__ wt_counter, uint2* __restrict__ bufs, uint32_t buf_stride, int go, int ge,
-    int32_t* __restrict__ scores, uint32_t* __restrict__ rescue, uint32_t* __restrict__ rescue_count) {
+    const uint32_t* __restrict__ order_skip, uint32_t* __restrict__ wt_counter, uint2* __restrict__ bufs,
+    uint32_t buf_stride, int go, int ge, int32_t* __restrict__ scores, uint32_t* __restrict__ rescue,
+    uint32_t* __restrict__ rescue_count) {
+    if (order_skip) order += *order_skip;
     const int lane = threadIdx.x & 31;
     const uint32_t gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint2* mybuf = bufs + (size_t)gwarp * buf_stride * 32 + lane;
@@ -684,11 +686,11 @@ int band_fast_blocks_per_sm(int strip_rows) {
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a) {
     if (a.strip_rows == 8)
         k_band_fast<8><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                            a.n_ptr, a.np_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                            a.n_ptr, a.np_ptr, a.order_skip, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                             a.rescue, a.rescue_count);
     else
         k_band_fast<16><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                             a.n_ptr, a.np_ptr, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
+                                             a.n_ptr, a.np_ptr, a.order_skip, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
                                              a.rescue, a.rescue_count);
     return cudaGetLastError();
 }

@@ -65,6 +65,20 @@ struct Dataset {
     QuerySet qs;
 };
 
+// Key of a captured scoring graph: sizes, settings and every buffer it reads
+// or writes (a reallocated buffer means a new capture).
+struct GraphKey {
+    uint64_t npad, wcap, n_res;
+    int32_t rows, go, ge;
+    uint32_t pair_steps, nq, pad_;
+    const void* ptrs[16];
+    bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
+};
+struct GraphEntry {
+    cudaGraphExec_t exec;
+    const void* extra;
+};
+
 struct Scheme {
     int32_t matrix[576];
     int32_t go = 11, ge = 1;
@@ -82,6 +96,11 @@ struct saber_gpu {
     int sm_count = 0;
     int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
     uint32_t pair_steps = saber::kPairStepsDefault;  // tuning: paired-strip threshold
+    // captured scoring graphs (saber_gpu_score_band_jobs with graphs on)
+    bool use_graphs = true;
+    uint64_t graph_captures = 0;
+    saber::DevBuf g_nreal;
+    std::vector<std::pair<saber::GraphKey, saber::GraphEntry>> graphs;
     // the handle's scheme and dataset (set_scheme / load_db / load_queries)
     saber::Scheme scheme;
     saber::Dataset main;

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "band_common.cuh"
@@ -75,8 +76,8 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
 // Packed-class keys order jobs by (strips, width, query) so that the 64
 // consecutive jobs of a warp task share their loop counts and widths; within
 // class 0 the paired jobs (bit 61; their strips counted in 2R rows) sort last.
-__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, int R, uint32_t pair_steps,
-                           const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
+__global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, const uint32_t* __restrict__ n_real,
+                           int R, uint32_t pair_steps, const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
                            uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                            int32_t* __restrict__ scores, uint32_t* __restrict__ counts,
                            unsigned long long* __restrict__ stats) {
@@ -84,9 +85,16 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
     uint64_t cells = 0, fcells = 0;
     uint32_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, cp = 0, bad = 0;
     unsigned long long w0 = 0, w1 = 0, w2 = 0;
+    // padded launches (captured graphs): entries past the real job count sort
+    // last as empty jobs and are neither scored nor counted
+    const uint64_t nreal = n_real ? *n_real : njobs;
     for (; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
-        saber_band_job j = jobs[t];
         vals[t] = (uint32_t)t;
+        if (t >= nreal) {
+            keys[t] = (3ull << 62) | t;
+            continue;
+        }
+        saber_band_job j = jobs[t];
         bool ok = j.query < nq && j.win_begin + (uint64_t)j.win_len <= n_res;
         int64_t m = ok ? (int64_t)(qoffs[j.query + 1] - qoffs[j.query]) : 0;
         int64_t lo = j.band_lo, hi = j.band_hi;
@@ -230,7 +238,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, h->strip_rows, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
+        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
         h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
     CU(h, cudaGetLastError());
@@ -296,6 +304,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         a.order = order + (pass == 0 ? 0 : n_fast);
         a.n_ptr = counts + (pass == 0 ? 0 : 7);
         a.np_ptr = pass == 0 ? counts + 9 : nullptr;
+        a.order_skip = nullptr;
         a.wt_counter = counts + (pass == 0 ? 6 : 8);
         a.bufs = h->bufs.as<uint2>();
         a.buf_stride = stride;
@@ -346,6 +355,190 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     local.t_fast_ms = t12;
     local.t_generic_ms = t23;
     if (st) *st = local;
+    return SABER_OK;
+}
+
+// Generic list for a captured scoring graph: the int32 class's jobs (after
+// the R-row and 8-row classes in the sorted order), counts read on the device.
+__global__ void k_copy_generic(const uint32_t* __restrict__ order, uint32_t* __restrict__ counts,
+                               uint32_t* __restrict__ list) {
+    const uint32_t n_fast = counts[0], n_fast8 = counts[7], n_gen = counts[1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_gen; i += gridDim.x * blockDim.x)
+        list[i] = order[n_fast + n_fast8 + i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[5] = n_gen;
+}
+
+static uint64_t pow2_at_least(uint64_t v, uint64_t lo) {
+    uint64_t p = lo;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// The scoring pipeline as a CUDA graph: the same kernels as score_pipeline
+// with every count kept on the device (the real job count in a device word,
+// padded entries sorted last as empty jobs), scratch sized for a power-of-two
+// job count and band width, captured once per (size bucket, buffers,
+// settings) and replayed.  Jobs and scores live in the handle's buffers.
+static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& ds, uint64_t njobs, uint64_t wmax,
+                                saber_score_stats* st) {
+    if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
+    if (!ds.has_db) return fail(h, SABER_ERR_STATE, "no database loaded");
+    if (!ds.qs.has) return fail(h, SABER_ERR_STATE, "no query set loaded");
+    const uint64_t npad = pow2_at_least(njobs, 1 << 12);
+    const uint64_t wcap = pow2_at_least(wmax + 1, 64);
+    if (npad >= (1ull << 31)) return fail(h, SABER_ERR_ARG, "too many jobs in one call");
+    cudaStream_t s = h->stream;
+    const QuerySet& qs = ds.qs;
+    CUALLOC(h, h->keys_in, npad * 8);
+    CUALLOC(h, h->keys_out, npad * 8);
+    CUALLOC(h, h->vals_in, npad * 4);
+    CUALLOC(h, h->vals_out, npad * 4);
+    CUALLOC(h, h->counts, 16 * 4);
+    CUALLOC(h, h->stats, 8 * 8);
+    CUALLOC(h, h->list, npad * 4);
+    CUALLOC(h, h->g_nreal, 16);
+    const int rows0 = h->strip_rows;
+    const unsigned grid0 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(rows0));
+    const unsigned grid8 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(kStripRowsMin));
+    const uint64_t warps = (uint64_t)std::max(grid0, grid8) * 256 / 32;
+    CUALLOC(h, h->bufs, warps * wcap * 32 * sizeof(uint2));
+    const unsigned gT = 128, gGrid = (unsigned)(h->sm_count * 4);
+    CUALLOC(h, h->slabs, (uint64_t)gGrid * gT * wcap * 4 * sizeof(int32_t));
+    size_t t_sort = 0;
+    CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t_sort, h->keys_in.as<uint64_t>(), h->keys_out.as<uint64_t>(),
+                                          h->vals_in.as<uint32_t>(), h->vals_out.as<uint32_t>(), (int)npad, 0, 64, s));
+    CUALLOC(h, h->cub_tmp, t_sort);
+    GraphKey key;
+    std::memset(&key, 0, sizeof(key));
+    key.npad = npad;
+    key.wcap = wcap;
+    key.rows = rows0;
+    key.go = sch.go;
+    key.ge = sch.ge;
+    key.pair_steps = h->pair_steps;
+    key.n_res = ds.n_res;  // scalar kernel parameters baked into the graph
+    key.nq = qs.nq;
+    const void* ptrs[16] = {h->jobs_dev.p, h->scores_dev.p, h->keys_in.p, h->keys_out.p, h->vals_in.p,
+                            h->vals_out.p, h->counts.p, h->stats.p, h->list.p, h->bufs.p, h->slabs.p,
+                            h->cub_tmp.p, ds.res.p, qs.prof.p, qs.offsets.p, qs.prof_off.p};
+    std::memcpy(key.ptrs, ptrs, sizeof(ptrs));
+    const void* extra = qs.prof_mpad.p;  // (pointer identity of the last profile table)
+    cudaGraphExec_t exec = nullptr;
+    for (auto& e : h->graphs)
+        if (e.first == key && e.second.extra == extra) exec = e.second.exec;
+    if (!exec) {
+        uint32_t* counts = h->counts.as<uint32_t>();
+        unsigned long long* stats = h->stats.as<unsigned long long>();
+        const saber_band_job* d_jobs = h->jobs_dev.as<saber_band_job>();
+        int32_t* d_scores = h->scores_dev.as<int32_t>();
+        CU(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        bool ok = true;
+        auto chk = [&](cudaError_t e) {
+            if (e != cudaSuccess) ok = false;
+        };
+        chk(cudaMemsetAsync(counts, 0, 16 * 4, s));
+        chk(cudaMemsetAsync(stats, 0, 8 * 8, s));
+        k_classify<<<nblocks(npad, 256, h->sm_count * 8), 256, 0, s>>>(
+            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq,
+            ds.n_res, h->keys_in.as<uint64_t>(), h->vals_in.as<uint32_t>(), d_scores, counts, stats);
+        chk(cudaGetLastError());
+        size_t tb = h->cub_tmp.cap;
+        chk(cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->keys_in.as<uint64_t>(), h->keys_out.as<uint64_t>(),
+                                            h->vals_in.as<uint32_t>(), h->vals_out.as<uint32_t>(), (int)npad, 0, 64,
+                                            s));
+        const uint32_t* order = h->vals_out.as<uint32_t>();
+        k_copy_generic<<<h->sm_count * 4, 256, 0, s>>>(order, counts, h->list.as<uint32_t>());
+        chk(cudaGetLastError());
+        for (int pass = 0; pass < 2; pass++) {
+            FastArgs a;
+            a.res = ds.res.as<uint8_t>();
+            a.prof = qs.prof.as<int16_t>();
+            a.prof_off = qs.prof_off.as<uint64_t>();
+            a.prof_mpad = qs.prof_mpad.as<uint32_t>();
+            a.qoffs = qs.offsets.as<uint64_t>();
+            a.jobs = d_jobs;
+            a.order = order;
+            a.n_ptr = counts + (pass == 0 ? 0 : 7);
+            a.np_ptr = pass == 0 ? counts + 9 : nullptr;
+            a.order_skip = pass == 0 ? nullptr : counts + 0;
+            a.wt_counter = counts + (pass == 0 ? 6 : 8);
+            a.bufs = h->bufs.as<uint2>();
+            a.buf_stride = (uint32_t)wcap;
+            a.go = sch.go;
+            a.ge = sch.ge;
+            a.scores = d_scores;
+            a.rescue = h->list.as<uint32_t>();
+            a.rescue_count = counts + 5;
+            a.strip_rows = pass == 0 ? rows0 : kStripRowsMin;
+            chk(launch_band_fast(pass == 0 ? grid0 : grid8, s, a));
+        }
+        GenericArgs g;
+        g.res = ds.res.as<uint8_t>();
+        g.prof = qs.prof.as<int16_t>();
+        g.prof_off = qs.prof_off.as<uint64_t>();
+        g.prof_mpad = qs.prof_mpad.as<uint32_t>();
+        g.qoffs = qs.offsets.as<uint64_t>();
+        g.jobs = d_jobs;
+        g.list = h->list.as<uint32_t>();
+        g.list_count = counts + 5;
+        g.slabs = h->slabs.as<int32_t>();
+        g.slab_stride = (uint32_t)wcap;
+        g.go = sch.go;
+        g.ge = sch.ge;
+        g.scores = d_scores;
+        chk(launch_band_generic(gGrid, gT, s, g));
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (e != cudaSuccess || !ok || !graph) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(h, SABER_ERR_CUDA, "capture of the scoring graph failed: %s", cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(h, SABER_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        if (h->graphs.size() >= 8) {
+            cudaGraphExecDestroy(h->graphs.front().second.exec);
+            h->graphs.erase(h->graphs.begin());
+        }
+        GraphEntry ge_{exec, extra};
+        h->graphs.push_back({key, ge_});
+        h->graph_captures++;
+    }
+    const uint32_t nreal = (uint32_t)njobs;
+    CU(h, cudaMemcpyAsync(h->g_nreal.p, &nreal, 4, cudaMemcpyHostToDevice, s));
+    cudaEvent_t e0, e1;
+    CU(h, cudaEventCreate(&e0));
+    CU(h, cudaEventCreate(&e1));
+    CU(h, cudaEventRecord(e0, s));
+    CU(h, cudaGraphLaunch(exec, s));
+    CU(h, cudaEventRecord(e1, s));
+    uint32_t hc[10];
+    unsigned long long hs[6];
+    CU(h, cudaMemcpyAsync(hc, h->counts.p, 10 * 4, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaMemcpyAsync(hs, h->stats.p, 6 * 8, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (hs[3] != 0)
+        return fail(h, SABER_ERR_ARG, "%llu job(s) reference a query or window outside the loaded data", hs[3]);
+    if (std::max<uint64_t>(std::max<uint64_t>(hs[1], hs[5]), hs[2]) + 1 > wcap)
+        return fail(h, SABER_ERR_STATE, "band width above the graph's capacity");
+    if (st) {
+        saber_score_stats local{};
+        local.jobs = njobs;
+        local.banded_cells = hs[0];
+        local.fast_cells = hs[4];
+        local.fast_jobs = hc[0] + hc[7];
+        local.generic_jobs = hc[1];
+        local.empty_jobs = hc[4];
+        local.i16_rescored = hc[5] - hc[1];
+        local.kernel_launches = 5;
+        local.library_launches = 9;
+        local.t_fast_ms = ms;
+        *st = local;
+    }
     return SABER_OK;
 }
 
@@ -990,6 +1183,8 @@ int saber_gpu_close(saber_gpu* h) {
         cudaStreamSynchronize(h->stream);
         cudaStreamDestroy(h->stream);
     }
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.second.exec);
+    h->graphs.clear();
     delete h;
     return SABER_OK;
 }
@@ -1032,11 +1227,43 @@ int saber_gpu_score_band_jobs(saber_gpu* h, const saber_band_job* jobs, uint64_t
         if (stats) *stats = saber_score_stats{};
         return SABER_OK;
     }
-    CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
-    CUALLOC(h, h->scores_dev, njobs * 4);
-    CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice, h->stream));
-    int rc = score_pipeline(h, h->scheme, h->main, h->jobs_dev.as<saber_band_job>(), njobs,
+    int rc;
+    if (h->use_graphs) {
+        // the widest clipped band sizes the graph's scratch (host cores)
+        const QuerySet& qs = h->main.qs;
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const uint64_t nt = std::max<uint64_t>(1, std::min<uint64_t>(hw, (njobs + 65535) / 65536));
+        std::vector<uint64_t> part(nt, 0);
+        auto scan_w = [&](uint64_t k) {
+            uint64_t wm = 0;
+            for (uint64_t t = k * njobs / nt; t < (k + 1) * njobs / nt; t++) {
+                const saber_band_job& j = jobs[t];
+                if (j.query >= qs.nq) continue;
+                int64_t lo = j.band_lo, hi = j.band_hi;
+                const int64_t w = clip_band((int64_t)(qs.offs[j.query + 1] - qs.offs[j.query]), j.win_len, lo, hi);
+                wm = std::max<uint64_t>(wm, (uint64_t)w);
+            }
+            part[k] = wm;
+        };
+        std::vector<std::thread> th;
+        for (uint64_t k = 1; k < nt; k++) th.emplace_back(scan_w, k);
+        scan_w(0);
+        for (auto& x : th) x.join();
+        uint64_t wmax = 0;
+        for (uint64_t v : part) wmax = std::max(wmax, v);
+        const uint64_t npad = pow2_at_least(njobs, 1 << 12);
+        CUALLOC(h, h->jobs_dev, npad * sizeof(saber_band_job));
+        CUALLOC(h, h->scores_dev, npad * 4);
+        CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice, h->stream));
+        rc = score_pipeline_graph(h, h->scheme, h->main, njobs, wmax, stats);
+    } else {
+        CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
+        CUALLOC(h, h->scores_dev, njobs * 4);
+        CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice,
+                              h->stream));
+        rc = score_pipeline(h, h->scheme, h->main, h->jobs_dev.as<saber_band_job>(), njobs,
                             h->scores_dev.as<int32_t>(), stats);
+    }
     if (rc != SABER_OK) return rc;
     CU(h, cudaMemcpyAsync(scores, h->scores_dev.p, njobs * 4, cudaMemcpyDeviceToHost, h->stream));
     CU(h, cudaStreamSynchronize(h->stream));
@@ -1162,6 +1389,16 @@ int saber_gpu_collected_regions(saber_gpu* h, float* rows, uint8_t* labels, floa
     if (logits) std::memcpy(logits, h->tr_logits.data(), m * 4);
     return SABER_OK;
 }
+
+int saber_gpu_set_graphs(saber_gpu* h, int32_t on) {
+    ENTER(h);
+    h->use_graphs = on != 0;
+    return SABER_OK;
+}
+
+int32_t saber_gpu_get_graphs(saber_gpu* h) { return h ? (h->use_graphs ? 1 : 0) : 0; }
+
+uint64_t saber_gpu_graph_captures(saber_gpu* h) { return h ? h->graph_captures : 0; }
 
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps) {
     ENTER(h);

@@ -219,6 +219,9 @@ def load_library():
         "saber_gpu_scan": (ctypes.c_int, [P, P, P, P, P, U64, P, P]),
         "saber_gpu_get_strip_rows": (I32, [P]),
         "saber_gpu_set_pair_steps": (ctypes.c_int, [P, U32]),
+        "saber_gpu_set_graphs": (ctypes.c_int, [P, I32]),
+        "saber_gpu_get_graphs": (I32, [P]),
+        "saber_gpu_graph_captures": (U64, [P]),
         "saber_gpu_search": (ctypes.c_int, [P, P, P, P, U64, P, P, U32, P, P, U64, P, P, U64, P, P]),
         "saber_gpu_triage_grads": (ctypes.c_int, [P, P, P, P, U32, ctypes.c_float, P, P]),
         "saber_gpu_triage_train": (ctypes.c_int, [P, P, P, P, U64, P, P]),
@@ -488,6 +491,19 @@ class Device:
     @strip_rows.setter
     def strip_rows(self, r):
         self._check(self.lib.saber_gpu_set_strip_rows(self.h, int(r)), "set_strip_rows")
+
+    @property
+    def graphs(self):
+        """Captured scoring graphs on (default) or off."""
+        return bool(self.lib.saber_gpu_get_graphs(self.h))
+
+    @graphs.setter
+    def graphs(self, on):
+        self._check(self.lib.saber_gpu_set_graphs(self.h, 1 if on else 0), "set_graphs")
+
+    @property
+    def graph_captures(self):
+        return int(self.lib.saber_gpu_graph_captures(self.h))
 
     @property
     def pair_steps(self):

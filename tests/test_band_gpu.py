@@ -197,3 +197,31 @@ def test_wide_full_window_bands(tuned, mode):
         got = dev.score_windows(q, None, subs, B62, 11, 1)
         want = [orc.banded_score(q, s, None, B62, 11, 1, -q.size, s.size)[0] for s in subs]
         assert list(got) == want
+
+
+def test_captured_graphs_match_step_launches(tuned):
+    """The scoring graph (device-side counts, padded sizes, replayed per size
+    bucket) gives the scores and cell counts of the step-by-step launches,
+    and a second batch of the same bucket replays without a new capture."""
+    dev = tuned
+    qs, ss, planted = synth.protein_db(61, 30, 2500)
+    bias = synth.query_bias(62, qs)
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    for mode in KERNEL_MODES:
+        dev.strip_rows, dev.pair_steps = mode
+        jobs = synth.band_jobs(63, qs, ss, planted, 5000, half_min=1, half_max=140)
+        jobs2 = synth.band_jobs(64, qs, ss, planted, 4500, half_min=1, half_max=140)
+        dev.graphs = False
+        want, st_w = dev.score_band_jobs(jobs)
+        want2, _ = dev.score_band_jobs(jobs2)
+        dev.graphs = True
+        got, st_g = dev.score_band_jobs(jobs)
+        n0 = dev.graph_captures
+        got2, _ = dev.score_band_jobs(jobs2)
+        assert np.array_equal(got, want), _report(got, want, jobs)
+        assert np.array_equal(got2, want2), _report(got2, want2, jobs2)
+        assert st_g["banded_cells"] == st_w["banded_cells"] and st_g["i16_rescored"] == st_w["i16_rescored"]
+        assert dev.graph_captures == n0
+    dev.graphs = True
