@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--strip-rows", type=int, default=16, help="rows per strip of the int16 kernel (8 or 16)")
     ap.add_argument("--no-autotune", action="store_true", help="keep --strip-rows and the default pairing")
     ap.add_argument("--no-search", action="store_true", help="skip the batched-search / learned-triage lines")
+    ap.add_argument("--search-only", action="store_true",
+                    help="only the batched-search section (printed as its own JSON line)")
+    ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
     ap.add_argument("--search-queries", type=int, default=2000)
     ap.add_argument("--search-subjects", type=int, default=500_000)
     return ap.parse_args()
@@ -176,15 +179,17 @@ def run_search(a, dev):
     from saber_gb300 import synth
     from saber_gb300 import triage as tr
     from saber_gb300.search import Searcher, SearchParams
-    t0 = time.perf_counter()
-    qa, sa, _ = synth.protein_db(a.seed + 501, max(a.search_queries // 2, 1), max(a.search_subjects * 2 // 5, 1),
-                                 reversed_frac=0.25, identity_range=(0.3, 0.6))
-    se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default"))
-    rows, y, _ = tr.collect(se, qa.codes, qa.offsets)
-    t1 = time.perf_counter()
-    model, st = tr.train(dev, rows, y, seed=a.seed + 1)
-    t2 = time.perf_counter()
-    thr = tr.threshold_for_recall(dev.triage_predict(model, rows), y, recall=0.999, margin=0.5)
+    triage = not a.no_triage
+    t0 = t1 = t2 = time.perf_counter()
+    if triage:
+        qa, sa, _ = synth.protein_db(a.seed + 501, max(a.search_queries // 2, 1), max(a.search_subjects * 2 // 5, 1),
+                                     reversed_frac=0.25, identity_range=(0.3, 0.6))
+        se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default"))
+        rows, y, _ = tr.collect(se, qa.codes, qa.offsets)
+        t1 = time.perf_counter()
+        model, st = tr.train(dev, rows, y, seed=a.seed + 1)
+        t2 = time.perf_counter()
+        thr = tr.threshold_for_recall(dev.triage_predict(model, rows), y, recall=0.999, margin=0.5)
     qb, sb, _ = synth.protein_db(a.seed + 502, a.search_queries, a.search_subjects, reversed_frac=0.25,
                                  identity_range=(0.3, 0.6))
     se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default"))
@@ -209,6 +214,19 @@ def run_search(a, dev):
                  int(r["s_start"]), int(r["s_end"]), float(r["evalue"])) for r in hits}
 
     plain, tp, cp = timed()
+    nq = a.search_queries
+    stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms")
+    out = {
+        "workload": "batched search, default preset: %d synthetic queries vs %d subjects (%d residues; 50%% "
+                    "background, 25%% planted 30-60%% identity, 25%% reversed), BLOSUM62 11/1, E<=10, -k 10"
+                    % (nq, a.search_subjects, int(sb.codes.size)),
+        "unit": "queries/s", "timing": "median of 3 calls, host wall clock around saber_gpu_search (query "
+                                        "codes in, hit records out)",
+        "plain": {"value": round(nq / tp, 1), "hits": int(len(plain)), "regions": cp["regions"],
+                  "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages}},
+    }
+    if not triage:
+        return out
     dev.set_triage(model, thr)
     try:
         call()
@@ -217,16 +235,7 @@ def run_search(a, dev):
         dev.set_triage(None)
     kp_, kt_ = keyset(plain), keyset(tri)
     total, kept = len(kp_), len(kp_ & kt_)
-    nq = a.search_queries
-    stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms")
-    return {
-        "workload": "batched search, default preset: %d synthetic queries vs %d subjects (%d residues; 50%% "
-                    "background, 25%% planted 30-60%% identity, 25%% reversed), BLOSUM62 11/1, E<=10, -k 10"
-                    % (nq, a.search_subjects, int(sb.codes.size)),
-        "unit": "queries/s", "timing": "median of 3 calls, host wall clock around saber_gpu_search (query "
-                                        "codes in, hit records out)",
-        "plain": {"value": round(nq / tp, 1), "hits": int(len(plain)), "regions": cp["regions"],
-                  "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages}},
+    out.update({
         "triage": {"value": round(nq / tt, 1), "regions_scored": ct["regions"], "regions_dropped": ct["triage_dropped"],
                    "banded_cells": ct["banded_cells"], "hits_kept": kept, "hits_plain": total,
                    "kept_frac": round(kept / max(total, 1), 5), "lost_hit_rate": round(1 - kept / max(total, 1), 5),
@@ -237,7 +246,14 @@ def run_search(a, dev):
                      "collect_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 2),
                      "data": "separately seeded database (%d queries x %d subjects)" % (len(qa.offsets) - 1,
                                                                                           len(sa.offsets) - 1)},
-    }
+    })
+    return out
+
+
+def run_search_only(a, local_rank):
+    from saber_gb300 import Device
+    dev = Device(local_rank)
+    print(json.dumps({"metric": "batched search queries/s", "search": run_search(a, dev)}), flush=True)
 
 
 def run_ours(a, rank, world, local_rank):
@@ -366,6 +382,9 @@ def main():
         torch.distributed.init_process_group("gloo")
     if a.impl == "reference":
         run_reference(a, rank, world)
+    elif a.search_only:
+        if rank == 0:
+            run_search_only(a, local_rank)
     else:
         run_ours(a, rank, world, local_rank)
     if world > 1:

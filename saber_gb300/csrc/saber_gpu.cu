@@ -803,18 +803,19 @@ static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const
         }
         const uint32_t nreq = (uint32_t)reqs.size();
         const uint32_t stride = (uint32_t)(wmax + 1);
-        uint64_t thr = kAlignSlabBudget / ((uint64_t)stride * 16);
-        if (thr < 128) thr = 128;
-        uint64_t want_thr = ((uint64_t)nreq + 127) / 128 * 128;
-        thr = std::min<uint64_t>(std::min<uint64_t>(thr, want_thr), (uint64_t)h->sm_count * 8 * 128);
-        thr = thr / 128 * 128;
+        // warp-per-job kernel: one row-buffer set per warp, one job per warp
+        uint64_t warps = kAlignSlabBudget / ((uint64_t)stride * 16);
+        if (warps < 4) warps = 4;
+        warps = std::min<uint64_t>(std::min<uint64_t>(warps, ((uint64_t)nreq + 3) / 4 * 4),
+                                   (uint64_t)h->sm_count * 6 * 4);
+        const uint64_t thr = std::max<uint64_t>(warps / 4 * 4, 4) * 32;
         const unsigned grid = (unsigned)(thr / 128);
         CUALLOC(h, h->al_reqs, nreq * sizeof(AlignReq));
         CUALLOC(h, h->al_outs, nreq * sizeof(AlignOut));
         CUALLOC(h, h->al_dir, dir_tot + 16);
         CUALLOC(h, h->al_opbytes, ops_tot + 16);
         CUALLOC(h, h->al_runs, (ops_tot + 16) * 4);
-        CUALLOC(h, h->al_slabs, thr * stride * 16);
+        CUALLOC(h, h->al_slabs, (thr / 32) * stride * 16);
         CU(h, cudaMemcpyAsync(h->al_reqs.p, reqs.data(), nreq * sizeof(AlignReq), cudaMemcpyHostToDevice, s));
         CU(h, launch_band_align(grid, s, h->al_reqs.as<AlignReq>(), nreq, h->al_dir.as<uint8_t>(),
                                 h->al_opbytes.as<uint8_t>(), h->al_runs.as<uint32_t>(), h->al_slabs.as<int32_t>(),

@@ -78,22 +78,28 @@ def _tb_workload(seed, nq, ns, nj):
     return qs, ss, bias, jobs
 
 
-def test_batched_align_matches_oracle(dev):
-    qs, ss, bias, jobs = _tb_workload(41, 12, 400, 300)
-    dev.set_scheme(B62, 11, 1)
+@pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8)])
+def test_batched_align_matches_oracle(dev, gaps):
+    """Direction bytes, best cell and CIGAR of the warp-per-job kernel (E by
+    a warp max-scan) against the oracle, including stop_at early exits."""
+    go, ge = gaps
+    qs, ss, bias, jobs = _tb_workload(41 + go, 12, 400, 300)
+    dev.set_scheme(B62, go, ge)
     dev.load_db(ss.codes, ss.offsets)
     dev.load_queries(qs.codes, qs.offsets, bias)
     aj = np.zeros(jobs.size, ALIGN_JOB_DTYPE)
     for f in ("query", "subject", "win_begin", "win_len", "band_lo", "band_hi"):
         aj[f] = jobs[f]
     aj["stop_at"] = 2 ** 31 - 1
+    aj["stop_at"][::5] = 60
     got = dev.banded_align(aj)
     for t, j in enumerate(jobs):
         q = qs.seq(j["query"])
         qb = bias[qs.offsets[j["query"]]:qs.offsets[j["query"] + 1]]
         s = ss.codes[j["win_begin"]:j["win_begin"] + j["win_len"]]
-        want = orc.banded_align(q, s, qb, B62, 11, 1, int(j["band_lo"]), int(j["band_hi"]))
-        assert _same(got[t], want), t
+        want = orc.banded_align(q, s, qb, B62, go, ge, int(j["band_lo"]), int(j["band_hi"]),
+                                stop_at=int(aj["stop_at"][t]))
+        assert _same(got[t], want), (t, gaps)
 
 
 def test_widening_traceback_driver_matches_oracle(dev):
