@@ -155,19 +155,24 @@ __global__ void k_presence(const uint32_t* __restrict__ cnt, uint64_t ncodes, un
 }
 
 // ---- database scan with the window filter ---------------------------------------
+constexpr int kMaxShapes = 32;
 struct ScanArgs {
     const uint8_t *sb, *res, *rem, *dst;
     uint64_t N;
-    const unsigned long long* pres;
-    const uint32_t *qoff, *qent;
+    const unsigned long long* pres;  // presence bitmaps of all shapes
+    const uint32_t *qoff, *qent;     // code -> batch-position tables of all shapes
     const uint8_t *qsb, *qfull, *qrem, *qdst;
     int cfil;
     uint32_t min_ids, kx;
-    uint32_t shape;
+    uint32_t nshapes, asize;
     uint2* surv;
     unsigned long long* nsurv;  // counter (may exceed cap: overflow)
     uint64_t cap;
     unsigned long long* ctr;    // [2] hits, [3] filtered
+    // per shape: care offsets, bitmap / table / entry bases
+    ShapeDev sh[kMaxShapes];
+    uint64_t pres_off[kMaxShapes], qoff_off[kMaxShapes];
+    uint32_t qent_off[kMaxShapes];
 };
 
 // 32-lane mask of byte equality between q[0..32) and s[0..32) & smask, from
@@ -229,72 +234,132 @@ __device__ __forceinline__ bool window_passes(const ScanArgs& a, uint64_t r, uin
     return ids + a.kx * ex >= a.min_ids;
 }
 
-// One shape over the database.  Each warp takes 32 consecutive positions,
-// computes their seed codes and presence, then works through all their hits
-// (one batch position each) as a warp queue, one hit per lane per round, so
-// that a position with many hits does not stall the other lanes; survivors
-// are appended with one atomic per warp round.  (A query byte of QSENT never
-// equals a masked-off subject byte, which is below 0x80.)
-__global__ void __launch_bounds__(256) k_scan(ScanArgs a, ShapeDev sh, uint32_t asize) {
-    const int lane = threadIdx.x & 31;
+// All shapes over the database in one pass.  Each warp takes 32
+// consecutive positions and, shape by shape, looks up their seed codes in
+// the shape's presence bitmap and code -> batch-position table; positions
+// with hits become (position, shape, entries) segments in a per-warp queue
+// in shared memory.  When the queue fills (and at the end) the warp works
+// through the queued hits, one per lane per round -- every shape's hits of
+// those positions together, so the rounds run full and the table lookups of
+// all shapes are in flight at once.  Survivors are appended with one atomic
+// per round.  (A query byte of QSENT never equals a masked-off subject byte,
+// which is below 0x80.)
+constexpr int kSegCap = 160;
+constexpr int kScanWarps = 8;
+
+__device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg, const uint32_t* seg_n,
+                                           const uint32_t* seg_e0, const uint64_t* seg_r, const uint8_t* seg_sh,
+                                           uint32_t* seg_start, unsigned long long& hits,
+                                           unsigned long long& filtered) {
+    // exclusive prefix of the segments' hit counts (5 per lane)
+    constexpr int kPer = kSegCap / 32;
+    uint32_t loc[kPer];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int t = 0; t < kPer; t++) {
+        const int sidx = lane * kPer + t;
+        loc[t] = sum;
+        sum += sidx < nseg ? seg_n[sidx] : 0u;
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t lbase = incl - sum;
+#pragma unroll
+    for (int t = 0; t < kPer; t++) seg_start[lane * kPer + t] = lbase + loc[t];
+    __syncwarp();
+    if (lane == 0) hits += total;
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        bool pass = false;
+        uint64_t r = 0;
+        uint32_t gsh = 0;
+        if (k < total) {
+            // owner: the last segment starting at or before k
+            int lo = 0, hi = nseg;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (seg_start[mid] <= k) lo = mid;
+                else hi = mid;
+            }
+            r = seg_r[lo];
+            const uint32_t sh = seg_sh[lo];
+            const uint32_t g = a.qent[seg_e0[lo] + (k - seg_start[lo])];
+            pass = a.min_ids == 0 || window_passes(a, r, g);
+            if (!pass) filtered++;
+            gsh = g | (sh << 27);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+        if (bal) {
+            const int leader = __ffs(bal) - 1;
+            unsigned long long slot0 = 0;
+            if (lane == leader) slot0 = atomicAdd(a.nsurv, (unsigned long long)__popc(bal));
+            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+            if (pass) {
+                const unsigned long long slot = slot0 + __popc(bal & ((1u << lane) - 1u));
+                if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)r, gsh);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
+    __shared__ uint32_t s_n[kScanWarps][kSegCap], s_e0[kScanWarps][kSegCap], s_start[kScanWarps][kSegCap];
+    __shared__ uint64_t s_r[kScanWarps][kSegCap];
+    __shared__ uint8_t s_sh[kScanWarps][kSegCap];
+    __shared__ ShapeDev s_shape[kMaxShapes];
+    for (uint32_t i = threadIdx.x; i < a.nshapes; i += blockDim.x) s_shape[i] = a.sh[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t warp0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long hits = 0, filtered = 0;
     for (uint64_t base = warp0 * 32; base < a.N; base += nwarps * 32) {
         const uint64_t r = base + lane;
-        uint32_t n = 0, e0 = 0;
-        if (r < a.N && a.rem[r] >= sh.span) {
-            const int64_t c = seed_code(a.sb + r, sh, asize);
-            if (c >= 0 && ((a.pres[c >> 6] >> (c & 63)) & 1ull)) {
-                e0 = a.qoff[c];
-                n = a.qoff[c + 1] - e0;
-            }
-        }
-        // exclusive prefix of the lanes' hit counts
-        uint32_t incl = n;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        const uint32_t start = incl - n;
-        if (lane == 0) hits += total;
-        for (uint32_t k0 = 0; k0 < total; k0 += 32) {
-            const uint32_t k = k0 + lane;
-            // owner lane: the last lane whose start is <= k
-            int lo = 0, hi = 32;
-#pragma unroll
-            for (int it = 0; it < 5; it++) {
-                const int mid = (lo + hi) >> 1;
-                if (__shfl_sync(0xffffffffu, start, mid) <= k) lo = mid;
-                else hi = mid;
-            }
-            const uint32_t ostart = __shfl_sync(0xffffffffu, start, lo);
-            const uint32_t oe0 = __shfl_sync(0xffffffffu, e0, lo);
-            const uint64_t orr = __shfl_sync(0xffffffffu, r, lo);
-            bool pass = false;
-            if (k < total) {
-                const uint32_t g = a.qent[oe0 + (k - ostart)];
-                pass = a.min_ids == 0 || window_passes(a, orr, g);
-                if (!pass) filtered++;
-                const uint32_t bal = __ballot_sync(__activemask(), pass);
-                if (pass) {
-                    const uint32_t gg = g;
-                    // one atomic per round, from the lowest passing lane
-                    const uint32_t mine = __popc(bal & ((1u << lane) - 1u));
-                    unsigned long long slot0 = 0;
-                    const int leader = __ffs(bal) - 1;
-                    if (lane == leader) slot0 = atomicAdd(a.nsurv, (unsigned long long)__popc(bal));
-                    slot0 = __shfl_sync(bal, slot0, leader);
-                    const unsigned long long slot = slot0 + mine;
-                    if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)orr, gg | (a.shape << 27));
+        const int rem = r < a.N ? a.rem[r] : 0;
+        int nseg = 0;
+        for (uint32_t si = 0; si < a.nshapes; si++) {
+            uint32_t n = 0, e0 = 0;
+            if (rem >= (int)s_shape[si].span) {
+                const int64_t c = seed_code(a.sb + r, s_shape[si], a.asize);
+                if (c >= 0 && ((a.pres[a.pres_off[si] + (c >> 6)] >> (c & 63)) & 1ull)) {
+                    const uint32_t* qo = a.qoff + a.qoff_off[si];
+                    e0 = qo[c];
+                    n = qo[c + 1] - e0;
+                    e0 += a.qent_off[si];
                 }
             }
+            const uint32_t bal = __ballot_sync(0xffffffffu, n > 0);
+            if (n > 0) {
+                const int slot = nseg + __popc(bal & ((1u << lane) - 1u));
+                s_n[w][slot] = n;
+                s_e0[w][slot] = e0;
+                s_r[w][slot] = r;
+                s_sh[w][slot] = (uint8_t)si;
+            }
+            nseg += __popc(bal);
+            if (nseg > kSegCap - 32) {
+                __syncwarp();
+                scan_flush(a, lane, nseg, s_n[w], s_e0[w], s_r[w], s_sh[w], s_start[w], hits, filtered);
+                nseg = 0;
+            }
+        }
+        if (nseg) {
+            __syncwarp();
+            scan_flush(a, lane, nseg, s_n[w], s_e0[w], s_r[w], s_sh[w], s_start[w], hits, filtered);
         }
     }
-    atomicAdd(&a.ctr[2], hits);
-    atomicAdd(&a.ctr[3], filtered);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) filtered += __shfl_xor_sync(0xffffffffu, filtered, o);
+    if (lane == 0) {
+        atomicAdd(&a.ctr[2], hits);
+        atomicAdd(&a.ctr[3], filtered);
+    }
 }
 
 // Keys of the per-query region order (region_order, engine.rs:493-495:
@@ -795,65 +860,93 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     uint64_t scap = std::max<uint64_t>(1 << 20, h->sc_surv.cap / 8);
     uint64_t nsurv = 0;
     const int cfil = (int)(minspan / 2);
+    // seed tables of all shapes, concatenated: per shape a code -> entry
+    // offset table (nc + 1 words), a presence bitmap and its batch positions
+    const uint32_t nsh = p->nshapes;
+    std::vector<uint64_t> qbase(nsh + 1, 0), pbase(nsh + 1, 0), ebase(nsh + 1, 0);
+    uint64_t ncmax = 0;
+    for (uint32_t si = 0; si < nsh; si++) {
+        const uint64_t nc = ncodes_of(p, si);
+        ncmax = std::max(ncmax, nc);
+        qbase[si + 1] = qbase[si] + nc + 1;
+        pbase[si + 1] = pbase[si] + (nc + 63) / 64 + 1;
+    }
+    CUALLOC(h, h->sc_qcnt, qbase[nsh] * 4);
+    CUALLOC(h, h->sc_qoff, qbase[nsh] * 4);
+    CUALLOC(h, h->sc_qpres, pbase[nsh] * 8);
+    CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, qbase[nsh] * 4, s));
+    CU(h, cudaMemsetAsync(h->sc_qpres.p, 0, pbase[nsh] * 8, s));
+    {
+        size_t tb = 0;
+        CU(h, cub::DeviceScan::ExclusiveSum(nullptr, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
+                                            (int)(ncmax + 1), s));
+        CUALLOC(h, h->cub_tmp, tb);
+    }
+    std::vector<uint32_t> nseed(nsh, 0);
+    for (uint32_t si = 0; si < nsh; si++) {
+        const uint64_t nc = ncodes_of(p, si);
+        const unsigned long long* freq = h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si];
+        uint32_t* cnt = h->sc_qcnt.as<uint32_t>() + qbase[si];
+        uint32_t* off = h->sc_qoff.as<uint32_t>() + qbase[si];
+        if (QN)
+            k_query_seeds<0><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
+                                                              shape_dev(p, si), p->alpha_size, freq, cnt, nullptr,
+                                                              nullptr, ctr);
+        size_t tb = h->cub_tmp.cap;
+        CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, cnt, off, (int)(nc + 1), s));
+        k_presence<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(
+            cnt, nc, h->sc_qpres.as<unsigned long long>() + pbase[si]);
+        CU(h, cudaMemcpyAsync(&nseed[si], off + nc, 4, cudaMemcpyDeviceToHost, s));
+    }
+    CU(h, cudaStreamSynchronize(s));
+    for (uint32_t si = 0; si < nsh; si++) ebase[si + 1] = ebase[si] + nseed[si];
+    if (ebase[nsh] >= (1ull << 32)) return fail(h, SABER_ERR_ARG, "too many query seeds in one batch");
+    CUALLOC(h, h->sc_qent, ebase[nsh] * 4 + 4);
+    CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, qbase[nsh] * 4, s));
+    for (uint32_t si = 0; si < nsh; si++)
+        if (QN && nseed[si])
+            k_query_seeds<1><<<nblocks(QN, 256), 256, 0, s>>>(
+                h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN, shape_dev(p, si), p->alpha_size,
+                h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si], h->sc_qcnt.as<uint32_t>() + qbase[si],
+                h->sc_qoff.as<uint32_t>() + qbase[si], h->sc_qent.as<uint32_t>() + ebase[si], ctr);
+    CU(h, cudaGetLastError());
     CU(h, cudaEventRecord(ev[1], s));
+    ScanArgs a;
+    a.sb = h->sc_sb.as<uint8_t>();
+    a.res = ds.res.as<uint8_t>();
+    a.rem = h->sc_rem.as<uint8_t>();
+    a.dst = h->sc_dst.as<uint8_t>();
+    a.N = N;
+    a.pres = h->sc_qpres.as<unsigned long long>();
+    a.qoff = h->sc_qoff.as<uint32_t>();
+    a.qent = h->sc_qent.as<uint32_t>();
+    a.qsb = h->sc_qsb.as<uint8_t>();
+    a.qfull = h->sc_qfull.as<uint8_t>();
+    a.qrem = h->sc_qrem.as<uint8_t>();
+    a.qdst = h->sc_qdst.as<uint8_t>();
+    a.cfil = cfil;
+    a.min_ids = p->hit_filter_min_ids;
+    a.kx = p->hit_filter_exact_weight;
+    a.nshapes = nsh;
+    a.asize = p->alpha_size;
+    a.nsurv = ctr + 10;
+    a.ctr = ctr;
+    for (uint32_t si = 0; si < nsh; si++) {
+        a.sh[si] = shape_dev(p, si);
+        a.pres_off[si] = pbase[si];
+        a.qoff_off[si] = qbase[si];
+        a.qent_off[si] = (uint32_t)ebase[si];
+    }
+    int scan_bps = 0;
+    CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&scan_bps, k_scan, kScanWarps * 32, 0));
+    const unsigned scan_grid = (unsigned)std::max(1, scan_bps) * (unsigned)h->sm_count;
     for (int attempt = 0; attempt < 8; attempt++) {
         CUALLOC(h, h->sc_surv, scap * 8);
-        CU(h, cudaMemsetAsync(ctr, 0, 32 * 8, s));
-        for (uint32_t si = 0; si < p->nshapes; si++) {
-            const uint64_t nc = ncodes_of(p, si);
-            const ShapeDev sh = shape_dev(p, si);
-            const unsigned long long* freq = h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si];
-            CUALLOC(h, h->sc_qcnt, (nc + 1) * 4);
-            CUALLOC(h, h->sc_qoff, (nc + 1) * 4);
-            CUALLOC(h, h->sc_qpres, ((nc + 63) / 64) * 8 + 8);
-            CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, (nc + 1) * 4, s));
-            CU(h, cudaMemsetAsync(h->sc_qpres.p, 0, ((nc + 63) / 64) * 8 + 8, s));
-            if (QN)
-                k_query_seeds<0><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
-                                                                  sh, p->alpha_size, freq, h->sc_qcnt.as<uint32_t>(),
-                                                                  nullptr, nullptr, ctr);
-            size_t tb = 0;
-            CU(h, cub::DeviceScan::ExclusiveSum(nullptr, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
-                                                (int)(nc + 1), s));
-            CUALLOC(h, h->cub_tmp, tb);
-            tb = h->cub_tmp.cap;
-            CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
-                                                (int)(nc + 1), s));
-            k_presence<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(h->sc_qcnt.as<uint32_t>(), nc,
-                                                                           h->sc_qpres.as<unsigned long long>());
-            uint32_t nseed = 0;
-            CU(h, cudaMemcpyAsync(&nseed, h->sc_qoff.as<uint32_t>() + nc, 4, cudaMemcpyDeviceToHost, s));
-            CU(h, cudaStreamSynchronize(s));
-            CUALLOC(h, h->sc_qent, (uint64_t)nseed * 4 + 4);
-            CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, (nc + 1) * 4, s));
-            if (QN && nseed)
-                k_query_seeds<1><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
-                                                                  sh, p->alpha_size, freq, h->sc_qcnt.as<uint32_t>(),
-                                                                  h->sc_qoff.as<uint32_t>(), h->sc_qent.as<uint32_t>(),
-                                                                  ctr);
-            if (!nseed || !N) continue;
-            ScanArgs a;
-            a.sb = h->sc_sb.as<uint8_t>();
-            a.res = ds.res.as<uint8_t>();
-            a.rem = h->sc_rem.as<uint8_t>();
-            a.dst = h->sc_dst.as<uint8_t>();
-            a.N = N;
-            a.pres = h->sc_qpres.as<unsigned long long>();
-            a.qoff = h->sc_qoff.as<uint32_t>();
-            a.qent = h->sc_qent.as<uint32_t>();
-            a.qsb = h->sc_qsb.as<uint8_t>();
-            a.qfull = h->sc_qfull.as<uint8_t>();
-            a.qrem = h->sc_qrem.as<uint8_t>();
-            a.qdst = h->sc_qdst.as<uint8_t>();
-            a.cfil = cfil;
-            a.min_ids = p->hit_filter_min_ids;
-            a.kx = p->hit_filter_exact_weight;
-            a.shape = si;
+        CU(h, cudaMemsetAsync(ctr + 2, 0, 9 * 8, s));  // hits, filtered, ..., survivors
+        if (ebase[nsh] && N) {
             a.surv = h->sc_surv.as<uint2>();
-            a.nsurv = ctr + 10;
             a.cap = scap;
-            a.ctr = ctr;
-            k_scan<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(a, sh, p->alpha_size);
+            k_scan<<<scan_grid, kScanWarps * 32, 0, s>>>(a);
             CU(h, cudaGetLastError());
         }
         unsigned long long hc[16];
