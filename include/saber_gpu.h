@@ -411,6 +411,15 @@ int32_t saber_gpu_get_strip_rows(saber_gpu* h);
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
 
+/* Tuning: bytes of seed tables (rank-compressed presence groups, entry
+ * offsets, batch positions) that one database pass of saber_gpu_scan looks
+ * up; the shapes are split into passes of at most this many bytes (at least
+ * one shape per pass) so that the tables stay resident in L2.  Default 48 MiB.
+ * Results do not depend on it.  No reference counterpart (the reference
+ * scans shape by shape on the CPU). */
+int saber_gpu_set_scan_table_bytes(saber_gpu* h, uint64_t bytes);
+uint64_t saber_gpu_get_scan_table_bytes(saber_gpu* h);
+
 /* Captured scoring graphs (default on): saber_gpu_score_band_jobs (and so
  * the batch engine's scoring stages) runs classify -> radix sort -> int16
  * kernels -> int32 kernel as one CUDA graph with every count kept on the

@@ -1409,6 +1409,14 @@ int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps) {
 
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h) { return h ? h->pair_steps : 0u; }
 
+int saber_gpu_set_scan_table_bytes(saber_gpu* h, uint64_t bytes) {
+    ENTER(h);
+    h->scan_table_bytes = bytes;
+    return SABER_OK;
+}
+
+uint64_t saber_gpu_get_scan_table_bytes(saber_gpu* h) { return h ? h->scan_table_bytes : 0u; }
+
 int saber_gpu_banded_align(saber_gpu* h, const saber_align_job* jobs, uint64_t njobs, uint64_t max_dir_bytes,
                            saber_alignment* out, uint32_t* ops, uint64_t ops_cap) {
     ENTER(h);

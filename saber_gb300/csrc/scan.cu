@@ -72,6 +72,14 @@ __global__ void k_dists(const uint64_t* __restrict__ offs, uint64_t nseq, uint64
     }
 }
 
+// Adds a per-thread count to a global counter with one atomic per warp
+// (every lane of the warp must call it).
+__device__ __forceinline__ void count_add(unsigned long long* dst, unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
 __device__ __forceinline__ int64_t seed_code(const uint8_t* __restrict__ sr, const ShapeDev& sh, uint32_t asize) {
     uint32_t c = 0;
     // unrolled to the largest weight so that the offsets stay in registers
@@ -95,7 +103,7 @@ __global__ void k_db_counts(const uint8_t* __restrict__ sb, const uint8_t* __res
         atomicAdd(&counts[c], 1u);
         t++;
     }
-    atomicAdd(total, t);
+    count_add(total, t);
 }
 
 __global__ void k_freq_bits(const uint32_t* __restrict__ counts, uint64_t ncodes, uint64_t cap,
@@ -120,11 +128,24 @@ __device__ __forceinline__ bool is_frequent(const unsigned long long* freq, uint
     return freq && ((freq[c >> 6] >> (c & 63)) & 1ull);
 }
 
-// pass 0: count per code; pass 1: scatter batch positions (cnt = cursors)
+// Seed tables of one shape, rank-compressed: grp[c / 32] = {presence bits of
+// codes c & ~31 .. c | 31, number of present codes before them}; the present
+// code of rank k owns entries coff[k] .. coff[k + 1] of the batch positions.
+// A present code's rank is grp.y + popc(grp.x & lanes below c % 32).
+__device__ __forceinline__ bool code_rank(const uint2* __restrict__ grp, uint32_t c, uint32_t& k) {
+    const uint2 g = grp[c >> 5];
+    const uint32_t bit = 1u << (c & 31);
+    k = g.y + __popc(g.x & (bit - 1u));
+    return (g.x & bit) != 0;
+}
+
+// pass 0: count per code; pass 1: scatter batch positions through the ranks
+// (cur = per-rank cursors)
 template <int PASS>
 __global__ void k_query_seeds(const uint8_t* __restrict__ qsb, const uint8_t* __restrict__ qrem, uint64_t QN,
                               ShapeDev sh, uint32_t asize, const unsigned long long* __restrict__ freq,
-                              uint32_t* __restrict__ cnt, const uint32_t* __restrict__ off, uint32_t* __restrict__ ent,
+                              uint32_t* __restrict__ cnt, const uint2* __restrict__ grp,
+                              const uint32_t* __restrict__ coff, uint32_t* __restrict__ ent,
                               unsigned long long* __restrict__ ctr) {
     unsigned long long kept = 0, skipped = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < QN; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -139,19 +160,46 @@ __global__ void k_query_seeds(const uint8_t* __restrict__ qsb, const uint8_t* __
             atomicAdd(&cnt[c], 1u);
             kept++;
         } else {
-            const uint32_t slot = atomicAdd(&cnt[c], 1u);
-            ent[off[c] + slot] = (uint32_t)i;
+            uint32_t k;
+            code_rank(grp, (uint32_t)c, k);
+            const uint32_t slot = atomicAdd(&cnt[k], 1u);
+            ent[coff[k] + slot] = (uint32_t)i;
         }
     }
     if (PASS == 0) {
-        atomicAdd(&ctr[0], kept);
-        atomicAdd(&ctr[1], skipped);
+        count_add(&ctr[0], kept);
+        count_add(&ctr[1], skipped);
     }
 }
 
-__global__ void k_presence(const uint32_t* __restrict__ cnt, uint64_t ncodes, unsigned long long* __restrict__ bits) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncodes; c += (uint64_t)gridDim.x * blockDim.x)
-        if (cnt[c]) atomicOr(&bits[c >> 6], 1ull << (c & 63));
+// presence bits and present-code counts of each 32-code group
+__global__ void k_group_bits(const uint32_t* __restrict__ cnt, uint64_t ncodes, uint2* __restrict__ grp,
+                             uint32_t* __restrict__ gcnt) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t g = w0; g * 32 < ncodes; g += nw) {
+        const uint64_t c = g * 32 + lane;
+        const uint32_t b = __ballot_sync(0xffffffffu, c < ncodes && cnt[c] > 0);
+        if (lane == 0) {
+            grp[g] = make_uint2(b, 0u);
+            gcnt[g] = __popc(b);
+        }
+    }
+}
+
+// ranks of the groups' first codes, and each present code's count at its rank
+__global__ void k_group_ranks(const uint32_t* __restrict__ cnt, uint64_t ncodes, const uint32_t* __restrict__ grank,
+                              uint2* __restrict__ grp, uint32_t* __restrict__ cntc) {
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncodes; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t g = (uint32_t)(c >> 5);
+        if ((c & 31) == 0) grp[g].y = grank[g];
+        const uint32_t n = cnt[c];
+        if (n) {
+            const uint32_t bits = grp[g].x;
+            cntc[grank[g] + __popc(bits & ((1u << (c & 31)) - 1u))] = n;
+        }
+    }
 }
 
 // ---- database scan with the window filter ---------------------------------------
@@ -159,44 +207,22 @@ constexpr int kMaxShapes = 32;
 struct ScanArgs {
     const uint8_t *sb, *res, *rem, *dst;
     uint64_t N;
-    const unsigned long long* pres;  // presence bitmaps of all shapes
-    const uint32_t *qoff, *qent;     // code -> batch-position tables of all shapes
-    const uint8_t *qsb, *qfull, *qrem, *qdst;
+    const uint2* grp;                // rank-compressed presence tables of all shapes
+    const uint32_t *coff, *qent;     // rank -> batch-position entries of all shapes
+    const uint4* qwin;               // per batch position: seed-letter window record (32 bytes)
+    const uint4* qwinx;              // per batch position: full-code window record (32 bytes)
     int cfil;
     uint32_t min_ids, kx;
-    uint32_t nshapes, asize;
+    uint32_t s0, s1, asize;          // this pass's shapes [s0, s1)
     uint2* surv;
     unsigned long long* nsurv;  // counter (may exceed cap: overflow)
     uint64_t cap;
     unsigned long long* ctr;    // [2] hits, [3] filtered
-    // per shape: care offsets, bitmap / table / entry bases
+    // per shape: care offsets, table / entry bases
     ShapeDev sh[kMaxShapes];
-    uint64_t pres_off[kMaxShapes], qoff_off[kMaxShapes];
+    uint64_t grp_off[kMaxShapes], coff_off[kMaxShapes];
     uint32_t qent_off[kMaxShapes];
 };
-
-// 32-lane mask of byte equality between q[0..32) and s[0..32) & smask, from
-// aligned 32-bit words (the caller guarantees q - 3 .. q + 36 and s - 3 ..
-// s + 36 are readable).
-__device__ __forceinline__ uint32_t eq_lanes(const uint8_t* q, const uint8_t* s, uint32_t smask) {
-    const uint32_t* qa = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(q) & ~(uintptr_t)3);
-    const uint32_t* sa = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(s) & ~(uintptr_t)3);
-    const uint32_t qs = (uint32_t)(reinterpret_cast<uintptr_t>(q) & 3u) * 8u;
-    const uint32_t ss = (uint32_t)(reinterpret_cast<uintptr_t>(s) & 3u) * 8u;
-    uint32_t E = 0, qn = __ldg(qa), sn = __ldg(sa);
-#pragma unroll
-    for (int w = 0; w < 8; w++) {
-        const uint32_t q0 = qn, s0 = sn;
-        qn = __ldg(qa + w + 1);
-        sn = __ldg(sa + w + 1);
-        const uint32_t x = __funnelshift_r(q0, qn, qs) ^ (__funnelshift_r(s0, sn, ss) & smask);
-        // 0x80 in every zero byte of x (no carries between bytes), then the
-        // four flags gathered into bits 28..31
-        const uint32_t z = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
-        E |= (((z >> 7) * 0x10204080u) >> 28) << (4 * w);
-    }
-    return E;
-}
 
 // Lanes [lo, hi) of a 32-lane mask (0 <= lo, hi <= 32).
 __device__ __forceinline__ uint32_t lane_range(int lo, int hi) {
@@ -204,62 +230,95 @@ __device__ __forceinline__ uint32_t lane_range(int lo, int hi) {
     return (uint32_t)(((1ull << hi) - 1ull) & ~((1ull << lo) - 1ull));
 }
 
-// One seed hit through the window filter (filter_scalar, scan.rs:1809-1856):
-// the 32-residue windows starting at r + cfil - 16 (subject) and g + cfil - 16
-// (query batch), restricted to lanes inside both sequences; reduced-letter
-// identities (query positions masked from seeding never count, the subject's
-// masked residues do) plus kx x exact identities must reach min_ids.
-__device__ __forceinline__ bool window_passes(const ScanArgs& a, uint64_t r, uint32_t g) {
-    const int sdst = a.dst[r], srem = a.rem[r];
-    const int t_lo = max(max(0, 16 - a.cfil - sdst), 16 - a.cfil - (int)a.qdst[g]);
-    const int t_hi = min(min(32, srem + 16 - a.cfil), (int)a.qrem[g] + 16 - a.cfil);
-    const int64_t so = (int64_t)r + a.cfil - 16, qo = (int64_t)g + a.cfil - 16;
-    uint32_t ids = 0, ex = 0;
-    if (so >= 4 && qo >= 4) {
-        const uint32_t L = lane_range(t_lo, t_hi);
-        const uint32_t E = eq_lanes(a.qsb + qo, a.sb + so, 0x7F7F7F7Fu) & L;
-        ids = __popc(E);
-        if (ids >= a.min_ids) return true;
-        if (a.kx == 0 || ids * (1 + a.kx) < a.min_ids) return false;
-        ex = __popc(E & eq_lanes(a.qfull + qo, a.res + so, 0xFFFFFFFFu));
-    } else {
-        for (int t = t_lo; t < t_hi; t++) {
-            const uint8_t qr = a.qsb[qo + t];
-            if (qr != kQSent && qr == (a.sb[so + t] & 0x7F)) {
-                ids++;
-                if (a.kx && a.qfull[qo + t] == a.res[so + t]) ex++;
-            }
-        }
+// Bits 4w .. 4w + 3 of the result: which bytes of Q[w] ^ S[w] are zero (a
+// carry-free zero-byte test, the four flags gathered with one multiply).
+__device__ __forceinline__ uint32_t eq_bytes8(const uint32_t (&Q)[8], const uint32_t (&S)[8], uint32_t smask) {
+    uint32_t E = 0;
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+        const uint32_t x = Q[w] ^ (S[w] & smask);
+        const uint32_t z = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x | 0x7F7F7F7Fu);
+        E |= (((z >> 7) * 0x10204080u) >> 28) << (4 * w);
     }
-    return ids + a.kx * ex >= a.min_ids;
+    return E;
 }
 
-// All shapes over the database in one pass.  Each warp takes 32
-// consecutive positions and, shape by shape, looks up their seed codes in
-// the shape's presence bitmap and code -> batch-position table; positions
-// with hits become (position, shape, entries) segments in a per-warp queue
-// in shared memory.  When the queue fills (and at the end) the warp works
-// through the queued hits, one per lane per round -- every shape's hits of
-// those positions together, so the rounds run full and the table lookups of
-// all shapes are in flight at once.  Survivors are appended with one atomic
-// per round.  (A query byte of QSENT never equals a masked-off subject byte,
-// which is below 0x80.)
-constexpr int kSegCap = 160;
-constexpr int kScanWarps = 8;
+__device__ __forceinline__ void ld256(uint32_t (&v)[8], const void* p) {
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+        : "l"(p));
+}
 
-__device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg, const uint32_t* seg_n,
-                                           const uint32_t* seg_e0, const uint64_t* seg_r, const uint8_t* seg_sh,
-                                           uint32_t* seg_start, unsigned long long& hits,
-                                           unsigned long long& filtered) {
-    // exclusive prefix of the segments' hit counts (5 per lane)
+// 8 words of a staged byte buffer from byte `idx` on (9 aligned word reads
+// and a funnel shift).
+__device__ __forceinline__ void staged_words(const uint32_t* buf, int idx, uint32_t (&S)[8]) {
+    const int wi = idx >> 2;
+    const uint32_t sh = (uint32_t)(idx & 3) * 8u;
+    uint32_t nx = buf[wi];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const uint32_t cur = nx;
+        nx = buf[wi + j + 1];
+        S[j] = __funnelshift_r(cur, nx, sh);
+    }
+}
+
+// The shapes [s0, s1) over the database in one pass (the window filter is
+// filter_scalar, scan.rs:1809-1856).  Each warp takes 32 consecutive
+// positions [base, base + 32) and stages the subject's seed letters and
+// residues of [base - 32, base + 96) in shared memory: every seed code and
+// every filter window of those positions reads from there.  Four shapes at a
+// time (their table lookups in flight together) the positions' seed codes go
+// through the shapes' rank-compressed presence tables; positions with hits
+// become (position, shape, entries) segments in a per-warp queue.  When the
+// queue fills (and at the end of the 32 positions) the warp works through
+// the queued hits, one per lane per round: the hit's query window is one
+// aligned 32-byte record (letters outside the query are QSENT, which never
+// equals a subject byte & 0x7F), the subject window comes from the staged
+// bytes, restricted to lanes inside the subject.  Survivors collect in
+// shared memory and go out 32 or more at a time.
+constexpr int kSegCap = 192;
+constexpr int kShapeUnroll = 4;
+constexpr int kScanWarps = 8;
+constexpr uint32_t kSurvStage = 64;
+
+struct WarpScan {
+    uint32_t* seg_n;   // kSegCap
+    uint32_t* seg_eb;  // kSegCap: entry base (offset - first hit index)
+    uint8_t* seg_rl;   // kSegCap: position - base
+    uint8_t* seg_sh;   // kSegCap: shape
+    uint2* sv;         // kSurvStage survivor records
+    const uint32_t* sbw;   // 32 staged words: seed letters of [base - 32, base + 96)
+    const uint32_t* resw;  // 32 staged words: residues of the same range
+    uint32_t nsv;      // staged survivors (warp-uniform)
+    uint32_t rd;       // this lane's position: rem | dst << 8
+    uint64_t base;
+};
+
+__device__ __forceinline__ void surv_drain(const ScanArgs& a, int lane, WarpScan& ws) {
+    __syncwarp();
+    unsigned long long slot0 = 0;
+    if (lane == 0) slot0 = atomicAdd(a.nsurv, (unsigned long long)ws.nsv);
+    slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+    for (uint32_t i = lane; i < ws.nsv; i += 32)
+        if (slot0 + i < a.cap) a.surv[slot0 + i] = ws.sv[i];
+    __syncwarp();
+    ws.nsv = 0;
+}
+
+// The queued segments' hits, 32 per round.  Each lane keeps kPer segments'
+// starts in registers; a round's owners come from the bits of the segments
+// that start inside it and the count of those that start before it.
+__device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg, WarpScan& ws,
+                                           unsigned long long& hits, unsigned long long& filtered) {
     constexpr int kPer = kSegCap / 32;
-    uint32_t loc[kPer];
+    uint32_t st[kPer];
     uint32_t sum = 0;
 #pragma unroll
     for (int t = 0; t < kPer; t++) {
         const int sidx = lane * kPer + t;
-        loc[t] = sum;
-        sum += sidx < nseg ? seg_n[sidx] : 0u;
+        st[t] = sum;
+        sum += sidx < nseg ? ws.seg_n[sidx] : 0u;
     }
     uint32_t incl = sum;
 #pragma unroll
@@ -270,95 +329,174 @@ __device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     const uint32_t lbase = incl - sum;
 #pragma unroll
-    for (int t = 0; t < kPer; t++) seg_start[lane * kPer + t] = lbase + loc[t];
+    for (int t = 0; t < kPer; t++) {
+        const int sidx = lane * kPer + t;
+        // segments past nseg never start inside a round
+        st[t] = sidx < nseg ? lbase + st[t] : 0xFFFFFFFFu;
+        if (sidx < nseg) ws.seg_eb[sidx] -= st[t];
+    }
     __syncwarp();
     if (lane == 0) hits += total;
     for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+        uint32_t B = 0, before = 0;
+#pragma unroll
+        for (int t = 0; t < kPer; t++) {
+            before += st[t] < k0;
+            const uint32_t d = st[t] - k0;
+            if (d < 32u) B |= 1u << d;
+        }
+        B = __reduce_or_sync(0xffffffffu, B);
+        before = __reduce_add_sync(0xffffffffu, before);
         const uint32_t k = k0 + lane;
+        const bool live = k < total;
+        const uint32_t lanes_le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+        const uint32_t own = live ? before + __popc(B & lanes_le) - 1u : 0u;
+        const int rl = ws.seg_rl[own];
+        // the subject position's rem | dst from the lane that scanned it
+        const uint32_t srd = __shfl_sync(0xffffffffu, ws.rd, rl);
         bool pass = false;
-        uint64_t r = 0;
-        uint32_t gsh = 0;
-        if (k < total) {
-            // owner: the last segment starting at or before k
-            int lo = 0, hi = nseg;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (seg_start[mid] <= k) lo = mid;
-                else hi = mid;
+        uint32_t g = 0;
+        if (live) {
+            g = a.qent[ws.seg_eb[own] + k];
+            if (a.min_ids == 0) {
+                pass = true;
+            } else {
+                uint32_t Q[8], S[8];
+                ld256(Q, a.qwin + 2 * (uint64_t)g);
+                const int idx = rl + a.cfil + 16;  // staged byte of r + cfil - 16
+                staged_words(ws.sbw, idx, S);
+                const int sdst = (int)(srd >> 8), srem = (int)(srd & 0xFFu);
+                const uint32_t L = lane_range(max(0, 16 - a.cfil - sdst), min(32, srem + 16 - a.cfil));
+                const uint32_t E = eq_bytes8(Q, S, 0x7F7F7F7Fu) & L;
+                const uint32_t ids = __popc(E);
+                if (ids >= a.min_ids) {
+                    pass = true;
+                } else if (a.kx != 0 && ids * (1 + a.kx) >= a.min_ids) {
+                    ld256(Q, a.qwinx + 2 * (uint64_t)g);
+                    staged_words(ws.resw, idx, S);
+                    const uint32_t ex = __popc(E & eq_bytes8(Q, S, 0xFFFFFFFFu));
+                    pass = ids + a.kx * ex >= a.min_ids;
+                }
             }
-            r = seg_r[lo];
-            const uint32_t sh = seg_sh[lo];
-            const uint32_t g = a.qent[seg_e0[lo] + (k - seg_start[lo])];
-            pass = a.min_ids == 0 || window_passes(a, r, g);
             if (!pass) filtered++;
-            gsh = g | (sh << 27);
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-        if (bal) {
-            const int leader = __ffs(bal) - 1;
-            unsigned long long slot0 = 0;
-            if (lane == leader) slot0 = atomicAdd(a.nsurv, (unsigned long long)__popc(bal));
-            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-            if (pass) {
-                const unsigned long long slot = slot0 + __popc(bal & ((1u << lane) - 1u));
-                if (slot < a.cap) a.surv[slot] = make_uint2((uint32_t)r, gsh);
-            }
-        }
+        if (pass)
+            ws.sv[ws.nsv + __popc(bal & ((1u << lane) - 1u))] =
+                make_uint2((uint32_t)(ws.base + rl), g | ((uint32_t)ws.seg_sh[own] << 27));
+        ws.nsv += __popc(bal);
+        if (ws.nsv >= 32) surv_drain(a, lane, ws);
     }
     __syncwarp();
 }
 
+// 4 bytes of buf at byte index i (4-aligned), `fill` outside [0, n)
+__device__ __forceinline__ uint32_t stage_word(const uint8_t* __restrict__ buf, int64_t i, uint64_t n, uint8_t fill) {
+    if (i >= 0 && (uint64_t)i + 4 <= n) return *reinterpret_cast<const uint32_t*>(buf + i);
+    uint32_t v = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int64_t p = i + j;
+        const uint32_t b = (p >= 0 && (uint64_t)p < n) ? buf[p] : fill;
+        v |= b << (8 * j);
+    }
+    return v;
+}
+
 __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
-    __shared__ uint32_t s_n[kScanWarps][kSegCap], s_e0[kScanWarps][kSegCap], s_start[kScanWarps][kSegCap];
-    __shared__ uint64_t s_r[kScanWarps][kSegCap];
-    __shared__ uint8_t s_sh[kScanWarps][kSegCap];
+    __shared__ uint32_t s_n[kScanWarps][kSegCap], s_eb[kScanWarps][kSegCap];
+    __shared__ uint8_t s_rl[kScanWarps][kSegCap], s_sh[kScanWarps][kSegCap];
+    __shared__ uint2 s_sv[kScanWarps][kSurvStage];
+    __shared__ uint32_t s_sbw[kScanWarps][32], s_resw[kScanWarps][32];
     __shared__ ShapeDev s_shape[kMaxShapes];
-    for (uint32_t i = threadIdx.x; i < a.nshapes; i += blockDim.x) s_shape[i] = a.sh[i];
+    for (uint32_t i = threadIdx.x; i < a.s1; i += blockDim.x) s_shape[i] = a.sh[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint64_t warp0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long hits = 0, filtered = 0;
+    WarpScan ws{s_n[w], s_eb[w], s_rl[w], s_sh[w], s_sv[w], s_sbw[w], s_resw[w], 0u, 0u, 0u};
+    const uint8_t* stb = reinterpret_cast<const uint8_t*>(s_sbw[w]) + 32 + lane;  // this lane's position
     for (uint64_t base = warp0 * 32; base < a.N; base += nwarps * 32) {
         const uint64_t r = base + lane;
+        const int64_t wb = (int64_t)base - 32 + 4 * lane;
+        __syncwarp();
+        s_sbw[w][lane] = stage_word(a.sb, wb, a.N, kNonSeed);
+        s_resw[w][lane] = stage_word(a.res, wb, a.N, 0xFFu);
         const int rem = r < a.N ? a.rem[r] : 0;
+        ws.rd = r < a.N ? ((uint32_t)rem | ((uint32_t)a.dst[r] << 8)) : 0u;
+        ws.base = base;
+        __syncwarp();
         int nseg = 0;
-        for (uint32_t si = 0; si < a.nshapes; si++) {
-            uint32_t n = 0, e0 = 0;
-            if (rem >= (int)s_shape[si].span) {
-                const int64_t c = seed_code(a.sb + r, s_shape[si], a.asize);
-                if (c >= 0 && ((a.pres[a.pres_off[si] + (c >> 6)] >> (c & 63)) & 1ull)) {
-                    const uint32_t* qo = a.qoff + a.qoff_off[si];
-                    e0 = qo[c];
-                    n = qo[c + 1] - e0;
-                    e0 += a.qent_off[si];
+        for (uint32_t s0 = a.s0; s0 < a.s1; s0 += kShapeUnroll) {
+            uint32_t n[kShapeUnroll], e0[kShapeUnroll];
+#pragma unroll
+            for (int j = 0; j < kShapeUnroll; j++) {
+                const uint32_t si = s0 + j;
+                n[j] = 0;
+                e0[j] = 0;
+                if (si < a.s1 && rem >= (int)s_shape[si].span) {
+                    const int64_t c = seed_code(stb, s_shape[si], a.asize);
+                    uint32_t k;
+                    if (c >= 0 && code_rank(a.grp + a.grp_off[si], (uint32_t)c, k)) {
+                        const uint32_t* co = a.coff + a.coff_off[si];
+                        e0[j] = co[k];
+                        n[j] = co[k + 1] - e0[j];
+                        e0[j] += a.qent_off[si];
+                    }
                 }
             }
-            const uint32_t bal = __ballot_sync(0xffffffffu, n > 0);
-            if (n > 0) {
-                const int slot = nseg + __popc(bal & ((1u << lane) - 1u));
-                s_n[w][slot] = n;
-                s_e0[w][slot] = e0;
-                s_r[w][slot] = r;
-                s_sh[w][slot] = (uint8_t)si;
+#pragma unroll
+            for (int j = 0; j < kShapeUnroll; j++) {
+                const uint32_t bal = __ballot_sync(0xffffffffu, n[j] > 0);
+                if (n[j] > 0) {
+                    const int slot = nseg + __popc(bal & ((1u << lane) - 1u));
+                    ws.seg_n[slot] = n[j];
+                    ws.seg_eb[slot] = e0[j];
+                    ws.seg_rl[slot] = (uint8_t)lane;
+                    ws.seg_sh[slot] = (uint8_t)(s0 + j);
+                }
+                nseg += __popc(bal);
             }
-            nseg += __popc(bal);
-            if (nseg > kSegCap - 32) {
+            if (nseg > kSegCap - 32 * kShapeUnroll) {
                 __syncwarp();
-                scan_flush(a, lane, nseg, s_n[w], s_e0[w], s_r[w], s_sh[w], s_start[w], hits, filtered);
+                scan_flush(a, lane, nseg, ws, hits, filtered);
                 nseg = 0;
             }
         }
         if (nseg) {
             __syncwarp();
-            scan_flush(a, lane, nseg, s_n[w], s_e0[w], s_r[w], s_sh[w], s_start[w], hits, filtered);
+            scan_flush(a, lane, nseg, ws, hits, filtered);
         }
     }
+    if (ws.nsv) surv_drain(a, lane, ws);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) filtered += __shfl_xor_sync(0xffffffffu, filtered, o);
     if (lane == 0) {
         atomicAdd(&a.ctr[2], hits);
         atomicAdd(&a.ctr[3], filtered);
+    }
+}
+
+// Window records of the batch positions: record g holds the 32 letters at
+// g + cfil - 16 + t (t < 32), QSENT where that position lies outside g's
+// query (the filter's query-side lane bounds).
+__global__ void k_query_windows(const uint8_t* __restrict__ qsb, const uint8_t* __restrict__ qfull,
+                                const uint8_t* __restrict__ qrem, const uint8_t* __restrict__ qdst, uint64_t QN,
+                                int cfil, uint8_t* __restrict__ win, uint8_t* __restrict__ winx) {
+    const uint64_t total = QN * 32;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t g = i >> 5;
+        const int t = (int)(i & 31);
+        const int lo = 16 - cfil - (int)qdst[g], hi = (int)qrem[g] + 16 - cfil;
+        uint8_t v = kQSent, vx = kQSent;
+        if (t >= lo && t < hi) {
+            const uint64_t q = g + (uint64_t)(int64_t)(cfil - 16 + t);
+            v = qsb[q];
+            vx = qfull[q];
+        }
+        win[i] = v;
+        winx[i] = vx;
     }
 }
 
@@ -677,8 +815,8 @@ __global__ void k_regions(RegionArgs a) {
                 }
         }
     }
-    atomicAdd(&a.ctr[7], hsps);
-    atomicAdd(&a.ctr[8], weak);
+    count_add(&a.ctr[7], hsps);
+    count_add(&a.ctr[8], weak);
 }
 
 // ---------------------------------------------------------------------------
@@ -736,10 +874,10 @@ int scan_build_db(saber_gpu* h, const saber_scan_params* p) {
     const uint64_t N = ds.n_res;
     AlphaMap am;
     memcpy(am.m, p->alpha_map, 24);
-    CUALLOC(h, h->sc_sb, N + 64);
+    CUALLOC(h, h->sc_sb, N + 128);
     CUALLOC(h, h->sc_rem, N + 64);
     CUALLOC(h, h->sc_dst, N + 64);
-    CU(h, cudaMemsetAsync(h->sc_sb.p, kNonSeed, N + 64, s));
+    CU(h, cudaMemsetAsync(h->sc_sb.p, kNonSeed, N + 128, s));
     CU(h, cudaMemsetAsync(h->sc_rem.p, 0, N + 64, s));
     CU(h, cudaMemsetAsync(h->sc_dst.p, 0, N + 64, s));
     if (N) {
@@ -812,6 +950,8 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         minspan = std::min(minspan, p->shape_span[si]);
     }
     if (p->max_regions_per_subject > 64) return fail(h, SABER_ERR_ARG, "max_regions_per_subject must be <= 64");
+    if (ds.n_res >= (1ull << 32))
+        return fail(h, SABER_ERR_ARG, "database too large for one scan (residues < 2^32): split it into volumes");
     if (ds.nsub >= (1ull << 24) || qs.nq >= (1u << 20) || qs.offs[qs.nq] >= (1ull << 27))
         return fail(h, SABER_ERR_ARG, "scan batch too large (subjects < 2^24, queries < 2^20, residues < 2^27)");
     for (uint32_t q = 0; q < qs.nq; q++)
@@ -835,13 +975,13 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     AlphaMap am;
     memcpy(am.m, p->alpha_map, 24);
     // query bytes and distances
-    CUALLOC(h, h->sc_qsb, QN + 64);
+    CUALLOC(h, h->sc_qsb, QN + 128);
     CUALLOC(h, h->sc_qfull, QN + 64);
     CUALLOC(h, h->sc_qrem, QN + 64);
     CUALLOC(h, h->sc_qdst, QN + 64);
     CUALLOC(h, h->sc_tmp, QN + 64);
     if (q_mask) CU(h, cudaMemcpyAsync(h->sc_tmp.p, q_mask, QN, cudaMemcpyHostToDevice, s));
-    CU(h, cudaMemsetAsync(h->sc_qsb.p, kQSent, QN + 64, s));
+    CU(h, cudaMemsetAsync(h->sc_qsb.p, kQSent, QN + 128, s));
     if (QN) {
         k_query_bytes<<<nblocks(QN, 256), 256, 0, s>>>(qs.codes.as<uint8_t>(), q_mask ? h->sc_tmp.as<uint8_t>() : nullptr,
                                                        QN, am, h->sc_qsb.as<uint8_t>(), h->sc_qfull.as<uint8_t>());
@@ -860,56 +1000,63 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     uint64_t scap = std::max<uint64_t>(1 << 20, h->sc_surv.cap / 8);
     uint64_t nsurv = 0;
     const int cfil = (int)(minspan / 2);
-    // seed tables of all shapes, concatenated: per shape a code -> entry
-    // offset table (nc + 1 words), a presence bitmap and its batch positions
+    // seed tables of all shapes, concatenated, rank-compressed: per shape the
+    // 32-code groups (presence bits, rank), at most QN + 1 entry offsets and
+    // QN batch positions -- sized by their bounds, so no host sync is needed
     const uint32_t nsh = p->nshapes;
-    std::vector<uint64_t> qbase(nsh + 1, 0), pbase(nsh + 1, 0), ebase(nsh + 1, 0);
+    std::vector<uint64_t> gbase(nsh + 1, 0);
     uint64_t ncmax = 0;
     for (uint32_t si = 0; si < nsh; si++) {
         const uint64_t nc = ncodes_of(p, si);
         ncmax = std::max(ncmax, nc);
-        qbase[si + 1] = qbase[si] + nc + 1;
-        pbase[si + 1] = pbase[si] + (nc + 63) / 64 + 1;
+        gbase[si + 1] = gbase[si] + (nc + 31) / 32;
     }
-    CUALLOC(h, h->sc_qcnt, qbase[nsh] * 4);
-    CUALLOC(h, h->sc_qoff, qbase[nsh] * 4);
-    CUALLOC(h, h->sc_qpres, pbase[nsh] * 8);
-    CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, qbase[nsh] * 4, s));
-    CU(h, cudaMemsetAsync(h->sc_qpres.p, 0, pbase[nsh] * 8, s));
+    const uint64_t ngmax = (ncmax + 31) / 32;
+    const uint64_t coff_n = QN + 1;
+    CUALLOC(h, h->sc_qcnt, std::max(ncmax, coff_n) * 4);
+    CUALLOC(h, h->sc_qpres, gbase[nsh] * 8 + 8);
+    CUALLOC(h, h->sc_gcnt, ngmax * 4 + 4);
+    CUALLOC(h, h->sc_grank, ngmax * 4 + 4);
+    CUALLOC(h, h->sc_cntc, coff_n * 4);
+    CUALLOC(h, h->sc_qoff, (uint64_t)nsh * coff_n * 4);
+    CUALLOC(h, h->sc_qent, (uint64_t)nsh * QN * 4 + 4);
     {
-        size_t tb = 0;
-        CU(h, cub::DeviceScan::ExclusiveSum(nullptr, tb, h->sc_qcnt.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
-                                            (int)(ncmax + 1), s));
-        CUALLOC(h, h->cub_tmp, tb);
+        size_t t1 = 0, t2 = 0;
+        CU(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, h->sc_gcnt.as<uint32_t>(), h->sc_grank.as<uint32_t>(),
+                                            (int)ngmax, s));
+        CU(h, cub::DeviceScan::ExclusiveSum(nullptr, t2, h->sc_cntc.as<uint32_t>(), h->sc_qoff.as<uint32_t>(),
+                                            (int)coff_n, s));
+        CUALLOC(h, h->cub_tmp, std::max(t1, t2));
     }
-    std::vector<uint32_t> nseed(nsh, 0);
+    uint32_t* cnt = h->sc_qcnt.as<uint32_t>();
     for (uint32_t si = 0; si < nsh; si++) {
-        const uint64_t nc = ncodes_of(p, si);
+        const uint64_t nc = ncodes_of(p, si), ng = (nc + 31) / 32;
+        const ShapeDev sh = shape_dev(p, si);
         const unsigned long long* freq = h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si];
-        uint32_t* cnt = h->sc_qcnt.as<uint32_t>() + qbase[si];
-        uint32_t* off = h->sc_qoff.as<uint32_t>() + qbase[si];
+        uint2* grp = h->sc_qpres.as<uint2>() + gbase[si];
+        uint32_t* coff = h->sc_qoff.as<uint32_t>() + (uint64_t)si * coff_n;
+        CU(h, cudaMemsetAsync(cnt, 0, nc * 4, s));
+        CU(h, cudaMemsetAsync(h->sc_cntc.p, 0, coff_n * 4, s));
         if (QN)
             k_query_seeds<0><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
-                                                              shape_dev(p, si), p->alpha_size, freq, cnt, nullptr,
+                                                              sh, p->alpha_size, freq, cnt, nullptr, nullptr,
                                                               nullptr, ctr);
+        k_group_bits<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(cnt, nc, grp, h->sc_gcnt.as<uint32_t>());
         size_t tb = h->cub_tmp.cap;
-        CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, cnt, off, (int)(nc + 1), s));
-        k_presence<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(
-            cnt, nc, h->sc_qpres.as<unsigned long long>() + pbase[si]);
-        CU(h, cudaMemcpyAsync(&nseed[si], off + nc, 4, cudaMemcpyDeviceToHost, s));
+        CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, h->sc_gcnt.as<uint32_t>(), h->sc_grank.as<uint32_t>(),
+                                            (int)ng, s));
+        k_group_ranks<<<nblocks(nc, 256, h->sm_count * 32), 256, 0, s>>>(cnt, nc, h->sc_grank.as<uint32_t>(), grp,
+                                                                         h->sc_cntc.as<uint32_t>());
+        tb = h->cub_tmp.cap;
+        CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, h->sc_cntc.as<uint32_t>(), coff, (int)coff_n, s));
+        // pass 1: the counts' buffer becomes the per-rank cursors
+        CU(h, cudaMemsetAsync(cnt, 0, coff_n * 4, s));
+        if (QN)
+            k_query_seeds<1><<<nblocks(QN, 256), 256, 0, s>>>(h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN,
+                                                              sh, p->alpha_size, freq, cnt, grp, coff,
+                                                              h->sc_qent.as<uint32_t>() + (uint64_t)si * QN, ctr);
+        CU(h, cudaGetLastError());
     }
-    CU(h, cudaStreamSynchronize(s));
-    for (uint32_t si = 0; si < nsh; si++) ebase[si + 1] = ebase[si] + nseed[si];
-    if (ebase[nsh] >= (1ull << 32)) return fail(h, SABER_ERR_ARG, "too many query seeds in one batch");
-    CUALLOC(h, h->sc_qent, ebase[nsh] * 4 + 4);
-    CU(h, cudaMemsetAsync(h->sc_qcnt.p, 0, qbase[nsh] * 4, s));
-    for (uint32_t si = 0; si < nsh; si++)
-        if (QN && nseed[si])
-            k_query_seeds<1><<<nblocks(QN, 256), 256, 0, s>>>(
-                h->sc_qsb.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), QN, shape_dev(p, si), p->alpha_size,
-                h->sc_freq.as<unsigned long long>() + h->sc_freq_off[si], h->sc_qcnt.as<uint32_t>() + qbase[si],
-                h->sc_qoff.as<uint32_t>() + qbase[si], h->sc_qent.as<uint32_t>() + ebase[si], ctr);
-    CU(h, cudaGetLastError());
     CU(h, cudaEventRecord(ev[1], s));
     ScanArgs a;
     a.sb = h->sc_sb.as<uint8_t>();
@@ -917,36 +1064,54 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     a.rem = h->sc_rem.as<uint8_t>();
     a.dst = h->sc_dst.as<uint8_t>();
     a.N = N;
-    a.pres = h->sc_qpres.as<unsigned long long>();
-    a.qoff = h->sc_qoff.as<uint32_t>();
+    a.grp = h->sc_qpres.as<uint2>();
+    a.coff = h->sc_qoff.as<uint32_t>();
     a.qent = h->sc_qent.as<uint32_t>();
-    a.qsb = h->sc_qsb.as<uint8_t>();
-    a.qfull = h->sc_qfull.as<uint8_t>();
-    a.qrem = h->sc_qrem.as<uint8_t>();
-    a.qdst = h->sc_qdst.as<uint8_t>();
+    CUALLOC(h, h->sc_qwin, QN * 32 + 32);
+    CUALLOC(h, h->sc_qwinx, QN * 32 + 32);
+    if (QN)
+        k_query_windows<<<nblocks(QN * 32, 256), 256, 0, s>>>(
+            h->sc_qsb.as<uint8_t>(), h->sc_qfull.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), h->sc_qdst.as<uint8_t>(),
+            QN, cfil, h->sc_qwin.as<uint8_t>(), h->sc_qwinx.as<uint8_t>());
+    a.qwin = h->sc_qwin.as<uint4>();
+    a.qwinx = h->sc_qwinx.as<uint4>();
     a.cfil = cfil;
     a.min_ids = p->hit_filter_min_ids;
     a.kx = p->hit_filter_exact_weight;
-    a.nshapes = nsh;
     a.asize = p->alpha_size;
     a.nsurv = ctr + 10;
     a.ctr = ctr;
     for (uint32_t si = 0; si < nsh; si++) {
         a.sh[si] = shape_dev(p, si);
-        a.pres_off[si] = pbase[si];
-        a.qoff_off[si] = qbase[si];
-        a.qent_off[si] = (uint32_t)ebase[si];
+        a.grp_off[si] = gbase[si];
+        a.coff_off[si] = (uint64_t)si * coff_n;
+        a.qent_off[si] = (uint32_t)((uint64_t)si * QN);
     }
+    // passes over groups of shapes whose tables stay within the L2 budget:
+    // as many shapes per pass as the largest shape's tables allow, rounded
+    // down to whole unroll groups
+    uint64_t shape_bytes = 0;
+    for (uint32_t si = 0; si < nsh; si++)
+        shape_bytes = std::max(shape_bytes, (gbase[si + 1] - gbase[si]) * 8 + coff_n * 4 + QN * 4);
+    uint64_t per_pass = std::max<uint64_t>(1, h->scan_table_bytes / std::max<uint64_t>(shape_bytes, 1));
+    if (per_pass >= (uint64_t)kShapeUnroll) per_pass -= per_pass % kShapeUnroll;
+    std::vector<std::pair<uint32_t, uint32_t>> passes;
+    for (uint32_t si = 0; si < nsh; si += (uint32_t)std::min<uint64_t>(per_pass, nsh))
+        passes.push_back({si, (uint32_t)std::min<uint64_t>(nsh, si + per_pass)});
     int scan_bps = 0;
     CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&scan_bps, k_scan, kScanWarps * 32, 0));
     const unsigned scan_grid = (unsigned)std::max(1, scan_bps) * (unsigned)h->sm_count;
     for (int attempt = 0; attempt < 8; attempt++) {
         CUALLOC(h, h->sc_surv, scap * 8);
         CU(h, cudaMemsetAsync(ctr + 2, 0, 9 * 8, s));  // hits, filtered, ..., survivors
-        if (ebase[nsh] && N) {
+        if (QN && N) {
             a.surv = h->sc_surv.as<uint2>();
             a.cap = scap;
-            k_scan<<<scan_grid, kScanWarps * 32, 0, s>>>(a);
+            for (const auto& ps : passes) {
+                a.s0 = ps.first;
+                a.s1 = ps.second;
+                k_scan<<<scan_grid, kScanWarps * 32, 0, s>>>(a);
+            }
             CU(h, cudaGetLastError());
         }
         unsigned long long hc[16];

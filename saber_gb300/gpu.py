@@ -230,6 +230,8 @@ def load_library():
         "saber_gpu_collect_regions": (ctypes.c_int, [P, I32]),
         "saber_gpu_collected_regions": (ctypes.c_int, [P, P, P, P, U64, P]),
         "saber_gpu_get_pair_steps": (U32, [P]),
+        "saber_gpu_set_scan_table_bytes": (ctypes.c_int, [P, U64]),
+        "saber_gpu_get_scan_table_bytes": (U64, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
     for name, (res, args) in sig.items():
@@ -513,6 +515,15 @@ class Device:
     @pair_steps.setter
     def pair_steps(self, v):
         self._check(self.lib.saber_gpu_set_pair_steps(self.h, int(v) & 0xFFFFFFFF), "set_pair_steps")
+
+    @property
+    def scan_table_bytes(self):
+        """Seed-table bytes per database pass of the scan (shapes split into passes)."""
+        return int(self.lib.saber_gpu_get_scan_table_bytes(self.h))
+
+    @scan_table_bytes.setter
+    def scan_table_bytes(self, v):
+        self._check(self.lib.saber_gpu_set_scan_table_bytes(self.h, int(v)), "set_scan_table_bytes")
 
     def probe_int_peak(self):
         """(DPX s16x2 lane-instructions/s, int32 max lane-instructions/s) of this GPU."""
