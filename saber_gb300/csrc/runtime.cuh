@@ -61,6 +61,7 @@ struct QuerySet {
 struct Dataset {
     DevBuf res, soff;
     uint64_t n_res = 0, nsub = 0;
+    uint64_t max_len = 0;  // longest subject
     bool has_db = false;
     QuerySet qs;
 };

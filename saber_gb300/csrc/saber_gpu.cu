@@ -604,8 +604,11 @@ static int load_db(saber_gpu* h, Dataset& ds, const uint8_t* residues, uint64_t 
     if ((!residues && n_res) || !offsets) return fail(h, SABER_ERR_ARG, "null database arrays");
     if (offsets[0] != 0 || offsets[nsub] != n_res)
         return fail(h, SABER_ERR_ARG, "subject offsets must run from 0 to n_residues");
-    for (uint64_t i = 0; i < nsub; i++)
+    uint64_t max_len = 0;
+    for (uint64_t i = 0; i < nsub; i++) {
         if (offsets[i + 1] < offsets[i]) return fail(h, SABER_ERR_ARG, "subject offsets must be non-decreasing");
+        max_len = std::max<uint64_t>(max_len, offsets[i + 1] - offsets[i]);
+    }
     ds.has_db = false;
     CUALLOC(h, ds.res, n_res + 64);
     CUALLOC(h, ds.soff, (nsub + 1) * 8);
@@ -620,6 +623,7 @@ static int load_db(saber_gpu* h, Dataset& ds, const uint8_t* residues, uint64_t 
     CU(h, cudaStreamSynchronize(s));
     ds.n_res = n_res;
     ds.nsub = nsub;
+    ds.max_len = max_len;
     ds.has_db = true;
     if (&ds == &h->main) {
         h->sc_key = 0;

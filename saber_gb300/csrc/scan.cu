@@ -557,7 +557,7 @@ __global__ void k_surv_keys(const uint2* __restrict__ surv, uint32_t n, const ui
         const uint64_t q = upper_idx(qoffs, nq, g);
         const int64_t qp = (int64_t)g - (int64_t)qoffs[q], sp = (int64_t)v.x - (int64_t)soffs[s];
         const int64_t d = sp - qp;
-        key1[i] = ((unsigned long long)s << 40) | ((unsigned long long)q << 20) | (unsigned long long)(d + kDBias);
+        key1[i] = ((unsigned long long)q << 44) | ((unsigned long long)s << 20) | (unsigned long long)(d + kDBias);
         key2[i] = ((uint32_t)qp << 5) | shape;
         val[i] = i;
     }
@@ -593,133 +593,158 @@ struct ChainArgs {
     unsigned long long* nhsp;
     uint64_t hcap;
     unsigned long long* ctr;          // [4] extensions, [5] avoided, [6] steps
+    uint32_t* next;                   // chain work counter (zero at launch)
 };
 
-// One direction of the ungapped X-drop (ungapped_xdrop, engine.rs:2460-2494,
-// step count of xdrop_cat, scan.rs:859-904), 32 positions per warp round:
-// position t (0-based) scores P[s[sp + dir (t + off)]][qp + dir (t + off)]
-// with off = 0 rightwards (dir = +1) and 1 leftwards (dir = -1).  The
-// running sum, the running best (starting at 0) and the first position where
-// the sum falls more than x below the best come from warp scans; as in the
-// scalar loops, the stop position is evaluated, later ones are not, and the
-// extent is the first position of the best sum (strictly greater than every
-// earlier one).  Returns the best; *ext = extent (0 if the best is 0),
-// *evaluated = positions evaluated.
-__device__ __forceinline__ int xdrop_dir(const int16_t* __restrict__ P, int mpad, const uint8_t* __restrict__ s,
-                                         int64_t qp, int64_t sp, int64_t n, int dir, int x, int lane, int64_t* ext,
-                                         int64_t* evaluated) {
-    const int off = dir > 0 ? 0 : 1;
-    int best = 0, cur = 0;
-    int64_t e = 0, done = 0;
-    for (int64_t base = 0; base < n; base += 32) {
-        const int64_t t = base + lane;
-        const bool valid = t < n;
-        int v = 0;
-        if (valid) {
-            const int64_t d = dir * (t + off);
-            v = P[(size_t)s[sp + d] * mpad + qp + d];
-        }
-        int c = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, c, o);
-            if (lane >= o) c += u;
-        }
-        c += cur;
-        int m = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, m, o);
-            if (lane >= o) m = max(m, u);
-        }
-        m = max(m, best);
-        const int prev = __shfl_up_sync(0xffffffffu, m, 1);
-        const int excl = lane == 0 ? best : prev;
-        const unsigned viol = __ballot_sync(0xffffffffu, valid && c < m - x);
-        const int64_t left = n - 1 - base;
-        int limit = left < 31 ? (int)left : 31;
-        if (viol) limit = min(limit, __ffs(viol) - 1);
-        const unsigned upto = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
-        const unsigned rec = __ballot_sync(0xffffffffu, valid && c > excl) & upto;
-        if (rec) e = base + (31 - __clz(rec)) + 1;
-        best = __shfl_sync(0xffffffffu, m, limit);
-        cur = __shfl_sync(0xffffffffu, c, limit);
-        done = base + limit + 1;
-        if (viol) break;
-    }
-    *ext = e;
-    *evaluated = done;
-    return best;
-}
-
-// One warp per chain (one subject, query and diagonal; hits in (query
+// Chains, one per lane (one subject, query and diagonal; hits in (query
 // position, shape) order): the coverage test and the X-drop extensions of
 // visit_scan (scan.rs:2384-2431), HSPs of at least thr appended with the
-// number of the chain's seed hits they cover.
+// number of the chain's seed hits they cover.  The ungapped X-drop
+// (ungapped_xdrop, engine.rs:2460-2494; step count of xdrop_cat,
+// scan.rs:859-904) runs as a per-lane state machine, 8 positions per warp
+// iteration: position t (0-based) of a direction scores
+// P[s[sp + dir (t + off)]][qp + dir (t + off)] (off = 0 rightwards, 1
+// leftwards); a strictly greater running sum is a new best and sets the
+// extent to t + 1, a sum more than x below the best stops the direction
+// after evaluating t.  So the warp's lanes stay converged whatever their
+// chains' lengths, and lanes that finish a chain take the next one from a
+// shared counter (chains are in query-major order, so a warp's lanes mostly
+// read one query's profile).
+constexpr int kXBlock = 8;
+
 __global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
     const int lane = threadIdx.x & 31;
-    const uint32_t warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    unsigned long long ext = 0, avoided = 0, steps = 0;
     const uint32_t nch = *a.nchains;
-    for (uint32_t c = warp0; c < nch; c += nwarps) {
-        const uint32_t b = a.starts[c];
-        const uint32_t e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
-        const unsigned long long key = a.key1s[b];
-        const uint64_t s = key >> 40, q = (key >> 20) & 0xFFFFF;
-        const int64_t q0 = (int64_t)a.qoffs[q], s0 = (int64_t)a.soffs[s];
-        const int64_t qlen = (int64_t)a.qoffs[q + 1] - q0;
-        const int64_t sl = (int64_t)a.soffs[s + 1] - s0;
-        const int16_t* P = a.prof + a.prof_off[q];
-        const int mpad = (int)a.prof_mpad[q];
-        const uint8_t* subj = a.res + s0;
-        int64_t cover = 0;
-        for (uint32_t i = b; i < e; i++) {
-            const uint2 v = a.surv[a.order[i]];
-            const int64_t qp = (int64_t)(v.y & ((1u << 27) - 1)) - q0;
-            const int64_t sp = (int64_t)v.x - s0;
-            if (qp < cover) {
-                avoided++;
-                continue;
-            }
-            ext++;
-            int64_t end_t, st_t, nr_done, nl_done;
-            const int64_t nr = qlen - qp < sl - sp ? qlen - qp : sl - sp;
-            const int64_t nl = qp < sp ? qp : sp;
-            const int br = xdrop_dir(P, mpad, subj, qp, sp, nr, 1, a.x, lane, &end_t, &nr_done);
-            const int bl = xdrop_dir(P, mpad, subj, qp, sp, nl, -1, a.x, lane, &st_t, &nl_done);
-            steps += (uint64_t)(nr_done + nl_done);
-            const int64_t hi = qp + end_t, lo = qp - st_t;
-            cover = hi;
-            const int score = br + bl;
-            if (score >= a.thr) {
-                // seed hits of the HSP: this one and the chain's later hits
-                // below hi (query positions ascend along the chain)
-                uint32_t nhits = 1;
-                for (uint32_t j0 = i + 1; j0 < e; j0 += 32) {
-                    const uint32_t j = j0 + lane;
-                    const bool in = j < e && (int64_t)(a.surv[a.order[j]].y & ((1u << 27) - 1)) - q0 < hi;
-                    const unsigned bal = __ballot_sync(0xffffffffu, in);
-                    const unsigned run = ~bal ? (unsigned)__ffs(~bal) - 1u : 32u;
-                    nhits += run;
-                    if (run < 32) break;
+    unsigned long long ext = 0, avoided = 0, steps = 0;
+    uint32_t i = 0, e = 0;  // survivors left in this lane's chain
+    bool retired = false;
+    int phase = 0;          // 0: next survivor, 1: rightwards, 2: leftwards
+    unsigned long long hkey = 0;
+    int64_t q0 = 0, s0 = 0, qlen = 0, sl = 0, cover = 0;
+    const int16_t* P = nullptr;
+    int mpad = 0;
+    const uint8_t* subj = nullptr;
+    int64_t qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
+    int cur = 0, best = 0, best_r = 0;
+    const uint32_t m27 = (1u << 27) - 1u;
+    while (true) {
+        const bool need = !retired && phase == 0 && i >= e;
+        const uint32_t nb = __ballot_sync(0xffffffffu, need);
+        if (nb) {
+            const int leader = __ffs(nb) - 1;
+            uint32_t c0 = 0;
+            if (lane == leader) c0 = atomicAdd(a.next, (uint32_t)__popc(nb));
+            c0 = __shfl_sync(0xffffffffu, c0, leader);
+            if (need) {
+                const uint32_t c = c0 + __popc(nb & ((1u << lane) - 1u));
+                if (c >= nch) {
+                    retired = true;
+                } else {
+                    i = a.starts[c];
+                    e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
+                    const unsigned long long key = a.key1s[i];
+                    const uint64_t q = key >> 44, s = (key >> 20) & 0xFFFFFF;
+                    hkey = (s << 40) | (q << 20) | (key & 0xFFFFF);  // subject-major HSP key
+                    q0 = (int64_t)a.qoffs[q];
+                    s0 = (int64_t)a.soffs[s];
+                    qlen = (int64_t)a.qoffs[q + 1] - q0;
+                    sl = (int64_t)a.soffs[s + 1] - s0;
+                    P = a.prof + a.prof_off[q];
+                    mpad = (int)a.prof_mpad[q];
+                    subj = a.res + s0;
+                    cover = 0;
                 }
-                if (lane == 0) {
-                    const unsigned long long slot = atomicAdd(a.nhsp, 1ull);
-                    if (slot < a.hcap) {
-                        a.hsp[slot] = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, nhits);
-                        a.hkey[slot] = key;
-                        a.hval[slot] = (uint32_t)slot;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, !retired) == 0) break;
+        bool emit = false;
+        uint4 hsp = make_uint4(0, 0, 0, 0);
+        if (!retired) {
+            if (phase == 0) {
+                const uint2 v = a.surv[a.order[i]];
+                qp = (int64_t)(v.y & m27) - q0;
+                sp = (int64_t)v.x - s0;
+                n = qlen - qp < sl - sp ? qlen - qp : sl - sp;
+                t = 0;
+                cur = best = 0;
+                xe = 0;
+                phase = 1;
+            }
+            const int64_t dir = phase == 1 ? 1 : -1, off = phase == 1 ? 0 : 1;
+            int sv[kXBlock];
+#pragma unroll
+            for (int u = 0; u < kXBlock; u++) {
+                const int64_t tt = t + u;
+                const int64_t d = dir * (tt + off);
+                sv[u] = tt < n ? (int)P[(size_t)subj[sp + d] * mpad + qp + d] : 0;
+            }
+            bool stop = false;
+            int64_t done = 0;
+#pragma unroll
+            for (int u = 0; u < kXBlock; u++) {
+                const int64_t tt = t + u;
+                if (!stop && tt < n) {
+                    cur += sv[u];
+                    if (cur > best) {
+                        best = cur;
+                        xe = tt + 1;
+                    } else if (cur < best - a.x) {
+                        stop = true;
+                        done = tt + 1;
                     }
                 }
             }
+            t += kXBlock;
+            if (stop || t >= n) {
+                if (!stop) done = n;
+                if (phase == 1) {
+                    best_r = best;
+                    end_r = xe;
+                    done_r = done;
+                    phase = 2;
+                    n = qp < sp ? qp : sp;
+                    t = 0;
+                    cur = best = 0;
+                    xe = 0;
+                } else {
+                    steps += (uint64_t)(done_r + done);
+                    ext++;
+                    const int64_t hi = qp + end_r, lo = qp - xe;
+                    cover = hi;
+                    const int score = best_r + best;
+                    // the chain's next hits below hi are covered (query
+                    // positions ascend along the chain); the HSP counts them
+                    uint32_t j = i + 1;
+                    while (j < e && (int64_t)(a.surv[a.order[j]].y & m27) - q0 < cover) j++;
+                    avoided += j - (i + 1);
+                    if (score >= a.thr) {
+                        emit = true;
+                        hsp = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, j - i);
+                    }
+                    i = j;
+                    phase = 0;
+                }
+            }
+        }
+        const uint32_t eb = __ballot_sync(0xffffffffu, emit);
+        if (eb) {
+            const int leader = __ffs(eb) - 1;
+            unsigned long long slot0 = 0;
+            if (lane == leader) slot0 = atomicAdd(a.nhsp, (unsigned long long)__popc(eb));
+            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+            if (emit) {
+                const unsigned long long slot = slot0 + __popc(eb & ((1u << lane) - 1u));
+                if (slot < a.hcap) {
+                    a.hsp[slot] = hsp;
+                    a.hkey[slot] = hkey;
+                    a.hval[slot] = (uint32_t)slot;
+                }
+            }
         }
     }
-    if (lane == 0) {
-        atomicAdd(&a.ctr[4], ext);
-        atomicAdd(&a.ctr[5], avoided);
-        atomicAdd(&a.ctr[6], steps);
-    }
+    count_add(&a.ctr[4], ext);
+    count_add(&a.ctr[5], avoided);
+    count_add(&a.ctr[6], steps);
 }
 
 struct RegionArgs {
@@ -950,6 +975,8 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         minspan = std::min(minspan, p->shape_span[si]);
     }
     if (p->max_regions_per_subject > 64) return fail(h, SABER_ERR_ARG, "max_regions_per_subject must be <= 64");
+    if (ds.max_len >= (uint64_t)kDBias)
+        return fail(h, SABER_ERR_ARG, "subject too long for the seed scan (< 2^19 residues)");
     if (ds.n_res >= (1ull << 32))
         return fail(h, SABER_ERR_ARG, "database too large for one scan (residues < 2^32): split it into volumes");
     if (ds.nsub >= (1ull << 24) || qs.nq >= (1u << 20) || qs.offs[qs.nq] >= (1ull << 27))
@@ -1144,25 +1171,37 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(), ds.nsub,
                                                      qs.offsets.as<uint64_t>(), qs.nq, h->sc_key1.as<unsigned long long>(),
                                                      h->sc_key2.as<uint32_t>(), h->sc_val.as<uint32_t>());
-        // stable two-key order: by (query position, shape), then by (subject, query, diagonal)
+        // stable two-key order: by (query position, shape), then by (query,
+        // subject, diagonal); the sorts cover only the keys' significant bits
+        auto bits_for = [](uint64_t v) {
+            int b = 1;
+            while (b < 64 && (v >> b)) b++;
+            return b;
+        };
+        uint64_t qmax = 1;
+        for (uint32_t q = 0; q < qs.nq; q++) qmax = std::max<uint64_t>(qmax, qs.offs[q + 1] - qs.offs[q]);
+        const int k2_end = std::min(32, 5 + bits_for(qmax));
+        const int k1_end = std::min(64, 44 + bits_for(qs.nq));
         size_t t1 = 0, t2 = 0, t3 = 0;
         CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t1, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, 32, s));
+                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end,
+                                              s));
         CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t2, h->sc_key1o.as<unsigned long long>(),
                                               h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), (int)ns, 0, 64, s));
+                                              h->sc_val.as<uint32_t>(), (int)ns, 0, k1_end, s));
         CU(h, cub::DeviceSelect::Flagged(nullptr, t3, thrust::counting_iterator<uint32_t>(0), h->sc_flags.as<uint8_t>(),
                                          h->sc_chains.as<uint32_t>(), h->sc_ctr.as<uint32_t>() + 40, (int)ns, s));
         CUALLOC(h, h->cub_tmp, std::max(t1, std::max(t2, t3)));
         size_t tb = h->cub_tmp.cap;
         CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, 32, s));
+                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end,
+                                              s));
         k_gather_key1<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(), ns,
                                                        h->sc_key1o.as<unsigned long long>());
         CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key1o.as<unsigned long long>(),
                                               h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), (int)ns, 0, 64, s));
-        // chains: runs of one (subject, query, diagonal)
+                                              h->sc_val.as<uint32_t>(), (int)ns, 0, k1_end, s));
+        // chains: runs of one (query, subject, diagonal)
         k_run_flags<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), ns, 0, h->sc_flags.as<uint8_t>());
         uint32_t* nchains = h->sc_ctr.as<uint32_t>() + 40;
         CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
@@ -1194,7 +1233,11 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         c.nhsp = ctr + 11;
         c.hcap = hcap;
         c.ctr = ctr;
-        k_chains<<<h->sm_count * 8, 256, 0, s>>>(c);
+        c.next = reinterpret_cast<uint32_t*>(ctr + 14);
+        CU(h, cudaMemsetAsync(c.next, 0, 4, s));
+        int chain_bps = 0;
+        CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&chain_bps, k_chains, 256, 0));
+        k_chains<<<(unsigned)std::max(1, chain_bps) * (unsigned)h->sm_count, 256, 0, s>>>(c);
         CU(h, cudaGetLastError());
         unsigned long long nh = 0;
         CU(h, cudaMemcpyAsync(&nh, ctr + 11, 8, cudaMemcpyDeviceToHost, s));
