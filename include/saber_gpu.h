@@ -332,6 +332,11 @@ typedef struct {
     uint64_t band_scored_regions, band_rescored, banded_cells, score_launches;
     uint64_t alignments;
     double t_prep_ms, t_scan_ms, t_triage_ms, t_plan_ms, t_score_ms, t_finish_ms, t_total_ms;  /* host wall clock */
+    /* inside t_score_ms: wall clock of the scoring calls (copies, kernels,
+     * synchronisation) and the device time of their kernels */
+    double t_score_calls_ms, t_score_device_ms;
+    /* inside t_finish_ms: wall clock of the traceback calls */
+    double t_finish_tb_ms;
 } saber_search_stats;
 
 /* Hits of every query of the batch, ordered by query, then (E-value, score

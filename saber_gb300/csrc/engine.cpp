@@ -17,6 +17,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include "region_sink.h"
+
 #include <cuda_runtime.h>  // float4, uint4
 
 #include "saber_gpu.h"
@@ -427,8 +429,11 @@ struct Engine {
         out.assign(jobs.size(), 0);
         if (jobs.empty()) return SABER_OK;
         saber_score_stats ss{};
+        const double t0 = now_ms();
         int rc = saber_gpu_score_band_jobs(h, jobs.data(), jobs.size(), out.data(), &ss);
         if (rc != SABER_OK) return rc;
+        st.t_score_calls_ms += now_ms() - t0;
+        st.t_score_device_ms += ss.t_prep_ms + ss.t_fast_ms + ss.t_generic_ms;
         st.banded_cells += ss.banded_cells;
         st.score_launches += 1;
         return SABER_OK;
@@ -761,9 +766,11 @@ struct Engine {
         std::vector<saber_alignment> out(need.size());
         std::vector<uint32_t> ops(cap);
         saber_traceback_stats ts{};
+        const double t0 = now_ms();
         int rc = saber_gpu_traceback(h, jobs.data(), jobs.size(), P.band_pad, P.traceback_max_bytes, out.data(),
                                      ops.data(), cap, &ts);
         if (rc != SABER_OK) return rc;
+        st.t_finish_tb_ms += now_ms() - t0;
         st.traceback.tracebacks += ts.tracebacks;
         st.traceback.band_widenings += ts.band_widenings;
         st.traceback.end_anchored += ts.end_anchored;
@@ -797,12 +804,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
 
 namespace saber {
 int scheme_matrix(saber_gpu* h, int32_t* out576);  // saber_gpu.cu
-int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                     std::vector<saber_region>& out, std::vector<uint4>& rstat, saber_scan_stats* st);
-int triage_regions(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
-                   const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
-                   const std::vector<float4>& qinfo, float lambda, float logk, std::vector<uint8_t>& keep,
-                   bool* active);
+int scan_search_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                        RegionSink& sink, saber_scan_stats* st);  // saber_gpu.cu
 void triage_set_labels(saber_gpu* h, const std::vector<uint64_t>& hit_regions);
 }
 
@@ -845,48 +848,28 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     } else if (nq && nsub) {
         std::vector<int32_t> thr(nq);
         for (uint32_t qi = 0; qi < nq; qi++) thr[qi] = (int32_t)preps[qi].region_thr;
-        std::vector<saber_region> regs;
-        std::vector<uint4> rstat;
-        rc = saber::scan_regions_all(h, &P.scan, q_mask, thr.data(), regs, rstat, &E.st.scan);
+        // candidate regions, capped per query and triaged (a no-op without a
+        // model or collection) on the device; the kept ones arrive grouped by
+        // query in region order, each with its position in the capped list
+        saber::RegionSink sink;
+        sink.lambda = (float)P.lambda;
+        sink.logk = (float)std::log(P.k);
+        rc = saber::scan_search_regions(h, &P.scan, q_mask, thr.data(), sink, &E.st.scan);
         if (rc != SABER_OK) return rc;
         t_scan_end = now_ms();
-        // learned triage (a no-op without a model or collection): regions
-        // arrive grouped by query in region order
-        const uint64_t nr = regs.size();
-        std::vector<uint64_t> qstart(nq + 1, 0);
-        for (const saber_region& r : regs) qstart[r.query + 1]++;
-        for (uint32_t qi = 0; qi < nq; qi++) qstart[qi + 1] += qstart[qi];
-        std::vector<uint32_t> rq(nr), rrank(nr);
-        std::vector<float4> qinfo(nq);
+        collecting = sink.collecting;
+        if (sink.triaged) E.st.triage_dropped += sink.ncap - sink.n;
+        const saber_region* R = sink.regs;
+        const uint32_t* src = sink.src;
+        const uint64_t nr = sink.n;
         parallel_for(nq, [&](size_t qi) {
-            const uint64_t b = qstart[qi], e = qstart[qi + 1];
-            for (uint64_t t = b; t < e; t++) {
-                rq[t] = (uint32_t)qi;
-                rrank[t] = (uint32_t)(t - b);
-            }
-            qinfo[qi] = make_float4((float)qlens[qi], (float)preps[qi].region_thr, e > b ? (float)regs[b].best : 0.f,
-                                    (float)(e - b));
-        });
-        std::vector<uint8_t> keep;
-        bool tri = false;
-        rc = saber::triage_regions(h, regs, rstat, rq, rrank, qinfo, (float)P.lambda, (float)std::log(P.k), keep, &tri);
-        if (rc != SABER_OK) return rc;
-        collecting = tri;
-        std::vector<uint64_t> dropped(nq, 0);
-        parallel_for(nq, [&](size_t qi) {
-            const uint64_t b = qstart[qi], e = qstart[qi + 1];
+            auto by_query = [](const saber_region& r, uint64_t q) { return r.query < q; };
+            const uint64_t b = (uint64_t)(std::lower_bound(R, R + nr, (uint64_t)qi, by_query) - R);
+            const uint64_t e = (uint64_t)(std::lower_bound(R + b, R + nr, (uint64_t)qi + 1, by_query) - R);
             auto& v = per_q[qi];
             v.reserve(e - b);
-            for (uint64_t t = b; t < e; t++) {
-                if (!keep[t]) {
-                    dropped[qi]++;
-                    continue;
-                }
-                const saber_region& r = regs[t];
-                v.push_back({r.subject, r.d_min, r.d_max, r.best, t});
-            }
+            for (uint64_t t = b; t < e; t++) v.push_back({R[t].subject, R[t].d_min, R[t].d_max, R[t].best, src[t]});
         });
-        for (uint64_t d : dropped) E.st.triage_dropped += d;
     }
     for (uint32_t qi = 0; qi < nq; qi++) {
         if (qlens[qi] == 0) per_q[qi].clear();

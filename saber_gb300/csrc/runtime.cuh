@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +12,7 @@
 #include <vector>
 
 #include "band_common.cuh"
+#include "region_sink.h"
 #include "saber_gpu.h"
 
 namespace saber {
@@ -38,6 +40,32 @@ struct DevBuf {
         cap = 0;
         size_t want = bytes < 256 ? 256 : bytes;
         cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+// Pinned host memory (grow-only, 25 % slack; contents are not preserved).
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t reserve(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes + bytes / 4, 4096);
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
         if (e == cudaSuccess) cap = want;
         return e;
     }
@@ -131,6 +159,9 @@ struct saber_gpu {
     uint64_t sc_key = 0;            // fingerprint of the database state built
     std::vector<uint64_t> sc_caps;  // per shape
     std::vector<uint64_t> sc_freq_off;
+    // device-side region cap / triage / compaction, pinned host staging
+    saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
+    saber::HostBuf pin_reg, pin_src;
     // traceback scratch
     saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
 };
@@ -165,7 +196,7 @@ static int fail(saber_gpu* h, int code, const char* fmt, ...) {
 
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
                  saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
-                 std::vector<saber_region>* all = nullptr, std::vector<uint4>* rstats = nullptr);
+                 RegionSink* sink = nullptr);
 
 static inline unsigned nblocks(uint64_t n, unsigned t, unsigned cap = 65535u * 16u) {
     uint64_t b = (n + t - 1) / t;

@@ -1087,12 +1087,13 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
     (h)->err.clear()
 
 namespace saber {
-// Every region of the scan into a host vector, for the host engine (engine.cpp).
-int scan_regions_all(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                     std::vector<saber_region>& out, std::vector<uint4>& rstat, saber_scan_stats* st) {
+// The batch's candidate regions for the host engine (engine.cpp): capped per
+// query and triaged on the device, kept ones in pinned memory (sink).
+int scan_search_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
+                        RegionSink& sink, saber_scan_stats* st) {
     ENTER(h);
     uint64_t n = 0;
-    return scan_regions(h, p, q_mask, region_thr, nullptr, 0, &n, st, &out, &rstat);
+    return scan_regions(h, p, q_mask, region_thr, nullptr, 0, &n, st, &sink);
 }
 
 int triage_grads(saber_gpu* h, const float* model, const float* X, const uint8_t* y, uint32_t n, float pos_weight,
@@ -1101,48 +1102,7 @@ int triage_train(saber_gpu* h, float* model, const float* X, const uint8_t* y, u
                  const saber_triage_train_cfg* cfg, saber_triage_train_stats* st);
 int triage_predict_host(saber_gpu* h, const float* model, const float* X, uint64_t n, float* logits);
 int triage_predict(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* d_X, uint64_t n, float* d_logit);
-int triage_region_features(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
-                           const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
-                           const std::vector<float4>& qinfo, float lambda, float logk);
 int triage_upload_model(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* host_model);
-
-// Triage of the batch's candidate regions for the host engine (engine.cpp):
-// keep[i] = 0 drops region i.  Without a model and without collection it
-// does nothing (the plain path); with collection it keeps the feature rows
-// (and logits) on the handle for saber_gpu_collected_regions.
-int triage_regions(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
-                   const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
-                   const std::vector<float4>& qinfo, float lambda, float logk, std::vector<uint8_t>& keep,
-                   bool* active) {
-    ENTER(h);
-    keep.assign(regs.size(), 1);
-    *active = h->tr_on || h->tr_collect;
-    if (!*active) return SABER_OK;
-    int rc = triage_region_features(h, regs, rstat, rquery, rrank, qinfo, lambda, logk);
-    if (rc != SABER_OK) return rc;
-    const uint64_t n = regs.size();
-    cudaStream_t s = h->stream;
-    if (h->tr_on) {
-        rc = triage_predict(h, h->tr_model, h->tr_wb, h->tr_X.as<float>(), n, h->tr_logit.as<float>());
-        if (rc != SABER_OK) return rc;
-    }
-    std::vector<float> logits(h->tr_on ? n : 0);
-    if (h->tr_on && n) CU(h, cudaMemcpyAsync(logits.data(), h->tr_logit.p, n * 4, cudaMemcpyDeviceToHost, s));
-    if (h->tr_collect) {
-        h->tr_rows.resize(n * SABER_TRIAGE_ROW_FLOATS);
-        if (n) CU(h, cudaMemcpyAsync(h->tr_rows.data(), h->tr_X.p, n * SABER_TRIAGE_ROW_FLOATS * 4,
-                                     cudaMemcpyDeviceToHost, s));
-    }
-    CU(h, cudaStreamSynchronize(s));
-    if (h->tr_on)
-        for (uint64_t i = 0; i < n; i++) keep[i] = logits[i] >= h->tr_threshold;
-    if (h->tr_collect) {
-        h->tr_logits = logits;
-        h->tr_logits.resize(n, 0.f);
-        h->tr_labels.assign(n, 0);
-    }
-    return SABER_OK;
-}
 
 // Labels of the collected regions (1 = produced a reported hit).
 void triage_set_labels(saber_gpu* h, const std::vector<uint64_t>& hit_regions) {

@@ -957,9 +957,181 @@ static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+// ---- the batch engine's regions: per-query cap and triage on the device ------
+int triage_region_features(saber_gpu* h, const saber_region* d_reg, const uint4* d_rstat, const uint32_t* d_rq,
+                           const uint32_t* d_rrank, const float4* d_qinfo, uint64_t n, float lambda, float logk);
+int triage_predict(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* d_X, uint64_t n, float* d_logit);
+
+__global__ void k_query_count(const saber_region* __restrict__ reg, uint32_t n, uint32_t* __restrict__ qcnt) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&qcnt[reg[i].query], 1u);
+}
+
+// rank of each region within its query (regions are grouped by query) and
+// whether it is within the query's first `cap`
+__global__ void k_cap_flags(const saber_region* __restrict__ reg, uint32_t n, const uint32_t* __restrict__ qstart,
+                            uint32_t cap, uint32_t* __restrict__ rank, uint8_t* __restrict__ flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i - qstart[reg[i].query];
+        rank[i] = r;
+        flag[i] = r < cap;
+    }
+}
+
+__global__ void k_gather_capped(const saber_region* __restrict__ reg, const uint4* __restrict__ rst,
+                                const uint32_t* __restrict__ rank, const uint32_t* __restrict__ idx, uint32_t n,
+                                saber_region* __restrict__ oreg, uint4* __restrict__ orst, uint32_t* __restrict__ orq,
+                                uint32_t* __restrict__ orank) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = idx[i];
+        const saber_region r = reg[k];
+        oreg[i] = r;
+        orst[i] = rst[k];
+        orq[i] = r.query;
+        orank[i] = rank[k];
+    }
+}
+
+// per query: (length, region threshold, best of its first region, regions after the cap)
+__global__ void k_query_info(const uint64_t* __restrict__ qoffs, const int32_t* __restrict__ rthr, int32_t thr0,
+                             const uint32_t* __restrict__ qcnt, const uint32_t* __restrict__ qstart,
+                             const saber_region* __restrict__ reg, uint32_t cap, uint32_t nq,
+                             float4* __restrict__ qinfo) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const uint32_t c = qcnt[q];
+        qinfo[q] = make_float4((float)(int64_t)(qoffs[q + 1] - qoffs[q]), (float)(rthr ? rthr[q] : thr0),
+                               c ? (float)reg[qstart[q]].best : 0.f, (float)(c < cap ? c : cap));
+    }
+}
+
+__global__ void k_keep_flags(const float* __restrict__ logit, uint32_t n, float thr, uint8_t* __restrict__ flag) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flag[i] = logit[i] >= thr;
+}
+
+__global__ void k_iota(uint32_t* __restrict__ v, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
+// Caps the sorted regions (sc_regions2 / sc_rstat2) at max_candidates per
+// query, runs the learned triage on them when a model is installed (or
+// collects their feature rows), and copies the kept regions with their
+// positions in the capped list to pinned host memory.
+static int region_sink(saber_gpu* h, const saber_scan_params* p, bool has_thr, uint64_t nregions, RegionSink& sk) {
+    const QuerySet& qs = h->main.qs;
+    cudaStream_t s = h->stream;
+    const uint32_t nq = qs.nq;
+    const uint32_t cap = std::max<uint32_t>(1, p->max_candidates);
+    sk.n = sk.ncap = 0;
+    sk.triaged = false;
+    sk.collecting = h->tr_collect;
+    if (h->tr_collect) {
+        h->tr_rows.clear();
+        h->tr_logits.clear();
+        h->tr_labels.clear();
+    }
+    if (!nregions) return SABER_OK;
+    const uint32_t n = (uint32_t)nregions;
+    const saber_region* reg = h->sc_regions2.as<saber_region>();
+    const uint4* rst = h->sc_rstat2.as<uint4>();
+    CUALLOC(h, h->rg_qcnt, ((uint64_t)nq + 1) * 4);
+    CUALLOC(h, h->rg_qstart, ((uint64_t)nq + 1) * 4);
+    CUALLOC(h, h->rg_rank, (uint64_t)n * 4);
+    CUALLOC(h, h->rg_flag, (uint64_t)n + 8);
+    CUALLOC(h, h->rg_idx, (uint64_t)n * 4 + 8);
+    CUALLOC(h, h->rg_idx2, (uint64_t)n * 4 + 8);
+    uint32_t* qcnt = h->rg_qcnt.as<uint32_t>();
+    uint32_t* qstart = h->rg_qstart.as<uint32_t>();
+    uint32_t* nsel = h->sc_ctr.as<uint32_t>() + 44;
+    CU(h, cudaMemsetAsync(qcnt, 0, ((uint64_t)nq + 1) * 4, s));
+    k_query_count<<<nblocks(n, 256), 256, 0, s>>>(reg, n, qcnt);
+    size_t t1 = 0, t2 = 0;
+    CU(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, qcnt, qstart, (int)nq + 1, s));
+    CU(h, cub::DeviceSelect::Flagged(nullptr, t2, thrust::counting_iterator<uint32_t>(0), h->rg_flag.as<uint8_t>(),
+                                     h->rg_idx.as<uint32_t>(), nsel, (int)n, s));
+    CUALLOC(h, h->cub_tmp, std::max(t1, t2));
+    size_t tb = h->cub_tmp.cap;
+    CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, qcnt, qstart, (int)nq + 1, s));
+    k_cap_flags<<<nblocks(n, 256), 256, 0, s>>>(reg, n, qstart, cap, h->rg_rank.as<uint32_t>(), h->rg_flag.as<uint8_t>());
+    tb = h->cub_tmp.cap;
+    CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), h->rg_flag.as<uint8_t>(),
+                                     h->rg_idx.as<uint32_t>(), nsel, (int)n, s));
+    uint32_t ncap = 0;
+    CU(h, cudaMemcpyAsync(&ncap, nsel, 4, cudaMemcpyDeviceToHost, s));
+    CU(h, cudaStreamSynchronize(s));
+    sk.ncap = ncap;
+    if (!ncap) return SABER_OK;
+    CUALLOC(h, h->tr_reg, (uint64_t)ncap * sizeof(saber_region));
+    CUALLOC(h, h->tr_rstat, (uint64_t)ncap * sizeof(uint4));
+    CUALLOC(h, h->tr_rq, (uint64_t)ncap * 4);
+    CUALLOC(h, h->tr_rrank, (uint64_t)ncap * 4);
+    k_gather_capped<<<nblocks(ncap, 256), 256, 0, s>>>(reg, rst, h->rg_rank.as<uint32_t>(), h->rg_idx.as<uint32_t>(),
+                                                       ncap, h->tr_reg.as<saber_region>(), h->tr_rstat.as<uint4>(),
+                                                       h->tr_rq.as<uint32_t>(), h->tr_rrank.as<uint32_t>());
+    CU(h, cudaGetLastError());
+    const saber_region* oreg = h->tr_reg.as<saber_region>();
+    uint32_t nout = ncap;
+    uint32_t* osrc = h->rg_idx2.as<uint32_t>();
+    bool have_src = false;
+    if (h->tr_on || h->tr_collect) {
+        CUALLOC(h, h->tr_qinfo, std::max<uint64_t>(nq, 1) * sizeof(float4));
+        if (nq)
+            k_query_info<<<nblocks(nq, 256), 256, 0, s>>>(qs.offsets.as<uint64_t>(),
+                                                          has_thr ? h->sc_rthr.as<int32_t>() : nullptr,
+                                                          (int32_t)p->hsp_threshold, qcnt, qstart, reg, cap, nq,
+                                                          h->tr_qinfo.as<float4>());
+        int rc = triage_region_features(h, h->tr_reg.as<saber_region>(), h->tr_rstat.as<uint4>(),
+                                        h->tr_rq.as<uint32_t>(), h->tr_rrank.as<uint32_t>(), h->tr_qinfo.as<float4>(),
+                                        ncap, sk.lambda, sk.logk);
+        if (rc != SABER_OK) return rc;
+        if (h->tr_on) {
+            rc = triage_predict(h, h->tr_model, h->tr_wb, h->tr_X.as<float>(), ncap, h->tr_logit.as<float>());
+            if (rc != SABER_OK) return rc;
+        }
+        if (h->tr_collect) {
+            h->tr_rows.resize((uint64_t)ncap * SABER_TRIAGE_ROW_FLOATS);
+            CU(h, cudaMemcpyAsync(h->tr_rows.data(), h->tr_X.p, (uint64_t)ncap * SABER_TRIAGE_ROW_FLOATS * 4,
+                                  cudaMemcpyDeviceToHost, s));
+            h->tr_logits.assign(ncap, 0.f);
+            if (h->tr_on)
+                CU(h, cudaMemcpyAsync(h->tr_logits.data(), h->tr_logit.p, (uint64_t)ncap * 4, cudaMemcpyDeviceToHost,
+                                      s));
+            h->tr_labels.assign(ncap, 0);
+        }
+        if (h->tr_on) {
+            k_keep_flags<<<nblocks(ncap, 256), 256, 0, s>>>(h->tr_logit.as<float>(), ncap, h->tr_threshold,
+                                                           h->rg_flag.as<uint8_t>());
+            tb = h->cub_tmp.cap;
+            CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
+                                             h->rg_flag.as<uint8_t>(), osrc, nsel, (int)ncap, s));
+            CU(h, cudaMemcpyAsync(&nout, nsel, 4, cudaMemcpyDeviceToHost, s));
+            CU(h, cudaStreamSynchronize(s));
+            CUALLOC(h, h->rg_out, (uint64_t)std::max<uint32_t>(nout, 1) * sizeof(saber_region));
+            if (nout)
+                k_gather_regions<<<nblocks(nout, 256), 256, 0, s>>>(h->tr_reg.as<saber_region>(), osrc, nout,
+                                                                   h->rg_out.as<saber_region>());
+            oreg = h->rg_out.as<saber_region>();
+            have_src = true;
+            sk.triaged = true;
+        }
+    }
+    if (!have_src) k_iota<<<nblocks(nout, 256), 256, 0, s>>>(osrc, nout);
+    CU(h, cudaGetLastError());
+    CUALLOC(h, h->pin_reg, (uint64_t)std::max<uint32_t>(nout, 1) * sizeof(saber_region));
+    CUALLOC(h, h->pin_src, (uint64_t)std::max<uint32_t>(nout, 1) * 4);
+    if (nout) {
+        CU(h, cudaMemcpyAsync(h->pin_reg.p, oreg, (uint64_t)nout * sizeof(saber_region), cudaMemcpyDeviceToHost, s));
+        CU(h, cudaMemcpyAsync(h->pin_src.p, osrc, (uint64_t)nout * 4, cudaMemcpyDeviceToHost, s));
+    }
+    CU(h, cudaStreamSynchronize(s));
+    sk.regs = h->pin_reg.as<saber_region>();
+    sk.src = h->pin_src.as<uint32_t>();
+    sk.n = nout;
+    return SABER_OK;
+}
+
 int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
-                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st,
-                 std::vector<saber_region>* all, std::vector<uint4>* rstats) {
+                 saber_region* out, uint64_t out_cap, uint64_t* n_out, saber_scan_stats* st, RegionSink* sink) {
     const Dataset& ds = h->main;
     const QuerySet& qs = ds.qs;
     if (!ds.has_db || !qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
@@ -1158,7 +1330,6 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     CU(h, cudaEventRecord(ev[2], s));
     uint64_t nregions = 0;
     std::vector<saber_region> regs;
-    std::vector<uint4> rstat_all;
     if (ns) {
         CUALLOC(h, h->sc_key1, (uint64_t)ns * 8);
         CUALLOC(h, h->sc_key1o, (uint64_t)ns * 8);
@@ -1286,7 +1457,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             CU(h, cudaMemcpyAsync(&nr, ctr + 12, 8, cudaMemcpyDeviceToHost, s));
             CU(h, cudaStreamSynchronize(s));
             nregions = std::min<uint64_t>(nr, rcap);
-            regs.resize(nregions);
+            if (!sink) regs.resize(nregions);
             if (nregions) {
                 // region_order on the device: stable passes by (d_min, d_max), subject, (query, best desc)
                 const uint32_t nrg = (uint32_t)nregions;
@@ -1321,14 +1492,12 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                 CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, rb, k64o, klo, ia, ib, (int)nrg, 0, 64, s));
                 k_gather_regions<<<nblocks(nrg, 256), 256, 0, s>>>(h->sc_regions.as<saber_region>(), ib, nrg,
                                                                    h->sc_regions2.as<saber_region>());
-                CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions2.p, nregions * sizeof(saber_region),
-                                      cudaMemcpyDeviceToHost, s));
-                if (rstats) {
+                if (sink) {
                     CUALLOC(h, h->sc_rstat2, (uint64_t)nrg * sizeof(uint4));
                     k_gather_uint4<<<nblocks(nrg, 256), 256, 0, s>>>(h->sc_rstat.as<uint4>(), ib, nrg,
                                                                      h->sc_rstat2.as<uint4>());
-                    rstat_all.resize(nregions);
-                    CU(h, cudaMemcpyAsync(rstat_all.data(), h->sc_rstat2.p, nregions * sizeof(uint4),
+                } else {
+                    CU(h, cudaMemcpyAsync(regs.data(), h->sc_regions2.p, nregions * sizeof(saber_region),
                                           cudaMemcpyDeviceToHost, s));
                 }
             }
@@ -1348,23 +1517,26 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     // per query in region_order (sorted on the device above), cap at max_candidates
     const uint64_t cap = std::max<uint32_t>(1, p->max_candidates);
     uint64_t w = 0;
-    size_t i = 0;
     bool overflow = false;
-    if (all) all->clear();
-    if (rstats) rstats->clear();
-    while (i < regs.size()) {
-        size_t j = i;
-        while (j < regs.size() && regs[j].query == regs[i].query) j++;
-        const uint64_t take = std::min<uint64_t>(j - i, cap);
-        local.regions_dropped_by_cap += (j - i) - take;
-        for (uint64_t k = 0; k < take; k++) {
-            if (all) all->push_back(regs[i + k]);
-            if (rstats) rstats->push_back(rstat_all.empty() ? make_uint4(0, 0, 0, 0) : rstat_all[i + k]);
-            else if (w < out_cap) out[w] = regs[i + k];
-            else overflow = true;
-            w++;
+    if (sink) {
+        int rc = region_sink(h, p, region_thr != nullptr, nregions, *sink);
+        if (rc != SABER_OK) return rc;
+        w = sink->ncap;
+        local.regions_dropped_by_cap = nregions - sink->ncap;
+    } else {
+        size_t i = 0;
+        while (i < regs.size()) {
+            size_t j = i;
+            while (j < regs.size() && regs[j].query == regs[i].query) j++;
+            const uint64_t take = std::min<uint64_t>(j - i, cap);
+            local.regions_dropped_by_cap += (j - i) - take;
+            for (uint64_t k = 0; k < take; k++) {
+                if (w < out_cap) out[w] = regs[i + k];
+                else overflow = true;
+                w++;
+            }
+            i = j;
         }
-        i = j;
     }
     local.regions = w;
     local.t_tables_ms = ev_ms(ev[0], ev[1]);

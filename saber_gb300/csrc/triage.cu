@@ -539,13 +539,11 @@ int triage_predict_host(saber_gpu* h, const float* model, const float* X, uint64
 // Region features for the engine: uploads the batch's regions and computes
 // the feature rows on the device (kept in h->tr_X); sequence features of the
 // database are computed once per loaded database.
-int triage_region_features(saber_gpu* h, const std::vector<saber_region>& regs, const std::vector<uint4>& rstat,
-                           const std::vector<uint32_t>& rquery, const std::vector<uint32_t>& rrank,
-                           const std::vector<float4>& qinfo, float lambda, float logk) {
+int triage_region_features(saber_gpu* h, const saber_region* d_reg, const uint4* d_rstat, const uint32_t* d_rq,
+                           const uint32_t* d_rrank, const float4* d_qinfo, uint64_t n, float lambda, float logk) {
     const Dataset& ds = h->main;
     const QuerySet& qs = ds.qs;
     cudaStream_t s = h->stream;
-    const uint64_t n = regs.size();
     if (!h->tr_sfeat_ok || h->tr_sfeat_key != (uint64_t)(uintptr_t)ds.res.p + ds.n_res) {
         CUALLOC(h, h->tr_sfeat, std::max<uint64_t>(ds.nsub, 1) * sizeof(float4));
         if (ds.nsub)
@@ -560,27 +558,14 @@ int triage_region_features(saber_gpu* h, const std::vector<saber_region>& regs, 
         k_seq_feats<<<(unsigned)std::min<uint64_t>((qs.nq + 7) / 8, 65535u * 8), 256, 0, s>>>(
             qs.codes.as<uint8_t>(), qs.offsets.as<uint64_t>(), qs.nq, h->tr_qfeat.as<float4>());
     const uint64_t nn = std::max<uint64_t>(n, 1);
-    CUALLOC(h, h->tr_reg, nn * sizeof(saber_region));
-    CUALLOC(h, h->tr_rstat, nn * sizeof(uint4));
-    CUALLOC(h, h->tr_rq, nn * 4);
-    CUALLOC(h, h->tr_rrank, nn * 4);
-    CUALLOC(h, h->tr_qinfo, std::max<uint64_t>(qinfo.size(), 1) * sizeof(float4));
     CUALLOC(h, h->tr_X, nn * kTIn * 4);
     CUALLOC(h, h->tr_logit, nn * 4);
-    if (n) {
-        CU(h, cudaMemcpyAsync(h->tr_reg.p, regs.data(), n * sizeof(saber_region), cudaMemcpyHostToDevice, s));
-        CU(h, cudaMemcpyAsync(h->tr_rstat.p, rstat.data(), n * sizeof(uint4), cudaMemcpyHostToDevice, s));
-        CU(h, cudaMemcpyAsync(h->tr_rq.p, rquery.data(), n * 4, cudaMemcpyHostToDevice, s));
-        CU(h, cudaMemcpyAsync(h->tr_rrank.p, rrank.data(), n * 4, cudaMemcpyHostToDevice, s));
-    }
-    if (!qinfo.empty())
-        CU(h, cudaMemcpyAsync(h->tr_qinfo.p, qinfo.data(), qinfo.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
     RegionFeatArgs a;
-    a.reg = h->tr_reg.as<saber_region>();
-    a.rstat = h->tr_rstat.as<uint4>();
-    a.rquery = h->tr_rq.as<uint32_t>();
-    a.rrank = h->tr_rrank.as<uint32_t>();
-    a.qinfo = h->tr_qinfo.as<float4>();
+    a.reg = d_reg;
+    a.rstat = d_rstat;
+    a.rquery = d_rq;
+    a.rrank = d_rrank;
+    a.qinfo = d_qinfo;
     a.qfeat = h->tr_qfeat.as<float4>();
     a.sfeat = h->tr_sfeat.as<float4>();
     a.soffs = ds.soff.as<uint64_t>();

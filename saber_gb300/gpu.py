@@ -105,7 +105,8 @@ class SearchStats(ctypes.Structure):
         (n, ctypes.c_uint64) for n in ("regions", "triage_dropped", "band_scored_regions", "band_rescored",
                                        "banded_cells", "score_launches", "alignments")] + [
         (n, ctypes.c_double) for n in ("t_prep_ms", "t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms",
-                                       "t_finish_ms", "t_total_ms")]
+                                       "t_finish_ms", "t_total_ms", "t_score_calls_ms", "t_score_device_ms",
+                                       "t_finish_tb_ms")]
 
     def as_dict(self):
         d = {}
