@@ -215,7 +215,8 @@ def run_search(a, dev):
 
     plain, tp, cp = timed()
     nq = a.search_queries
-    stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms")
+    stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms",
+              "t_score_calls_ms", "t_score_device_ms", "t_finish_tb_ms")
     out = {
         "workload": "batched search, default preset: %d synthetic queries vs %d subjects (%d residues; 50%% "
                     "background, 25%% planted 30-60%% identity, 25%% reversed), BLOSUM62 11/1, E<=10, -k 10"

@@ -337,6 +337,8 @@ typedef struct {
     double t_score_calls_ms, t_score_device_ms;
     /* inside t_finish_ms: wall clock of the traceback calls */
     double t_finish_tb_ms;
+    /* the scoring calls' device time by part (saber_score_stats) */
+    double t_score_prep_ms, t_score_fast_ms, t_score_generic_ms;
 } saber_search_stats;
 
 /* Hits of every query of the batch, ordered by query, then (E-value, score

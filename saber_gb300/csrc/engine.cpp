@@ -434,6 +434,9 @@ struct Engine {
         if (rc != SABER_OK) return rc;
         st.t_score_calls_ms += now_ms() - t0;
         st.t_score_device_ms += ss.t_prep_ms + ss.t_fast_ms + ss.t_generic_ms;
+        st.t_score_prep_ms += ss.t_prep_ms;
+        st.t_score_fast_ms += ss.t_fast_ms;
+        st.t_score_generic_ms += ss.t_generic_ms;
         st.banded_cells += ss.banded_cells;
         st.score_launches += 1;
         return SABER_OK;
@@ -642,7 +645,10 @@ struct Engine {
         std::unordered_map<uint64_t, Aln> tb;
         std::vector<QState> state(nq);
         for (size_t qi = 0; qi < nq; qi++) state[qi].done = orders[qi].empty();
-        const size_t chunk = std::max<size_t>(4, 2 * (size_t)P.max_target_seqs * P.max_hsps);
+        // speculative tracebacks per query and round: as many candidates as
+        // the report can take (more rounds follow only where candidates
+        // fail, are duplicates or repeat a subject)
+        const size_t chunk = std::max<size_t>(4, (size_t)P.max_target_seqs * P.max_hsps);
         for (;;) {
             std::vector<std::pair<uint32_t, uint32_t>> need;
             for (uint32_t qi = 0; qi < nq; qi++) {

@@ -267,72 +267,137 @@ __global__ void k_adam(float* __restrict__ w, const float* __restrict__ g, float
     }
 }
 
-// ---- fused inference: one block of 256 threads per 32 regions ------------------
-// layer 1 into shared memory, layer 2 streamed against W2 with the output
-// layer folded in (each hidden unit's ReLU times W3 summed per region); the
-// arithmetic is that of the training forward pass (fp32 activations)
-constexpr int kInferRows = 32;
-__global__ void __launch_bounds__(256) k_mlp_infer(const float* __restrict__ X, uint64_t n,
-                                                   const float* __restrict__ model,
+// ---- fused inference on the tensor cores -------------------------------------
+// One warp per 16 regions, mma.sync m16n8k16 (bf16 operands, fp32
+// accumulation).  The weights are bf16 already; the activations (the
+// normalised inputs and the layer-1 outputs) are fp32 and enter as a
+// bf16 pair hi + lo (lo = the rounding residual), two products per tile, so
+// the result matches the fp32-activation forward pass of training to about
+// 2^-16 relative.  Layer 1 runs in chunks of 16 hidden units whose
+// accumulator tiles are, register for register, the A operand of layer 2;
+// layer 3 (256 -> 1) is a quad reduction of the layer-2 accumulators.
+constexpr size_t kPackOff = ((kModelFloats * 2 + 255) / 256) * 256;        // bytes into the bf16 buffer
+constexpr size_t kPackBytes = (size_t)(2 + 16) * 32 * 32 * sizeof(uint2);  // W1 and W2 fragments
+
+// B fragments of a row-major [K][256] bf16 weight, K = 16 kt: for tile (kt,
+// nt) and lane l, {W[k][n], W[k + 1][n]} and {W[k + 8][n], W[k + 9][n]} with
+// k = 16 kt + 2 (l % 4), n = 8 nt + l / 4.
+__global__ void k_pack_b(const __nv_bfloat16* __restrict__ W, int kt_n, uint2* __restrict__ out) {
+    const int total = kt_n * 32 * 32;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int lane = t & 31, nt = (t >> 5) & 31, kt = t >> 10;
+        const int k = kt * 16 + 2 * (lane & 3), n = nt * 8 + (lane >> 2);
+        auto u = [&](int kk) { return (uint32_t)__bfloat16_as_ushort(W[(size_t)kk * kTHid + n]); };
+        out[t] = make_uint2(u(k) | (u(k + 1) << 16), u(k + 8) | (u(k + 9) << 16));
+    }
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint2 b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
+}
+
+// (x, y) -> packed bf16 pairs hi and lo with x ~ hi.x + lo.x, y ~ hi.y + lo.y
+__device__ __forceinline__ void split2(float x, float y, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x, y);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x - __bfloat162float(h.x), y - __bfloat162float(h.y));
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_infer(const float* __restrict__ X, uint64_t n,
+                                                   const float* __restrict__ model, const uint2* __restrict__ pk,
                                                    const __nv_bfloat16* __restrict__ wb, float* __restrict__ logit) {
-    __shared__ float xs[kInferRows][kTIn + 1];
-    __shared__ float h1[kInferRows][kTHid + 4];
-    __shared__ float part[kInferRows][17];
-    const uint64_t r0 = (uint64_t)blockIdx.x * kInferRows;
-    const int t = threadIdx.x;
-    for (int e = t; e < kInferRows * kTIn; e += 256) {
-        const int r = e / kTIn, k = e % kTIn;
-        const uint64_t gr = r0 + r;
-        xs[r][k] = (gr < n && k < kTFeat) ? (X[gr * kTIn + k] - model[kOffMu + k]) * model[kOffIsd + k] : 0.f;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t r0 = warp * 16;
+    if (r0 >= n) return;
+    const int qr = lane >> 2, qc = 2 * (lane & 3);
+    const uint64_t ra = r0 + qr, rb = r0 + qr + 8;
+    // layer-1 A operand: normalised inputs, 2 k-steps of 16, hi and lo
+    uint32_t xa[2][4], xl[2][4];
+#pragma unroll
+    for (int ks = 0; ks < 2; ks++) {
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {  // k and k + 8
+            const int k = ks * 16 + hf * 8 + qc;
+            float v[2][2];
+#pragma unroll
+            for (int rr = 0; rr < 2; rr++) {
+                const uint64_t r = rr ? rb : ra;
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int kk = k + e;
+                    v[rr][e] = (r < n && kk < kTFeat) ? (X[r * kTIn + kk] - model[kOffMu + kk]) * model[kOffIsd + kk]
+                                                      : 0.f;
+                }
+            }
+            split2(v[0][0], v[0][1], xa[ks][hf * 2 + 0], xl[ks][hf * 2 + 0]);
+            split2(v[1][0], v[1][1], xa[ks][hf * 2 + 1], xl[ks][hf * 2 + 1]);
+        }
     }
-    __syncthreads();
-    const __nv_bfloat16* W1 = wb + kOffW1;
-    const __nv_bfloat16* W2 = wb + kOffW2;
+    const uint2* P1 = pk;
+    const uint2* P2 = pk + 2 * 32 * 32;
+    float acc[32][4];
+#pragma unroll
+    for (int nt = 0; nt < 32; nt++) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll 1
+    for (int ch = 0; ch < 16; ch++) {
+        // layer 1, hidden units 16 ch .. 16 ch + 15 (n-tiles 2 ch, 2 ch + 1)
+        float h[2][4];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            h[j][0] = h[j][1] = h[j][2] = h[j][3] = 0.f;
+            const int nt = 2 * ch + j;
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++) {
+                const uint2 b = P1[(ks * 32 + nt) * 32 + lane];
+                mma_bf16(h[j], xa[ks][0], xa[ks][1], xa[ks][2], xa[ks][3], b);
+                mma_bf16(h[j], xl[ks][0], xl[ks][1], xl[ks][2], xl[ks][3], b);
+            }
+            const float b0 = model[kOffB1 + nt * 8 + qc], b1 = model[kOffB1 + nt * 8 + qc + 1];
+            h[j][0] = fmaxf(h[j][0] + b0, 0.f);
+            h[j][1] = fmaxf(h[j][1] + b1, 0.f);
+            h[j][2] = fmaxf(h[j][2] + b0, 0.f);
+            h[j][3] = fmaxf(h[j][3] + b1, 0.f);
+        }
+        // the two accumulator tiles are the layer-2 A operand of k-step ch
+        uint32_t ah[4], al[4];
+        split2(h[0][0], h[0][1], ah[0], al[0]);
+        split2(h[0][2], h[0][3], ah[1], al[1]);
+        split2(h[1][0], h[1][1], ah[2], al[2]);
+        split2(h[1][2], h[1][3], ah[3], al[3]);
+#pragma unroll
+        for (int nt = 0; nt < 32; nt++) {
+            const uint2 b = P2[(ch * 32 + nt) * 32 + lane];
+            mma_bf16(acc[nt], ah[0], ah[1], ah[2], ah[3], b);
+            mma_bf16(acc[nt], al[0], al[1], al[2], al[3], b);
+        }
+    }
+    // layer 3
     const __nv_bfloat16* W3 = wb + kOffW3;
-    {
-        float w1[kTFeat];
+    float sa = 0.f, sb = 0.f;
 #pragma unroll
-        for (int k = 0; k < kTFeat; k++) w1[k] = __bfloat162float(W1[k * kTHid + t]);
-        const float b = model[kOffB1 + t];
-        for (int r = 0; r < kInferRows; r++) {
-            float a = 0.f;
-#pragma unroll
-            for (int k = 0; k < kTFeat; k++) a = fmaf(xs[r][k], w1[k], a);
-            h1[r][t] = fmaxf(a + b, 0.f);
-        }
+    for (int nt = 0; nt < 32; nt++) {
+        const int c = nt * 8 + qc;
+        const float b0 = model[kOffB2 + c], b1 = model[kOffB2 + c + 1];
+        const float w0 = __bfloat162float(W3[c]), w1 = __bfloat162float(W3[c + 1]);
+        sa = fmaf(fmaxf(acc[nt][0] + b0, 0.f), w0, sa);
+        sa = fmaf(fmaxf(acc[nt][1] + b1, 0.f), w1, sa);
+        sb = fmaf(fmaxf(acc[nt][2] + b0, 0.f), w0, sb);
+        sb = fmaf(fmaxf(acc[nt][3] + b1, 0.f), w1, sb);
     }
-    __syncthreads();
-    const int rg = t >> 4, cg = t & 15;
-    float acc[2][16];
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 16; j++) acc[i][j] = 0.f;
-    for (int k = 0; k < kTHid; k++) {
-        float w[16];
-        const __nv_bfloat16* wr = W2 + (long)k * kTHid + cg * 16;
-#pragma unroll
-        for (int j = 0; j < 16; j++) w[j] = __bfloat162float(wr[j]);
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const float a = h1[rg * 2 + i][k];
-#pragma unroll
-            for (int j = 0; j < 16; j++) acc[i][j] = fmaf(a, w[j], acc[i][j]);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 2; i++) {
-        float s = 0.f;
-#pragma unroll
-        for (int j = 0; j < 16; j++)
-            s = fmaf(fmaxf(acc[i][j] + model[kOffB2 + cg * 16 + j], 0.f), __bfloat162float(W3[cg * 16 + j]), s);
-        part[rg * 2 + i][cg] = s;
-    }
-    __syncthreads();
-    if (t < kInferRows) {
-        float s = 0.f;
-        for (int j = 0; j < 16; j++) s += part[t][j];
-        if (r0 + t < n) logit[r0 + t] = s + model[kOffB3];
+    sa += __shfl_xor_sync(0xffffffffu, sa, 1);
+    sa += __shfl_xor_sync(0xffffffffu, sa, 2);
+    sb += __shfl_xor_sync(0xffffffffu, sb, 1);
+    sb += __shfl_xor_sync(0xffffffffu, sb, 2);
+    if ((lane & 3) == 0) {
+        if (ra < n) logit[ra] = sa + model[kOffB3];
+        if (rb < n) logit[rb] = sb + model[kOffB3];
     }
 }
 
@@ -357,10 +422,15 @@ static int upload_model(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* ho
 
 int triage_upload_model(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* host_model) {
     CUALLOC(h, model, kModelFloats * 4);
-    CUALLOC(h, wb, kModelFloats * 2);
+    CUALLOC(h, wb, kPackOff + kPackBytes);
     CU(h, cudaMemcpyAsync(model.p, host_model, kModelFloats * 4, cudaMemcpyHostToDevice, h->stream));
     k_to_bf16<<<nblocks(kModelFloats, 256), 256, 0, h->stream>>>(model.as<float>(), kModelFloats,
                                                                  wb.as<__nv_bfloat16>());
+    // tensor-core fragments of W1 (2 x 32 tiles) and W2 (16 x 32 tiles)
+    const __nv_bfloat16* w = wb.as<__nv_bfloat16>();
+    uint2* pk = reinterpret_cast<uint2*>(wb.as<uint8_t>() + kPackOff);
+    k_pack_b<<<nblocks(2 * 32 * 32, 256), 256, 0, h->stream>>>(w + kOffW1, 2, pk);
+    k_pack_b<<<nblocks(16 * 32 * 32, 256), 256, 0, h->stream>>>(w + kOffW2, 16, pk + 2 * 32 * 32);
     CU(h, cudaGetLastError());
     return SABER_OK;
 }
@@ -516,8 +586,10 @@ int triage_train(saber_gpu* h, float* model, const float* X, const uint8_t* y, u
 // logits of n feature rows with the installed model or the given one
 int triage_predict(saber_gpu* h, DevBuf& model, DevBuf& wb, const float* d_X, uint64_t n, float* d_logit) {
     if (n == 0) return SABER_OK;
-    k_mlp_infer<<<(unsigned)((n + kInferRows - 1) / kInferRows), 256, 0, h->stream>>>(
-        d_X, n, model.as<float>(), wb.as<__nv_bfloat16>(), d_logit);
+    const uint64_t warps = (n + 15) / 16;
+    k_mlp_infer<<<(unsigned)((warps + 3) / 4), 128, 0, h->stream>>>(
+        d_X, n, model.as<float>(), reinterpret_cast<const uint2*>(wb.as<uint8_t>() + kPackOff),
+        wb.as<__nv_bfloat16>(), d_logit);
     CU(h, cudaGetLastError());
     return SABER_OK;
 }
