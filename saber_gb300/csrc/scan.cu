@@ -612,7 +612,7 @@ struct ChainArgs {
 // read one query's profile).
 constexpr int kXBlock = 8;
 
-__global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
+__global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
     const int lane = threadIdx.x & 31;
     const uint32_t nch = *a.nchains;
     unsigned long long ext = 0, avoided = 0, steps = 0;
@@ -620,11 +620,14 @@ __global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
     bool retired = false;
     int phase = 0;          // 0: next survivor, 1: rightwards, 2: leftwards
     unsigned long long hkey = 0;
-    int64_t q0 = 0, s0 = 0, qlen = 0, sl = 0, cover = 0;
+    // positions fit 32 bits: queries and subjects are shorter than 2^19,
+    // residue offsets below 2^32
+    uint32_t q0 = 0;
+    int qlen = 0, sl = 0, cover = 0;
     const int16_t* P = nullptr;
     int mpad = 0;
     const uint8_t* subj = nullptr;
-    int64_t qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
+    int qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
     int cur = 0, best = 0, best_r = 0;
     const uint32_t m27 = (1u << 27) - 1u;
     while (true) {
@@ -645,10 +648,10 @@ __global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
                     const unsigned long long key = a.key1s[i];
                     const uint64_t q = key >> 44, s = (key >> 20) & 0xFFFFFF;
                     hkey = (s << 40) | (q << 20) | (key & 0xFFFFF);  // subject-major HSP key
-                    q0 = (int64_t)a.qoffs[q];
-                    s0 = (int64_t)a.soffs[s];
-                    qlen = (int64_t)a.qoffs[q + 1] - q0;
-                    sl = (int64_t)a.soffs[s + 1] - s0;
+                    q0 = (uint32_t)a.qoffs[q];
+                    const uint64_t s0 = a.soffs[s];
+                    qlen = (int)(a.qoffs[q + 1] - q0);
+                    sl = (int)(a.soffs[s + 1] - s0);
                     P = a.prof + a.prof_off[q];
                     mpad = (int)a.prof_mpad[q];
                     subj = a.res + s0;
@@ -662,27 +665,27 @@ __global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
         if (!retired) {
             if (phase == 0) {
                 const uint2 v = a.surv[a.order[i]];
-                qp = (int64_t)(v.y & m27) - q0;
-                sp = (int64_t)v.x - s0;
+                qp = (int)((v.y & m27) - q0);
+                sp = (int)(v.x - (uint32_t)(subj - a.res));
                 n = qlen - qp < sl - sp ? qlen - qp : sl - sp;
                 t = 0;
                 cur = best = 0;
                 xe = 0;
                 phase = 1;
             }
-            const int64_t dir = phase == 1 ? 1 : -1, off = phase == 1 ? 0 : 1;
+            const int dir = phase == 1 ? 1 : -1, off = phase == 1 ? 0 : 1;
             int sv[kXBlock];
 #pragma unroll
             for (int u = 0; u < kXBlock; u++) {
-                const int64_t tt = t + u;
-                const int64_t d = dir * (tt + off);
+                const int tt = t + u;
+                const int d = dir * (tt + off);
                 sv[u] = tt < n ? (int)P[(size_t)subj[sp + d] * mpad + qp + d] : 0;
             }
             bool stop = false;
-            int64_t done = 0;
+            int done = 0;
 #pragma unroll
             for (int u = 0; u < kXBlock; u++) {
-                const int64_t tt = t + u;
+                const int tt = t + u;
                 if (!stop && tt < n) {
                     cur += sv[u];
                     if (cur > best) {
@@ -709,13 +712,13 @@ __global__ void __launch_bounds__(256) k_chains(ChainArgs a) {
                 } else {
                     steps += (uint64_t)(done_r + done);
                     ext++;
-                    const int64_t hi = qp + end_r, lo = qp - xe;
+                    const int hi = qp + end_r, lo = qp - xe;
                     cover = hi;
                     const int score = best_r + best;
                     // the chain's next hits below hi are covered (query
                     // positions ascend along the chain); the HSP counts them
                     uint32_t j = i + 1;
-                    while (j < e && (int64_t)(a.surv[a.order[j]].y & m27) - q0 < cover) j++;
+                    while (j < e && (int)((a.surv[a.order[j]].y & m27) - q0) < cover) j++;
                     avoided += j - (i + 1);
                     if (score >= a.thr) {
                         emit = true;
