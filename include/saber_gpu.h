@@ -418,6 +418,14 @@ int32_t saber_gpu_get_strip_rows(saber_gpu* h);
 int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
 
+/* Tuning: a job whose sweep in one lane would take more than `steps` column
+ * steps (strips x (width + strip rows - 1)) is scored by the warp-per-job
+ * int32 kernel instead, so one long job does not set the launch's length;
+ * 0xFFFFFFFF keeps every job on the int16 lanes.  Default 4096.  Results
+ * do not depend on it.  No reference counterpart. */
+int saber_gpu_set_long_steps(saber_gpu* h, uint32_t steps);
+uint32_t saber_gpu_get_long_steps(saber_gpu* h);
+
 /* Tuning: bytes of seed tables (rank-compressed presence groups, entry
  * offsets, batch positions) that one database pass of saber_gpu_scan looks
  * up; the shapes are split into passes of at most this many bytes (at least

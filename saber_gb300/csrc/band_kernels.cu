@@ -581,9 +581,18 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
     }
 }
 
-// int32 kernel, one job per thread: the scalar recurrence of
-// banded.rs:134-224 with H/F rows in a per-thread global slab.  Used for
-// bands narrower than a strip and to rescore int16 results at the limit.
+// int32 banded scoring, one warp per job (banded_score_i32, banded.rs:134-224,
+// the recurrence of the reference's scalar kernel): narrow bands, the jobs
+// whose strip sweep in one lane would be long, and int16 results at the
+// overflow limit.  The warp sweeps the band row by row, 32 band cells per
+// lane step.  Per row i and band cell k (j = i + lo + k): F and the diagonal
+// come from the previous row's H and F (k + 1 and k); H0 = max(diag, F, 0).
+// E along the row is an exclusive max-scan of H0[k'] + k' ge over the row's
+// cells k' < k, minus go + (k - 1) ge: with ge <= go, reopening after a gap
+// run never beats extending it, so E of H0 equals E of H.  H = max(H0, E).
+// The profile column of row i is staged in shared memory.  Row buffers (H and
+// F, previous and current, w + 1 entries with entry w kept at NEG) are per
+// warp in global scratch.
 __global__ void __launch_bounds__(128) k_band_generic(
     const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
@@ -591,83 +600,91 @@ __global__ void __launch_bounds__(128) k_band_generic(
     const uint32_t* __restrict__ list, const uint32_t* __restrict__ list_count, int32_t* __restrict__ slabs,
     uint32_t slab_stride, int go, int ge, int32_t* __restrict__ scores) {
     const int NEG = INT32_MIN / 4;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
+    const int VNEG = INT32_MIN / 2;  // below every scanned value
+    __shared__ int32_t col[4][24];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t n = *list_count;
-    int32_t* hp = slabs + (size_t)tid * slab_stride * 4;
-    int32_t* fp = hp + slab_stride;
-    int32_t* hc = fp + slab_stride;
-    int32_t* fc = hc + slab_stride;
-    for (uint32_t t = tid; t < n; t += nthreads) {
+    int32_t* const base_hp = slabs + (size_t)warp * slab_stride * 4;
+    for (uint32_t t = warp; t < n; t += nwarps) {
         const uint32_t jid = list[t];
         const saber_band_job jj = jobs[jid];
         const uint32_t q = jj.query;
         const int64_t m = (int64_t)(qoffs[q + 1] - qoffs[q]);
         const int64_t nn = jj.win_len;
         int64_t lo = jj.band_lo, hi = jj.band_hi;
-        const int64_t w = clip_band(m, nn, lo, hi);
+        const int w = (int)clip_band(m, nn, lo, hi);
         if (w == 0) {
-            scores[jid] = 0;
+            if (lane == 0) scores[jid] = 0;
             continue;
         }
         const int16_t* qprof = prof + prof_off[q];
         const int64_t mpad = prof_mpad[q];
         const uint8_t* s = res + jj.win_begin;
-        int32_t* a_hp = hp;
-        int32_t* a_fp = fp;
-        int32_t* a_hc = hc;
-        int32_t* a_fc = fc;
-        for (int64_t k = 0; k <= w; k++) {
-            a_hp[k] = NEG;
-            a_fp[k] = NEG;
-            a_hc[k] = NEG;
-            a_fc[k] = NEG;
+        int32_t* hp = base_hp;
+        int32_t* fp = hp + slab_stride;
+        int32_t* hc = fp + slab_stride;
+        int32_t* fc = hc + slab_stride;
+        for (int k = lane; k <= w; k += 32) {
+            hp[k] = NEG;
+            fp[k] = NEG;
+            hc[k] = NEG;
+            fc[k] = NEG;
         }
         int32_t best = 0;
         for (int64_t i = 0; i < m; i++) {
-            int64_t kmin = -(i + lo);
-            if (kmin < 0) kmin = 0;
-            int64_t kmax = nn - 1 - i - lo;
-            if (kmax > w - 1) kmax = w - 1;
-            if (kmin > kmax) {
-                for (int64_t k = 0; k < w; k++) {
-                    a_hc[k] = NEG;
-                    a_fc[k] = NEG;
+            __syncwarp();
+            if (lane < 24) col[wib][lane] = qprof[(size_t)lane * mpad + i];
+            __syncwarp();
+            int64_t kmin64 = -(i + lo);
+            if (kmin64 < 0) kmin64 = 0;
+            int64_t kmax64 = nn - 1 - i - lo;
+            if (kmax64 > w - 1) kmax64 = w - 1;
+            const int kmin = (int)(kmin64 > w ? w : kmin64), kmax = (int)(kmax64 < -1 ? -1 : kmax64);
+            const int64_t jb = i + lo;
+            int carry = VNEG;
+            for (int c0 = 0; c0 < w; c0 += 32) {
+                const int k = c0 + lane;
+                const bool valid = k >= kmin && k <= kmax;
+                int h0 = NEG, f = NEG;
+                if (valid) {
+                    const int64_t j = jb + k;
+                    f = i >= 1 ? max(hp[k + 1] - go, fp[k + 1] - ge) : NEG;
+                    const int hd = (i >= 1 && j >= 1) ? hp[k] : 0;
+                    h0 = max(max(hd + (int)col[wib][s[j]], f), 0);
                 }
-            } else {
-                int32_t e = NEG, h_left = NEG;
-                const int64_t base = i + lo;
-                for (int64_t k = kmin; k <= kmax; k++) {
-                    const int64_t j = base + k;
-                    int32_t ecand = max(h_left - go, e - ge);
-                    e = k > kmin ? ecand : NEG;
-                    int32_t f = i >= 1 ? max(a_hp[k + 1] - go, a_fp[k + 1] - ge) : NEG;
-                    int32_t hd = (i >= 1 && j >= 1) ? a_hp[k] : 0;
-                    int32_t sub = (int32_t)qprof[(size_t)s[j] * mpad + i];
-                    int32_t diag = hd + sub;
-                    int32_t h = max(max(max(diag, e), f), 0);
-                    a_hc[k] = h;
-                    a_fc[k] = f;
-                    h_left = h;
-                    best = max(best, h);
+                const int v = valid ? h0 + k * ge : VNEG;
+                int incl = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl = max(incl, u);
                 }
-                for (int64_t k = 0; k < kmin; k++) {
-                    a_hc[k] = NEG;
-                    a_fc[k] = NEG;
+                int excl = __shfl_up_sync(0xffffffffu, incl, 1);
+                if (lane == 0) excl = VNEG;
+                excl = max(excl, carry);
+                carry = max(carry, __shfl_sync(0xffffffffu, incl, 31));
+                const int e = excl - go - (k - 1) * ge;
+                const int h = valid ? max(h0, e) : NEG;
+                if (k < w) {
+                    hc[k] = h;
+                    fc[k] = valid ? f : NEG;
                 }
-                for (int64_t k = kmax + 1; k < w; k++) {
-                    a_hc[k] = NEG;
-                    a_fc[k] = NEG;
-                }
+                best = max(best, h);
             }
-            int32_t* tmp = a_hp;
-            a_hp = a_hc;
-            a_hc = tmp;
-            tmp = a_fp;
-            a_fp = a_fc;
-            a_fc = tmp;
+            __syncwarp();
+            int32_t* tmp = hp;
+            hp = hc;
+            hc = tmp;
+            tmp = fp;
+            fp = fc;
+            fc = tmp;
         }
-        scores[jid] = best;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if (lane == 0) scores[jid] = best;
+        __syncwarp();
     }
 }
 

@@ -99,7 +99,7 @@ struct Dataset {
 struct GraphKey {
     uint64_t npad, wcap, n_res;
     int32_t rows, go, ge;
-    uint32_t pair_steps, nq, pad_;
+    uint32_t pair_steps, nq, long_steps;
     const void* ptrs[16];
     bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
@@ -125,6 +125,7 @@ struct saber_gpu {
     int sm_count = 0;
     int strip_rows = saber::kStripRows;  // tuning: rows per strip of the int16 kernel
     uint32_t pair_steps = saber::kPairStepsDefault;  // tuning: paired-strip threshold
+    uint32_t long_steps = saber::kLongStepsDefault;  // tuning: lane sweeps longer than this go to the warp kernel
     // captured scoring graphs (saber_gpu_score_band_jobs with graphs on)
     bool use_graphs = true;
     uint64_t graph_captures = 0;

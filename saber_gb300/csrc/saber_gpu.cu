@@ -71,13 +71,15 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
 // Classes (the top two key bits, so the sort makes them contiguous):
 //   0: width >= R (R = the handle's strip rows), packed int16 kernel with R rows
 //   1: 8 <= width < R when R = 16, packed int16 kernel with 8 rows
-//   2: narrower bands and out-of-range sizes, int32 kernel
+//   2: narrower bands, out-of-range sizes and sweeps longer than long_steps
+//      column steps in one lane: the warp-per-job int32 kernel, largest first
 //   3: empty jobs (score 0, written here)
 // Packed-class keys order jobs by (strips, width, query) so that the 64
 // consecutive jobs of a warp task share their loop counts and widths; within
 // class 0 the paired jobs (bit 61; their strips counted in 2R rows) sort last.
 __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njobs, const uint32_t* __restrict__ n_real,
-                           int R, uint32_t pair_steps, const uint64_t* __restrict__ qoffs, uint32_t nq, uint64_t n_res,
+                           int R, uint32_t pair_steps, uint32_t long_steps, const uint64_t* __restrict__ qoffs,
+                           uint32_t nq, uint64_t n_res,
                            uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                            int32_t* __restrict__ scores, uint32_t* __restrict__ counts,
                            unsigned long long* __restrict__ stats) {
@@ -127,8 +129,13 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
             ns = last / (2 * R) - first / (2 * R) + 1;
         }
         if (cls != 2 && (w >= (1 << 16) || ns >= (1 << 13))) cls = 2;
+        // a sweep longer than long_steps column steps in one lane goes to the
+        // warp-per-job int32 kernel
+        if (cls != 2 && (uint64_t)ns * (uint64_t)(w + (pair ? 2 * R : rows) - 1) > long_steps) cls = 2;
         if (cls == 2) {
-            keys[t] = (2ull << 62) | t;
+            // largest first, so that the warps' static share ends together
+            const uint64_t sz = jc >> 4 < 0x7FFFFFFFull ? jc >> 4 : 0x7FFFFFFFull;
+            keys[t] = (2ull << 62) | ((0x7FFFFFFFull - sz) << 31) | t;
             c2++;
             w2 = max(w2, (unsigned long long)w);
         } else {
@@ -238,7 +245,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
+        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, h->long_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
         h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
     CU(h, cudaGetLastError());
@@ -322,9 +329,9 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         // int32 kernel over narrow bands and rescued jobs (count read on the device)
         const unsigned T = 128;
         const unsigned grid = (unsigned)(h->sm_count * 4);
-        const uint64_t threads = (uint64_t)grid * T;
+        const uint64_t warps = (uint64_t)grid * T / 32;
         const uint32_t stride = (uint32_t)(wmax_all + 1);
-        CUALLOC(h, h->slabs, threads * stride * 4 * sizeof(int32_t));
+        CUALLOC(h, h->slabs, warps * stride * 4 * sizeof(int32_t));
         GenericArgs a;
         a.res = ds.res.as<uint8_t>();
         a.prof = qs.prof.as<int16_t>();
@@ -403,7 +410,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     const uint64_t warps = (uint64_t)std::max(grid0, grid8) * 256 / 32;
     CUALLOC(h, h->bufs, warps * wcap * 32 * sizeof(uint2));
     const unsigned gT = 128, gGrid = (unsigned)(h->sm_count * 4);
-    CUALLOC(h, h->slabs, (uint64_t)gGrid * gT * wcap * 4 * sizeof(int32_t));
+    CUALLOC(h, h->slabs, (uint64_t)gGrid * (gT / 32) * wcap * 4 * sizeof(int32_t));
     size_t t_sort = 0;
     CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t_sort, h->keys_in.as<uint64_t>(), h->keys_out.as<uint64_t>(),
                                           h->vals_in.as<uint32_t>(), h->vals_out.as<uint32_t>(), (int)npad, 0, 64, s));
@@ -416,6 +423,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     key.go = sch.go;
     key.ge = sch.ge;
     key.pair_steps = h->pair_steps;
+    key.long_steps = h->long_steps;
     key.n_res = ds.n_res;  // scalar kernel parameters baked into the graph
     key.nq = qs.nq;
     const void* ptrs[16] = {h->jobs_dev.p, h->scores_dev.p, h->keys_in.p, h->keys_out.p, h->vals_in.p,
@@ -439,7 +447,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
         chk(cudaMemsetAsync(counts, 0, 16 * 4, s));
         chk(cudaMemsetAsync(stats, 0, 8 * 8, s));
         k_classify<<<nblocks(npad, 256, h->sm_count * 8), 256, 0, s>>>(
-            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, qs.offsets.as<uint64_t>(), qs.nq,
+            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, h->long_steps, qs.offsets.as<uint64_t>(), qs.nq,
             ds.n_res, h->keys_in.as<uint64_t>(), h->vals_in.as<uint32_t>(), d_scores, counts, stats);
         chk(cudaGetLastError());
         size_t tb = h->cub_tmp.cap;
@@ -1372,6 +1380,14 @@ int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps) {
 }
 
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h) { return h ? h->pair_steps : 0u; }
+
+int saber_gpu_set_long_steps(saber_gpu* h, uint32_t steps) {
+    ENTER(h);
+    h->long_steps = steps;
+    return SABER_OK;
+}
+
+uint32_t saber_gpu_get_long_steps(saber_gpu* h) { return h ? h->long_steps : 0u; }
 
 int saber_gpu_set_scan_table_bytes(saber_gpu* h, uint64_t bytes) {
     ENTER(h);

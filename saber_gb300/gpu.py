@@ -232,6 +232,8 @@ def load_library():
         "saber_gpu_collected_regions": (ctypes.c_int, [P, P, P, P, U64, P]),
         "saber_gpu_get_pair_steps": (U32, [P]),
         "saber_gpu_set_scan_table_bytes": (ctypes.c_int, [P, U64]),
+        "saber_gpu_set_long_steps": (ctypes.c_int, [P, U32]),
+        "saber_gpu_get_long_steps": (U32, [P]),
         "saber_gpu_get_scan_table_bytes": (U64, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
     }
@@ -516,6 +518,15 @@ class Device:
     @pair_steps.setter
     def pair_steps(self, v):
         self._check(self.lib.saber_gpu_set_pair_steps(self.h, int(v) & 0xFFFFFFFF), "set_pair_steps")
+
+    @property
+    def long_steps(self):
+        """Lane-sweep length (column steps) above which a job goes to the warp-per-job kernel."""
+        return int(self.lib.saber_gpu_get_long_steps(self.h))
+
+    @long_steps.setter
+    def long_steps(self, v):
+        self._check(self.lib.saber_gpu_set_long_steps(self.h, int(v) & 0xFFFFFFFF), "set_long_steps")
 
     @property
     def scan_table_bytes(self):
