@@ -421,8 +421,9 @@ uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
 /* Tuning: a job whose sweep in one lane would take more than `steps` column
  * steps (strips x (width + strip rows - 1)) is scored by the warp-per-job
  * int32 kernel instead, so one long job does not set the launch's length;
- * 0xFFFFFFFF keeps every job on the int16 lanes.  Default 4096.  Results
- * do not depend on it.  No reference counterpart. */
+ * 0xFFFFFFFF (the default) keeps every job on the int16 lanes, the faster
+ * choice for large batches; small batches of long jobs gain from a few
+ * thousand.  Results do not depend on it.  No reference counterpart. */
 int saber_gpu_set_long_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_long_steps(saber_gpu* h);
 
