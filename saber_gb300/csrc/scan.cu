@@ -575,8 +575,7 @@ __global__ void k_run_flags(const unsigned long long* __restrict__ key, uint32_t
 }
 
 struct ChainArgs {
-    const uint2* surv;
-    const uint32_t* order;            // survivors in chain order
+    const uint2* surv;                // survivors in chain order
     const unsigned long long* key1s;  // sorted chain keys
     const uint32_t* starts;           // chain starts
     const uint32_t* nchains;
@@ -629,6 +628,8 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
     const uint8_t* subj = nullptr;
     int qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
     int cur = 0, best = 0, best_r = 0;
+    uint2 vnext = make_uint2(0, 0);
+    bool have_next = false;  // vnext holds survivor i + 1 of this lane's chain
     const uint32_t m27 = (1u << 27) - 1u;
     while (true) {
         const bool need = !retired && phase == 0 && i >= e;
@@ -645,6 +646,7 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
                 } else {
                     i = a.starts[c];
                     e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
+                    have_next = false;
                     const unsigned long long key = a.key1s[i];
                     const uint64_t q = key >> 44, s = (key >> 20) & 0xFFFFFF;
                     hkey = (s << 40) | (q << 20) | (key & 0xFFFFF);  // subject-major HSP key
@@ -664,7 +666,10 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
         uint4 hsp = make_uint4(0, 0, 0, 0);
         if (!retired) {
             if (phase == 0) {
-                const uint2 v = a.surv[a.order[i]];
+                const uint2 v = have_next ? vnext : a.surv[i];
+                // the chain's next survivor, for the coverage test at the end
+                have_next = i + 1 < e;
+                if (have_next) vnext = a.surv[i + 1];
                 qp = (int)((v.y & m27) - q0);
                 sp = (int)(v.x - (uint32_t)(subj - a.res));
                 n = qlen - qp < sl - sp ? qlen - qp : sl - sp;
@@ -718,7 +723,11 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
                     // the chain's next hits below hi are covered (query
                     // positions ascend along the chain); the HSP counts them
                     uint32_t j = i + 1;
-                    while (j < e && (int)((a.surv[a.order[j]].y & m27) - q0) < cover) j++;
+                    if (j < e && (int)((vnext.y & m27) - q0) < cover) {
+                        j++;
+                        have_next = false;
+                        while (j < e && (int)((a.surv[j].y & m27) - q0) < cover) j++;
+                    }
                     avoided += j - (i + 1);
                     if (score >= a.thr) {
                         emit = true;
@@ -1386,9 +1395,13 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         CUALLOC(h, h->sc_hkeyo, hcap * 8);
         CUALLOC(h, h->sc_hval, hcap * 4);
         CUALLOC(h, h->sc_hvalo, hcap * 4);
+        // survivors in chain order (one gather, so the chains read them directly)
+        CUALLOC(h, h->sc_surv2, (uint64_t)ns * 8);
+        k_gather_u64_by<<<nblocks(ns, 256), 256, 0, s>>>(
+            reinterpret_cast<const unsigned long long*>(h->sc_surv.p), h->sc_val.as<uint32_t>(), ns,
+            h->sc_surv2.as<unsigned long long>());
         ChainArgs c;
-        c.surv = h->sc_surv.as<uint2>();
-        c.order = h->sc_val.as<uint32_t>();
+        c.surv = h->sc_surv2.as<uint2>();
         c.key1s = h->sc_key1.as<unsigned long long>();
         c.starts = h->sc_chains.as<uint32_t>();
         c.nchains = nchains;
