@@ -582,9 +582,11 @@ struct ChainArgs {
     uint32_t nsurv;
     const uint64_t *soffs, *qoffs;
     const uint8_t* res;               // canonical residues
-    const int16_t* prof;              // query profiles (S + bias), rows c, stride mpad
-    const uint64_t* prof_off;
-    const uint32_t* prof_mpad;
+    uint64_t n_res;                   // residues (the buffer holds 64 more)
+    const uint8_t* qcodes;            // query batch codes (16 bytes of padding)
+    const int8_t* qbias;              // per batch position score bias, or null
+    uint64_t qn;                      // batch positions
+    const int32_t* matrix;            // 24 x 24 scores
     int thr, x;
     uint4* hsp;                       // (lo, hi, score, seed hits)
     unsigned long long* hkey;
@@ -611,7 +613,29 @@ struct ChainArgs {
 // read one query's profile).
 constexpr int kXBlock = 8;
 
+// 8 consecutive bytes of buf from byte index x on (bytes outside [0, limit)
+// read as 0): two words, from three aligned loads when all are in range.
+__device__ __forceinline__ uint2 load8(const uint8_t* __restrict__ buf, int64_t x, uint64_t limit) {
+    if (x >= 0 && (uint64_t)x + 12 <= limit) {
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(buf + (x & ~(int64_t)3));
+        const uint32_t sh = (uint32_t)(x & 3) * 8u;
+        const uint32_t w0 = w[0], w1 = w[1], w2 = w[2];
+        return make_uint2(__funnelshift_r(w0, w1, sh), __funnelshift_r(w1, w2, sh));
+    }
+    uint32_t v[2] = {0u, 0u};
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        const int64_t p = x + b;
+        const uint32_t c = (p >= 0 && (uint64_t)p < limit) ? buf[p] : 0u;
+        v[b >> 2] |= c << (8 * (b & 3));
+    }
+    return make_uint2(v[0], v[1]);
+}
+
 __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
+    __shared__ int32_t smat[576];
+    for (int t = threadIdx.x; t < 576; t += blockDim.x) smat[t] = a.matrix[t];
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const uint32_t nch = *a.nchains;
     unsigned long long ext = 0, avoided = 0, steps = 0;
@@ -623,8 +647,6 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
     // residue offsets below 2^32
     uint32_t q0 = 0;
     int qlen = 0, sl = 0, cover = 0;
-    const int16_t* P = nullptr;
-    int mpad = 0;
     const uint8_t* subj = nullptr;
     int qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
     int cur = 0, best = 0, best_r = 0;
@@ -654,8 +676,6 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
                     const uint64_t s0 = a.soffs[s];
                     qlen = (int)(a.qoffs[q + 1] - q0);
                     sl = (int)(a.soffs[s + 1] - s0);
-                    P = a.prof + a.prof_off[q];
-                    mpad = (int)a.prof_mpad[q];
                     subj = a.res + s0;
                     cover = 0;
                 }
@@ -678,13 +698,28 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
                 xe = 0;
                 phase = 1;
             }
-            const int dir = phase == 1 ? 1 : -1, off = phase == 1 ? 0 : 1;
+            // the block's 8 positions as byte runs of query codes, biases and
+            // subject residues (ascending addresses; leftwards reads them
+            // backwards); scores from the matrix in shared memory, as the
+            // profile P[c][i] = S(q_i, c) + bias_i holds them
+            const bool right = phase == 1;
+            const int64_t gq = (int64_t)q0 + qp + (right ? t : -(t + kXBlock));
+            const int64_t gs = (int64_t)(subj - a.res) + sp + (right ? t : -(t + kXBlock));
+            const uint2 qc8 = load8(a.qcodes, gq, a.qn + 16);
+            const uint2 sc8 = load8(a.res, gs, a.n_res + 64);
+            const uint2 qb8 = a.qbias ? load8(reinterpret_cast<const uint8_t*>(a.qbias), gq, a.qn + 16)
+                                      : make_uint2(0u, 0u);
             int sv[kXBlock];
 #pragma unroll
             for (int u = 0; u < kXBlock; u++) {
-                const int tt = t + u;
-                const int d = dir * (tt + off);
-                sv[u] = tt < n ? (int)P[(size_t)subj[sp + d] * mpad + qp + d] : 0;
+                const int b = right ? u : kXBlock - 1 - u;  // byte of position t + u
+                const uint32_t wq = b < 4 ? qc8.x : qc8.y, ws = b < 4 ? sc8.x : sc8.y, wb = b < 4 ? qb8.x : qb8.y;
+                const int sh = 8 * (b & 3);
+                int qcode = (int)((wq >> sh) & 0xFFu);
+                qcode = qcode < 24 ? qcode : 22;
+                const int scode = (int)((ws >> sh) & 0xFFu);
+                const int bias = (int)(int8_t)((wb >> sh) & 0xFFu);
+                sv[u] = smat[qcode * 24 + (scode < 24 ? scode : 22)] + bias;
             }
             bool stop = false;
             int done = 0;
@@ -1409,9 +1444,11 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         c.soffs = ds.soff.as<uint64_t>();
         c.qoffs = qs.offsets.as<uint64_t>();
         c.res = ds.res.as<uint8_t>();
-        c.prof = qs.prof.as<int16_t>();
-        c.prof_off = qs.prof_off.as<uint64_t>();
-        c.prof_mpad = qs.prof_mpad.as<uint32_t>();
+        c.n_res = ds.n_res;
+        c.qcodes = qs.codes.as<uint8_t>();
+        c.qbias = qs.has_bias ? qs.bias.as<int8_t>() : nullptr;
+        c.qn = qs.offs[qs.nq];
+        c.matrix = h->scheme.d_matrix.as<int32_t>();
         c.thr = p->hsp_threshold;
         c.x = p->x_drop;
         c.hsp = h->sc_hsp.as<uint4>();
