@@ -172,6 +172,12 @@ __global__ void k_query_seeds(const uint8_t* __restrict__ qsb, const uint8_t* __
     }
 }
 
+// (first entry, entries) of each rank, the entries offset by the shape's base
+__global__ void k_entry_ranges(const uint32_t* __restrict__ coff, uint64_t n, uint32_t base, uint2* __restrict__ rng) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        rng[k] = make_uint2(coff[k] + base, coff[k + 1] - coff[k]);
+}
+
 // presence bits and present-code counts of each 32-code group
 __global__ void k_group_bits(const uint32_t* __restrict__ cnt, uint64_t ncodes, uint2* __restrict__ grp,
                              uint32_t* __restrict__ gcnt) {
@@ -208,7 +214,8 @@ struct ScanArgs {
     const uint8_t *sb, *res, *rem, *dst;
     uint64_t N;
     const uint2* grp;                // rank-compressed presence tables of all shapes
-    const uint32_t *coff, *qent;     // rank -> batch-position entries of all shapes
+    const uint2* rng;                // rank -> (first entry, entries) of all shapes
+    const uint32_t* qent;            // batch positions of all shapes
     const uint4* qwin;               // per batch position: seed-letter window record (32 bytes)
     const uint4* qwinx;              // per batch position: full-code window record (32 bytes)
     int cfil;
@@ -220,8 +227,7 @@ struct ScanArgs {
     unsigned long long* ctr;    // [2] hits, [3] filtered
     // per shape: care offsets, table / entry bases
     ShapeDev sh[kMaxShapes];
-    uint64_t grp_off[kMaxShapes], coff_off[kMaxShapes];
-    uint32_t qent_off[kMaxShapes];
+    uint64_t grp_off[kMaxShapes], rng_off[kMaxShapes];
 };
 
 // Lanes [lo, hi) of a 32-lane mask (0 <= lo, hi <= 32).
@@ -439,10 +445,9 @@ __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
                     const int64_t c = seed_code(stb, s_shape[si], a.asize);
                     uint32_t k;
                     if (c >= 0 && code_rank(a.grp + a.grp_off[si], (uint32_t)c, k)) {
-                        const uint32_t* co = a.coff + a.coff_off[si];
-                        e0[j] = co[k];
-                        n[j] = co[k + 1] - e0[j];
-                        e0[j] += a.qent_off[si];
+                        const uint2 r = a.rng[a.rng_off[si] + k];
+                        e0[j] = r.x;
+                        n[j] = r.y;
                     }
                 }
             }
@@ -1266,6 +1271,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     CUALLOC(h, h->sc_cntc, coff_n * 4);
     CUALLOC(h, h->sc_qoff, (uint64_t)nsh * coff_n * 4);
     CUALLOC(h, h->sc_qent, (uint64_t)nsh * QN * 4 + 4);
+    CUALLOC(h, h->sc_qrng, (uint64_t)nsh * QN * 8 + 8);
     {
         size_t t1 = 0, t2 = 0;
         CU(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, h->sc_gcnt.as<uint32_t>(), h->sc_grank.as<uint32_t>(),
@@ -1295,6 +1301,9 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                                                                          h->sc_cntc.as<uint32_t>());
         tb = h->cub_tmp.cap;
         CU(h, cub::DeviceScan::ExclusiveSum(h->cub_tmp.p, tb, h->sc_cntc.as<uint32_t>(), coff, (int)coff_n, s));
+        if (QN)
+            k_entry_ranges<<<nblocks(QN, 256), 256, 0, s>>>(coff, QN, (uint32_t)((uint64_t)si * QN),
+                                                            h->sc_qrng.as<uint2>() + (uint64_t)si * QN);
         // pass 1: the counts' buffer becomes the per-rank cursors
         CU(h, cudaMemsetAsync(cnt, 0, coff_n * 4, s));
         if (QN)
@@ -1311,7 +1320,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     a.dst = h->sc_dst.as<uint8_t>();
     a.N = N;
     a.grp = h->sc_qpres.as<uint2>();
-    a.coff = h->sc_qoff.as<uint32_t>();
+    a.rng = h->sc_qrng.as<uint2>();
     a.qent = h->sc_qent.as<uint32_t>();
     CUALLOC(h, h->sc_qwin, QN * 32 + 32);
     CUALLOC(h, h->sc_qwinx, QN * 32 + 32);
@@ -1330,15 +1339,14 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     for (uint32_t si = 0; si < nsh; si++) {
         a.sh[si] = shape_dev(p, si);
         a.grp_off[si] = gbase[si];
-        a.coff_off[si] = (uint64_t)si * coff_n;
-        a.qent_off[si] = (uint32_t)((uint64_t)si * QN);
+        a.rng_off[si] = (uint64_t)si * QN;
     }
     // passes over groups of shapes whose tables stay within the L2 budget:
     // as many shapes per pass as the largest shape's tables allow, rounded
     // down to whole unroll groups
     uint64_t shape_bytes = 0;
     for (uint32_t si = 0; si < nsh; si++)
-        shape_bytes = std::max(shape_bytes, (gbase[si + 1] - gbase[si]) * 8 + coff_n * 4 + QN * 4);
+        shape_bytes = std::max(shape_bytes, (gbase[si + 1] - gbase[si]) * 8 + QN * 8 + QN * 4);
     uint64_t per_pass = std::max<uint64_t>(1, h->scan_table_bytes / std::max<uint64_t>(shape_bytes, 1));
     if (per_pass >= (uint64_t)kShapeUnroll) per_pass -= per_pass % kShapeUnroll;
     std::vector<std::pair<uint32_t, uint32_t>> passes;
