@@ -13,11 +13,18 @@
 #include <cstring>
 #include <atomic>
 #include <limits>
+#include <memory>
 #include <thread>
 #include <unordered_map>
 #include <vector>
 
 #include "region_sink.h"
+
+namespace saber {
+// Pinned host staging owned by the handle (slot 0..3, grow-only, contents
+// not preserved); null when the allocation fails.  saber_gpu.cu
+void* pinned_scratch(saber_gpu* h, int slot, size_t bytes);
+}  // namespace saber
 
 #include <cuda_runtime.h>  // float4, uint4
 
@@ -425,12 +432,12 @@ struct Engine {
         return j;
     }
 
-    int score(const std::vector<saber_band_job>& jobs, std::vector<int32_t>& out) {
-        out.assign(jobs.size(), 0);
-        if (jobs.empty()) return SABER_OK;
+    int score(const saber_band_job* jobs, size_t n, std::vector<int32_t>& out) {
+        out.assign(n, 0);
+        if (n == 0) return SABER_OK;
         saber_score_stats ss{};
         const double t0 = now_ms();
-        int rc = saber_gpu_score_band_jobs(h, jobs.data(), jobs.size(), out.data(), &ss);
+        int rc = saber_gpu_score_band_jobs(h, jobs, n, out.data(), &ss);
         if (rc != SABER_OK) return rc;
         st.t_score_calls_ms += now_ms() - t0;
         st.t_score_device_ms += ss.t_prep_ms + ss.t_fast_ms + ss.t_generic_ms;
@@ -442,7 +449,9 @@ struct Engine {
         return SABER_OK;
     }
 
-    // engine.rs:1021-1099, batched over the queries
+    // engine.rs:1021-1099, batched over the queries.  The jobs are built in
+    // the handle's pinned staging buffers (no zero-fill, fast copies), every
+    // per-region loop runs over the queries in parallel.
     int score_windows(const std::vector<Prep>& preps, const std::vector<std::vector<Region>>& per_q,
                       const std::vector<std::vector<Plan>>& plans, const std::vector<int64_t>& qlens,
                       std::vector<std::vector<int64_t>>& scores) {
@@ -455,8 +464,11 @@ struct Engine {
         scores.resize(nq);
         std::vector<size_t> base(nq + 1, 0);
         for (size_t qi = 0; qi < nq; qi++) base[qi + 1] = base[qi] + per_q[qi].size();
-        std::vector<saber_band_job> s1(base[nq]);
-        std::vector<Ref> r1(base[nq]);
+        const size_t n1 = base[nq];
+        saber_band_job* s1 = static_cast<saber_band_job*>(saber::pinned_scratch(h, 0, n1 * sizeof(saber_band_job)));
+        if (n1 && !s1) return SABER_ERR_NOMEM;
+        std::unique_ptr<Ref[]> r1(new Ref[n1 ? n1 : 1]);
+        std::vector<uint64_t> banded(nq, 0);
         parallel_for(nq, [&](size_t q) {
             const uint32_t qi = (uint32_t)q;
             scores[qi].assign(per_q[qi].size(), 0);
@@ -474,19 +486,24 @@ struct Engine {
                     band_clip(blo, bhi, m, n);
                     s1[k] = job(qi, r.subject, pl.lo, pl.hi, blo, bhi);
                     r1[k] = {qi, ri, 1};
+                    banded[qi]++;
                 } else {
                     s1[k] = job(qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi);
                     r1[k] = {qi, ri, 2};
+                    banded[qi]++;
                 }
             }
         });
+        for (uint64_t v : banded) st.band_scored_regions += v;
         std::vector<int32_t> sc1;
-        int rc = score(s1, sc1);
+        int rc = score(s1, n1, sc1);
         if (rc != SABER_OK) return rc;
         // stage-2 decision per region (f64 threshold of the region's subject length)
         const double re = region_evalue();
-        std::vector<uint8_t> again(r1.size(), 0);
+        std::vector<uint8_t> again(n1, 0);
+        std::vector<size_t> n2q(nq + 1, 0);
         parallel_for(nq, [&](size_t q) {
+            size_t c = 0;
             for (size_t k = base[q]; k < base[q + 1]; k++) {
                 const Ref& x = r1[k];
                 if (x.kind != 1) {
@@ -497,26 +514,37 @@ struct Engine {
                 const Prep& pr = preps[x.qi];
                 const double thr = P.score_prefilter_frac *
                                    pr.qs.floor_lower_bound(re, false, 0.0, slen(r.subject), pr.region_floor);
-                if ((double)sc1[k] >= thr) again[k] = 1;
-                else scores[x.qi][x.ri] = sc1[k];
+                if ((double)sc1[k] >= thr) {
+                    again[k] = 1;
+                    c++;
+                } else {
+                    scores[x.qi][x.ri] = sc1[k];
+                }
+            }
+            n2q[q + 1] = c;
+        });
+        for (size_t q = 0; q < nq; q++) n2q[q + 1] += n2q[q];
+        const size_t n2 = n2q[nq];
+        saber_band_job* s2 = static_cast<saber_band_job*>(saber::pinned_scratch(h, 1, n2 * sizeof(saber_band_job)));
+        if (n2 && !s2) return SABER_ERR_NOMEM;
+        std::unique_ptr<Ref[]> r2(new Ref[n2 ? n2 : 1]);
+        parallel_for(nq, [&](size_t q) {
+            size_t w = n2q[q];
+            for (size_t k = base[q]; k < base[q + 1]; k++) {
+                if (!again[k]) continue;
+                const Ref& x = r1[k];
+                const Region& r = per_q[x.qi][x.ri];
+                const Plan& pl = plans[x.qi][x.ri];
+                s2[w] = job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi);
+                r2[w] = x;
+                w++;
             }
         });
-        std::vector<saber_band_job> s2;
-        std::vector<Ref> r2;
-        for (size_t k = 0; k < r1.size(); k++) {
-            const Ref& x = r1[k];
-            st.band_scored_regions += x.kind != 0;
-            if (!again[k]) continue;
-            const Region& r = per_q[x.qi][x.ri];
-            const Plan& pl = plans[x.qi][x.ri];
-            s2.push_back(job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi));
-            r2.push_back(x);
-        }
         std::vector<int32_t> sc2;
-        rc = score(s2, sc2);
+        rc = score(s2, n2, sc2);
         if (rc != SABER_OK) return rc;
-        for (size_t k = 0; k < r2.size(); k++) scores[r2[k].qi][r2[k].ri] = sc2[k];
-        st.band_rescored += s2.size();
+        for (size_t k = 0; k < n2; k++) scores[r2[k].qi][r2[k].ri] = sc2[k];
+        st.band_rescored += n2;
         return SABER_OK;
     }
 

@@ -163,6 +163,7 @@ struct saber_gpu {
     // device-side region cap / triage / compaction, pinned host staging
     saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
     saber::HostBuf pin_reg, pin_src;
+    saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
     // traceback scratch
     saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
 };

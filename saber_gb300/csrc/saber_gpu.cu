@@ -1095,6 +1095,13 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
     (h)->err.clear()
 
 namespace saber {
+// Pinned host staging for the host engine (engine.cpp).
+void* pinned_scratch(saber_gpu* h, int slot, size_t bytes) {
+    if (!h || slot < 0 || slot >= 4) return nullptr;
+    cudaSetDevice(h->device);
+    return h->pin_scratch[slot].reserve(std::max<size_t>(bytes, 64)) == cudaSuccess ? h->pin_scratch[slot].p : nullptr;
+}
+
 // The batch's candidate regions for the host engine (engine.cpp): capped per
 // query and triaged on the device, kept ones in pinned memory (sink).
 int scan_search_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask, const int32_t* region_thr,
