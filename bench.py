@@ -49,6 +49,13 @@ def parse():
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
     ap.add_argument("--search-queries", type=int, default=2000)
     ap.add_argument("--search-subjects", type=int, default=500_000)
+    ap.add_argument("--nn-search", action="store_true",
+                    help="only the blastn (nn) batched search: DNA queries of 1-10 kb vs a synthetic genome-scale "
+                         "database (its own JSON line)")
+    ap.add_argument("--nn-queries", type=int, default=2000)
+    ap.add_argument("--nn-bases", type=float, default=500e6, help="database size in bases (subjects of 1-10 kb)")
+    ap.add_argument("--long-steps", type=int, default=0,
+                    help="scoring: one-lane sweeps longer than this go to the warp-per-job kernel (0: library default)")
     return ap.parse_args()
 
 
@@ -251,6 +258,50 @@ def run_search(a, dev):
     return out
 
 
+def run_nn_search(a, local_rank):
+    """blastn (nn) batched search: DNA queries of 1-10 kb (uniform ACGT)
+    against a database of 1-10 kb subjects, 10 % of them planted homologs at
+    80-95 % identity with indels at 0.01 per base; +2/-3 with SABER gaps 7/2,
+    one contiguous 11-mer shape, no window filter, E <= 10, -k 10; through
+    the C ABI batch engine, median of 2 calls after a warm-up."""
+    from saber_gb300 import Device, synth
+    from saber_gb300.search import Searcher, SearchParams
+    dev = Device(local_rank)
+    if a.long_steps:
+        dev.long_steps = a.long_steps
+    nsub = max(1, int(a.nn_bases / 5500))
+    t0 = time.perf_counter()
+    qs, ss, _ = synth.dna_db(a.seed + 700, a.nn_queries, nsub)
+    t1 = time.perf_counter()
+    se = Searcher(dev, ss.codes, ss.offsets, SearchParams.nucleotide(), gap_open=7, gap_extend=2,
+                  nucleotide=(2, -3))
+    cpar = se.cparams()
+
+    def call():
+        return dev.search(cpar, se.db_codes, se.db_offsets, qs.codes, qs.offsets)
+
+    call()
+    ts, out = [], None
+    for _ in range(2):
+        t = time.perf_counter()
+        out = call()
+        ts.append(time.perf_counter() - t)
+    tp = float(np.median(ts))
+    st = out[2]
+    keys = ("seed_positions", "hits", "ungapped_extensions", "extensions_avoided", "xdrop_steps", "hsps",
+            "regions", "banded_cells", "tb_tracebacks")
+    print(json.dumps({"metric": "batched nn search queries/s", "nn": {
+        "workload": "blastn (nn) batched search: %d DNA queries (%d bases) vs %d subjects (%d bases; 10%% planted "
+                    "80-95%% identity homologs, indels 0.01), +2/-3, gaps 7/2, 11-mers, E<=10, -k 10"
+                    % (len(qs.offsets) - 1, int(qs.codes.size), nsub, int(ss.codes.size)),
+        "unit": "queries/s", "value": round((len(qs.offsets) - 1) / tp, 1), "s_per_search": round(tp, 3),
+        "hits": int(len(out[0])), "counters": {k: int(st[k]) for k in keys if k in st},
+        "stages_ms": {k: round(v, 1) for k, v in st.items() if k.startswith("t_")},
+        "data_gen_s": round(t1 - t0, 1), "long_steps": dev.long_steps,
+        "timing": "median of 2 calls, host wall clock around saber_gpu_search"}}),
+        flush=True)
+
+
 def run_search_only(a, local_rank):
     from saber_gb300 import Device
     dev = Device(local_rank)
@@ -383,6 +434,9 @@ def main():
         torch.distributed.init_process_group("gloo")
     if a.impl == "reference":
         run_reference(a, rank, world)
+    elif a.nn_search:
+        if rank == 0:
+            run_nn_search(a, local_rank)
     elif a.search_only:
         if rank == 0:
             run_search_only(a, local_rank)

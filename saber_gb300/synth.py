@@ -211,18 +211,23 @@ def dna_db(seed, n_queries, n_subjects, qlen=(1000, 10000), slen=(1000, 10000), 
             ident = rng.uniform(*identity_range)
             sub = rng.random(seg.size) > ident
             seg[sub] = (seg[sub] + rng.integers(1, 4, size=int(sub.sum()))) % 4
+            # indel events at rate indel_rate per position: a deletion skips,
+            # an insertion adds, geometric(1/3) bases (mean 3)
+            ev = np.flatnonzero(rng.random(seg.size) < indel_rate)
+            is_del = rng.random(ev.size) < 0.5
+            klen = rng.geometric(1.0 / 3.0, size=ev.size)
             out = []
-            i = 0
-            while i < seg.size:
-                if rng.random() < indel_rate:
-                    k = int(rng.geometric(1.0 / 3.0))
-                    if rng.random() < 0.5:
-                        i += k
-                    else:
-                        out.append(rng.integers(0, 4, size=k).astype(np.uint8))
-                    continue
-                out.append(seg[i:i + 1])
-                i += 1
+            prev = 0
+            for e, d, k in zip(ev.tolist(), is_del.tolist(), klen.tolist()):
+                if e < prev:
+                    continue  # inside a deleted stretch
+                out.append(seg[prev:e])
+                if d:
+                    prev = e + k
+                else:
+                    out.append(rng.integers(0, 4, size=k).astype(np.uint8))
+                    prev = e
+            out.append(seg[prev:])
             body = np.concatenate(out) if out else np.zeros(0, np.uint8)
             cut = int(rng.integers(0, bg.size + 1))
             bg = np.concatenate([bg[:cut], body, bg[cut:]]).astype(np.uint8)
