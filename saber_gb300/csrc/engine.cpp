@@ -73,6 +73,26 @@ double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Memo of a pure function of the subject length (per query): direct-mapped,
+// so a collision only recomputes.
+struct LenMemo {
+    static constexpr int kSlots = 512;
+    int64_t key[kSlots];
+    double val[kSlots];
+    LenMemo() {
+        for (int i = 0; i < kSlots; i++) key[i] = -1;
+    }
+    template <class F>
+    double get(int64_t n, F f) {
+        const int i = (int)(((uint64_t)n * 0x9E3779B97F4A7C15ull) >> 55);
+        if (key[i] != n) {
+            key[i] = n;
+            val[i] = f();
+        }
+        return val[i];
+    }
+};
+
 // ---- statistics (src/scoring/stats.rs) ------------------------------------
 
 // BLAST_ComputeLengthAdjustment (stats.rs:458-520)
@@ -343,10 +363,12 @@ struct Engine {
             span_lo[i] = regs[i].dmin;
             span_hi[i] = regs[i].dmax;
         }
-        // group by subject
+        // group by subject (stable: the index breaks ties)
+        std::vector<uint64_t> keyed(n);
+        for (size_t i = 0; i < n; i++) keyed[i] = ((uint64_t)regs[i].subject << 32) | (uint64_t)i;
+        std::sort(keyed.begin(), keyed.end());
         std::vector<size_t> by(n);
-        for (size_t i = 0; i < n; i++) by[i] = i;
-        std::stable_sort(by.begin(), by.end(), [&](size_t a, size_t b) { return regs[a].subject < regs[b].subject; });
+        for (size_t i = 0; i < n; i++) by[i] = (size_t)(keyed[i] & 0xFFFFFFFFu);
         std::vector<size_t> idx;
         for (size_t a = 0; a < n;) {
             size_t b = a;
@@ -504,6 +526,7 @@ struct Engine {
         std::vector<size_t> n2q(nq + 1, 0);
         parallel_for(nq, [&](size_t q) {
             size_t c = 0;
+            LenMemo memo;  // the threshold depends on the query and the subject length only
             for (size_t k = base[q]; k < base[q + 1]; k++) {
                 const Ref& x = r1[k];
                 if (x.kind != 1) {
@@ -512,8 +535,10 @@ struct Engine {
                 }
                 const Region& r = per_q[x.qi][x.ri];
                 const Prep& pr = preps[x.qi];
-                const double thr = P.score_prefilter_frac *
-                                   pr.qs.floor_lower_bound(re, false, 0.0, slen(r.subject), pr.region_floor);
+                const int64_t sl = slen(r.subject);
+                const double thr = memo.get(sl, [&]() {
+                    return P.score_prefilter_frac * pr.qs.floor_lower_bound(re, false, 0.0, sl, pr.region_floor);
+                });
                 if ((double)sc1[k] >= thr) {
                     again[k] = 1;
                     c++;
@@ -644,6 +669,7 @@ struct Engine {
             const QStats& qs = preps[qi].qs;
             auto& order = orders[qi];
             const auto& regs = per_q[qi];
+            LenMemo lb, sp;  // search spaces depend on the query and the subject length only
             for (uint32_t i = 0; i < regs.size(); i++) {
                 const int64_t sc = scores[qi][i];
                 if (qs.database_model) {
@@ -652,8 +678,8 @@ struct Engine {
                 }
                 if (sc <= 0 || (has_bits && qs.bitscore(sc) < P.min_bitscore)) continue;
                 const int64_t n = slen(regs[i].subject);
-                if (qs.evalue_in(sc, qs.space_lower_bound(n)) > ecut) continue;
-                const double e = qs.evalue_for(sc, n);
+                if (qs.evalue_in(sc, lb.get(n, [&]() { return qs.space_lower_bound(n); })) > ecut) continue;
+                const double e = qs.evalue_in(sc, sp.get(n, [&]() { return qs.space_for(n); }));
                 if (e <= ecut) order.push_back({e, i});
             }
             const auto& sc_ = scores[qi];
