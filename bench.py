@@ -233,8 +233,35 @@ def run_search(a, dev):
         "plain": {"value": round(nq / tp, 1), "hits": int(len(plain)), "regions": cp["regions"],
                   "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages}},
     }
+    # two batches in flight (SearchPool: two handles, host stages of one batch
+    # overlapping device stages of the other); the second batch is another
+    # 2,000 seeded queries of the same model
+    from saber_gb300.search import SearchPool
+    qc, _, _ = synth.protein_db(a.seed + 503, a.search_queries, 1, reversed_frac=0.25, identity_range=(0.3, 0.6))
+    batches = [(qb.codes, qb.offsets), (qc.codes, qc.offsets)]
+    pool = SearchPool(sb.codes, sb.offsets, SearchParams("default"), slots=2)
+
+    def pooled(reps=3):
+        pool.raw_batches(batches)
+        ts, res = [], None
+        for _ in range(reps):
+            t = time.perf_counter()
+            res = pool.raw_batches(batches)
+            ts.append(time.perf_counter() - t)
+        return res, float(np.median(ts))
+
+    pres, pt = pooled()
+    nq2 = sum(len(b[1]) - 1 for b in batches)
+    out["plain"]["two_batches_in_flight"] = {
+        "value": round(nq2 / pt, 1), "queries": nq2,
+        "same_hits_as_single_handle": bool(keyset(pres[0][0]) == keyset(plain))}
     if not triage:
         return out
+    for se_ in pool.searchers:
+        se_.dev.set_triage(model, thr)
+    tres, tpt = pooled()
+    for se_ in pool.searchers:
+        se_.dev.set_triage(None)
     dev.set_triage(model, thr)
     try:
         call()
@@ -247,7 +274,9 @@ def run_search(a, dev):
         "triage": {"value": round(nq / tt, 1), "regions_scored": ct["regions"], "regions_dropped": ct["triage_dropped"],
                    "banded_cells": ct["banded_cells"], "hits_kept": kept, "hits_plain": total,
                    "kept_frac": round(kept / max(total, 1), 5), "lost_hit_rate": round(1 - kept / max(total, 1), 5),
-                   "threshold": round(thr, 4), "stages_ms": {k: round(ct[k], 1) for k in stages}},
+                   "threshold": round(thr, 4), "stages_ms": {k: round(ct[k], 1) for k in stages},
+                   "two_batches_in_flight": {"value": round(nq2 / tpt, 1), "queries": nq2,
+                                             "same_hits_as_single_handle": bool(keyset(tres[0][0]) == kt_)}},
         "speedup": round(tp / tt, 3),
         "training": {"regions": int(y.size), "positives": int(y.sum()), "steps": st["steps"],
                      "final_loss": round(st["final_loss"], 5), "pos_weight": round(st["pos_weight"], 2),

@@ -588,3 +588,43 @@ def _overlaps(a, b):
 
 def decode_protein(codes):
     return bytes(ALPHABET[c] if c < 24 else ord("X") for c in codes).decode()
+
+
+class SearchPool:
+    """Several query batches in flight on one GPU: one handle (stream,
+    scratch, resident database) per slot, batches dealt to the slots round
+    robin and searched from one host thread per slot, so that one batch's
+    host stages (plans, E-values, hit construction) overlap another's device
+    stages.  Each batch's hits are those of Searcher.search on it alone."""
+
+    def __init__(self, db_codes, db_offsets, params=None, slots=2, device=0, triage=None, **kw):
+        from .gpu import Device
+        self.searchers = [Searcher(Device(device), db_codes, db_offsets, params, **kw) for _ in range(slots)]
+        if triage is not None:
+            for se in self.searchers:
+                se.dev.set_triage(*triage)
+
+    def raw_batches(self, batches):
+        """dev.search results (hits, ops, stats) of each (q_codes, q_offsets) batch, in order."""
+        import threading
+        out = [None] * len(batches)
+        err = []
+
+        def work(slot):
+            se = self.searchers[slot]
+            cp = se.cparams()
+            try:
+                for b in range(slot, len(batches), len(self.searchers)):
+                    qc, qo = batches[b][0], batches[b][1]
+                    out[b] = se.dev.search(cp, se.db_codes, se.db_offsets, qc, qo)
+            except Exception as e:  # re-raised in the caller's thread
+                err.append(e)
+
+        threads = [threading.Thread(target=work, args=(s,)) for s in range(len(self.searchers))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if err:
+            raise err[0]
+        return out

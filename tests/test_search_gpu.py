@@ -80,3 +80,20 @@ def test_nucleotide_search_matches_oracle(dev):
     assert sum(len(h) for h in want) >= 5
     _compare(got, want)
     assert [len(h) for h in got] == [len(h) for h in se.search_py(qs.codes, qs.offsets)]
+
+
+@pytest.mark.gpu
+def test_search_pool_matches_single_handle(dev):
+    """Batches searched concurrently on a pool of handles give each batch the
+    hits of a plain search of that batch alone."""
+    from saber_gb300.search import Searcher, SearchPool, SearchParams
+    qa, sa, _ = synth.protein_db(91, 40, 3000, reversed_frac=0.25, identity_range=(0.3, 0.6))
+    qb, _, _ = synth.protein_db(92, 30, 1, reversed_frac=0.25, identity_range=(0.3, 0.6))
+    batches = [(qa.codes, qa.offsets), (qb.codes, qb.offsets), (qa.codes, qa.offsets)]
+    pool = SearchPool(sa.codes, sa.offsets, SearchParams("default"), slots=2)
+    got = pool.raw_batches(batches)
+    se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default"))
+    for (qc, qo), (hits, ops, st) in zip(batches, got):
+        want, wops, _ = dev.search(se.cparams(), se.db_codes, se.db_offsets, qc, qo)
+        assert np.array_equal(hits, want) and np.array_equal(ops, wops)
+    assert sum(len(h) for h, _, _ in got) > 0
