@@ -146,7 +146,8 @@ struct saber_gpu {
         sc_qcnt, sc_qoff, sc_qent, sc_qpres, sc_surv, sc_key1, sc_key2, sc_val, sc_key1o, sc_key2o, sc_valo,
         sc_chains, sc_hsp, sc_hkey, sc_hkeyo, sc_hval, sc_hvalo, sc_pairs, sc_regions, sc_rthr, sc_ctr, sc_tmp,
         sc_rk64a, sc_rk64b, sc_rk64c, sc_rk32a, sc_rk32b, sc_ridxa, sc_ridxb, sc_regions2, sc_rstat, sc_rstat2,
-        sc_flags, sc_gcnt, sc_grank, sc_cntc, sc_qwin, sc_qwinx, sc_surv2, sc_qrng;
+        sc_flags, sc_gcnt, sc_grank, sc_cntc, sc_qwin, sc_qwinx, sc_surv2, sc_qrng, sc_cb, sc_combtab;
+    bool sc_comb = false;  // the database's combined filter codes (sc_cb) are built
     uint64_t scan_table_bytes = 48ull << 20;  // tuning: seed-table bytes per scan pass (L2 budget)
     bool has_db_mask = false;
     // learned triage: installed model, per-call feature buffers, collection

@@ -208,6 +208,11 @@ __global__ void k_group_ranks(const uint32_t* __restrict__ cnt, uint64_t ncodes,
     }
 }
 
+// combined filter codes of the 256 residue values (comb_table)
+struct CombTab {
+    uint8_t t[256];
+};
+
 // ---- database scan with the window filter ---------------------------------------
 constexpr int kMaxShapes = 32;
 struct ScanArgs {
@@ -218,6 +223,7 @@ struct ScanArgs {
     const uint32_t* qent;            // batch positions of all shapes
     const uint4* qwin;               // per batch position: seed-letter window record (32 bytes)
     const uint4* qwinx;              // per batch position: full-code window record (32 bytes)
+    const uint8_t* cb;               // combined filter codes of the database (combined mode)
     int cfil;
     uint32_t min_ids, kx;
     uint32_t s0, s1, asize;          // this pass's shapes [s0, s1)
@@ -315,6 +321,7 @@ __device__ __forceinline__ void surv_drain(const ScanArgs& a, int lane, WarpScan
 // The queued segments' hits, 32 per round.  Each lane keeps kPer segments'
 // starts in registers; a round's owners come from the bits of the segments
 // that start inside it and the count of those that start before it.
+template <bool COMB>
 __device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg, WarpScan& ws,
                                            unsigned long long& hits, unsigned long long& filtered) {
     constexpr int kPer = kSegCap / 32;
@@ -366,6 +373,27 @@ __device__ __forceinline__ void scan_flush(const ScanArgs& a, int lane, int nseg
             g = a.qent[ws.seg_eb[own] + k];
             if (a.min_ids == 0) {
                 pass = true;
+            } else if (COMB) {
+                // one compare of combined codes: equal low nibbles are
+                // reduced-letter identities, equal bytes exact ones; the
+                // reference's decision (ids >= min_ids, else ids + kx * exact
+                // >= min_ids) is ids + kx * exact >= min_ids since exact <= ids
+                uint32_t Q[8], S[8];
+                ld256(Q, a.qwin + 2 * (uint64_t)g);
+                const int idx = rl + a.cfil + 16;  // staged byte of r + cfil - 16
+                staged_words(ws.resw, idx, S);
+                const int sdst = (int)(srd >> 8), srem = (int)(srd & 0xFFu);
+                const uint32_t L = lane_range(max(0, 16 - a.cfil - sdst), min(32, srem + 16 - a.cfil));
+                uint32_t Er = 0, Ee = 0;
+#pragma unroll
+                for (int w = 0; w < 8; w++) {
+                    const uint32_t x = Q[w] ^ S[w];
+                    const uint32_t zr = ~((x & 0x0F0F0F0Fu) + 0x0F0F0F0Fu) & 0x10101010u;
+                    const uint32_t ze = ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+                    Er |= (((zr >> 4) * 0x10204080u) >> 28) << (4 * w);
+                    Ee |= (((ze >> 7) * 0x10204080u) >> 28) << (4 * w);
+                }
+                pass = __popc(Er & L) + a.kx * __popc(Ee & L) >= a.min_ids;
             } else {
                 uint32_t Q[8], S[8];
                 ld256(Q, a.qwin + 2 * (uint64_t)g);
@@ -409,6 +437,7 @@ __device__ __forceinline__ uint32_t stage_word(const uint8_t* __restrict__ buf, 
     return v;
 }
 
+template <bool COMB>
 __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
     __shared__ uint32_t s_n[kScanWarps][kSegCap], s_eb[kScanWarps][kSegCap];
     __shared__ uint8_t s_rl[kScanWarps][kSegCap], s_sh[kScanWarps][kSegCap];
@@ -428,7 +457,7 @@ __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
         const int64_t wb = (int64_t)base - 32 + 4 * lane;
         __syncwarp();
         s_sbw[w][lane] = stage_word(a.sb, wb, a.N, kNonSeed);
-        s_resw[w][lane] = stage_word(a.res, wb, a.N, 0xFFu);
+        s_resw[w][lane] = COMB ? stage_word(a.cb, wb, a.N, 0xEEu) : stage_word(a.res, wb, a.N, 0xFFu);
         const int rem = r < a.N ? a.rem[r] : 0;
         ws.rd = r < a.N ? ((uint32_t)rem | ((uint32_t)a.dst[r] << 8)) : 0u;
         ws.base = base;
@@ -465,13 +494,13 @@ __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
             }
             if (nseg > kSegCap - 32 * kShapeUnroll) {
                 __syncwarp();
-                scan_flush(a, lane, nseg, ws, hits, filtered);
+                scan_flush<COMB>(a, lane, nseg, ws, hits, filtered);
                 nseg = 0;
             }
         }
         if (nseg) {
             __syncwarp();
-            scan_flush(a, lane, nseg, ws, hits, filtered);
+            scan_flush<COMB>(a, lane, nseg, ws, hits, filtered);
         }
     }
     if (ws.nsv) surv_drain(a, lane, ws);
@@ -486,9 +515,13 @@ __global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
 // Window records of the batch positions: record g holds the 32 letters at
 // g + cfil - 16 + t (t < 32), QSENT where that position lies outside g's
 // query (the filter's query-side lane bounds).
+// With `comb` (a combined code table) a single record of combined codes is
+// written to `win`: (group index << 4 | letter) where the letter counts, 0xFF
+// elsewhere; `winx` is then unused.
 __global__ void k_query_windows(const uint8_t* __restrict__ qsb, const uint8_t* __restrict__ qfull,
                                 const uint8_t* __restrict__ qrem, const uint8_t* __restrict__ qdst, uint64_t QN,
-                                int cfil, uint8_t* __restrict__ win, uint8_t* __restrict__ winx) {
+                                int cfil, const CombTab* __restrict__ comb, uint8_t* __restrict__ win,
+                                uint8_t* __restrict__ winx) {
     const uint64_t total = QN * 32;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t g = i >> 5;
@@ -500,8 +533,14 @@ __global__ void k_query_windows(const uint8_t* __restrict__ qsb, const uint8_t* 
             v = qsb[q];
             vx = qfull[q];
         }
-        win[i] = v;
-        winx[i] = vx;
+        if (comb) {
+            // letter from the seed byte, group index from the full code
+            win[i] = v == kQSent ? (uint8_t)0xFF
+                                 : (uint8_t)((vx < 24 ? (comb->t[vx] & 0xF0u) : 0xF0u) | (v & 0x0Fu));
+        } else {
+            win[i] = v;
+            winx[i] = vx;
+        }
     }
 }
 
@@ -945,12 +984,49 @@ static uint64_t fingerprint(const saber_gpu* h, const saber_scan_params* p) {
     return f;
 }
 
+// Combined filter codes for alphabets of at most 14 letters whose groups
+// hold at most 15 codes: byte = (index of the code within its letter's group)
+// << 4 | letter, so that equal low nibbles are a reduced-letter identity and
+// equal bytes an exact one.  Subject residues without a letter are 0xEE;
+// query positions that never count are 0xFF; query codes >= 24 take group
+// index 15, which no residue has.  Returns false when the alphabet does not
+// fit (the filter then compares separate letter and residue records).
+static bool comb_table(const saber_scan_params* p, uint8_t* tab /* 256 */) {
+    if (p->alpha_size > 14) return false;
+    int cnt[256] = {0};
+    for (int c = 0; c < 256; c++) tab[c] = 0xEE;
+    for (int c = 0; c < 24; c++) {
+        const uint8_t L = p->alpha_map[c];
+        if (L == 255) continue;
+        if (L >= p->alpha_size) return false;
+        if (cnt[L] >= 15) return false;
+        tab[c] = (uint8_t)((cnt[L]++ << 4) | L);
+    }
+    return true;
+}
+
+__global__ void k_comb_bytes(const uint8_t* __restrict__ res, uint64_t N, CombTab tab, uint8_t* __restrict__ cb) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N; r += (uint64_t)gridDim.x * blockDim.x)
+        cb[r] = tab.t[res[r]];
+}
+
 int scan_build_db(saber_gpu* h, const saber_scan_params* p) {
     const Dataset& ds = h->main;
     cudaStream_t s = h->stream;
     const uint64_t N = ds.n_res;
     AlphaMap am;
     memcpy(am.m, p->alpha_map, 24);
+    {
+        CombTab ct;
+        h->sc_comb = comb_table(p, ct.t);
+        if (h->sc_comb) {
+            CUALLOC(h, h->sc_cb, N + 128);
+            CU(h, cudaMemsetAsync(h->sc_cb.p, 0xEE, N + 128, s));
+            if (N) k_comb_bytes<<<nblocks(N, 256, h->sm_count * 32), 256, 0, s>>>(ds.res.as<uint8_t>(), N, ct,
+                                                                                 h->sc_cb.as<uint8_t>());
+            CU(h, cudaGetLastError());
+        }
+    }
     CUALLOC(h, h->sc_sb, N + 128);
     CUALLOC(h, h->sc_rem, N + 64);
     CUALLOC(h, h->sc_dst, N + 64);
@@ -1324,10 +1400,16 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     a.qent = h->sc_qent.as<uint32_t>();
     CUALLOC(h, h->sc_qwin, QN * 32 + 32);
     CUALLOC(h, h->sc_qwinx, QN * 32 + 32);
+    CombTab ctab;
+    const bool comb = h->sc_comb && comb_table(p, ctab.t);
+    CUALLOC(h, h->sc_combtab, sizeof(CombTab));
+    if (comb) CU(h, cudaMemcpyAsync(h->sc_combtab.p, &ctab, sizeof(CombTab), cudaMemcpyHostToDevice, s));
     if (QN)
         k_query_windows<<<nblocks(QN * 32, 256), 256, 0, s>>>(
             h->sc_qsb.as<uint8_t>(), h->sc_qfull.as<uint8_t>(), h->sc_qrem.as<uint8_t>(), h->sc_qdst.as<uint8_t>(),
-            QN, cfil, h->sc_qwin.as<uint8_t>(), h->sc_qwinx.as<uint8_t>());
+            QN, cfil, comb ? h->sc_combtab.as<CombTab>() : nullptr, h->sc_qwin.as<uint8_t>(),
+            h->sc_qwinx.as<uint8_t>());
+    a.cb = comb ? h->sc_cb.as<uint8_t>() : nullptr;
     a.qwin = h->sc_qwin.as<uint4>();
     a.qwinx = h->sc_qwinx.as<uint4>();
     a.cfil = cfil;
@@ -1353,7 +1435,8 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     for (uint32_t si = 0; si < nsh; si += (uint32_t)std::min<uint64_t>(per_pass, nsh))
         passes.push_back({si, (uint32_t)std::min<uint64_t>(nsh, si + per_pass)});
     int scan_bps = 0;
-    CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&scan_bps, k_scan, kScanWarps * 32, 0));
+    CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&scan_bps, comb ? k_scan<true> : k_scan<false>,
+                                                        kScanWarps * 32, 0));
     const unsigned scan_grid = (unsigned)std::max(1, scan_bps) * (unsigned)h->sm_count;
     for (int attempt = 0; attempt < 8; attempt++) {
         CUALLOC(h, h->sc_surv, scap * 8);
@@ -1364,7 +1447,8 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             for (const auto& ps : passes) {
                 a.s0 = ps.first;
                 a.s1 = ps.second;
-                k_scan<<<scan_grid, kScanWarps * 32, 0, s>>>(a);
+                if (comb) k_scan<true><<<scan_grid, kScanWarps * 32, 0, s>>>(a);
+                else k_scan<false><<<scan_grid, kScanWarps * 32, 0, s>>>(a);
             }
             CU(h, cudaGetLastError());
         }
