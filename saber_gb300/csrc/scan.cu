@@ -590,8 +590,18 @@ __device__ __forceinline__ uint64_t upper_idx(const uint64_t* offs, uint64_t n, 
     return lo;
 }
 
+// Bit layout of the chain keys: (query, subject, diagonal + dbias) above
+// `low` bits.  In the composite layout the low bits hold (query position,
+// shape), so one sort gives the chain order; otherwise (fields too wide for
+// 64 bits) the keys are query << 44 | subject << 20 | diagonal + 2^19 and a
+// first stable sort by (query position, shape) precedes.
+struct KeyLayout {
+    int low, bs, bd, bsh;  // bits below the chain key, of the subject, of the diagonal, of the shape
+    int64_t dbias;
+};
+
 __global__ void k_surv_keys(const uint2* __restrict__ surv, uint32_t n, const uint64_t* __restrict__ soffs,
-                            uint64_t nsub, const uint64_t* __restrict__ qoffs, uint32_t nq,
+                            uint64_t nsub, const uint64_t* __restrict__ qoffs, uint32_t nq, KeyLayout L,
                             unsigned long long* __restrict__ key1, uint32_t* __restrict__ key2,
                             uint32_t* __restrict__ val) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -601,8 +611,14 @@ __global__ void k_surv_keys(const uint2* __restrict__ surv, uint32_t n, const ui
         const uint64_t q = upper_idx(qoffs, nq, g);
         const int64_t qp = (int64_t)g - (int64_t)qoffs[q], sp = (int64_t)v.x - (int64_t)soffs[s];
         const int64_t d = sp - qp;
-        key1[i] = ((unsigned long long)q << 44) | ((unsigned long long)s << 20) | (unsigned long long)(d + kDBias);
-        key2[i] = ((uint32_t)qp << 5) | shape;
+        const unsigned long long ck =
+            (((unsigned long long)q << L.bs | s) << L.bd) | (unsigned long long)(d + L.dbias);
+        if (L.low) {
+            key1[i] = (ck << L.low) | ((unsigned long long)qp << L.bsh) | shape;
+        } else {
+            key1[i] = ck;
+            key2[i] = ((uint32_t)qp << 5) | shape;
+        }
         val[i] = i;
     }
 }
@@ -621,6 +637,7 @@ __global__ void k_run_flags(const unsigned long long* __restrict__ key, uint32_t
 struct ChainArgs {
     const uint2* surv;                // survivors in chain order
     const unsigned long long* key1s;  // sorted chain keys
+    KeyLayout kl;
     const uint32_t* starts;           // chain starts
     const uint32_t* nchains;
     uint32_t nsurv;
@@ -713,9 +730,11 @@ __global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
                     i = a.starts[c];
                     e = c + 1 < nch ? a.starts[c + 1] : a.nsurv;
                     have_next = false;
-                    const unsigned long long key = a.key1s[i];
-                    const uint64_t q = key >> 44, s = (key >> 20) & 0xFFFFFF;
-                    hkey = (s << 40) | (q << 20) | (key & 0xFFFFF);  // subject-major HSP key
+                    const unsigned long long ck = a.key1s[i] >> a.kl.low;
+                    const uint64_t q = ck >> (a.kl.bs + a.kl.bd);
+                    const uint64_t s = (ck >> a.kl.bd) & ((1ull << a.kl.bs) - 1);
+                    const int64_t d = (int64_t)(ck & ((1ull << a.kl.bd) - 1)) - a.kl.dbias;
+                    hkey = (s << 40) | (q << 20) | (uint64_t)(d + kDBias);  // subject-major HSP key
                     q0 = (uint32_t)a.qoffs[q];
                     const uint64_t s0 = a.soffs[s];
                     qlen = (int)(a.qoffs[q + 1] - q0);
@@ -1478,11 +1497,9 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         CUALLOC(h, h->sc_valo, (uint64_t)ns * 4);
         CUALLOC(h, h->sc_flags, (uint64_t)ns + 8);
         CUALLOC(h, h->sc_chains, (uint64_t)ns * 4 + 8);
-        k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(), ds.nsub,
-                                                     qs.offsets.as<uint64_t>(), qs.nq, h->sc_key1.as<unsigned long long>(),
-                                                     h->sc_key2.as<uint32_t>(), h->sc_val.as<uint32_t>());
-        // stable two-key order: by (query position, shape), then by (query,
-        // subject, diagonal); the sorts cover only the keys' significant bits
+        // chain order (query, subject, diagonal, query position, shape): one
+        // sort of composite keys when the fields fit 64 bits, else two stable
+        // sorts; the sorts cover only the keys' significant bits
         auto bits_for = [](uint64_t v) {
             int b = 1;
             while (b < 64 && (v >> b)) b++;
@@ -1490,8 +1507,26 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         };
         uint64_t qmax = 1;
         for (uint32_t q = 0; q < qs.nq; q++) qmax = std::max<uint64_t>(qmax, qs.offs[q + 1] - qs.offs[q]);
+        const uint64_t smax = std::max<uint64_t>(ds.max_len, 1);
+        KeyLayout kl;
+        {
+            const int bq = bits_for(qs.nq ? qs.nq - 1 : 0), bs = bits_for(ds.nsub ? ds.nsub - 1 : 0);
+            const int bd = bits_for(qmax + smax), bp = bits_for(qmax), bsh = bits_for(p->nshapes - 1);
+            if (bq + bs + bd + bp + bsh <= 64) {
+                kl = KeyLayout{bp + bsh, bs, bd, bsh, (int64_t)qmax};
+            } else {
+                kl = KeyLayout{0, 24, 20, 5, (int64_t)kDBias};
+            }
+        }
+        const int chain_bits = bits_for(qs.nq ? qs.nq - 1 : 0) + kl.bs + kl.bd;
+        k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(), ds.nsub,
+                                                     qs.offsets.as<uint64_t>(), qs.nq, kl,
+                                                     kl.low ? h->sc_key1o.as<unsigned long long>()
+                                                            : h->sc_key1.as<unsigned long long>(),
+                                                     h->sc_key2.as<uint32_t>(),
+                                                     kl.low ? h->sc_valo.as<uint32_t>() : h->sc_val.as<uint32_t>());
         const int k2_end = std::min(32, 5 + bits_for(qmax));
-        const int k1_end = std::min(64, 44 + bits_for(qs.nq));
+        const int k1_end = std::min(64, chain_bits + kl.low);
         size_t t1 = 0, t2 = 0, t3 = 0;
         CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t1, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
                                               h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end,
@@ -1503,16 +1538,20 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                                          h->sc_chains.as<uint32_t>(), h->sc_ctr.as<uint32_t>() + 40, (int)ns, s));
         CUALLOC(h, h->cub_tmp, std::max(t1, std::max(t2, t3)));
         size_t tb = h->cub_tmp.cap;
-        CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end,
-                                              s));
-        k_gather_key1<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(), ns,
-                                                       h->sc_key1o.as<unsigned long long>());
+        if (!kl.low) {
+            CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key2.as<uint32_t>(),
+                                                  h->sc_key2o.as<uint32_t>(), h->sc_val.as<uint32_t>(),
+                                                  h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end, s));
+            k_gather_key1<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(),
+                                                           h->sc_valo.as<uint32_t>(), ns,
+                                                           h->sc_key1o.as<unsigned long long>());
+        }
         CU(h, cub::DeviceRadixSort::SortPairs(h->cub_tmp.p, tb, h->sc_key1o.as<unsigned long long>(),
                                               h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
                                               h->sc_val.as<uint32_t>(), (int)ns, 0, k1_end, s));
         // chains: runs of one (query, subject, diagonal)
-        k_run_flags<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), ns, 0, h->sc_flags.as<uint8_t>());
+        k_run_flags<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_key1.as<unsigned long long>(), ns, kl.low,
+                                                     h->sc_flags.as<uint8_t>());
         uint32_t* nchains = h->sc_ctr.as<uint32_t>() + 40;
         CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
                                          h->sc_flags.as<uint8_t>(), h->sc_chains.as<uint32_t>(), nchains, (int)ns, s));
@@ -1531,6 +1570,7 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         c.surv = h->sc_surv2.as<uint2>();
         c.key1s = h->sc_key1.as<unsigned long long>();
         c.starts = h->sc_chains.as<uint32_t>();
+        c.kl = kl;
         c.nchains = nchains;
         c.nsurv = ns;
         c.soffs = ds.soff.as<uint64_t>();
