@@ -699,6 +699,7 @@ struct Engine {
         std::unordered_map<uint64_t, Aln> tb;
         std::vector<QState> state(nq);
         for (size_t qi = 0; qi < nq; qi++) state[qi].done = orders[qi].empty();
+        tb.reserve(nq * std::max<size_t>(4, (size_t)P.max_target_seqs * P.max_hsps) + 16);
         // speculative tracebacks per query and round: as many candidates as
         // the report can take (more rounds follow only where candidates
         // fail, are duplicates or repeat a subject)
@@ -848,7 +849,7 @@ struct Engine {
             a.s_start = o.s_start;
             a.s_end = o.s_end;
             if (a.present) a.runs.assign(ops.begin() + o.ops_offset, ops.begin() + o.ops_offset + o.n_ops);
-            tb[key(need[k].first, need[k].second)] = std::move(a);
+            tb.insert_or_assign(key(need[k].first, need[k].second), std::move(a));
         }
         return SABER_OK;
     }
