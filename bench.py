@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--search-only", action="store_true",
                     help="only the batched-search section (printed as its own JSON line)")
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
+    ap.add_argument("--no-pool", action="store_true", help="search section without the two-batches-in-flight lines")
     ap.add_argument("--search-queries", type=int, default=2000)
     ap.add_argument("--search-subjects", type=int, default=500_000)
     ap.add_argument("--nn-search", action="store_true",
@@ -239,7 +240,7 @@ def run_search(a, dev):
     from saber_gb300.search import SearchPool
     qc, _, _ = synth.protein_db(a.seed + 503, a.search_queries, 1, reversed_frac=0.25, identity_range=(0.3, 0.6))
     batches = [(qb.codes, qb.offsets), (qc.codes, qc.offsets)]
-    pool = SearchPool(sb.codes, sb.offsets, SearchParams("default"), slots=2)
+    pool = None if a.no_pool else SearchPool(sb.codes, sb.offsets, SearchParams("default"), slots=2)
 
     def pooled(reps=3):
         pool.raw_batches(batches)
@@ -250,18 +251,20 @@ def run_search(a, dev):
             ts.append(time.perf_counter() - t)
         return res, float(np.median(ts))
 
-    pres, pt = pooled()
     nq2 = sum(len(b[1]) - 1 for b in batches)
-    out["plain"]["two_batches_in_flight"] = {
-        "value": round(nq2 / pt, 1), "queries": nq2,
-        "same_hits_as_single_handle": bool(keyset(pres[0][0]) == keyset(plain))}
+    if not a.no_pool:
+        pres, pt = pooled()
+        out["plain"]["two_batches_in_flight"] = {
+            "value": round(nq2 / pt, 1), "queries": nq2,
+            "same_hits_as_single_handle": bool(keyset(pres[0][0]) == keyset(plain))}
     if not triage:
         return out
-    for se_ in pool.searchers:
-        se_.dev.set_triage(model, thr)
-    tres, tpt = pooled()
-    for se_ in pool.searchers:
-        se_.dev.set_triage(None)
+    if not a.no_pool:
+        for se_ in pool.searchers:
+            se_.dev.set_triage(model, thr)
+        tres, tpt = pooled()
+        for se_ in pool.searchers:
+            se_.dev.set_triage(None)
     dev.set_triage(model, thr)
     try:
         call()
@@ -274,9 +277,7 @@ def run_search(a, dev):
         "triage": {"value": round(nq / tt, 1), "regions_scored": ct["regions"], "regions_dropped": ct["triage_dropped"],
                    "banded_cells": ct["banded_cells"], "hits_kept": kept, "hits_plain": total,
                    "kept_frac": round(kept / max(total, 1), 5), "lost_hit_rate": round(1 - kept / max(total, 1), 5),
-                   "threshold": round(thr, 4), "stages_ms": {k: round(ct[k], 1) for k in stages},
-                   "two_batches_in_flight": {"value": round(nq2 / tpt, 1), "queries": nq2,
-                                             "same_hits_as_single_handle": bool(keyset(tres[0][0]) == kt_)}},
+                   "threshold": round(thr, 4), "stages_ms": {k: round(ct[k], 1) for k in stages}},
         "speedup": round(tp / tt, 3),
         "training": {"regions": int(y.size), "positives": int(y.sum()), "steps": st["steps"],
                      "final_loss": round(st["final_loss"], 5), "pos_weight": round(st["pos_weight"], 2),
@@ -284,6 +285,9 @@ def run_search(a, dev):
                      "data": "separately seeded database (%d queries x %d subjects)" % (len(qa.offsets) - 1,
                                                                                           len(sa.offsets) - 1)},
     })
+    if not a.no_pool:
+        out["triage"]["two_batches_in_flight"] = {"value": round(nq2 / tpt, 1), "queries": nq2,
+                                                  "same_hits_as_single_handle": bool(keyset(tres[0][0]) == kt_)}
     return out
 
 
