@@ -129,7 +129,7 @@ struct saber_gpu {
     // captured scoring graphs (saber_gpu_score_band_jobs with graphs on)
     bool use_graphs = true;
     uint64_t graph_captures = 0;
-    saber::DevBuf g_nreal;
+    saber::DevBuf g_nreal, g_wmax;
     std::vector<std::pair<saber::GraphKey, saber::GraphEntry>> graphs;
     // the handle's scheme and dataset (set_scheme / load_db / load_queries)
     saber::Scheme scheme;

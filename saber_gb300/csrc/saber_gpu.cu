@@ -60,6 +60,22 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
     }
 }
 
+// Widest clipped band of the jobs that reference a loaded query.
+__global__ void k_job_wmax(const saber_band_job* __restrict__ jobs, uint64_t njobs,
+                           const uint64_t* __restrict__ qoffs, uint32_t nq, unsigned long long* __restrict__ wmax) {
+    unsigned long long wm = 0;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
+        const saber_band_job j = jobs[t];
+        if (j.query >= nq) continue;
+        int64_t lo = j.band_lo, hi = j.band_hi;
+        const int64_t w = clip_band((int64_t)(qoffs[j.query + 1] - qoffs[j.query]), j.win_len, lo, hi);
+        wm = max(wm, (unsigned long long)w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+    if ((threadIdx.x & 31) == 0 && wm) atomicMax(wmax, wm);
+}
+
 // stats layout (uint64): 0 cells, 1 wmax of the R-row class, 2 wmax of the
 //   int32 class, 3 bad job count, 4 cells of the packed classes, 5 wmax of
 //   the 8-row class
@@ -1209,32 +1225,23 @@ int saber_gpu_score_band_jobs(saber_gpu* h, const saber_band_job* jobs, uint64_t
     }
     int rc;
     if (h->use_graphs) {
-        // the widest clipped band sizes the graph's scratch (host cores)
+        // the widest clipped band sizes the graph's scratch: one reduction on
+        // the device after the copy, 8 bytes read back
         const QuerySet& qs = h->main.qs;
-        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        const uint64_t nt = std::max<uint64_t>(1, std::min<uint64_t>(hw, (njobs + 65535) / 65536));
-        std::vector<uint64_t> part(nt, 0);
-        auto scan_w = [&](uint64_t k) {
-            uint64_t wm = 0;
-            for (uint64_t t = k * njobs / nt; t < (k + 1) * njobs / nt; t++) {
-                const saber_band_job& j = jobs[t];
-                if (j.query >= qs.nq) continue;
-                int64_t lo = j.band_lo, hi = j.band_hi;
-                const int64_t w = clip_band((int64_t)(qs.offs[j.query + 1] - qs.offs[j.query]), j.win_len, lo, hi);
-                wm = std::max<uint64_t>(wm, (uint64_t)w);
-            }
-            part[k] = wm;
-        };
-        std::vector<std::thread> th;
-        for (uint64_t k = 1; k < nt; k++) th.emplace_back(scan_w, k);
-        scan_w(0);
-        for (auto& x : th) x.join();
-        uint64_t wmax = 0;
-        for (uint64_t v : part) wmax = std::max(wmax, v);
         const uint64_t npad = pow2_at_least(njobs, 1 << 12);
         CUALLOC(h, h->jobs_dev, npad * sizeof(saber_band_job));
         CUALLOC(h, h->scores_dev, npad * 4);
+        CUALLOC(h, h->g_wmax, 8);
         CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice, h->stream));
+        CU(h, cudaMemsetAsync(h->g_wmax.p, 0, 8, h->stream));
+        if (qs.has)
+            k_job_wmax<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, h->stream>>>(
+                h->jobs_dev.as<saber_band_job>(), njobs, qs.offsets.as<uint64_t>(), qs.nq,
+                h->g_wmax.as<unsigned long long>());
+        CU(h, cudaGetLastError());
+        unsigned long long wmax = 0;
+        CU(h, cudaMemcpyAsync(&wmax, h->g_wmax.p, 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(h, cudaStreamSynchronize(h->stream));
         rc = score_pipeline_graph(h, h->scheme, h->main, njobs, wmax, stats);
     } else {
         CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
