@@ -418,20 +418,44 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
     __stcg(pbuf + (size_t)wmax * 32, c.neg2);
 
     uint32_t best = 0;
-    const int gend = wmax + 2 * R;
+    const int gfull = wmax + 2 * R;
     for (int t = 0; t < nsmax; t++) {
         const HalfStrip ha = half_strip(J, t, 2 * R);
         const int16_t* hb_rows = ha.rows + R;
-        StripState<R> st;
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            st.Hd[r] = c.neg2;
-            st.X[r] = c.neg2;
+        // Step g reads window column col0 + g in the low half and col0 + g - 1
+        // in the high half.  As in the two-job lanes, the warp sweeps only the
+        // steps that reach a window column of one of its jobs, a late start
+        // being = 1 (mod 4) past the triangle, from H = 0 rows, with the
+        // boundary entries of the skipped steps set as those steps would set
+        // them.
+        int s_lo = 1 << 30, s_hi = -1;
+        if (ha.n > 0) {
+            const int a0 = max(0, -ha.col0 - 1), a1 = min(gfull - 1, ha.n - ha.col0);
+            if (a0 <= a1) {
+                s_lo = a0;
+                s_hi = a1;
+            }
         }
-        uint32_t diag0 = __byte_perm(__ldcg(pbuf), c.neg2, 0x5410);
-        uint32_t lastH = c.neg2, lastY = c.neg2;
+        const int w_lo = __reduce_min_sync(0xffffffffu, s_lo), w_hi = __reduce_max_sync(0xffffffffu, s_hi);
+        int g0 = 0, gend = gfull;
+        if (w_hi >= 0 && w_lo <= w_hi) {
+            g0 = ((w_lo - 1) & ~3) + 1;  // largest value = 1 (mod 4) not above w_lo
+            if (g0 < 2 * R + 1) g0 = 0;
+            gend = w_hi + 1 < gfull ? w_hi + 1 : gfull;
+        }
+        StripState<R> st;
+        uint32_t diag0, lastH, lastY;
         PairPipe<R> p;
-        {
+        int g;
+        if (g0 == 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                st.Hd[r] = c.neg2;
+                st.X[r] = c.neg2;
+            }
+            diag0 = __byte_perm(__ldcg(pbuf), c.neg2, 0x5410);
+            lastH = c.neg2;
+            lastY = c.neg2;
             p.w = code_word(ha, 0);
             p.w2 = code_word(ha, 4);
             const int ca0 = (int)(p.w & 0xFFu);
@@ -439,11 +463,33 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)kSentCode * ha.mpad);
             p.nxt.top.x = __ldcg(pbuf + 32);
             p.cprev = ca0;
+            PairTriangle<R, 2 * R>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
+            g = 2 * R + 1;
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                st.Hd[r] = 0u;
+                st.X[r] = c.neg2;
+            }
+            const int kskip = min(g0 - 2 * R, wmax);
+            for (int k = 0; k < kskip; k++) __stcg(pbuf + (size_t)k * 32, top0);
+            diag0 = 0u;
+            lastH = 0u;
+            lastY = c.neg2;
+            // code words of the groups holding steps g0 - 1 .. g0 + 2 and the next
+            p.w = code_word(ha, g0 - 1);
+            p.w2 = code_word(ha, g0 + 3);
+            const int ca0 = (int)((p.w >> 8) & 0xFFu);  // step g0 (= 1 mod 4)
+            const int cb0 = (int)(p.w & 0xFFu);         // the high half's: the low half's at g0 - 1
+            ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
+            ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb0 * ha.mpad);
+            p.nxt.top.x = __ldcg(pbuf + (size_t)(g0 + 1 <= wmax ? g0 + 1 : wmax) * 32);
+            p.cprev = ca0;
+            g = g0;
         }
-        PairTriangle<R, 2 * R>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
-        int g = 2 * R + 1;
-        // (g + 1) & 3 runs 2, 3, 0, 1 from g = 2R + 1 (R a multiple of 4)
-        for (; g + 4 <= wmin; g += 4) {
+        const int gmid = wmin < gend ? wmin : gend;
+        // (g + 1) & 3 runs 2, 3, 0, 1 from g = 1 (mod 4) (R a multiple of 4)
+        for (; g + 4 <= gmid; g += 4) {
             pair_advance<R, 2>(p, ha, hb_rows, pbuf, g, wmax);
             pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g, p.cur, c, best, 0, 0);
             pair_advance<R, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
@@ -531,28 +577,81 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         __stcg(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
 
         uint32_t best = 0;
+        const int ufull = wmax + R - 1;
         for (int t = 0; t < nsmax; t++) {
             const HalfStrip ha = half_strip(A, t, R), hb = half_strip(B, t, R);
-            StripState<R> st;
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                st.Hd[r] = c.neg2;
-                st.X[r] = c.neg2;
+            // Step u reads window column col0 + u in every row of a half.  The
+            // warp sweeps only the steps that reach a window column of one of
+            // its halves: steps left of column -1 hold sentinel cells only (H =
+            // 0, E and F below zero, whatever came before), steps right of the
+            // last column feed nothing that a later strip reads (its own
+            // columns end R steps earlier).  A sweep that starts late starts
+            // at a multiple of 4 past the left triangle, from H = 0 rows.
+            int s_lo = 1 << 30, s_hi = -1;
+            if (ha.n > 0) {
+                const int a0 = max(0, -ha.col0 - 1), a1 = min(ufull - 1, ha.n - 1 - ha.col0);
+                if (a0 <= a1) {
+                    s_lo = a0;
+                    s_hi = a1;
+                }
             }
-            uint32_t diag0 = __ldcg(mybuf).x;
+            if (hb.n > 0) {
+                const int b0 = max(0, -hb.col0 - 1), b1 = min(ufull - 1, hb.n - 1 - hb.col0);
+                if (b0 <= b1) {
+                    s_lo = min(s_lo, b0);
+                    s_hi = max(s_hi, b1);
+                }
+            }
+            const int w_lo = __reduce_min_sync(0xffffffffu, s_lo), w_hi = __reduce_max_sync(0xffffffffu, s_hi);
+            int u0 = 0, uend = ufull;
+            if (w_hi >= 0 && w_lo <= w_hi) {
+                u0 = (w_lo >> 2) << 2;
+                if (u0 < R) u0 = 0;
+                uend = w_hi + 1;
+            }
+            StripState<R> st;
+            uint32_t diag0;
             Pipe<R> p;
-            {
+            int u;
+            if (u0 == 0) {
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    st.Hd[r] = c.neg2;
+                    st.X[r] = c.neg2;
+                }
+                diag0 = __ldcg(mybuf).x;
                 p.wa = code_word(ha, 0);
                 p.wb = code_word(hb, 0);
                 p.wa2 = code_word(ha, 4);
                 p.wb2 = code_word(hb, 4);
                 fetch_step<R>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf, 1);
+                LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
+                u = R;
+            } else {
+                // the skipped columns are sentinel columns: H = 0 to the left
+                // and on the diagonal, E below zero; the boundary entries the
+                // skipped steps would have written get those values too (a
+                // later strip that sweeps from step 0 reads them)
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    st.Hd[r] = 0u;
+                    st.X[r] = c.neg2;
+                }
+                const int kskip = min(u0 - R + 1, wmax);
+                for (int k = 0; k < kskip; k++) __stcg(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
+                diag0 = 0u;
+                p.wa = code_word(ha, u0);
+                p.wb = code_word(hb, u0);
+                p.wa2 = code_word(ha, u0 + 4);
+                p.wb2 = code_word(hb, u0 + 4);
+                fetch_step<R>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf,
+                              u0 + 1 <= wmax ? u0 + 1 : wmax);
+                u = u0;
             }
-            LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
             // middle steps (every row in band for every half), four at a time
             // so that the code bytes are selected at compile time
-            int u = R;
-            for (; u + 4 <= wmin; u += 4) {
+            const int umid = wmin < uend ? wmin : uend;
+            for (; u + 4 <= umid; u += 4) {
                 pipe_advance<R, 1>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
                 pipe_advance<R, 2>(p, ha, hb, mybuf, u + 1, wmax);
@@ -563,7 +662,6 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 strip_step<R, 1, 0>(st, diag0, mybuf, u + 3, p.cur, c, best, 0, 0);
             }
             // the rest, with the right-edge masks (all ones while u < wmin)
-            const int uend = wmax + R - 1;
             for (; u < uend; u++) {
                 pipe_advance<R, -1>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);

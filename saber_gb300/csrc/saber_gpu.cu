@@ -155,8 +155,16 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
             c2++;
             w2 = max(w2, (unsigned long long)w);
         } else {
-            keys[t] = ((uint64_t)cls << 62) | (pair << 61) | ((uint64_t)ns << 48) | ((uint64_t)w << 32) |
-                      (uint64_t)j.query;
+            // within (strips, width): jobs ordered by the first strip's
+            // window geometry (steps before column -1, steps to the last
+            // column), so that a warp's jobs share the step range it sweeps
+            const int64_t srows = pair ? 2 * R : rows;
+            const int64_t col0 = lo + (first / srows) * srows;
+            const int64_t left = col0 < -1 ? -col0 - 1 : 0;
+            const int64_t right = (int64_t)j.win_len - (pair ? 0 : 1) - col0;
+            const uint64_t low = ((uint64_t)(left < 65535 ? left : 65535) << 16) |
+                                 (uint64_t)(right < 0 ? 0 : (right < 65535 ? right : 65535));
+            keys[t] = ((uint64_t)cls << 62) | (pair << 61) | ((uint64_t)ns << 48) | ((uint64_t)w << 32) | low;
             cp += (uint32_t)pair;
             fcells += jc;
             if (cls == 0) {
