@@ -81,6 +81,26 @@ def test_random_band_jobs_match_oracle(tuned, gaps, mode):
     assert st["fast_jobs"] > 0 and st["generic_jobs"] > 0
 
 
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+def test_step_windows_mixed_geometry(tuned, mode):
+    """Wide bands on long queries, windows anywhere in the subject: many
+    strips start far left of their window or end far right of it, with
+    different geometries side by side in a warp (the kernels sweep only the
+    steps that reach a window column of one of the warp's jobs)."""
+    dev = tuned
+    qs, ss, planted = synth.protein_db(61, 30, 400, max_len=1500)
+    bias = synth.query_bias(62, qs)
+    jobs = synth.band_jobs(63, qs, ss, planted, 3000, half_min=40, half_max=600, win_min=10, win_max=2000)
+    dev.strip_rows, dev.pair_steps = mode
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    got, st = dev.score_band_jobs(jobs)
+    want, cells = _oracle_jobs(qs, ss, bias, jobs, B62, 11, 1)
+    assert np.array_equal(got, want), _report(got, want, jobs)
+    assert st["banded_cells"] == cells
+
+
 def test_device_resident_path_matches_host_path(dev):
     torch = pytest.importorskip("torch")
     qs, ss, planted = synth.protein_db(21, 30, 2000)
