@@ -200,6 +200,8 @@ def run_search(a, dev):
         thr = tr.threshold_for_recall(dev.triage_predict(model, rows), y, recall=0.999, margin=0.5)
     qb, sb, _ = synth.protein_db(a.seed + 502, a.search_queries, a.search_subjects, reversed_frac=0.25,
                                  identity_range=(0.3, 0.6))
+    if a.long_steps:
+        dev.long_steps = a.long_steps
     se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default"))
     cpar = se2.cparams()
 

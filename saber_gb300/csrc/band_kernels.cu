@@ -679,6 +679,106 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
     }
 }
 
+// One long job on a warp, int32 (banded_score_i32, banded.rs:134-224): the
+// lanes sweep consecutive strips of kPipeRows rows in a pipeline, lane l on
+// strips first + l, first + l + 32, ..., each kPipeLag steps behind the lane
+// before it.  A strip reads the row above from one boundary row per warp
+// (band index k holds (H, F) of the last row of the latest strip that passed
+// it) and writes its own last row there; kPipeLag > kPipeRows steps of lag
+// put every read after the write it needs, and a round period of at least
+// 31 kPipeLag + kPipeRows + 1 steps does the same for lane 0's next strip.
+// Step u of a strip is window column col0 + u in every row (row r at band
+// index u - r); a strip sweeps only the steps of window columns.  Cells
+// outside the band, the window or the query are NEG (the reference's
+// kmin / kmax), the diagonal of column 0 is 0 and row 0 has no F.
+constexpr int kPipeRows = 8;
+constexpr int kPipeLag = kPipeRows + 1;
+
+__device__ __forceinline__ void band_pipe_job(const int16_t* __restrict__ qprof, int64_t mpad,
+                                              const uint8_t* __restrict__ s, int m, int nn, int lo, int w,
+                                              int first, int last, int go, int ge, int2* __restrict__ buf,
+                                              int lane, int32_t& best_out) {
+    const int NEG = INT32_MIN / 4;
+    constexpr int RR = kPipeRows;
+    const int s0 = first / RR, ns = last / RR - s0 + 1;
+    for (int k = lane; k <= w; k += 32) buf[k] = make_int2(NEG, NEG);
+    // each strip's steps: window columns [0, nn) only
+    auto ustart = [&](int st) { const int c0 = lo + st * RR; return c0 < 0 ? -c0 : 0; };
+    auto uend = [&](int st) {  // exclusive
+        const int c0 = lo + st * RR;
+        const int e = nn - c0;
+        return e < w + RR - 1 ? e : w + RR - 1;
+    };
+    int lmax = 1;
+    for (int st = s0 + lane; st < s0 + ns; st += 32) lmax = max(lmax, uend(st) - ustart(st));
+    lmax = __reduce_max_sync(0xffffffffu, lmax);
+    const int P = max(lmax, 31 * kPipeLag + RR + 1);
+    const int rounds = (ns + 31) / 32;
+    const long long T = (long long)(rounds - 1) * P + 31 * kPipeLag + lmax;
+    __syncwarp();
+    int Hl[RR], El[RR];
+    int best = 0;
+    int u = 0, ue = 0, i0 = 0, col0 = 0;
+    int diag0 = NEG;
+    int c = -lane * kPipeLag, st = s0 + lane;  // this lane's count within its round, and its strip
+    for (long long tg = 0; tg < T; tg++) {
+        if (c == 0 && st < s0 + ns) {
+            i0 = st * RR;
+            col0 = lo + i0;
+            u = ustart(st);
+            ue = uend(st);
+#pragma unroll
+            for (int r = 0; r < RR; r++) {
+                Hl[r] = NEG;
+                El[r] = NEG;
+            }
+            diag0 = buf[u < w ? u : w].x;
+        }
+        const bool act = c >= 0 && st < s0 + ns && u < ue;
+        if (act) {
+            const int j = col0 + u;
+            const bool colok = j >= 0 && j < nn;
+            const int code = colok ? s[j] : 0;
+            int sub[RR];
+            {
+                const uint4 pv = *reinterpret_cast<const uint4*>(qprof + (size_t)code * mpad + i0);
+                const uint32_t wv[4] = {pv.x, pv.y, pv.z, pv.w};
+#pragma unroll
+                for (int r = 0; r < RR; r++) sub[r] = (int)(int16_t)((wv[r >> 1] >> (16 * (r & 1))) & 0xFFFFu);
+            }
+            const int2 top = buf[u + 1 < w ? u + 1 : w];  // entry w stays NEG
+            int Hup = top.x, Fup = top.y;
+            int diag = diag0;
+            diag0 = top.x;  // the next step's diagonal of row 0: this step's row above
+#pragma unroll
+            for (int r = 0; r < RR; r++) {
+                const int k = u - r, i = i0 + r;
+                const bool valid = colok && k >= 0 && k < w && i < m;
+                const int F = i >= 1 ? max(Hup - go, Fup - ge) : NEG;
+                const int d = (i >= 1 && j >= 1) ? diag : 0;
+                const int E = max(Hl[r] - go, El[r] - ge);
+                int H = max(max(d + sub[r], E), max(F, 0));
+                const int hold = Hl[r];
+                Hl[r] = valid ? H : NEG;
+                El[r] = valid ? E : NEG;
+                Hup = Hl[r];
+                Fup = valid ? F : NEG;
+                diag = hold;
+                if (valid) best = max(best, H);
+            }
+            const int kl = u - RR + 1;
+            if (kl >= 0 && kl < w) buf[kl] = make_int2(Hup, Fup);
+            u++;
+        }
+        __syncwarp();
+        if (++c == P) {  // next round: strip + 32
+            c = 0;
+            st += 32;
+        }
+    }
+    best_out = __reduce_max_sync(0xffffffffu, best);
+}
+
 // int32 banded scoring, one warp per job (banded_score_i32, banded.rs:134-224,
 // the recurrence of the reference's scalar kernel): narrow bands, the jobs
 // whose strip sweep in one lane would be long, and int16 results at the
@@ -720,6 +820,20 @@ __global__ void __launch_bounds__(128) k_band_generic(
         const int16_t* qprof = prof + prof_off[q];
         const int64_t mpad = prof_mpad[q];
         const uint8_t* s = res + jj.win_begin;
+        {
+            // long jobs: strips pipelined over the lanes
+            const int64_t first = hi < 0 ? -hi : 0;
+            int64_t last = nn - 1 - lo;
+            if (last > m - 1) last = m - 1;
+            if (w >= 32 && last / kPipeRows - first / kPipeRows + 1 >= 8) {
+                int32_t b;
+                band_pipe_job(qprof, mpad, s, (int)m, (int)nn, (int)lo, w, (int)first, (int)last, go, ge,
+                              reinterpret_cast<int2*>(base_hp), lane, b);
+                if (lane == 0) scores[jid] = b;
+                __syncwarp();
+                continue;
+            }
+        }
         int32_t* hp = base_hp;
         int32_t* fp = hp + slab_stride;
         int32_t* hc = fp + slab_stride;

@@ -147,7 +147,13 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
         if (cls != 2 && (w >= (1 << 16) || ns >= (1 << 13))) cls = 2;
         // a sweep longer than long_steps column steps in one lane goes to the
         // warp-per-job int32 kernel
-        if (cls != 2 && (uint64_t)ns * (uint64_t)(w + (pair ? 2 * R : rows) - 1) > long_steps) cls = 2;
+        if (cls != 2) {
+            // the sweep's steps per strip: the band's, or the window's when
+            // the band is wider (the kernels sweep window columns only)
+            const int64_t srw = pair ? 2 * R : rows;
+            const int64_t span = w + srw - 1 < (int64_t)j.win_len + srw ? w + srw - 1 : (int64_t)j.win_len + srw;
+            if ((uint64_t)ns * (uint64_t)span > long_steps) cls = 2;
+        }
         if (cls == 2) {
             // largest first, so that the warps' static share ends together
             const uint64_t sz = jc >> 4 < 0x7FFFFFFFull ? jc >> 4 : 0x7FFFFFFFull;

@@ -101,6 +101,30 @@ def test_step_windows_mixed_geometry(tuned, mode):
     assert st["banded_cells"] == cells
 
 
+@pytest.mark.parametrize("long_steps", [0, 3000])
+def test_long_job_kernels_match_oracle(tuned, long_steps):
+    """Jobs routed away from the int16 lanes (every job, or the long ones):
+    the warp-per-job int32 kernel, rows in parallel for short jobs and strips
+    pipelined over the lanes for long ones, bit-exact with the oracle."""
+    dev = tuned
+    qs, ss, planted = synth.protein_db(71, 30, 400, max_len=1500)
+    bias = synth.query_bias(72, qs)
+    jobs = np.concatenate([
+        synth.band_jobs(73, qs, ss, planted, 1500, half_min=1, half_max=200),
+        synth.band_jobs(74, qs, ss, planted, 500, half_min=40, half_max=900, win_min=10, win_max=2000)])
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    try:
+        dev.long_steps = long_steps
+        got, st = dev.score_band_jobs(jobs)
+    finally:
+        dev.long_steps = 0xFFFFFFFF
+    want, cells = _oracle_jobs(qs, ss, bias, jobs, B62, 11, 1)
+    assert np.array_equal(got, want), _report(got, want, jobs)
+    assert st["banded_cells"] == cells and st["generic_jobs"] > 0
+
+
 def test_device_resident_path_matches_host_path(dev):
     torch = pytest.importorskip("torch")
     qs, ss, planted = synth.protein_db(21, 30, 2000)
