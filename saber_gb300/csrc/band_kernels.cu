@@ -40,6 +40,11 @@
 
 namespace saber {
 
+// Boundary-row stores: plain write-back stores, so that the lane's later
+// loads of the same entries (cached in L1) see them.
+template <class T>
+__device__ __forceinline__ void stbuf(T* p, T v) { *p = v; }
+
 __device__ __forceinline__ uint32_t pk2(int v) { return (uint32_t)(uint16_t)(int16_t)v * 0x10001u; }
 __device__ __forceinline__ int lo16(uint32_t v) { return (int)(int16_t)(v & 0xFFFFu); }
 __device__ __forceinline__ int hi16(uint32_t v) { return (int)(int16_t)(v >> 16); }
@@ -178,7 +183,7 @@ __device__ __forceinline__ void fetch_step(StepLoads<R>& L, const HalfStrip& ha,
         L.a[0] = __ldg(reinterpret_cast<const uint4*>(pa));
         L.b[0] = __ldg(reinterpret_cast<const uint4*>(pb));
     }
-    L.top = __ldcg(buf + (size_t)kin * 32);  // boundary rows live in L2, not L1
+    L.top = __ldca(buf + (size_t)kin * 32);  // boundary rows: the lane's own writes, cached in L1
 }
 
 template <int R>
@@ -230,7 +235,7 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
         else if (r == R - 1 || (MODE == 0 && r == U)) best = __vimax_s16x2_relu(best, H);
         else hprev = H;
     }
-    if (MODE != 0 || U == R - 1) __stcg(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Yup));
+    if (MODE != 0 || U == R - 1) stbuf(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Yup));
 }
 
 // The pipelined column loop state of one strip: the loads of step u + 1 are
@@ -312,7 +317,7 @@ __device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha
     const int kin = g + 2 <= wmax ? g + 2 : wmax;
     ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca * ha.mpad);
     ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb * ha.mpad);
-    p.nxt.top.x = __ldcg(pbuf + (size_t)kin * 32);
+    p.nxt.top.x = __ldca(pbuf + (size_t)kin * 32);
 }
 
 // One step g of a super-strip.  PH 0: compile-time step G <= 2R (low rows
@@ -353,7 +358,7 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
     }
     lastH = Hup;
     lastY = Yup;
-    if (g >= 2 * R) __stcg(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Hup, Yup, 0x7632));
+    if (g >= 2 * R) stbuf(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Hup, Yup, 0x7632));
 }
 
 template <int R, int G>
@@ -414,8 +419,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
     const int nsmax = __reduce_max_sync(0xffffffffu, J.ns);
     if (!has) J.w = wmin;
     const uint32_t top0 = (uint32_t)(uint16_t)kNeg16 << 16;  // H = 0, F + go unreachable
-    for (int k = 0; k < wmax; k++) __stcg(pbuf + (size_t)k * 32, top0);
-    __stcg(pbuf + (size_t)wmax * 32, c.neg2);
+    for (int k = 0; k < wmax; k++) stbuf(pbuf + (size_t)k * 32, top0);
+    stbuf(pbuf + (size_t)wmax * 32, c.neg2);
 
     uint32_t best = 0;
     const int gfull = wmax + 2 * R;
@@ -453,7 +458,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
                 st.Hd[r] = c.neg2;
                 st.X[r] = c.neg2;
             }
-            diag0 = __byte_perm(__ldcg(pbuf), c.neg2, 0x5410);
+            diag0 = __byte_perm(__ldca(pbuf), c.neg2, 0x5410);
             lastH = c.neg2;
             lastY = c.neg2;
             p.w = code_word(ha, 0);
@@ -461,7 +466,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             const int ca0 = (int)(p.w & 0xFFu);
             ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
             ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)kSentCode * ha.mpad);
-            p.nxt.top.x = __ldcg(pbuf + 32);
+            p.nxt.top.x = __ldca(pbuf + 32);
             p.cprev = ca0;
             PairTriangle<R, 2 * R>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
             g = 2 * R + 1;
@@ -472,7 +477,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
                 st.X[r] = c.neg2;
             }
             const int kskip = min(g0 - 2 * R, wmax);
-            for (int k = 0; k < kskip; k++) __stcg(pbuf + (size_t)k * 32, top0);
+            for (int k = 0; k < kskip; k++) stbuf(pbuf + (size_t)k * 32, top0);
             diag0 = 0u;
             lastH = 0u;
             lastY = c.neg2;
@@ -483,7 +488,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             const int cb0 = (int)(p.w & 0xFFu);         // the high half's: the low half's at g0 - 1
             ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
             ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb0 * ha.mpad);
-            p.nxt.top.x = __ldcg(pbuf + (size_t)(g0 + 1 <= wmax ? g0 + 1 : wmax) * 32);
+            p.nxt.top.x = __ldca(pbuf + (size_t)(g0 + 1 <= wmax ? g0 + 1 : wmax) * 32);
             p.cprev = ca0;
             g = g0;
         }
@@ -573,8 +578,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         // Boundary of the row above each job's first strip: H = 0 (the
         // reference's hd = 0 on row 0), F + go unreachable; position wmax
         // lies outside every band.
-        for (int k = 0; k < wmax; k++) __stcg(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
-        __stcg(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
+        for (int k = 0; k < wmax; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
+        stbuf(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
 
         uint32_t best = 0;
         const int ufull = wmax + R - 1;
@@ -619,7 +624,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                     st.Hd[r] = c.neg2;
                     st.X[r] = c.neg2;
                 }
-                diag0 = __ldcg(mybuf).x;
+                diag0 = __ldca(mybuf).x;
                 p.wa = code_word(ha, 0);
                 p.wb = code_word(hb, 0);
                 p.wa2 = code_word(ha, 4);
@@ -638,7 +643,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                     st.X[r] = c.neg2;
                 }
                 const int kskip = min(u0 - R + 1, wmax);
-                for (int k = 0; k < kskip; k++) __stcg(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
+                for (int k = 0; k < kskip; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
                 diag0 = 0u;
                 p.wa = code_word(ha, u0);
                 p.wb = code_word(hb, u0);
