@@ -419,11 +419,13 @@ int saber_gpu_set_pair_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
 
 /* Tuning: a job whose sweep in one lane would take more than `steps` column
- * steps (strips x (width + strip rows - 1)) is scored by the warp-per-job
- * int32 kernel instead, so one long job does not set the launch's length;
- * 0xFFFFFFFF (the default) keeps every job on the int16 lanes, the faster
- * choice for large batches; small batches of long jobs gain from a few
- * thousand.  Results do not depend on it.  No reference counterpart. */
+ * steps (strips x the steps of a strip, window columns only) is scored by
+ * the int32 kernel instead, which pipelines a long job's strips over a
+ * warp's lanes, so one long job does not set the launch's length.
+ * 0xFFFFFFFF keeps every job on the int16 lanes (the faster choice for large
+ * batches); 0xFFFFFFFE (the default) picks 2048 for batches smaller than the
+ * lanes' job slots and 0xFFFFFFFF otherwise.  Results do not depend on it.
+ * No reference counterpart. */
 int saber_gpu_set_long_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_long_steps(saber_gpu* h);
 

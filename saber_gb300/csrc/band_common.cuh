@@ -18,7 +18,10 @@ constexpr int kProfPad = 32;
 // Default pairing threshold: a job whose R-row sweep takes more than this
 // many column steps (strips x (width + R - 1)) is swept as paired strips.
 constexpr uint32_t kPairStepsDefault = 2048;
-constexpr uint32_t kLongStepsDefault = 0xFFFFFFFFu;
+constexpr uint32_t kLongStepsNever = 0xFFFFFFFFu;
+constexpr uint32_t kLongStepsAuto = 0xFFFFFFFEu;  // kLongStepsSmall for batches smaller than the lanes' job slots
+constexpr uint32_t kLongStepsSmall = 2048;
+constexpr uint32_t kLongStepsDefault = kLongStepsAuto;
 // Residue code used for positions outside a window or a query: its profile
 // entries are kSent, so such cells never beat a real cell (banded.rs:123-131
 // excludes them; the kernels compute them harmlessly instead of branching).

@@ -238,6 +238,16 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
 // ---------------------------------------------------------------------------
 // the scoring pipeline (device-resident jobs and scores)
 // ---------------------------------------------------------------------------
+// The long-job threshold of a call: in the automatic mode, a batch smaller
+// than the int16 lanes' job slots leaves most lanes idle while its longest
+// sweeps run alone, so sweeps above kLongStepsSmall steps go to the
+// warp-pipelined int32 kernel; larger batches keep every job on the lanes.
+static uint32_t long_steps_for(const saber_gpu* h, uint64_t njobs) {
+    if (h->long_steps != kLongStepsAuto) return h->long_steps;
+    const uint64_t slots = (uint64_t)h->sm_count * band_fast_blocks_per_sm(h->strip_rows) * 256 / 32 * 64;
+    return njobs < slots ? kLongStepsSmall : kLongStepsNever;
+}
+
 static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, const saber_band_job* d_jobs,
                           uint64_t njobs, int32_t* d_scores, saber_score_stats* st) {
     if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
@@ -275,7 +285,8 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, h->long_steps, qs.offsets.as<uint64_t>(), qs.nq, ds.n_res,
+        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, long_steps_for(h, njobs), qs.offsets.as<uint64_t>(), qs.nq,
+        ds.n_res,
         h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
     CU(h, cudaGetLastError());
@@ -453,7 +464,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     key.go = sch.go;
     key.ge = sch.ge;
     key.pair_steps = h->pair_steps;
-    key.long_steps = h->long_steps;
+    key.long_steps = long_steps_for(h, njobs);
     key.n_res = ds.n_res;  // scalar kernel parameters baked into the graph
     key.nq = qs.nq;
     const void* ptrs[16] = {h->jobs_dev.p, h->scores_dev.p, h->keys_in.p, h->keys_out.p, h->vals_in.p,
@@ -477,7 +488,8 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
         chk(cudaMemsetAsync(counts, 0, 16 * 4, s));
         chk(cudaMemsetAsync(stats, 0, 8 * 8, s));
         k_classify<<<nblocks(npad, 256, h->sm_count * 8), 256, 0, s>>>(
-            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, h->long_steps, qs.offsets.as<uint64_t>(), qs.nq,
+            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, long_steps_for(h, njobs),
+            qs.offsets.as<uint64_t>(), qs.nq,
             ds.n_res, h->keys_in.as<uint64_t>(), h->vals_in.as<uint32_t>(), d_scores, counts, stats);
         chk(cudaGetLastError());
         size_t tb = h->cub_tmp.cap;

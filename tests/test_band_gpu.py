@@ -101,7 +101,7 @@ def test_step_windows_mixed_geometry(tuned, mode):
     assert st["banded_cells"] == cells
 
 
-@pytest.mark.parametrize("long_steps", [0, 3000])
+@pytest.mark.parametrize("long_steps", [0, 3000, 0xFFFFFFFF])
 def test_long_job_kernels_match_oracle(tuned, long_steps):
     """Jobs routed away from the int16 lanes (every job, or the long ones):
     the warp-per-job int32 kernel, rows in parallel for short jobs and strips
@@ -115,11 +115,12 @@ def test_long_job_kernels_match_oracle(tuned, long_steps):
     dev.set_scheme(B62, 11, 1)
     dev.load_db(ss.codes, ss.offsets)
     dev.load_queries(qs.codes, qs.offsets, bias)
+    keep = dev.long_steps
     try:
         dev.long_steps = long_steps
         got, st = dev.score_band_jobs(jobs)
     finally:
-        dev.long_steps = 0xFFFFFFFF
+        dev.long_steps = keep
     want, cells = _oracle_jobs(qs, ss, bias, jobs, B62, 11, 1)
     assert np.array_equal(got, want), _report(got, want, jobs)
     assert st["banded_cells"] == cells and st["generic_jobs"] > 0
