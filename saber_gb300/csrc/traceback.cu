@@ -156,7 +156,11 @@ __global__ void __launch_bounds__(128) k_band_align_warp(const AlignReq* __restr
             int prevH = NEG, prevE = NEG;  // H and E at k - 1 for lane 0 (carry)
             int rowbest = 0;
             int64_t rowk = 0;
-            for (int64_t c0 = 0; c0 < w; c0 += 32) {
+            // only the chunks that hold the row's window cells: the next row
+            // reads this row's H and F at its own cells' k and k + 1, inside
+            // [kmin - 1, kmax + 1]; at kmin - 1 only as the diagonal of column
+            // 0, which is 0 by rule, and entry w stays NEG
+            for (int64_t c0 = (kmin / 32) * 32; c0 <= kmax; c0 += 32) {
                 const int64_t k = c0 + lane;
                 const bool inb = k < w;
                 const bool valid = inb && k >= kmin && k <= kmax;
