@@ -48,6 +48,7 @@ def parse():
                     help="only the batched-search section (printed as its own JSON line)")
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
     ap.add_argument("--no-pool", action="store_true", help="search section without the two-batches-in-flight lines")
+    ap.add_argument("--no-masking", action="store_true", help="search section without the tantan masking line")
     ap.add_argument("--search-queries", type=int, default=2000)
     ap.add_argument("--search-subjects", type=int, default=500_000)
     ap.add_argument("--nn-search", action="store_true",
@@ -192,7 +193,7 @@ def run_search(a, dev):
     if triage:
         qa, sa, _ = synth.protein_db(a.seed + 501, max(a.search_queries // 2, 1), max(a.search_subjects * 2 // 5, 1),
                                      reversed_frac=0.25, identity_range=(0.3, 0.6))
-        se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default"))
+        se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default", masking="none"))
         rows, y, _ = tr.collect(se, qa.codes, qa.offsets)
         t1 = time.perf_counter()
         model, st = tr.train(dev, rows, y, seed=a.seed + 1)
@@ -202,7 +203,7 @@ def run_search(a, dev):
                                  identity_range=(0.3, 0.6))
     if a.long_steps:
         dev.long_steps = a.long_steps
-    se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default"))
+    se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default", masking="none"))
     cpar = se2.cparams()
 
     def call():
@@ -242,7 +243,7 @@ def run_search(a, dev):
     from saber_gb300.search import SearchPool
     qc, _, _ = synth.protein_db(a.seed + 503, a.search_queries, 1, reversed_frac=0.25, identity_range=(0.3, 0.6))
     batches = [(qb.codes, qb.offsets), (qc.codes, qc.offsets)]
-    pool = None if a.no_pool else SearchPool(sb.codes, sb.offsets, SearchParams("default"), slots=2)
+    pool = None if a.no_pool else SearchPool(sb.codes, sb.offsets, SearchParams("default", masking="none"), slots=2)
 
     def pooled(reps=3):
         pool.raw_batches(batches)
@@ -254,6 +255,8 @@ def run_search(a, dev):
         return res, float(np.median(ts))
 
     nq2 = sum(len(b[1]) - 1 for b in batches)
+    if not a.no_masking:
+        out["masking"] = run_masking(a, dev, sb, qb)
     if not a.no_pool:
         pres, pt = pooled()
         out["plain"]["two_batches_in_flight"] = {
@@ -291,6 +294,58 @@ def run_search(a, dev):
         out["triage"]["two_batches_in_flight"] = {"value": round(nq2 / tpt, 1), "queries": nq2,
                                                   "same_hits_as_single_handle": bool(keyset(tres[0][0]) == kt_)}
     return out
+
+
+def run_masking(a, dev, sb, qb):
+    """Tantan seed masking (masking.rs) on the GPU: the search's database
+    masked on the device (saber_gpu_tantan_mask_db, as the reference's scan
+    database recomputes it) and the query batch through the C ABI with host
+    buffers; the oracle's scalar C restatement on one host core over a
+    bounded sample of the queries is the CPU baseline, and the GPU masks of
+    that sample must equal the oracle's."""
+    from oracle import oracle as orc
+    from saber_gb300 import masking, scoring
+    P = masking.TantanParams()
+    b62 = scoring.matrix("BLOSUM62")
+
+    def med(f, reps=3):
+        f()
+        ts, r = [], None
+        for _ in range(reps):
+            t = time.perf_counter()
+            r = f()
+            ts.append(time.perf_counter() - t)
+        return r, float(np.median(ts))
+
+    (n_db, lam), tdb = med(lambda: dev.tantan_mask_db(P, b62))
+    dev.load_db_mask(None)
+    (qm, _, n_q, _), tq = med(lambda: dev.tantan_mask(P, b62, qb.codes, qb.offsets))
+    # CPU sample: whole queries until about cpu_seconds / 4 of oracle work
+    t0, k = time.perf_counter(), 0
+    offs = qb.offsets.astype(np.int64)
+    budget = max(a.cpu_seconds / 4, 0.5)
+    parts = []
+    while k < len(offs) - 1 and time.perf_counter() - t0 < budget:
+        k1 = min(k + 64, len(offs) - 1)
+        parts.append(orc.tantan_mask(qb.codes[offs[k]:offs[k1]], offs[k:k1 + 1] - offs[k], b62)[0])
+        k = k1
+    tc = time.perf_counter() - t0
+    om = np.concatenate(parts)
+    nres_db, nres_q = int(sb.codes.size), int(qb.codes.size)
+    return {
+        "workload": "tantan protein defaults (r 0.005, e 0.05, W 50, d 0.9, BLOSUM62, lambda %.17g), posterior >= "
+                    "0.5" % lam,
+        "unit": "residues/s", "timing": "median of 3 calls, host wall clock",
+        "database": {"residues": nres_db, "subjects": int(len(sb.offsets) - 1), "masked": n_db,
+                     "ms": round(tdb * 1e3, 2), "value": round(nres_db / tdb, 1)},
+        "queries": {"residues": nres_q, "queries": int(len(qb.offsets) - 1), "masked": n_q,
+                    "ms": round(tq * 1e3, 2), "value": round(nres_q / tq, 1),
+                    "e2e": "host codes in, host mask out"},
+        "cpu_baseline": {"value": round(int(offs[k]) / tc, 1), "unit": "residues/s", "cores": 1, "kind": "port",
+                         "sample": "first %d queries (%d residues, %.1f s), oracle scalar C restatement of "
+                                   "masking.rs compute_body" % (k, int(offs[k]), tc)},
+        "gpu_equals_oracle_on_sample": bool(np.array_equal(qm[:offs[k]], om)),
+    }
 
 
 def run_nn_search(a, local_rank):

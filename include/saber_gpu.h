@@ -184,6 +184,42 @@ typedef struct {
  * scan.rs:123-141 applies them).  NULL clears the mask. */
 int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residues);
 
+/* ---- tantan seed masking (masking.rs) -----------------------------------------
+ *
+ * Tantan's HMM (Frith 2011): posterior probability that each residue lies in
+ * a tandem repeat, from a scaled forward-backward pass in f32 that rounds
+ * every operation as the reference's scalar body does (masking.rs:429-529);
+ * positions with posterior >= min_prob are masked from seeding.  Model
+ * parameters follow TantanParams (masking.rs:36-49); lambda <= 0 derives it
+ * from the matrix (implied_lambda, masking.rs:531-583). */
+typedef struct {
+    double repeat_start;  /* r, default 0.005 */
+    double repeat_end;    /* e, default 0.05 */
+    uint32_t max_period;  /* W repeat states, default 50, at most 64 */
+    uint32_t pad_;
+    double decay;         /* d, default 0.9 */
+    double min_prob;      /* mask threshold, default 0.5 */
+    double lambda;        /* <= 0: implied by the matrix */
+} saber_tantan_params;
+
+/* The lambda implied by a 24x24 matrix (its 20 standard letters); NaN when
+ * no root exists.  Host only (masking.rs:531-583). */
+double saber_tantan_implied_lambda(const int32_t* matrix576);
+/* Tantan::mask over a batch of sequences (masking.rs:191-196), computed on
+ * the GPU: codes / offsets[nseq + 1] on the host; mask[i] = 1 where the
+ * posterior >= min_prob (indexed like codes); probs (NULL = not wanted)
+ * receives the posteriors.  *n_masked = masked positions; *lambda_out
+ * (nullable) = the lambda used.  The reference masks queries with BLOSUM62
+ * (engine.rs:575-577). */
+int saber_gpu_tantan_mask(saber_gpu* h, const saber_tantan_params* params, const int32_t* matrix576,
+                          const uint8_t* codes, const uint64_t* offsets, uint64_t nseq, uint8_t* mask,
+                          float* probs, uint64_t* n_masked, double* lambda_out);
+/* Masks the loaded database on the device and installs the result as its
+ * seed mask (as saber_gpu_load_db_mask would): the reference's scan database
+ * with tantan recomputed (scan.rs:1078-1123). */
+int saber_gpu_tantan_mask_db(saber_gpu* h, const saber_tantan_params* params, const int32_t* matrix576,
+                             uint64_t* n_masked, double* lambda_out);
+
 /* Engine::search_scan's candidate regions for the loaded query set against
  * the loaded database (scan.rs:1261-1497 up to the per-query candidate cap):
  * seed tables of the batch, database scan with the window filter,

@@ -165,6 +165,28 @@ int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsu
 /* auto_occ_cap (src/search/index.rs:329-336). */
 uint64_t orc_auto_occ_cap(uint64_t total, uint64_t ncodes, uint64_t db_residues, uint64_t ref_residues);
 
+/* ---- tantan seed masking (oracle/tantan.c) ---- */
+
+/* TantanParams (masking.rs:36-49); defaults 0.005, 0.05, 50, 0.9, 0.5. */
+typedef struct {
+    double repeat_start, repeat_end;
+    uint32_t max_period;
+    double decay, min_prob;
+} orc_tantan_params;
+
+/* implied_lambda (masking.rs:531-583); NaN when no root is found. */
+double orc_tantan_lambda(const int32_t* matrix576);
+/* Tantan::with_params tables (masking.rs:162-179); returns the lambda used. */
+double orc_tantan_tables(const int32_t* matrix576, const orc_tantan_params* p, double lambda, float* lr768,
+                         float* b2f);
+/* compute_body (masking.rs:429-529) for one sequence. */
+int orc_tantan_probs(const uint8_t* seq, size_t n, const float* lr768, const float* b2f, const orc_tantan_params* p,
+                     float* post);
+/* Tantan::mask (masking.rs:191-196) over offsets[nseq + 1]; returns the
+ * number of masked positions (-1 on allocation failure). */
+int64_t orc_tantan_mask(const uint8_t* codes, const uint64_t* offsets, uint64_t nseq, const int32_t* matrix576,
+                        const orc_tantan_params* p, double lambda, uint8_t* mask, float* probs);
+
 #ifdef __cplusplus
 }
 #endif

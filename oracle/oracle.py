@@ -232,3 +232,53 @@ def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, 
     if n < 0:
         raise MemoryError("region buffer too small")
     return out[:n].copy(), {k: int(getattr(ctr, k)) for k, _ in ctr._fields_}
+
+
+class TantanParams(ctypes.Structure):
+    """TantanParams (masking.rs:36-49) with tantan's protein defaults."""
+    _fields_ = [("repeat_start", ctypes.c_double), ("repeat_end", ctypes.c_double), ("max_period", ctypes.c_uint32),
+                ("decay", ctypes.c_double), ("min_prob", ctypes.c_double)]
+
+    def __init__(self, repeat_start=0.005, repeat_end=0.05, max_period=50, decay=0.9, min_prob=0.5):
+        super().__init__(repeat_start, repeat_end, max_period, decay, min_prob)
+
+
+def tantan_lambda(matrix):
+    """implied_lambda (masking.rs:531-583); NaN when no root exists."""
+    f = lib().orc_tantan_lambda
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_void_p]
+    m = _a(np.asarray(matrix).reshape(576), np.int32)
+    return float(f(_p(m)))
+
+
+def tantan_tables(matrix, params=None, lam=0.0):
+    """Tantan::with_params (masking.rs:162-179) -> (lambda, lr float32[24][32], b2f float32[W])."""
+    p = params or TantanParams()
+    f = lib().orc_tantan_tables
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    m = _a(np.asarray(matrix).reshape(576), np.int32)
+    lr = np.zeros(24 * 32, np.float32)
+    b2f = np.zeros(max(1, p.max_period), np.float32)
+    lam = f(_p(m), ctypes.byref(p), float(lam), _p(lr), _p(b2f))
+    return float(lam), lr.reshape(24, 32), b2f
+
+
+def tantan_mask(codes, offsets, matrix, params=None, lam=0.0):
+    """Tantan::mask (masking.rs:191-196) over a batch -> (mask bool array, posteriors float32, masked count)."""
+    p = params or TantanParams()
+    f = lib().orc_tantan_mask
+    f.restype = ctypes.c_int64
+    P = ctypes.c_void_p
+    f.argtypes = [P, P, ctypes.c_uint64, P, P, ctypes.c_double, P, P]
+    c = _a(codes, np.uint8)
+    o = _a(offsets, np.uint64)
+    m = _a(np.asarray(matrix).reshape(576), np.int32)
+    n = int(o[-1]) if o.size else 0
+    mask = np.zeros(max(n, 1), np.uint8)
+    probs = np.zeros(max(n, 1), np.float32)
+    k = f(_p(c), _p(o), max(o.size - 1, 0), _p(m), ctypes.byref(p), float(lam), _p(mask), _p(probs))
+    if k < 0:
+        raise MemoryError("oracle tantan allocation")
+    return mask[:n].astype(bool), probs[:n], int(k)

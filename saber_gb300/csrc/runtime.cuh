@@ -165,6 +165,8 @@ struct saber_gpu {
     saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
     saber::HostBuf pin_reg, pin_src;
     saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
+    // tantan masking scratch
+    saber::DevBuf tt_ord, tt_base, tt_F, tt_BS, tt_count, tt_codes, tt_offs, tt_mask, tt_probs;
     // traceback scratch
     saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
 };

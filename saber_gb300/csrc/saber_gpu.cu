@@ -1137,6 +1137,12 @@ extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx
     (h)->err.clear()
 
 namespace saber {
+double tantan_implied_lambda(const int32_t* m);
+int tantan_mask_host(saber_gpu* h, const saber_tantan_params* p, const int32_t* matrix576, const uint8_t* codes,
+                     const uint64_t* offsets, uint64_t nseq, uint8_t* mask, float* probs, uint64_t* n_masked,
+                     double* lambda_out);
+int tantan_mask_db(saber_gpu* h, const saber_tantan_params* p, const int32_t* matrix576, uint64_t* n_masked,
+                   double* lambda_out);
 // Pinned host staging for the host engine (engine.cpp).
 void* pinned_scratch(saber_gpu* h, int slot, size_t bytes) {
     if (!h || slot < 0 || slot >= 4) return nullptr;
@@ -1507,6 +1513,23 @@ int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residue
     CU(h, cudaStreamSynchronize(h->stream));
     h->has_db_mask = true;
     return SABER_OK;
+}
+
+double saber_tantan_implied_lambda(const int32_t* matrix576) {
+    return matrix576 ? saber::tantan_implied_lambda(matrix576) : NAN;
+}
+
+int saber_gpu_tantan_mask(saber_gpu* h, const saber_tantan_params* params, const int32_t* matrix576,
+                          const uint8_t* codes, const uint64_t* offsets, uint64_t nseq, uint8_t* mask, float* probs,
+                          uint64_t* n_masked, double* lambda_out) {
+    ENTER(h);
+    return saber::tantan_mask_host(h, params, matrix576, codes, offsets, nseq, mask, probs, n_masked, lambda_out);
+}
+
+int saber_gpu_tantan_mask_db(saber_gpu* h, const saber_tantan_params* params, const int32_t* matrix576,
+                             uint64_t* n_masked, double* lambda_out) {
+    ENTER(h);
+    return saber::tantan_mask_db(h, params, matrix576, n_masked, lambda_out);
 }
 
 int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask, const int32_t* region_thr,

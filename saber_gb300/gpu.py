@@ -236,6 +236,9 @@ def load_library():
         "saber_gpu_get_long_steps": (U32, [P]),
         "saber_gpu_get_scan_table_bytes": (U64, [P]),
         "saber_gpu_score_band_jobs_noalloc": (ctypes.c_int, [P, P, U64, I32, P]),
+        "saber_tantan_implied_lambda": (ctypes.c_double, [P]),
+        "saber_gpu_tantan_mask": (ctypes.c_int, [P, P, P, P, P, U64, P, P, P, P]),
+        "saber_gpu_tantan_mask_db": (ctypes.c_int, [P, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -393,6 +396,28 @@ class Device:
     def load_db_mask(self, mask):
         m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
         self._check(self.lib.saber_gpu_load_db_mask(self.h, _ptr(m), 0 if m is None else m.size), "load_db_mask")
+
+    def tantan_mask(self, params, matrix, codes, offsets, want_probs=False):
+        """Tantan seed mask of a batch of sequences -> (mask bool array, posteriors or None, masked, lambda)."""
+        c = np.ascontiguousarray(codes, dtype=np.uint8)
+        o = np.ascontiguousarray(offsets, dtype=np.uint64)
+        m = np.ascontiguousarray(np.asarray(matrix).reshape(576), dtype=np.int32)
+        n = int(o[-1]) if o.size else 0
+        mask = np.zeros(max(n, 1), np.uint8)
+        probs = np.zeros(max(n, 1), np.float32) if want_probs else None
+        nm, lam = ctypes.c_uint64(), ctypes.c_double()
+        self._check(self.lib.saber_gpu_tantan_mask(self.h, ctypes.byref(params), _ptr(m), _ptr(c), _ptr(o),
+                                                   max(o.size - 1, 0), _ptr(mask), _ptr(probs), ctypes.byref(nm),
+                                                   ctypes.byref(lam)), "tantan_mask")
+        return mask[:n].astype(bool), None if probs is None else probs[:n], int(nm.value), float(lam.value)
+
+    def tantan_mask_db(self, params, matrix):
+        """Mask the loaded database on the device and install it as its seed mask -> (masked, lambda)."""
+        m = np.ascontiguousarray(np.asarray(matrix).reshape(576), dtype=np.int32)
+        nm, lam = ctypes.c_uint64(), ctypes.c_double()
+        self._check(self.lib.saber_gpu_tantan_mask_db(self.h, ctypes.byref(params), _ptr(m), ctypes.byref(nm),
+                                                      ctypes.byref(lam)), "tantan_mask_db")
+        return int(nm.value), float(lam.value)
 
     def scan(self, params, q_mask=None, region_thr=None, out_cap=None):
         """Candidate regions of the loaded query set (REGION_DTYPE, ordered by query and region order)."""

@@ -20,6 +20,7 @@ import numpy as np
 from . import presets as _presets
 from .bias import composition_bias
 from .gpu import JOB_DTYPE, TB_JOB_DTYPE, SearchParamsC, scan_params
+from .masking import MaskingMode, Tantan
 from .scoring import ALPHABET, matrix as _matrix, nucleotide as _nt_matrix
 from .stats import SearchStatistics, gapped_nucleotide, gapped_protein
 
@@ -64,6 +65,9 @@ class SearchParams:
         self.exhaustive = exhaustive
         self.ref_db_residues = REF_DB_RESIDUES
         self.evalue_model = "per-subject"
+        # tantan seed masking of the queries and the database (--masking,
+        # src/bin/main.rs:299-302, 472-517): the reference's default
+        self.masking = MaskingMode.TANTAN
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -166,7 +170,16 @@ class Searcher:
         self.stats = SearchStatistics(kp, int(self.db_codes.size), self.nsub, self.p.evalue_model)
         dev.set_scheme(self.matrix, gap_open, gap_extend)
         dev.load_db(self.db_codes, self.db_offsets)
-        dev.load_db_mask(db_mask)
+        # seed masks: tantan on both sides for protein searches unless masking
+        # is "none" (engine.rs:575-577; scan.rs:1078-1123); an explicit db_mask
+        # replaces the database's
+        masking = MaskingMode.parse(self.p.masking) if self.is_protein else MaskingMode.NONE
+        self.tantan = Tantan.protein(dev) if masking == MaskingMode.TANTAN else None
+        self.db_residues_masked = 0
+        if db_mask is not None or self.tantan is None:
+            dev.load_db_mask(db_mask)
+        else:
+            self.db_residues_masked = self.tantan.mask_database()
         if self.p.alphabet == "murphy10":
             amap, asz = _presets.alphabet_map()
         elif self.is_protein:
@@ -209,6 +222,17 @@ class Searcher:
         else:
             pr.region_thr = self.p.hsp_threshold
         return pr
+
+    def query_mask(self, q_codes, q_offsets, q_mask=None):
+        """The batch's query seed mask (Engine::prepare, engine.rs:769-775):
+        the caller's, else tantan's when masking is on, else none."""
+        if q_mask is not None:
+            m = np.ascontiguousarray(q_mask, dtype=np.uint8)
+            return m, int(np.count_nonzero(m))
+        if self.tantan is None or int(q_offsets[-1]) == 0:
+            return None, 0
+        m, n = self.tantan.mask(q_codes, q_offsets)
+        return m.view(np.uint8), n
 
     # ---- plan_windows (engine.rs:1223-1324) ----
     def window(self, d_min, d_max, subject, qlen):
@@ -307,7 +331,9 @@ class Searcher:
         """Hits of every query of the batch: list (per query) of Hit, in report order."""
         q_offsets = np.ascontiguousarray(q_offsets, dtype=np.uint64)
         nq = q_offsets.size - 1
+        q_mask, n_masked = self.query_mask(q_codes, q_offsets, q_mask)
         hits, ops, st = self.dev.search(self.cparams(), self.db_codes, self.db_offsets, q_codes, q_offsets, q_mask)
+        st["query_residues_masked"] = n_masked
         out = [[] for _ in range(nq)]
         for r in hits:
             o, n = int(r["ops_offset"]), int(r["n_ops"])
@@ -330,10 +356,11 @@ class Searcher:
         q_offsets = np.ascontiguousarray(q_offsets, dtype=np.uint64)
         nq = q_offsets.size - 1
         qlens = np.diff(q_offsets.astype(np.int64))
+        q_mask, n_masked = self.query_mask(q_codes, q_offsets, q_mask)
         preps = [self.prepare(q_codes[q_offsets[i]:q_offsets[i + 1]]) for i in range(nq)]
         bias = np.concatenate([p.bias for p in preps]) if nq else np.zeros(0, np.int8)
         self.dev.load_queries(q_codes, q_offsets, bias)
-        ctr = {"queries": nq}
+        ctr = {"queries": nq, "query_residues_masked": n_masked}
         # candidate regions (engine.rs:1014-1019 for the exhaustive preset)
         per_q = [[] for _ in range(nq)]
         if self.p.exhaustive:

@@ -55,7 +55,10 @@ def test_gpu_search_reproduces_recorded_hit(dev, case, run, want):
     # the 1.4 frequent-seed cap drops (v1.2.0 seeded differently); the
     # exhaustive preset scores the pair without seeding
     preset = "exhaustive" if case["name"] == "sat" else "default"
-    P = SearchParams(preset, comp_bias="--comp-bias off" not in run)
+    # the runs without --masking none used the reference's default tantan
+    # masking of the query and the database
+    P = SearchParams(preset, comp_bias="--comp-bias off" not in run,
+                     masking="none" if "--masking none" in run else "tantan")
     se = Searcher(dev, s, np.array([0, len(s)], np.uint64), P)
     hits = se.search(q, np.array([0, len(q)], np.uint64))[0]
     assert len(hits) == 1

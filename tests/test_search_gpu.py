@@ -31,6 +31,8 @@ def _case(dev, preset, seed, nq, ns, masks=True, **kw):
     rng = np.random.default_rng(seed + 1)
     db_mask = (rng.random(ss.codes.size) < 0.02).astype(np.uint8) if masks else None
     q_mask = (rng.random(qs.codes.size) < 0.03).astype(np.uint8) if masks else None
+    if not masks:
+        kw.setdefault("masking", "none")
     P = SearchParams(preset, **kw)
     se = Searcher(dev, ss.codes, ss.offsets, P, db_mask=db_mask)
     got = se.search(qs.codes, qs.offsets, q_mask)
