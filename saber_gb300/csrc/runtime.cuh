@@ -167,6 +167,8 @@ struct saber_gpu {
     saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
     // tantan masking scratch
     saber::DevBuf tt_ord, tt_base, tt_F, tt_BS, tt_count, tt_codes, tt_offs, tt_mask, tt_probs;
+    std::vector<int32_t> tt_lambda_matrix;  // the matrix whose implied lambda is cached
+    double tt_lambda = 0.0;
     // traceback scratch
     saber::DevBuf al_reqs, al_outs, al_dir, al_opbytes, al_runs, al_slabs, al_packed, al_pack_off;
 };

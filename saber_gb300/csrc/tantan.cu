@@ -162,8 +162,16 @@ static int tantan_model(saber_gpu* h, const int32_t* m, const saber_tantan_param
     if (w > (uint32_t)kTtMaxW) return fail(h, SABER_ERR_ARG, "tantan max_period %u above %d", w, kTtMaxW);
     lambda = p->lambda;
     if (!(lambda > 0.0)) {
-        lambda = tantan_implied_lambda(m);
-        if (std::isnan(lambda)) lambda = 0.3176;  // masking.rs:163
+        // implied by the matrix; cached per handle (a grid scan and 80
+        // bisection steps, each a 20x20 inversion)
+        if (h->tt_lambda_matrix.size() == 576 && std::equal(m, m + 576, h->tt_lambda_matrix.begin())) {
+            lambda = h->tt_lambda;
+        } else {
+            lambda = tantan_implied_lambda(m);
+            if (std::isnan(lambda)) lambda = 0.3176;  // masking.rs:163
+            h->tt_lambda_matrix.assign(m, m + 576);
+            h->tt_lambda = lambda;
+        }
     }
     std::memset(&M, 0, sizeof(M));
     for (int a = 0; a < 24; a++)
@@ -346,6 +354,250 @@ __global__ void __launch_bounds__(kTtWarps * 32, 4) k_tantan(const __grid_consta
     if (lane == 0 && masked) atomicAdd(n_masked, (unsigned long long)masked);
 }
 
+// ---- eight lanes per sequence ------------------------------------------------------
+//
+// The default model (W = 50) runs four sequences per warp, eight lanes each:
+// lane k of a group holds states k + 8j (j = 0..7, registers v[j]), so each
+// of the reference's eight accumulators is one lane's in-register chain over
+// the full chunks, the combination tree is three xor shuffles inside the group
+// (every lane ends with the same sum: each level adds a pair in both orders,
+// and IEEE addition commutes), and the remaining states W mod 8 sit in
+// register W/8 of lanes 0.. and are added by broadcast, in order.
+//
+// Partner codes come from a per-group ring of 128 codes in shared memory,
+// stored twice (slots q & 127 and 128 + (q & 127)) so that the code of
+// position p-1-k-8j is at the fixed offset ((p-1-k) & 127) + 128 - 8j; ring
+// slots of positions before the sequence hold 24 (no partner, ratio 0).
+// The scratch row of a position keeps lane k's eight states contiguous
+// (index 8k + j: two 16-byte stores per lane).
+constexpr int kTg = 8;          // lanes per sequence
+constexpr int kTgSeqs = 4;      // sequences per warp
+constexpr int kRingPitch = 264; // bytes per group ring (256 + 8: the two words a group reads never share a
+                                // bank with the neighbouring groups')
+
+template <int W>
+__device__ __forceinline__ float tg_sum(const float (&v)[8]) {
+    constexpr int C = W / 8, R = W % 8;
+    float acc = 0.f;
+    if (C > 0) {
+        acc = __fadd_rn(0.f, v[0]);
+#pragma unroll
+        for (int j = 1; j < C; j++) acc = __fadd_rn(acc, v[j]);
+    }
+    acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 1, kTg));
+    acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 2, kTg));
+    acc = __fadd_rn(acc, __shfl_xor_sync(kFull, acc, 4, kTg));
+#pragma unroll
+    for (int r = 0; r < R; r++) acc = __fadd_rn(acc, __shfl_sync(kFull, v[C < 8 ? C : 7], r, kTg));
+    return acc;
+}
+
+// Ring chunk c (positions 32c .. 32c+31) of one group: lane k loads the
+// codes of positions 32c + 4k .. 32c + 4k + 3 (24 before the sequence) as
+// one word and stores it into both copies of the ring.
+__device__ __forceinline__ uint32_t tg_load(const uint8_t* __restrict__ x, int64_t n, int64_t c, int k) {
+    const int64_t q0 = 32 * c + 4 * k;
+    uint32_t word = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        const int64_t q = q0 + t;
+        const uint32_t code = q < 0 ? 24u : (q < n ? (uint32_t)min((int)x[q], 23) : 0u);
+        word |= code << (8 * t);
+    }
+    return word;
+}
+__device__ __forceinline__ void tg_store(uint8_t* ring, int64_t c, int k, uint32_t word) {
+    const int slot = (int)((32 * c + 4 * k) & 127);
+    *reinterpret_cast<uint32_t*>(ring + slot) = word;
+    *reinterpret_cast<uint32_t*>(ring + 128 + slot) = word;
+}
+
+template <int W>
+__global__ void __launch_bounds__(kTtWarps * 32, 4) k_tantan8(const __grid_constant__ TantanModel M,
+                                                              const uint8_t* __restrict__ codes,
+                                                              const uint64_t* __restrict__ offs,
+                                                              const uint32_t* __restrict__ ord,
+                                                              const uint64_t* __restrict__ base, uint64_t k0,
+                                                              uint64_t k1, float* __restrict__ fwdF,
+                                                              float2* __restrict__ fwdBS, uint8_t* __restrict__ mask,
+                                                              float* __restrict__ probs,
+                                                              unsigned long long* __restrict__ n_masked) {
+    static_assert(W >= 1 && W <= kTtMaxW, "repeat states");
+    constexpr int J = (W + 7) / 8;  // registers holding states
+    __shared__ float lr[24 * 33];
+    __shared__ __align__(16) uint8_t rings[kTtWarps * kTgSeqs * kRingPitch];
+    for (int i = threadIdx.x; i < 24 * 33; i += blockDim.x) {
+        const int r = i / 33, c = i % 33;
+        lr[i] = c < 32 ? M.lr[r * 32 + c] : 0.f;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, g = lane >> 3, k = lane & 7;
+    const int wib = threadIdx.x >> 5;
+    uint8_t* ring = rings + (wib * kTgSeqs + g) * kRingPitch;
+    const uint64_t kk = k0 + ((uint64_t)blockIdx.x * kTtWarps + wib) * kTgSeqs + g;
+    int64_t n = 0;
+    uint64_t st = 0;
+    float* F = fwdF;
+    float2* BS = fwdBS;
+    if (kk < k1) {
+        const uint32_t sid = ord[kk];
+        st = offs[sid];
+        n = (int64_t)(offs[sid + 1] - st);
+        F = fwdF + base[kk] * (uint64_t)kTtMaxW + 8 * k;
+        BS = fwdBS + base[kk];
+    }
+    const int64_t nmax = (int64_t)__reduce_max_sync(kFull, (unsigned)n);
+    if (nmax == 0) return;
+    const uint8_t* x = codes + st;
+    float b2f[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) b2f[j] = j < J ? M.b2f[k + 8 * j] : 0.f;
+    const float b2b = M.b2b, f2f = M.f2f, f2b = M.f2b;
+    // ring: 24 everywhere (positions before the sequence), then chunks 0 and 1
+#pragma unroll
+    for (int t = 0; t < 8; t++) *reinterpret_cast<uint32_t*>(ring + 32 * t + 4 * k) = 0x18181818u;
+    __syncwarp();
+
+    // ---- forward (masking.rs:476-497) ----
+    float pb = 1.f, pf[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) pf[j] = 0.f;
+    float mb = 0.f, ms = 0.f;
+    uint32_t wnext = tg_load(x, n, 0, k);  // codes one chunk ahead
+    for (int64_t p = 0; p < nmax; p++) {
+        if ((p & 31) == 0) {
+            __syncwarp();
+            tg_store(ring, p >> 5, k, wnext);
+            __syncwarp();
+            wnext = tg_load(x, n, (p >> 5) + 1, k);
+        }
+        const int xrow = 33 * (int)ring[p & 127];
+        const uint8_t* rp = ring + ((p - 1 - k) & 127) + 128;
+        float e[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) e[j] = j < J ? lr[xrow + rp[-8 * j]] : 0.f;
+        const float sum_f = tg_sum<W>(pf);
+        float c[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) c[j] = __fmul_rn(__fadd_rn(__fmul_rn(pb, b2f[j]), __fmul_rn(pf[j], f2f)), e[j]);
+        const float cb = __fadd_rn(__fmul_rn(pb, b2b), __fmul_rn(sum_f, f2b));
+        const float tot = __fadd_rn(cb, tg_sum<W>(c));
+        const float s = tot > 0.f ? __fdiv_rn(1.f, tot) : 1.f;
+        pb = __fmul_rn(cb, s);
+#pragma unroll
+        for (int j = 0; j < 8; j++) pf[j] = __fmul_rn(c[j], s);
+        if (p < n) {
+            float4* row = reinterpret_cast<float4*>(F + p * kTtMaxW);
+            row[0] = make_float4(pf[0], pf[1], pf[2], pf[3]);
+            row[1] = make_float4(pf[4], pf[5], pf[6], pf[7]);
+        }
+        const int j8 = (int)(p & 7);
+        if (k == j8) {
+            mb = pb;
+            ms = s;
+        }
+        if (j8 == 7 || p == nmax - 1) {
+            const int64_t q = (p & ~(int64_t)7) + k;
+            if (q < n && q <= p) BS[q] = make_float2(mb, ms);
+        }
+    }
+
+    // ---- backward with the same scales (masking.rs:499-528) ----
+    float nb = 1.f, nf[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) nf[j] = f2b;
+    // B values and scales one block of eight positions ahead, codes one
+    // chunk ahead, the F row one position ahead
+    auto bs_load = [&](int64_t blk) {
+        const int64_t q = 8 * blk + k;
+        return blk >= 0 && q < n ? BS[q] : make_float2(0.f, 0.f);
+    };
+    float2 bs = bs_load((nmax - 1) >> 3), bsn = bs_load(((nmax - 1) >> 3) - 1);
+    float keep = 0.f;
+    unsigned masked = 0;
+    float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb4 = ra;
+    {
+        const int64_t p = nmax - 1;
+        if (p < n) {
+            const float4* row = reinterpret_cast<const float4*>(F + p * kTtMaxW);
+            ra = row[0];
+            rb4 = row[1];
+        }
+        const uint32_t w0 = tg_load(x, n, p >> 5, k), w1 = tg_load(x, n, (p >> 5) - 1, k),
+                       w2 = tg_load(x, n, (p >> 5) - 2, k);
+        __syncwarp();
+        tg_store(ring, p >> 5, k, w0);
+        tg_store(ring, (p >> 5) - 1, k, w1);
+        tg_store(ring, (p >> 5) - 2, k, w2);
+        __syncwarp();
+        wnext = tg_load(x, n, (p >> 5) - 3, k);
+    }
+    for (int64_t p = nmax - 1; p >= 0; p--) {
+        if ((p & 31) == 31 && p != nmax - 1) {
+            __syncwarp();
+            tg_store(ring, (p >> 5) - 2, k, wnext);
+            __syncwarp();
+            wnext = tg_load(x, n, (p >> 5) - 3, k);
+        }
+        const int j8 = (int)(p & 7);
+        if (j8 == 7 && p != nmax - 1) {
+            bs = bsn;
+            bsn = bs_load((p >> 3) - 1);
+        }
+        float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb4 = na;
+        if (p > 0 && p - 1 < n) {
+            const float4* row = reinterpret_cast<const float4*>(F + (p - 1) * kTtMaxW);
+            na = row[0];
+            nb4 = row[1];
+        }
+        const float rbv = __shfl_sync(kFull, bs.x, j8, kTg), s = __shfl_sync(kFull, bs.y, j8, kTg);
+        const float r[8] = {ra.x, ra.y, ra.z, ra.w, rb4.x, rb4.y, rb4.z, rb4.w};
+        const bool active = p < n;
+        const float onb = nb;
+        float onf[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) onf[j] = nf[j];
+        {
+            const int xrow = 33 * (int)ring[p & 127];
+            const uint8_t* rp = ring + ((p - 1 - k) & 127) + 128;
+            float be[8], t[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                be[j] = j < J ? __fmul_rn(lr[xrow + rp[-8 * j]], onf[j]) : 0.f;
+                t[j] = __fmul_rn(b2f[j], be[j]);
+            }
+            const float to_fg = tg_sum<W>(t);
+            if (active && p > 0) {
+                const float fb = __fmul_rn(f2b, onb);
+#pragma unroll
+                for (int j = 0; j < 8; j++) nf[j] = __fmul_rn(__fadd_rn(__fmul_rn(f2f, be[j]), fb), s);
+                nb = __fmul_rn(__fadd_rn(__fmul_rn(b2b, onb), to_fg), s);
+            }
+        }
+        float pr[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) pr[j] = __fmul_rn(r[j], onf[j]);
+        const float pbv = __fmul_rn(rbv, onb);
+        const float pfv = tg_sum<W>(pr);
+        const float z = __fadd_rn(pbv, pfv);
+        const float post = z > 0.f ? __fdiv_rn(pfv, z) : 0.f;
+        if (k == j8) keep = post;
+        if (j8 == 0) {
+            const int64_t q = p + k;
+            const bool ok = q < n;
+            const bool m = ok && (double)keep >= M.min_prob;
+            if (ok) {
+                mask[st + q] = m ? 1 : 0;
+                if (probs) probs[st + q] = keep;
+            }
+            masked += __popc(__ballot_sync(kFull, m));
+        }
+        ra = na;
+        rb4 = nb4;
+    }
+    if (lane == 0 && masked) atomicAdd(n_masked, (unsigned long long)masked);
+}
+
 // ---- host driver ------------------------------------------------------------------
 
 // Scratch rows (positions) per launch: 64 F floats + one float2 each.
@@ -360,6 +612,8 @@ int tantan_run(saber_gpu* h, const TantanModel& M, const uint8_t* d_codes, const
     *n_masked = 0;
     if (nseq == 0) return SABER_OK;
     if (nseq > 0xffffffffull) return fail(h, SABER_ERR_ARG, "too many sequences for tantan");
+    for (uint64_t i = 0; i < nseq; i++)
+        if (h_offs[i + 1] - h_offs[i] >= (1ull << 31)) return fail(h, SABER_ERR_ARG, "sequence too long for tantan");
     // longest first (a counting sort on the length, lengths above 2^22 in one
     // bucket; ties by index), then launches bounded by the scratch budget
     uint64_t maxn = 0;
@@ -404,9 +658,17 @@ int tantan_run(saber_gpu* h, const TantanModel& M, const uint8_t* d_codes, const
     CU(h, cudaMemsetAsync(h->tt_count.p, 0, sizeof(unsigned long long), h->stream));
     for (size_t c = 0; c + 1 < cuts.size(); c++) {
         const uint64_t k0 = cuts[c], k1 = cuts[c + 1];
+        if (M.w == 50) {  // tantan's protein default: eight lanes per sequence
+            const uint64_t per_block = (uint64_t)kTtWarps * kTgSeqs;
+            const unsigned blocks = (unsigned)((k1 - k0 + per_block - 1) / per_block);
+            k_tantan8<50><<<blocks, kTtWarps * 32, 0, h->stream>>>(
+                M, d_codes, d_offs, (const uint32_t*)h->tt_ord.p, (const uint64_t*)h->tt_base.p, k0, k1,
+                (float*)h->tt_F.p, (float2*)h->tt_BS.p, d_mask, d_probs, (unsigned long long*)h->tt_count.p);
+            CU(h, cudaGetLastError());
+            continue;
+        }
         const unsigned blocks = (unsigned)((k1 - k0 + kTtWarps - 1) / kTtWarps);
-        auto kern = M.w == 50 ? k_tantan<50> : k_tantan<0>;  // tantan's protein default, specialised
-        kern<<<blocks, kTtWarps * 32, 0, h->stream>>>(
+        k_tantan<0><<<blocks, kTtWarps * 32, 0, h->stream>>>(
             M, d_codes, d_offs, (const uint32_t*)h->tt_ord.p, (const uint64_t*)h->tt_base.p, k0, k1,
             (float*)h->tt_F.p, (float2*)h->tt_BS.p, d_mask, d_probs, (unsigned long long*)h->tt_count.p);
         CU(h, cudaGetLastError());
