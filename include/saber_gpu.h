@@ -220,6 +220,19 @@ int saber_gpu_tantan_mask(saber_gpu* h, const saber_tantan_params* params, const
 int saber_gpu_tantan_mask_db(saber_gpu* h, const saber_tantan_params* params, const int32_t* matrix576,
                              uint64_t* n_masked, double* lambda_out);
 
+/* ---- six-frame translation (translation.rs) ------------------------------------
+ *
+ * Frames 0..5 of every nucleotide sequence (codes 0..3 = ACGT, 4 = N; frames
+ * 3..5 on the reverse complement, read from the sequence end) translated with
+ * a 64-entry codon table (protein codes, index a*16 + b*4 + c), codons
+ * holding N give X (CodonTable::translate_codes, translation.rs:277-308).
+ * out receives frame f of sequence s as segment 6*s + f (the reference's
+ * translated database order, index.rs:1351-1368; a query's frames in
+ * driver.rs:387-402); out_offsets[6*nseq + 1] its bounds.  At most
+ * 2 x (nucleotides) residues; SABER_ERR_CAP when out_cap is smaller. */
+int saber_gpu_translate6(saber_gpu* h, const uint8_t* nt, const uint64_t* nt_offsets, uint64_t nseq,
+                         const uint8_t* codon64, uint8_t* out, uint64_t out_cap, uint64_t* out_offsets);
+
 /* Engine::search_scan's candidate regions for the loaded query set against
  * the loaded database (scan.rs:1261-1497 up to the per-query candidate cap):
  * seed tables of the batch, database scan with the window filter,
@@ -342,8 +355,12 @@ typedef struct {
     double lambda, k, h, alpha, beta;
     uint32_t even_scores_only;
     uint32_t pad_;
-    /* the scan (its db_length must be the database residues) */
+    /* the scan; its db_length is the database length of the statistics (the
+     * residues; a translated database: its nucleotides / 3, driver.rs:575-583) */
     saber_scan_params scan;
+    /* sequences of the statistics; 0 = the loaded subjects (a translated
+     * database: its nucleotide sequences, driver.rs:575-583) */
+    uint64_t stats_num_seqs;
 } saber_search_params;
 
 /* One reported alignment (Hit, engine.rs:310-357): 1-based inclusive

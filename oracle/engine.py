@@ -152,14 +152,16 @@ def m8_line(qid, sid, h):
 
 
 def search_batch(db_codes, db_offsets, q_codes, q_offsets, params, matrix, go, ge, kp, scan_params, db_mask=None,
-                 q_mask=None, is_protein=True):
-    """Hits per query (lists of dicts in report order) for one batch."""
+                 q_mask=None, is_protein=True, stats_size=None):
+    """Hits per query (lists of dicts in report order) for one batch.
+    stats_size: (database length, sequences) of the statistics when they are
+    not the residues and subjects (translated databases, driver.rs:575-583)."""
     from saber_gb300.bias import composition_bias
     from saber_gb300.stats import SearchStatistics
     P = params
     slen = np.diff(np.asarray(db_offsets, np.int64))
     nsub = slen.size
-    stats = SearchStatistics(kp, int(len(db_codes)), nsub, P.evalue_model)
+    stats = SearchStatistics(kp, *(stats_size or (int(len(db_codes)), nsub)), P.evalue_model)
     nq = len(q_offsets) - 1
     e_reg = max(P.evalue, 10.0)
     if P.ref_db_residues > 0 and stats.db_length > P.ref_db_residues:
@@ -294,3 +296,41 @@ def _make_hit(q, sfull, subject, s_off, al, exact, qs, matrix, is_protein):
                 s_start=al["s_start"] + s_off + 1, s_end=al["s_end"] + s_off, columns=sum(l for _, l in al["ops"]),
                 matches=mt, mismatches=mm, positives=ps, gap_opens=go_, gap_columns=gc, q_len=len(q),
                 s_len=len(sfull), ops=al["ops"], exact=exact)
+
+
+def finish_record_nx(frame_hits, max_target_seqs, max_hsps):
+    """finish_record for nx (driver.rs:481-501): frame_hits = hit lists of the
+    record's frames 0..5; returns (frame, hit) pairs after the merge (stable
+    sort by score descending, subject, frame; then max_hsps per subject and
+    max_target_seqs subjects)."""
+    import functools
+    flat = []
+    for f in range(6):
+        for h in frame_hits[f]:
+            flat.append((f, h))
+
+    def cmp(a, b):
+        if a[1]["score"] != b[1]["score"]:
+            return -1 if a[1]["score"] > b[1]["score"] else 1
+        if a[1]["subject"] != b[1]["subject"]:
+            return -1 if a[1]["subject"] < b[1]["subject"] else 1
+        return (a[0] > b[0]) - (a[0] < b[0])
+    flat.sort(key=functools.cmp_to_key(cmp))
+    count, out, nsubj = {}, [], 0
+    for f, h in flat:
+        c = count.setdefault(h["subject"], 0)
+        if c >= max_hsps or (c == 0 and nsubj >= max_target_seqs):
+            continue
+        if c == 0:
+            nsubj += 1
+        count[h["subject"]] = c + 1
+        out.append((f, h))
+    return out
+
+
+def frame_nt_range(frame, p_start, p_end, nt_len):
+    """protein_to_nt (translation.rs:323-337) and frame_label (:316-318)."""
+    if frame < 3:
+        return frame + 3 * p_start - 2, frame + 3 * p_end, frame + 1
+    off = frame - 3
+    return nt_len - (off + 3 * p_start - 2) + 1, nt_len - (off + 3 * p_end) + 1, -(off + 1)

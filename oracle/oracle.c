@@ -572,7 +572,7 @@ int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsu
             uint64_t b = soffs[s], e = soffs[s + 1];
             const int64_t sl = (int64_t)(e - b);
             if ((uint64_t)sl < span) continue;
-            for (int64_t p = 0; p + span <= (uint64_t)sl; p++) {
+            for (int64_t p = 0; p + (int64_t)span <= sl; p++) {
                 int64_t c = code_at(sb + b + p, offs, w, asize);
                 if (c < 0) continue;
                 /* entries of code c */

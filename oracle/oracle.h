@@ -187,6 +187,12 @@ int orc_tantan_probs(const uint8_t* seq, size_t n, const float* lr768, const flo
 int64_t orc_tantan_mask(const uint8_t* codes, const uint64_t* offsets, uint64_t nseq, const int32_t* matrix576,
                         const orc_tantan_params* p, double lambda, uint8_t* mask, float* probs);
 
+/* ---- six-frame translation (oracle/translate.c) ---- */
+
+/* CodonTable::translate_codes (translation.rs:277-299): frame 0..5 of
+ * nucleotide codes (0..3, 4 = N) into protein codes; returns the count. */
+size_t orc_translate_codes(const uint8_t* nt, size_t n, unsigned frame, const uint8_t* aa64, uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

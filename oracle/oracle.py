@@ -282,3 +282,24 @@ def tantan_mask(codes, offsets, matrix, params=None, lam=0.0):
     if k < 0:
         raise MemoryError("oracle tantan allocation")
     return mask[:n].astype(bool), probs[:n], int(k)
+
+
+def translate6(nt, nt_offsets, aa64):
+    """Six frames of every sequence (translate_codes, translation.rs:277-299)
+    -> (protein codes, offsets[6 * nseq + 1]); subject 6 * s + f is frame f of s."""
+    f = lib().orc_translate_codes
+    f.restype = ctypes.c_size_t
+    f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint, ctypes.c_void_p, ctypes.c_void_p]
+    nt = _a(nt, np.uint8)
+    offs = np.asarray(nt_offsets, np.int64)
+    aa = _a(aa64, np.uint8)
+    parts, lens = [], []
+    for s in range(offs.size - 1):
+        seq = np.ascontiguousarray(nt[offs[s]:offs[s + 1]])
+        for fr in range(6):
+            out = np.zeros(max(seq.size // 3 + 1, 1), np.uint8)
+            k = f(_p(seq), seq.size, fr, _p(aa), _p(out))
+            parts.append(out[:k])
+            lens.append(k)
+    codes = np.concatenate(parts) if parts else np.zeros(0, np.uint8)
+    return codes, np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)

@@ -10,7 +10,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libsaber_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["saber_gpu.cu", "band_kernels.cu", "probe.cu", "noalloc.cu", "traceback.cu", "scan.cu", "triage.cu", "tantan.cu", "engine.cpp"]
+SOURCES = ["saber_gpu.cu", "band_kernels.cu", "probe.cu", "noalloc.cu", "traceback.cu", "scan.cu", "triage.cu", "tantan.cu", "translate.cu", "engine.cpp"]
 # host C++ of the search engine and of the tantan model tables: f64 arithmetic must round like the
 # reference's (no fused multiply-add)
 HOST_FLAGS = {"engine.cpp": ["-Xcompiler", "-ffp-contract=off"], "tantan.cu": ["-Xcompiler", "-ffp-contract=off"]}

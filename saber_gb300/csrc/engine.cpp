@@ -329,7 +329,8 @@ struct Engine {
     // engine.rs:759-786
     Prep prepare(int64_t qlen) const {
         Prep pr;
-        pr.qs = for_query(kp, P.evalue_model == 1, (int64_t)P.scan.db_length, (int64_t)nsub, std::max<int64_t>(qlen, 1));
+        const int64_t nseq = P.stats_num_seqs ? (int64_t)P.stats_num_seqs : (int64_t)nsub;
+        pr.qs = for_query(kp, P.evalue_model == 1, (int64_t)P.scan.db_length, nseq, std::max<int64_t>(qlen, 1));
         pr.floor = pr.qs.min_score(P.evalue, has_bits, P.min_bitscore);
         const double re = region_evalue();
         if (re == P.evalue && !has_bits) pr.region_floor = pr.floor;

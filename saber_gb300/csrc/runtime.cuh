@@ -165,6 +165,8 @@ struct saber_gpu {
     saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
     saber::HostBuf pin_reg, pin_src;
     saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
+    // six-frame translation scratch
+    saber::DevBuf tr_nt, tr_offs, tr_out_offs, tr_chunks, tr_aa, tr_out;
     // tantan masking scratch
     saber::DevBuf tt_ord, tt_base, tt_F, tt_BS, tt_count, tt_codes, tt_offs, tt_mask, tt_probs;
     std::vector<int32_t> tt_lambda_matrix;  // the matrix whose implied lambda is cached

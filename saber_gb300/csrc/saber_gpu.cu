@@ -1143,6 +1143,8 @@ int tantan_mask_host(saber_gpu* h, const saber_tantan_params* p, const int32_t* 
                      double* lambda_out);
 int tantan_mask_db(saber_gpu* h, const saber_tantan_params* p, const int32_t* matrix576, uint64_t* n_masked,
                    double* lambda_out);
+int translate6_host(saber_gpu* h, const uint8_t* nt, const uint64_t* nt_offsets, uint64_t nseq,
+                    const uint8_t* codon64, uint8_t* out, uint64_t out_cap, uint64_t* out_offsets);
 // Pinned host staging for the host engine (engine.cpp).
 void* pinned_scratch(saber_gpu* h, int slot, size_t bytes) {
     if (!h || slot < 0 || slot >= 4) return nullptr;
@@ -1530,6 +1532,12 @@ int saber_gpu_tantan_mask_db(saber_gpu* h, const saber_tantan_params* params, co
                              uint64_t* n_masked, double* lambda_out) {
     ENTER(h);
     return saber::tantan_mask_db(h, params, matrix576, n_masked, lambda_out);
+}
+
+int saber_gpu_translate6(saber_gpu* h, const uint8_t* nt, const uint64_t* nt_offsets, uint64_t nseq,
+                         const uint8_t* codon64, uint8_t* out, uint64_t out_cap, uint64_t* out_offsets) {
+    ENTER(h);
+    return saber::translate6_host(h, nt, nt_offsets, nseq, codon64, out, out_cap, out_offsets);
 }
 
 int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask, const int32_t* region_thr,

@@ -96,7 +96,8 @@ class SearchParamsC(ctypes.Structure):
                 ("evalue_model", ctypes.c_uint32), ("is_protein", ctypes.c_uint32),
                 ("lambda_", ctypes.c_double), ("k", ctypes.c_double), ("h", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
-                ("even_scores_only", ctypes.c_uint32), ("pad_", ctypes.c_uint32), ("scan", ScanParams)]
+                ("even_scores_only", ctypes.c_uint32), ("pad_", ctypes.c_uint32), ("scan", ScanParams),
+                ("stats_num_seqs", ctypes.c_uint64)]
 
 
 class SearchStats(ctypes.Structure):
@@ -239,6 +240,7 @@ def load_library():
         "saber_tantan_implied_lambda": (ctypes.c_double, [P]),
         "saber_gpu_tantan_mask": (ctypes.c_int, [P, P, P, P, P, U64, P, P, P, P]),
         "saber_gpu_tantan_mask_db": (ctypes.c_int, [P, P, P, P, P]),
+        "saber_gpu_translate6": (ctypes.c_int, [P, P, P, U64, P, P, U64, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -418,6 +420,19 @@ class Device:
         self._check(self.lib.saber_gpu_tantan_mask_db(self.h, ctypes.byref(params), _ptr(m), ctypes.byref(nm),
                                                       ctypes.byref(lam)), "tantan_mask_db")
         return int(nm.value), float(lam.value)
+
+    def translate6(self, nt, nt_offsets, codon64):
+        """Six frames of every nucleotide sequence -> (protein codes, offsets[6 * nseq + 1])."""
+        x = np.ascontiguousarray(nt, dtype=np.uint8)
+        o = np.ascontiguousarray(nt_offsets, dtype=np.uint64)
+        aa = np.ascontiguousarray(codon64, dtype=np.uint8)
+        nseq = max(o.size - 1, 0)
+        total = int(o[-1] - o[0]) if o.size else 0
+        out = np.zeros(max(2 * total + 6, 1), np.uint8)
+        offs = np.zeros(6 * nseq + 1, np.uint64)
+        self._check(self.lib.saber_gpu_translate6(self.h, _ptr(x) if x.size else None, _ptr(o), nseq, _ptr(aa),
+                                                  _ptr(out), out.size, _ptr(offs)), "translate6")
+        return out[:int(offs[-1])].copy(), offs
 
     def scan(self, params, q_mask=None, region_thr=None, out_cap=None):
         """Candidate regions of the loaded query set (REGION_DTYPE, ordered by query and region order)."""

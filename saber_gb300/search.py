@@ -154,7 +154,10 @@ class Searcher:
     runs one batch of queries end to end."""
 
     def __init__(self, dev, db_codes, db_offsets, params=None, matrix_name="BLOSUM62", gap_open=11, gap_extend=1,
-                 db_mask=None, nucleotide=None):
+                 db_mask=None, nucleotide=None, stats_size=None):
+        """stats_size: (database length, sequences) of the statistics when they
+        are not the loaded residues and subjects (a translated database:
+        nucleotides / 3 and nucleotide sequences, driver.rs:575-583)."""
         self.dev = dev
         self.p = params or SearchParams()
         self.is_protein = nucleotide is None
@@ -167,7 +170,9 @@ class Searcher:
         kp = gapped_protein(matrix_name, gap_open, gap_extend) if self.is_protein else \
             gapped_nucleotide(nucleotide[0], nucleotide[1], gap_open, gap_extend)
         self.karlin = kp
-        self.stats = SearchStatistics(kp, int(self.db_codes.size), self.nsub, self.p.evalue_model)
+        self.stats_size = stats_size
+        db_len, db_seqs = stats_size if stats_size else (int(self.db_codes.size), self.nsub)
+        self.stats = SearchStatistics(kp, db_len, db_seqs, self.p.evalue_model)
         dev.set_scheme(self.matrix, gap_open, gap_extend)
         dev.load_db(self.db_codes, self.db_offsets)
         # seed masks: tantan on both sides for protein searches unless masking
@@ -191,7 +196,7 @@ class Searcher:
             hsp_threshold=self.p.hsp_threshold, x_drop=self.p.x_drop_ungapped, window_slack=self.p.window_slack,
             max_regions_per_subject=self.p.max_regions_per_subject, max_candidates=min(self.p.max_candidates, I32_MAX),
             seed_max_occ=self.p.seed_max_occ, ref_db_residues=self.p.ref_db_residues,
-            db_length=int(self.db_codes.size))
+            db_length=self.stats.db_length if stats_size else int(self.db_codes.size))
         self.counters = {}
 
     # ---- query preparation (engine.rs:714-786) ----
@@ -325,6 +330,7 @@ class Searcher:
         c.lambda_, c.k, c.h, c.alpha, c.beta = kp.lambda_, kp.k, kp.h, kp.alpha, kp.beta
         c.even_scores_only = int(bool(kp.even_scores_only))
         c.scan = self.scan_params
+        c.stats_num_seqs = self.stats.db_num_seqs if self.stats_size else 0
         return c
 
     def search(self, q_codes, q_offsets, q_mask=None):

@@ -233,3 +233,49 @@ def dna_db(seed, n_queries, n_subjects, qlen=(1000, 10000), slen=(1000, 10000), 
             bg = np.concatenate([bg[:cut], body, bg[cut:]]).astype(np.uint8)
         subs.append(bg)
     return _concat(qs), _concat(subs), planted
+
+
+def back_translate(rng, protein, n_frac=0.0):
+    """DNA codes (0..3 = A, C, G, T; 4 = N) encoding a protein with random
+    synonymous codons of the standard code; X and residues without a codon
+    (B, Z) become NNN, and a fraction n_frac of bases is set to N."""
+    from .translation import codon_table
+    ct = codon_table("standard")
+    by_aa = {}
+    for idx, aa in enumerate(ct.tolist()):
+        by_aa.setdefault(aa, []).append(idx)
+    out = np.full((len(protein), 3), 4, np.uint8)
+    for i, aa in enumerate(np.asarray(protein).tolist()):
+        cands = by_aa.get(aa)
+        if cands:
+            c = cands[int(rng.integers(0, len(cands)))]
+            out[i] = (c // 16, (c // 4) % 4, c % 4)
+    dna = out.reshape(-1)
+    if n_frac > 0:
+        dna[rng.random(dna.size) < n_frac] = 4
+    return dna
+
+
+def reverse_complement(dna):
+    """Reverse complement of DNA codes (N stays N)."""
+    d = np.asarray(dna, np.uint8)[::-1]
+    return np.where(d > 3, d, 3 - d).astype(np.uint8)
+
+
+def translated_db(seed, n_queries, n_subjects, mode, flank=(0, 300), **kw):
+    """A protein workload (protein_db) with one side as DNA: mode "nx" turns
+    the queries into DNA, "pn" the subjects; each DNA sequence is the
+    back-translated protein between random flanks, on the minus strand for
+    half of them (so hits come from all six frames)."""
+    qs, ss, planted = protein_db(seed, n_queries, n_subjects, **kw)
+    rng = np.random.default_rng(seed + 7)
+    side = qs if mode == "nx" else ss
+    seqs = []
+    for i in range(len(side)):
+        body = back_translate(rng, side.seq(i), n_frac=0.002)
+        left = rng.integers(0, 4, size=int(rng.integers(flank[0], flank[1] + 1))).astype(np.uint8)
+        right = rng.integers(0, 4, size=int(rng.integers(flank[0], flank[1] + 1))).astype(np.uint8)
+        dna = np.concatenate([left, body, right])
+        seqs.append(reverse_complement(dna) if rng.random() < 0.5 else dna)
+    dna = _concat(seqs)
+    return (dna, ss, planted) if mode == "nx" else (qs, dna, planted)
