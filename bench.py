@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--nn-search", action="store_true",
                     help="only the blastn (nn) batched search: DNA queries of 1-10 kb vs a synthetic genome-scale "
                          "database (its own JSON line)")
+    ap.add_argument("--translated", action="store_true",
+                    help="only the translated searches (nx, pn) and the six-frame translation (its own JSON line)")
+    ap.add_argument("--tr-records", type=int, default=1000, help="nx DNA query records / pn protein queries")
+    ap.add_argument("--tr-subjects", type=int, default=100_000, help="nx protein subjects / pn DNA sequences")
     ap.add_argument("--nn-queries", type=int, default=2000)
     ap.add_argument("--nn-bases", type=float, default=500e6, help="database size in bases (subjects of 1-10 kb)")
     ap.add_argument("--long-steps", type=int, default=0,
@@ -392,6 +396,71 @@ def run_nn_search(a, local_rank):
         flush=True)
 
 
+def run_translated(a, local_rank):
+    """Translated searches through the library's host buffers, default
+    preset, tantan on both sides: nx (DNA query records, six frames each,
+    merged per record, against a protein database) and pn (protein queries
+    against a DNA database stored as six frames per sequence), each on a
+    seeded workload whose DNA side is back-translated proteins with random
+    flanks, half on the minus strand.  The six-frame translation of the pn
+    database is timed alone (kernel through the C ABI, host buffers) with
+    the oracle's scalar C on one host core as its CPU baseline."""
+    from oracle import oracle as orc
+    from saber_gb300 import Device, synth
+    from saber_gb300.search import SearchParams
+    from saber_gb300.translated import BlastxSearcher, TblastnSearcher
+    from saber_gb300.translation import codon_table
+    dev = Device(local_rank)
+
+    def med(f, reps=3):
+        f()
+        ts, r = [], None
+        for _ in range(reps):
+            t = time.perf_counter()
+            r = f()
+            ts.append(time.perf_counter() - t)
+        return r, float(np.median(ts))
+
+    out = {"metric": "translated search queries/s", "unit": "queries/s",
+           "timing": "median of 3 calls, host wall clock (sequences in, merged results out)"}
+    dna_q, ps, _ = synth.translated_db(a.seed + 601, a.tr_records, a.tr_subjects, "nx", planted_frac=0.1)
+    bx = BlastxSearcher(dev, ps.codes, ps.offsets, SearchParams("default"))
+    res, t = med(lambda: bx.search(dna_q.codes, dna_q.offsets))
+    c = bx.counters
+    out["nx"] = {"workload": "%d DNA query records (%d nt) x six frames vs %d protein subjects (%d residues)"
+                 % (len(dna_q), int(dna_q.codes.size), len(ps), int(ps.codes.size)),
+                 "value": round(len(dna_q) / t, 1), "ms": round(t * 1e3, 1),
+                 "hits": int(sum(len(r) for r in res)), "regions": int(c.get("regions", 0)),
+                 "frames_with_hits": sorted({h["query_frame"] for r in res for h in r})}
+    pq, dna_s, _ = synth.translated_db(a.seed + 602, a.tr_records, a.tr_subjects, "pn", planted_frac=0.1)
+    t0 = time.perf_counter()
+    tn = TblastnSearcher(dev, dna_s.codes, dna_s.offsets, SearchParams("default"))
+    tload = time.perf_counter() - t0
+    res, t = med(lambda: tn.search(pq.codes, pq.offsets))
+    c = tn.counters
+    out["pn"] = {"workload": "%d protein queries vs %d DNA sequences (%d nt, %d frame residues)"
+                 % (len(pq), len(dna_s), int(dna_s.codes.size), int(tn.se.db_codes.size)),
+                 "value": round(len(pq) / t, 1), "ms": round(t * 1e3, 1), "database_setup_s": round(tload, 2),
+                 "hits": int(sum(len(r) for r in res)), "regions": int(c.get("regions", 0)),
+                 "frames_with_hits": sorted({h["subject_frame"] for r in res for h in r})}
+    aa = codon_table()
+    (tc, to), tt = med(lambda: dev.translate6(dna_s.codes, dna_s.offsets, aa))
+    k = min(len(dna_s), 2000)
+    t0 = time.perf_counter()
+    oc, oo = orc.translate6(dna_s.codes[:int(dna_s.offsets[k])], dna_s.offsets[:k + 1], aa)
+    tcpu = time.perf_counter() - t0
+    nt_bytes = int(dna_s.codes.size)
+    out["translate6"] = {
+        "workload": "six frames of %d DNA sequences (%d nt -> %d residues)" % (len(dna_s), nt_bytes, int(tc.size)),
+        "unit": "nt/s", "value": round(nt_bytes / tt, 1), "ms": round(tt * 1e3, 2),
+        "e2e": "host nucleotides in, host frames out",
+        "equals_oracle_on_sample": bool(np.array_equal(tc[:int(to[6 * k])], oc)),
+        "cpu_baseline": {"value": round(int(dna_s.offsets[k]) / tcpu, 1), "unit": "nt/s", "cores": 1,
+                         "kind": "port", "sample": "first %d sequences (%d nt), oracle scalar C restatement of "
+                                                   "translate_codes" % (k, int(dna_s.offsets[k]))}}
+    print(json.dumps(out), flush=True)
+
+
 def run_search_only(a, local_rank):
     from saber_gb300 import Device
     dev = Device(local_rank)
@@ -527,6 +596,9 @@ def main():
     elif a.nn_search:
         if rank == 0:
             run_nn_search(a, local_rank)
+    elif a.translated:
+        if rank == 0:
+            run_translated(a, local_rank)
     elif a.search_only:
         if rank == 0:
             run_search_only(a, local_rank)

@@ -241,15 +241,19 @@ def back_translate(rng, protein, n_frac=0.0):
     (B, Z) become NNN, and a fraction n_frac of bases is set to N."""
     from .translation import codon_table
     ct = codon_table("standard")
-    by_aa = {}
+    table = np.full((256, 6), -1, np.int64)  # codons per protein code
+    count = np.zeros(256, np.int64)
     for idx, aa in enumerate(ct.tolist()):
-        by_aa.setdefault(aa, []).append(idx)
-    out = np.full((len(protein), 3), 4, np.uint8)
-    for i, aa in enumerate(np.asarray(protein).tolist()):
-        cands = by_aa.get(aa)
-        if cands:
-            c = cands[int(rng.integers(0, len(cands)))]
-            out[i] = (c // 16, (c // 4) % 4, c % 4)
+        table[aa, count[aa]] = idx
+        count[aa] += 1
+    p = np.asarray(protein, np.uint8)
+    k = np.floor(rng.random(p.size) * np.maximum(count[p], 1)).astype(np.int64)
+    c = table[p, k]
+    out = np.full((p.size, 3), 4, np.uint8)
+    ok = c >= 0
+    out[ok, 0] = c[ok] // 16
+    out[ok, 1] = (c[ok] // 4) % 4
+    out[ok, 2] = c[ok] % 4
     dna = out.reshape(-1)
     if n_frac > 0:
         dna[rng.random(dna.size) < n_frac] = 4
