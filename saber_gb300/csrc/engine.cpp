@@ -826,11 +826,12 @@ struct Engine {
             cap += (uint64_t)j.win_len + (q_offsets[qi + 1] - q_offsets[qi]) + 2;
         }
         std::vector<saber_alignment> out(need.size());
-        std::vector<uint32_t> ops(cap);
+        // the library writes only the runs it returns: no zero fill of the bound
+        std::unique_ptr<uint32_t[]> ops(new uint32_t[cap]);
         saber_traceback_stats ts{};
         const double t0 = now_ms();
         int rc = saber_gpu_traceback(h, jobs.data(), jobs.size(), P.band_pad, P.traceback_max_bytes, out.data(),
-                                     ops.data(), cap, &ts);
+                                     ops.get(), cap, &ts);
         if (rc != SABER_OK) return rc;
         st.t_finish_tb_ms += now_ms() - t0;
         st.traceback.tracebacks += ts.tracebacks;
@@ -849,7 +850,7 @@ struct Engine {
             a.q_end = o.q_end;
             a.s_start = o.s_start;
             a.s_end = o.s_end;
-            if (a.present) a.runs.assign(ops.begin() + o.ops_offset, ops.begin() + o.ops_offset + o.n_ops);
+            if (a.present) a.runs.assign(ops.get() + o.ops_offset, ops.get() + o.ops_offset + o.n_ops);
             tb.insert_or_assign(key(need[k].first, need[k].second), std::move(a));
         }
         return SABER_OK;

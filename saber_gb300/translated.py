@@ -43,6 +43,10 @@ def to_result(h, q_frame=None, q_nt_len=None, s_frame=None, s_seq=None, s_nt_len
     coordinates and frames; q_frame / s_frame 0..5 or None."""
     r = Hit(h)
     r["query_frame"], r["subject_frame"] = 0, 0
+    # identity and coverages come from the engine hit (frame coordinates and
+    # lengths), as to_result computes them before mapping
+    r["query_cover_engine"], r["subject_cover_engine"] = h.query_cover(), h.subject_cover()
+    r["q_start_engine"], r["s_start_engine"] = h["q_start"], h["s_start"]
     if q_frame is not None:
         r["q_start"], r["q_end"] = protein_to_nt(q_frame, h["q_start"], h["q_end"], q_nt_len)
         r["query_frame"] = frame_label(q_frame)
