@@ -183,6 +183,10 @@ typedef struct {
  * masked from seeding (the tantan runs of the index, index.rs mask_runs;
  * scan.rs:123-141 applies them).  NULL clears the mask. */
 int saber_gpu_load_db_mask(saber_gpu* h, const uint8_t* mask, uint64_t n_residues);
+/* The same mask given as nruns sorted half-open runs [runs[2r], runs[2r+1])
+ * of database residues, as a SABERIDX index stores it (section "maskruns",
+ * index.rs:613-617); expanded on the device. */
+int saber_gpu_load_db_mask_runs(saber_gpu* h, const uint64_t* runs, uint64_t nruns);
 
 /* ---- tantan seed masking (masking.rs) -----------------------------------------
  *

@@ -165,6 +165,7 @@ struct saber_gpu {
     saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
     saber::HostBuf pin_reg, pin_src;
     saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
+    saber::DevBuf mask_runs;  // database mask runs being expanded
     // six-frame translation scratch
     saber::DevBuf tr_nt, tr_offs, tr_out_offs, tr_chunks, tr_aa, tr_out;
     // tantan masking scratch

@@ -26,6 +26,16 @@ namespace saber {
 // ---------------------------------------------------------------------------
 // small kernels
 // ---------------------------------------------------------------------------
+// Database seed mask from half-open runs [runs[2r], runs[2r+1]): one warp per
+// run, lanes over its bytes (the index's mask runs, index.rs:613-617).
+__global__ void k_fill_runs(const uint64_t* __restrict__ runs, uint64_t nruns, uint8_t* __restrict__ mask) {
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    for (uint64_t r = warp; r < nruns; r += nwarps)
+        for (uint64_t i = runs[2 * r] + lane; i < runs[2 * r + 1]; i += 32) mask[i] = 1;
+}
+
 __global__ void k_canon(uint8_t* __restrict__ r, uint64_t n) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     for (; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -1538,6 +1548,30 @@ int saber_gpu_translate6(saber_gpu* h, const uint8_t* nt, const uint64_t* nt_off
                          const uint8_t* codon64, uint8_t* out, uint64_t out_cap, uint64_t* out_offsets) {
     ENTER(h);
     return saber::translate6_host(h, nt, nt_offsets, nseq, codon64, out, out_cap, out_offsets);
+}
+
+int saber_gpu_load_db_mask_runs(saber_gpu* h, const uint64_t* runs, uint64_t nruns) {
+    ENTER(h);
+    h->sc_key = 0;  // the scan's database state depends on the mask
+    if (!h->main.has_db) return fail(h, SABER_ERR_STATE, "no database loaded");
+    if (nruns && !runs) return fail(h, SABER_ERR_ARG, "null runs");
+    const uint64_t n = h->main.n_res;
+    for (uint64_t r = 0; r < nruns; r++)
+        if (runs[2 * r] > runs[2 * r + 1] || runs[2 * r + 1] > n)
+            return fail(h, SABER_ERR_ARG, "mask run %llu out of the database", (unsigned long long)r);
+    CUALLOC(h, h->db_mask, n + 64);
+    CU(h, cudaMemsetAsync(h->db_mask.p, 0, n + 64, h->stream));
+    if (nruns) {
+        CUALLOC(h, h->mask_runs, nruns * 2 * sizeof(uint64_t));
+        CU(h, cudaMemcpyAsync(h->mask_runs.p, runs, nruns * 2 * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                              h->stream));
+        k_fill_runs<<<nblocks(nruns * 32, 256, h->sm_count * 16), 256, 0, h->stream>>>(
+            (const uint64_t*)h->mask_runs.p, nruns, h->db_mask.as<uint8_t>());
+        CU(h, cudaGetLastError());
+    }
+    CU(h, cudaStreamSynchronize(h->stream));
+    h->has_db_mask = true;
+    return SABER_OK;
 }
 
 int saber_gpu_scan(saber_gpu* h, const saber_scan_params* params, const uint8_t* q_mask, const int32_t* region_thr,

@@ -241,6 +241,7 @@ def load_library():
         "saber_gpu_tantan_mask": (ctypes.c_int, [P, P, P, P, P, U64, P, P, P, P]),
         "saber_gpu_tantan_mask_db": (ctypes.c_int, [P, P, P, P, P]),
         "saber_gpu_translate6": (ctypes.c_int, [P, P, P, U64, P, P, U64, P]),
+        "saber_gpu_load_db_mask_runs": (ctypes.c_int, [P, P, U64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -398,6 +399,12 @@ class Device:
     def load_db_mask(self, mask):
         m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
         self._check(self.lib.saber_gpu_load_db_mask(self.h, _ptr(m), 0 if m is None else m.size), "load_db_mask")
+
+    def load_db_mask_runs(self, runs):
+        """Seed mask of the loaded database from half-open (start, end) runs, expanded on the device."""
+        r = np.ascontiguousarray(np.asarray(runs, np.uint64).reshape(-1, 2))
+        self._check(self.lib.saber_gpu_load_db_mask_runs(self.h, _ptr(r) if r.size else None, r.shape[0]),
+                    "load_db_mask_runs")
 
     def tantan_mask(self, params, matrix, codes, offsets, want_probs=False):
         """Tantan seed mask of a batch of sequences -> (mask bool array, posteriors or None, masked, lambda)."""

@@ -154,10 +154,12 @@ class Searcher:
     runs one batch of queries end to end."""
 
     def __init__(self, dev, db_codes, db_offsets, params=None, matrix_name="BLOSUM62", gap_open=11, gap_extend=1,
-                 db_mask=None, nucleotide=None, stats_size=None):
+                 db_mask=None, nucleotide=None, stats_size=None, db_mask_runs=None):
         """stats_size: (database length, sequences) of the statistics when they
         are not the loaded residues and subjects (a translated database:
-        nucleotides / 3 and nucleotide sequences, driver.rs:575-583)."""
+        nucleotides / 3 and nucleotide sequences, driver.rs:575-583).
+        db_mask_runs: the database seed mask as half-open runs (a SABERIDX
+        file's "maskruns"), expanded on the device."""
         self.dev = dev
         self.p = params or SearchParams()
         self.is_protein = nucleotide is None
@@ -181,7 +183,9 @@ class Searcher:
         masking = MaskingMode.parse(self.p.masking) if self.is_protein else MaskingMode.NONE
         self.tantan = Tantan.protein(dev) if masking == MaskingMode.TANTAN else None
         self.db_residues_masked = 0
-        if db_mask is not None or self.tantan is None:
+        if db_mask_runs is not None:
+            dev.load_db_mask_runs(db_mask_runs)
+        elif db_mask is not None or self.tantan is None:
             dev.load_db_mask(db_mask)
         else:
             self.db_residues_masked = self.tantan.mask_database()
@@ -198,6 +202,15 @@ class Searcher:
             seed_max_occ=self.p.seed_max_occ, ref_db_residues=self.p.ref_db_residues,
             db_length=self.stats.db_length if stats_size else int(self.db_codes.size))
         self.counters = {}
+
+    @classmethod
+    def from_index(cls, dev, index, params=None, **kw):
+        """A searcher over a SABERIDX database (saber_gb300.index.SeedIndex):
+        its residues, offsets and stored mask runs, and for a translated
+        database its statistics sizes (run_with_index, driver.rs:615+)."""
+        if index.is_translated:
+            kw.setdefault("stats_size", index.stats_size())
+        return cls(dev, index.residues, index.subject_offsets, params, db_mask_runs=index.mask_runs, **kw)
 
     # ---- query preparation (engine.rs:714-786) ----
     def region_evalue(self):
