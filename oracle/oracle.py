@@ -224,11 +224,9 @@ def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, 
     cap = out_cap or max(1024, (qo.size - 1) * params.max_candidates)
     out = np.zeros(cap, REGION_DTYPE)
     ctr = ScanCounters()
-    n = f(_p(res), so.size - 1 if so.size else 0, None, None, None, None, 0, None, None, None, None, None, None, 0,
-          None) if False else f(_p(res), _p(so), so.size - 1, _p(dm) if dm is not None else None, _p(qc), _p(qo),
-                                qo.size - 1, _p(qb) if qb is not None else None, _p(qm) if qm is not None else None,
-                                _p(rt) if rt is not None else None, _p(m), ctypes.byref(params), _p(out), cap,
-                                ctypes.byref(ctr))
+    n = f(_p(res), _p(so), so.size - 1, _p(dm) if dm is not None else None, _p(qc), _p(qo), qo.size - 1,
+          _p(qb) if qb is not None else None, _p(qm) if qm is not None else None,
+          _p(rt) if rt is not None else None, _p(m), ctypes.byref(params), _p(out), cap, ctypes.byref(ctr))
     if n < 0:
         raise MemoryError("region buffer too small")
     return out[:n].copy(), {k: int(getattr(ctr, k)) for k, _ in ctr._fields_}
