@@ -56,6 +56,7 @@ def parse():
                          "database (its own JSON line)")
     ap.add_argument("--translated", action="store_true",
                     help="only the translated searches (nx, pn) and the six-frame translation (its own JSON line)")
+    ap.add_argument("--no-translated", action="store_true", help="skip the translated-search lines")
     ap.add_argument("--tr-records", type=int, default=1000, help="nx DNA query records / pn protein queries")
     ap.add_argument("--tr-subjects", type=int, default=100_000, help="nx protein subjects / pn DNA sequences")
     ap.add_argument("--nn-queries", type=int, default=2000)
@@ -396,7 +397,7 @@ def run_nn_search(a, local_rank):
         flush=True)
 
 
-def run_translated(a, local_rank):
+def run_translated(a, dev):
     """Translated searches through the library's host buffers, default
     preset, tantan on both sides: nx (DNA query records, six frames each,
     merged per record, against a protein database) and pn (protein queries
@@ -406,11 +407,10 @@ def run_translated(a, local_rank):
     database is timed alone (kernel through the C ABI, host buffers) with
     the oracle's scalar C on one host core as its CPU baseline."""
     from oracle import oracle as orc
-    from saber_gb300 import Device, synth
+    from saber_gb300 import synth
     from saber_gb300.search import SearchParams
     from saber_gb300.translated import BlastxSearcher, TblastnSearcher
     from saber_gb300.translation import codon_table
-    dev = Device(local_rank)
 
     def med(f, reps=3):
         f()
@@ -458,7 +458,7 @@ def run_translated(a, local_rank):
         "cpu_baseline": {"value": round(int(dna_s.offsets[k]) / tcpu, 1), "unit": "nt/s", "cores": 1,
                          "kind": "port", "sample": "first %d sequences (%d nt), oracle scalar C restatement of "
                                                    "translate_codes" % (k, int(dna_s.offsets[k]))}}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_search_only(a, local_rank):
@@ -578,8 +578,12 @@ def run_ours(a, rank, world, local_rank):
            "cells_per_step": int(cells // max(a.steps, 1))}
     if not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(qs, ss, bias, jobs, mat, a.cpu_seconds)
-    if not a.no_search:
+    # the search and translated sections run at N = 1 only (the other ranks
+    # would wait at the barrier meanwhile)
+    if not a.no_search and world == 1:
         out["search"] = run_search(a, dev)
+    if not a.no_translated and world == 1:
+        out["translated"] = run_translated(a, dev)
     print(json.dumps(out), flush=True)
 
 
@@ -598,7 +602,8 @@ def main():
             run_nn_search(a, local_rank)
     elif a.translated:
         if rank == 0:
-            run_translated(a, local_rank)
+            from saber_gb300 import Device
+            print(json.dumps(run_translated(a, Device(local_rank))), flush=True)
     elif a.search_only:
         if rank == 0:
             run_search_only(a, local_rank)
