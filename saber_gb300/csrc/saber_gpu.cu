@@ -801,15 +801,19 @@ struct AlignResult {
     int32_t score = 0;
     uint32_t q_start = 0, q_end = 0, s_start = 0, s_end = 0;
     uint64_t cells = 0;
-    std::vector<uint32_t> runs;  // (len << 8) | op
+    // op runs ((len << 8) | op): n_runs from run_off of pools[pool], the
+    // packed runs of the launch that produced the result
+    uint32_t pool = 0, n_runs = 0;
+    uint64_t run_off = 0;
 };
+using RunPools = std::vector<std::vector<uint32_t>>;
 
 // Budget of the direction-byte pool per launch (larger batches are split).
 constexpr uint64_t kDirPoolBudget = 2ull << 30;
 constexpr uint64_t kAlignSlabBudget = 512ull << 20;
 
 static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const std::vector<AlignHostReq>& in,
-                       uint64_t max_dir_bytes, std::vector<AlignResult>& out) {
+                       uint64_t max_dir_bytes, std::vector<AlignResult>& out, RunPools& pools) {
     if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
     if (!ds.has_db || !ds.qs.has) return fail(h, SABER_ERR_STATE, "no database or query set loaded");
     const QuerySet& qs = ds.qs;
@@ -913,6 +917,8 @@ static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const
             CU(h, cudaMemcpyAsync(hostruns.data(), h->al_packed.p, packed * 4, cudaMemcpyDeviceToHost, s));
             CU(h, cudaStreamSynchronize(s));
         }
+        const uint32_t pid = (uint32_t)pools.size();
+        pools.push_back(std::move(hostruns));
         for (uint32_t t = 0; t < nreq; t++) {
             AlignResult& r = out[idx[t]];
             const AlignOut& o = outs[t];
@@ -923,14 +929,16 @@ static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const
             r.s_start = o.s_start;
             r.s_end = o.s_end;
             r.cells = o.cells;
-            r.runs.assign(hostruns.begin() + dst[t], hostruns.begin() + dst[t] + cnt[t]);
+            r.pool = pid;
+            r.run_off = dst[t];
+            r.n_runs = cnt[t];
         }
     }
     return SABER_OK;
 }
 
-static void put_alignment(const AlignResult& r, int status, saber_alignment* o, uint32_t* ops, uint64_t ops_cap,
-                          uint64_t& ops_used, bool& overflow) {
+static void put_alignment(const AlignResult& r, const RunPools& pools, int status, saber_alignment* o, uint32_t* ops,
+                          uint64_t ops_cap, uint64_t& ops_used, bool& overflow) {
     o->status = status;
     o->score = r.score;
     o->q_start = r.q_start;
@@ -938,14 +946,14 @@ static void put_alignment(const AlignResult& r, int status, saber_alignment* o, 
     o->s_start = r.s_start;
     o->s_end = r.s_end;
     o->cells = r.cells;
-    o->n_ops = (uint32_t)r.runs.size();
+    o->n_ops = r.n_runs;
     o->ops_offset = (uint32_t)ops_used;
-    if (ops_used + r.runs.size() > ops_cap) {
+    if (ops_used + r.n_runs > ops_cap) {
         overflow = true;
-    } else if (!r.runs.empty()) {
-        memcpy(ops + ops_used, r.runs.data(), r.runs.size() * 4);
+    } else if (r.n_runs) {
+        memcpy(ops + ops_used, pools[r.pool].data() + r.run_off, (size_t)r.n_runs * 4);
     }
-    ops_used += r.runs.size();
+    ops_used += r.n_runs;
 }
 
 // Engine::traceback (src/search/engine.rs:1328-1393) and traceback_from_end
@@ -976,6 +984,7 @@ static int traceback_driver(saber_gpu* h, const saber_traceback_job* jobs, uint6
     }
     auto mlen = [&](uint64_t t) { return (int64_t)(qs.offs[jobs[t].query + 1] - qs.offs[jobs[t].query]); };
     std::vector<AlignResult> res;
+    RunPools pools;
     for (int round = 0; round < 64; round++) {
         std::vector<AlignHostReq> reqs;
         std::vector<uint64_t> who;
@@ -1030,7 +1039,7 @@ static int traceback_driver(saber_gpu* h, const saber_traceback_job* jobs, uint6
             }
         }
         if (reqs.empty()) break;
-        int rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res);
+        int rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res, pools);
         if (rc != SABER_OK) return rc;
         local.launches++;
         for (size_t k = 0; k < reqs.size(); k++) {
@@ -1124,7 +1133,7 @@ static int traceback_driver(saber_gpu* h, const saber_traceback_job* jobs, uint6
             out[t].ops_offset = (uint32_t)used;
             continue;
         }
-        put_alignment(x.best, x.status, &out[t], ops, ops_cap, used, overflow);
+        put_alignment(x.best, pools, x.status, &out[t], ops, ops_cap, used, overflow);
     }
     if (st) *st = local;
     if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
@@ -1464,11 +1473,13 @@ int saber_gpu_banded_align(saber_gpu* h, const saber_align_job* jobs, uint64_t n
         reqs[t] = AlignHostReq{jobs[t].query, jobs[t].win_begin, jobs[t].win_len, jobs[t].band_lo, jobs[t].band_hi,
                                jobs[t].stop_at, true};
     std::vector<AlignResult> res;
-    int rc = align_batch(h, h->scheme, h->main, reqs, max_dir_bytes, res);
+    RunPools pools;
+    int rc = align_batch(h, h->scheme, h->main, reqs, max_dir_bytes, res, pools);
     if (rc != SABER_OK) return rc;
     uint64_t used = 0;
     bool overflow = false;
-    for (uint64_t t = 0; t < njobs; t++) put_alignment(res[t], res[t].status, &out[t], ops, ops_cap, used, overflow);
+    for (uint64_t t = 0; t < njobs; t++)
+        put_alignment(res[t], pools, res[t].status, &out[t], ops, ops_cap, used, overflow);
     if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
     return SABER_OK;
 }
@@ -1493,11 +1504,12 @@ int saber_gpu_banded_align_one(saber_gpu* h, const uint8_t* query, uint32_t m, c
     if (hi < lo) return SABER_OK;
     std::vector<AlignHostReq> reqs(1, AlignHostReq{0, 0, n, lo, hi, stop_at, true});
     std::vector<AlignResult> res;
-    rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res);
+    RunPools pools;
+    rc = align_batch(h, h->scheme, ds, reqs, max_dir_bytes, res, pools);
     if (rc != SABER_OK) return rc;
     uint64_t used = 0;
     bool overflow = false;
-    put_alignment(res[0], res[0].status, out, ops, ops_cap, used, overflow);
+    put_alignment(res[0], pools, res[0].status, out, ops, ops_cap, used, overflow);
     if (overflow) return fail(h, SABER_ERR_ARG, "ops buffer too small: %llu runs needed", (unsigned long long)used);
     return SABER_OK;
 }
