@@ -455,12 +455,16 @@ struct Engine {
         return j;
     }
 
-    int score(const saber_band_job* jobs, size_t n, std::vector<int32_t>& out) {
-        out.assign(n, 0);
+    // Scores of n jobs into the handle's pinned staging slot `slot` (fast
+    // copies, no zero fill); *out stays valid until the slot is reused.
+    int score(const saber_band_job* jobs, size_t n, int slot, const int32_t** out) {
+        int32_t* sc = static_cast<int32_t*>(saber::pinned_scratch(h, slot, n * sizeof(int32_t)));
+        if (!sc) return SABER_ERR_NOMEM;
+        *out = sc;
         if (n == 0) return SABER_OK;
         saber_score_stats ss{};
         const double t0 = now_ms();
-        int rc = saber_gpu_score_band_jobs(h, jobs, n, out.data(), &ss);
+        int rc = saber_gpu_score_band_jobs(h, jobs, n, sc, &ss);
         if (rc != SABER_OK) return rc;
         st.t_score_calls_ms += now_ms() - t0;
         st.t_score_device_ms += ss.t_prep_ms + ss.t_fast_ms + ss.t_generic_ms;
@@ -518,8 +522,8 @@ struct Engine {
             }
         });
         for (uint64_t v : banded) st.band_scored_regions += v;
-        std::vector<int32_t> sc1;
-        int rc = score(s1, n1, sc1);
+        const int32_t* sc1 = nullptr;
+        int rc = score(s1, n1, 2, &sc1);
         if (rc != SABER_OK) return rc;
         // stage-2 decision per region (f64 threshold of the region's subject length)
         const double re = region_evalue();
@@ -566,8 +570,8 @@ struct Engine {
                 w++;
             }
         });
-        std::vector<int32_t> sc2;
-        rc = score(s2, n2, sc2);
+        const int32_t* sc2 = nullptr;
+        rc = score(s2, n2, 3, &sc2);
         if (rc != SABER_OK) return rc;
         for (size_t k = 0; k < n2; k++) scores[r2[k].qi][r2[k].ri] = sc2[k];
         st.band_rescored += n2;
