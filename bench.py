@@ -472,8 +472,9 @@ def run_ours(a, rank, world, local_rank):
     from saber_gb300 import Device
     from saber_gb300.gpu import JOB_DTYPE
     from saber_gb300.scoring import matrix
+    from saber_gb300.replicas import rank_seed, whole_job
     torch.cuda.set_device(local_rank)
-    seed = a.seed + 1000 * rank
+    seed = rank_seed(a.seed, rank)
     qs, ss, planted, bias, jobs = workload(seed, a.queries, a.subjects, a.jobs)
     mat = matrix("BLOSUM62")
     dev = Device(local_rank)
@@ -522,12 +523,8 @@ def run_ours(a, rank, world, local_rank):
         rescored += st["i16_rescored"]
     torch.cuda.synchronize()
     clk = clocks.stop()
-    t = torch.tensor([tot_ms], dtype=torch.float64)
-    c = torch.tensor([float(cells)], dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
-    value = c.item() / (t.item() * 1e-3) / 1e9
+    all_cells, max_ms = whole_job(cells, tot_ms, world)
+    value = all_cells / (max_ms * 1e-3) / 1e9
 
     # end to end: pinned host jobs in, scores out, through the C ABI
     h_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).pin_memory()
@@ -542,10 +539,8 @@ def run_ours(a, rank, world, local_rank):
         t0 = time.perf_counter()
         dev.score_band_jobs_ptr(h_jobs.data_ptr(), jobs.size, h_scores.data_ptr())
         e2e_s += time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e = c.item() / te.item() / 1e9
+    _, max_e2e_s = whole_job(cells, e2e_s, world)
+    e2e = all_cells / max_e2e_s / 1e9
     same = bool(np.array_equal(h_scores.numpy(), d_scores.cpu().numpy()))
 
     if rank != 0:
