@@ -56,7 +56,7 @@ class SeedIndex:
         rd64 = lambda o: int.from_bytes(mm[o:o + 8], "little")  # noqa: E731
         version = rd32(8)
         if version != FORMAT_VERSION:
-            raise IndexError_("%s: SABER index format v%d, this build reads v%d" % (path, version, FORMAT_VERSION))
+            raise IndexError_("%s: SABER index format v%d, this reader reads v%d" % (path, version, FORMAT_VERSION))
         if size < HEADER_BYTES:
             raise IndexError_("%s: truncated index (header incomplete)" % path)
         if rd32(12) != ENDIAN_MARK:

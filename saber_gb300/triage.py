@@ -8,7 +8,7 @@ weights with fp32 accumulation, trained on the GPU with the library's own
 forward / backward / Adam kernels.  This module builds training sets from
 plain searches (labels: the region produced a reported hit), initialises and
 trains the model, picks a conservative logit threshold and measures what it
-keeps.  The plain path stays the judge: with a model installed every kept
+keeps.  The plain path stays the arbiter: with a model installed every kept
 region is still scored exactly, and the lost-hit rate is measured against
 the plain search of the same batch.
 """

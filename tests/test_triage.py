@@ -1,6 +1,6 @@
 """Learned triage: the GPU forward / backward kernels against the float64
 oracle (oracle/triage.py), training, and the triaged search against the
-plain search (the judge): hits kept with identical scores, regions saved."""
+plain search (the arbiter): hits kept with identical scores, regions saved."""
 import numpy as np
 import pytest
 
