@@ -98,3 +98,10 @@ def test_search_over_index(dev, tmp_path):
                              gapped_protein("BLOSUM62", 11, 1), se.scan_params, dbm.view(np.uint8), qm.view(np.uint8))
     assert sum(len(h) for h in want) > 0
     _compare(got, want)
+
+
+def test_empty_database(tmp_path):
+    p = str(tmp_path / "empty.sdx")
+    IX.write_index(p, np.zeros(0, np.uint8), np.zeros(1, np.uint64), ids=[])
+    idx = IX.SeedIndex(p, verify_sections=True)
+    assert idx.num_subjects == 0 and idx.residues.size == 0 and idx.mask_runs is None

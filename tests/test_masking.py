@@ -178,3 +178,23 @@ def test_search_with_tantan_matches_oracle_engine(dev):
     _compare(got, want)
     # the python engine over the same device calls sees the same masks
     _compare(se.search_py(qs.codes, qs.offsets), want)
+
+
+@pytest.mark.gpu
+def test_gpu_mask_across_launches_and_odd_codes(dev):
+    """Two 5 M-residue sequences exceed one launch's 8 M scratch rows (the
+    batch is cut into launches, longest first); codes above 23 are clamped
+    to 23 as the reference does; an empty batch and empty sequences."""
+    rng = np.random.default_rng(11)
+    lens = np.array([5_000_000, 0, 37, 5_000_000, 0], np.int64)
+    codes = rng.integers(0, 20, int(lens.sum())).astype(np.uint8)
+    for s in range(0, codes.size - 500, 250_000):
+        codes[s:s + 300] = np.tile(rng.integers(0, 20, 7).astype(np.uint8), 43)[:300]
+    codes[5_000_000:5_000_037] = np.array([24, 30, 255] * 12 + [23], np.uint8)
+    offs = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint64)
+    m, p, n, _ = dev.tantan_mask(masking.TantanParams(), B62, codes, offs, want_probs=True)
+    wm, wp, wn = orc.tantan_mask(codes, offs, B62)
+    assert np.array_equal(p.view(np.uint32), wp.view(np.uint32))
+    assert np.array_equal(m, wm) and n == wn and n > 0
+    m0, p0, n0, _ = dev.tantan_mask(masking.TantanParams(), B62, np.zeros(0, np.uint8), np.zeros(1, np.uint64))
+    assert m0.size == 0 and n0 == 0
