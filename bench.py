@@ -240,7 +240,13 @@ def run_search(a, dev):
         "unit": "queries/s", "timing": "median of 3 calls, host wall clock around saber_gpu_search (query "
                                         "codes in, hit records out)",
         "plain": {"value": round(nq / tp, 1), "hits": int(len(plain)), "regions": cp["regions"],
-                  "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages}},
+                  "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages},
+                  # the scan stage as database bytes (1 per residue) per second; it is bound by
+                  # the L1 data pipe and issue (seed-table lookups), not by HBM
+                  "scan_db_gb_per_s": round(int(sb.codes.size) / (cp["t_scan_ms"] * 1e-3) / 1e9, 2)
+                  if cp["t_scan_ms"] > 0 else None,
+                  "score_device_gcups": round(cp["banded_cells"] / (cp["t_score_device_ms"] * 1e-3) / 1e9, 1)
+                  if cp["t_score_device_ms"] > 0 else None},
     }
     # two batches in flight (SearchPool: two handles, host stages of one batch
     # overlapping device stages of the other); the second batch is another
@@ -392,6 +398,8 @@ def run_nn_search(a, local_rank):
         "unit": "queries/s", "value": round((len(qs.offsets) - 1) / tp, 1), "s_per_search": round(tp, 3),
         "hits": int(len(out[0])), "counters": {k: int(st[k]) for k in keys if k in st},
         "stages_ms": {k: round(v, 1) for k, v in st.items() if k.startswith("t_")},
+        "score_device_gcups": round(st["banded_cells"] / (st["t_score_device_ms"] * 1e-3) / 1e9, 1)
+        if st.get("t_score_device_ms", 0) > 0 else None,
         "data_gen_s": round(t1 - t0, 1), "long_steps": dev.long_steps,
         "timing": "median of 2 calls, host wall clock around saber_gpu_search"}}),
         flush=True)
