@@ -10,7 +10,7 @@
 // genetic code.
 //
 // Byte work bound by HBM: one thread per output residue (three input bytes
-// read through L1, one written).  The host lists chunks of 1,024 outputs of
+// read through L1, one written).  The host lists chunks of 4,096 outputs of
 // one frame (segment index, first output), so a block finds its frame
 // without a search.
 #include <cuda_runtime.h>
@@ -22,7 +22,7 @@
 namespace saber {
 
 constexpr unsigned kTrThreads = 256;
-constexpr unsigned kTrPerThread = 4;
+constexpr unsigned kTrPerThread = 16;
 constexpr uint64_t kTrChunk = kTrThreads * kTrPerThread;
 
 __global__ void __launch_bounds__(kTrThreads) k_translate6(const uint8_t* __restrict__ nt,
