@@ -65,3 +65,23 @@ def test_open_without_gpu_reports_error():
         pytest.skip("a GPU is present")
     with pytest.raises(gpu.SaberGpuError):
         gpu.Device(0)
+
+
+def test_headers_compile_as_plain_c(tmp_path):
+    """The boundary is plain C: every header compiles as C99 on its own and
+    a C translation unit can call through it."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c", h],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    src = tmp_path / "use.c"
+    src.write_text('#include "saber_gpu.h"\nint main(void) { saber_gpu* h = 0; saber_tantan_params p = {0};\n'
+                   '  (void)p; return saber_gpu_open(0, &h); }\n')
+    r = subprocess.run([cc, "-std=c99", "-I", os.path.join(REPO, "include"), "-c", str(src), "-o",
+                        str(tmp_path / "use.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
