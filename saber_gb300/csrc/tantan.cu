@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kTtWarps * 32, 4) k_tantan8(const __grid_const
     const int lane = threadIdx.x & 31, g = lane >> 3, k = lane & 7;
     const int wib = threadIdx.x >> 5;
     uint8_t* ring = rings + (wib * kTgSeqs + g) * kRingPitch;
-    const uint64_t kk = k0 + ((uint64_t)blockIdx.x * kTtWarps + wib) * kTgSeqs + g;
+    const uint64_t kk = k0 + ((uint64_t)blockIdx.x * (blockDim.x >> 5) + wib) * kTgSeqs + g;
     int64_t n = 0;
     uint64_t st = 0;
     float* F = fwdF;
@@ -659,9 +659,13 @@ int tantan_run(saber_gpu* h, const TantanModel& M, const uint8_t* d_codes, const
     for (size_t c = 0; c + 1 < cuts.size(); c++) {
         const uint64_t k0 = cuts[c], k1 = cuts[c + 1];
         if (M.w == 50) {  // tantan's protein default: eight lanes per sequence
-            const uint64_t per_block = (uint64_t)kTtWarps * kTgSeqs;
+            // a batch too small to fill every SM with full blocks (a query
+            // batch) runs two warps per block: more SMs, less contention
+            // on each sequence's serial chain
+            const unsigned warps = (k1 - k0) < (uint64_t)h->sm_count * kTtWarps * kTgSeqs ? 2u : kTtWarps;
+            const uint64_t per_block = (uint64_t)warps * kTgSeqs;
             const unsigned blocks = (unsigned)((k1 - k0 + per_block - 1) / per_block);
-            k_tantan8<50><<<blocks, kTtWarps * 32, 0, h->stream>>>(
+            k_tantan8<50><<<blocks, warps * 32, 0, h->stream>>>(
                 M, d_codes, d_offs, (const uint32_t*)h->tt_ord.p, (const uint64_t*)h->tt_base.p, k0, k1,
                 (float*)h->tt_F.p, (float2*)h->tt_BS.p, d_mask, d_probs, (unsigned long long*)h->tt_count.p);
             CU(h, cudaGetLastError());
