@@ -152,14 +152,18 @@ def m8_line(qid, sid, h):
 
 
 def search_batch(db_codes, db_offsets, q_codes, q_offsets, params, matrix, go, ge, kp, scan_params, db_mask=None,
-                 q_mask=None, is_protein=True, stats_size=None):
+                 q_mask=None, is_protein=True, stats_size=None, threads=1):
     """Hits per query (lists of dicts in report order) for one batch.
     stats_size: (database length, sequences) of the statistics when they are
-    not the residues and subjects (translated databases, driver.rs:575-583)."""
+    not the residues and subjects (translated databases, driver.rs:575-583).
+    threads: host threads of the scan and of the banded scores (every window
+    is scored on its own, so the hits do not depend on it)."""
     from saber_gb300.bias import composition_bias
+    from saber_gb300.gpu import JOB_DTYPE
     from saber_gb300.stats import SearchStatistics
     P = params
     slen = np.diff(np.asarray(db_offsets, np.int64))
+    soff = np.asarray(db_offsets, np.int64)
     nsub = slen.size
     stats = SearchStatistics(kp, *(stats_size or (int(len(db_codes)), nsub)), P.evalue_model)
     nq = len(q_offsets) - 1
@@ -186,32 +190,57 @@ def search_batch(db_codes, db_offsets, q_codes, q_offsets, params, matrix, go, g
     elif nq and nsub:
         rthr = np.array([p[5] for p in preps], np.int32)
         regs, _ = orc.scan_regions(db_codes, db_offsets, db_mask, q_codes, q_offsets, bias, q_mask, rthr, matrix,
-                                   scan_params)
+                                   scan_params, threads=threads)
         for r in regs:
             regs_q[int(r["query"])].append((int(r["subject"]), int(r["d_min"]), int(r["d_max"]), int(r["best"])))
+    # score_windows (engine.rs:1021-1099) for every query: the first stage
+    # (the full window, the region's narrow band, or the plan band), then the
+    # plan band for the narrow scores that pass the prefilter threshold
+    wn, fb = P.score_prefilter_band, P.score_band
+    plans_q, jobs1, jobs2, where2 = [], [], [], []
+    for qi in range(nq):
+        q, b, qs, floor, rfloor, _ = preps[qi]
+        m = len(q)
+        regs = regs_q[qi] if m else []
+        plans = plan_windows(regs, m, slen, P.hsp_threshold, P.window_slack, P.score_band, P.exhaustive)
+        plans_q.append(plans)
+        for (s, dmin, dmax, best), (lo, hi, band) in zip(regs, plans):
+            n = hi - lo
+            if band is None:
+                jobs1.append((qi, s, soff[s] + lo, n, -m, n, 0))
+            elif 0 < wn < fb:
+                nlo, nhi = _clip(dmin - wn - lo, dmax + wn - lo, m, n)
+                jobs1.append((qi, s, soff[s] + lo, n, nlo, nhi, 1))
+            else:
+                jobs1.append((qi, s, soff[s] + lo, n, band[0], band[1], 0))
+    j1 = np.array(jobs1, JOB_DTYPE) if jobs1 else np.zeros(0, JOB_DTYPE)
+    sc1 = orc.score_band_jobs(db_codes, q_codes, q_offsets, bias, j1, matrix, go, ge, threads)[0] if j1.size \
+        else np.zeros(0, np.int32)
+    k = 0
+    for qi in range(nq):
+        qs, rfloor = preps[qi][2], preps[qi][4]
+        for (s, dmin, dmax, best), (lo, hi, band) in zip(regs_q[qi] if len(preps[qi][0]) else [], plans_q[qi]):
+            if j1[k]["flags"] == 1:
+                thr = P.score_prefilter_frac * qs.floor_lower_bound(e_reg, None, int(slen[s]), rfloor)
+                if not float(sc1[k]) < thr:
+                    jobs2.append((qi, s, soff[s] + lo, hi - lo, band[0], band[1], 0))
+                    where2.append(k)
+            k += 1
+    scores_all = sc1.copy()
+    if jobs2:
+        sc2 = orc.score_band_jobs(db_codes, q_codes, q_offsets, bias, np.array(jobs2, JOB_DTYPE), matrix, go, ge,
+                                  threads)[0]
+        scores_all[np.array(where2, np.int64)] = sc2
     out = []
+    k = 0
     for qi in range(nq):
         q, b, qs, floor, rfloor, _ = preps[qi]
         m = len(q)
         regs = regs_q[qi] if m else []
         bo = b if np.any(b != 0) else None
-        plans = plan_windows(regs, m, slen, P.hsp_threshold, P.window_slack, P.score_band, P.exhaustive)
-        # score_windows, engine.rs:1021-1099
-        scores = []
-        wn, fb = P.score_prefilter_band, P.score_band
-        for (s, dmin, dmax, best), (lo, hi, band) in zip(regs, plans):
-            sub = np.asarray(db_codes[db_offsets[s] + lo:db_offsets[s] + hi])
-            if band is None:
-                scores.append(orc.banded_score(q, sub, bo, matrix, go, ge, -m, len(sub))[0])
-                continue
-            if 0 < wn < fb:
-                nlo, nhi = _clip(dmin - wn - lo, dmax + wn - lo, m, len(sub))
-                sc = orc.banded_score(q, sub, bo, matrix, go, ge, nlo, nhi)[0]
-                thr = P.score_prefilter_frac * qs.floor_lower_bound(e_reg, None, int(slen[s]), rfloor)
-                if float(sc) < thr:
-                    scores.append(sc)
-                    continue
-            scores.append(orc.banded_score(q, sub, bo, matrix, go, ge, band[0], band[1])[0])
+        plans = plans_q[qi]
+        scores = [int(x) for x in scores_all[k:k + len(regs)]]
+        k += len(regs)
         # finish, engine.rs:1127-1221
         ecut = P.evalue if (P.evalue > 0 and math.isfinite(P.evalue)) else math.inf
         order = []

@@ -494,12 +494,265 @@ static int64_t code_at(const uint8_t* sr, const uint16_t* offs, uint32_t w, uint
     return c;
 }
 
+/* Work split of the scan oracle over host threads.  Subjects (counting and
+ * hit passes) and (subject, query) pairs (the visit) are independent units;
+ * per-thread outputs are merged and put in the total orders the sequential
+ * statement uses (cmp_surv, cmp_region), so the result does not depend on
+ * the thread count. */
+typedef struct {
+    void (*fn)(void* ctx, uint64_t b, uint64_t e, int tid);
+    void* ctx;
+    uint64_t n, chunk, next;
+    int tid_next;
+} par_ctx;
+
+static void* par_worker(void* arg) {
+    par_ctx* p = (par_ctx*)arg;
+    int tid = __atomic_fetch_add(&p->tid_next, 1, __ATOMIC_RELAXED);
+    for (;;) {
+        uint64_t b = __atomic_fetch_add(&p->next, p->chunk, __ATOMIC_RELAXED);
+        if (b >= p->n) break;
+        uint64_t e = b + p->chunk < p->n ? b + p->chunk : p->n;
+        p->fn(p->ctx, b, e, tid);
+    }
+    return NULL;
+}
+
+static void par_for(uint64_t n, uint64_t chunk, int threads, void (*fn)(void*, uint64_t, uint64_t, int), void* ctx) {
+    par_ctx p = {fn, ctx, n, chunk ? chunk : 1, 0, 0};
+    pthread_t tid[256];
+    int started = 0;
+    for (int t = 1; t < threads && t < 256; t++) {
+        if (pthread_create(&tid[started], NULL, par_worker, &p) != 0) break;
+        started++;
+    }
+    par_worker(&p);
+    for (int t = 0; t < started; t++) pthread_join(tid[t], NULL);
+}
+
+typedef struct {
+    surv_t* v;
+    size_t n, cap;
+    orc_scan_counters c;
+    orc_region* r;
+    size_t nr, rcap;
+} scan_local;
+
+typedef struct {
+    const uint8_t* res; const uint64_t* soffs; const uint8_t* sb;
+    const uint8_t* qred; const uint8_t* qfull; const uint8_t* qcodes; const uint64_t* qoffs;
+    const int8_t* qbias; const int32_t* region_thr; const int32_t* matrix;
+    const orc_scan_params* P;
+    uint32_t span, w, asize;
+    const uint16_t* offs;
+    int64_t cfil;
+    uint32_t* cnt;       /* code counts of the counting pass (atomic adds) */
+    uint64_t total;      /* valid positions of the counting pass (atomic add) */
+    const seed_t* seeds; /* batch seeds of the shape, code order */
+    size_t nseed;
+    uint32_t shape;
+    const surv_t* sv;    /* sorted survivors (visit pass) */
+    const size_t* grp;   /* (subject, query) group starts, ngrp + 1 entries */
+    scan_local* loc;
+} scan_ctx;
+
+/* frequent codes: counts of the database's valid codes (scan.rs:1184-1238) */
+static void scan_count(void* vc, uint64_t b0, uint64_t e0, int tid) {
+    scan_ctx* c = (scan_ctx*)vc;
+    uint64_t total = 0;
+    for (uint64_t s = b0; s < e0; s++) {
+        uint64_t b = c->soffs[s], e = c->soffs[s + 1];
+        if (e - b < c->span) continue;
+        for (uint64_t p = b; p + c->span <= e; p++) {
+            int64_t code = code_at(c->sb + p, c->offs, c->w, c->asize);
+            if (code >= 0) { __atomic_fetch_add(&c->cnt[code], 1u, __ATOMIC_RELAXED); total++; }
+        }
+    }
+    __atomic_fetch_add(&c->total, total, __ATOMIC_RELAXED);
+}
+
+/* database positions: hits and window filter (scan.rs:1603-1856) */
+static void scan_hits(void* vc, uint64_t b0, uint64_t e0, int tid) {
+    scan_ctx* c = (scan_ctx*)vc;
+    scan_local* L = &c->loc[tid];
+    const orc_scan_params* P = c->P;
+    for (uint64_t s = b0; s < e0; s++) {
+        uint64_t b = c->soffs[s], e = c->soffs[s + 1];
+        const int64_t sl = (int64_t)(e - b);
+        if ((uint64_t)sl < c->span) continue;
+        for (int64_t p = 0; p + (int64_t)c->span <= sl; p++) {
+            int64_t code = code_at(c->sb + b + p, c->offs, c->w, c->asize);
+            if (code < 0) continue;
+            /* entries of the code */
+            size_t lo = 0, hi = c->nseed;
+            while (lo < hi) { size_t mid = (lo + hi) / 2; if (c->seeds[mid].code < (uint32_t)code) lo = mid + 1; else hi = mid; }
+            for (size_t k = lo; k < c->nseed && c->seeds[k].code == (uint32_t)code; k++) {
+                const uint32_t q = c->seeds[k].q, qp = c->seeds[k].p;
+                L->c.hits++;
+                if (P->hit_filter_min_ids > 0) {
+                    const int64_t ss = p + c->cfil - 16;
+                    const int64_t qs = (int64_t)qp + c->cfil - 16;
+                    const int64_t qlen = (int64_t)(c->qoffs[q + 1] - c->qoffs[q]);
+                    uint32_t r = 0, ex = 0;
+                    for (int t = 0; t < 32; t++) {
+                        int64_t j = ss + t, i = qs + t;
+                        if (j < 0 || j >= sl) continue;
+                        if (i < 0 || i >= qlen) continue;
+                        uint8_t qr = c->qred[c->qoffs[q] + i];
+                        if (qr != 0xFE && qr == (c->sb[b + j] & 0x7F)) {
+                            r++;
+                            if (P->hit_filter_exact_weight > 0 && c->qfull[c->qoffs[q] + i] == c->res[b + j]) ex++;
+                        }
+                    }
+                    if (r + P->hit_filter_exact_weight * ex < P->hit_filter_min_ids) {
+                        L->c.hits_filtered++;
+                        continue;
+                    }
+                }
+                if (L->n == L->cap) { L->cap = L->cap ? 2 * L->cap : 1024; L->v = (surv_t*)realloc(L->v, L->cap * sizeof(surv_t)); }
+                surv_t* o = &L->v[L->n++];
+                o->subject = (uint32_t)s; o->query = q; o->qp = qp; o->sp = (uint32_t)p; o->shape = c->shape;
+            }
+        }
+    }
+}
+
+static void push_region(scan_local* L, orc_region r) {
+    if (L->nr == L->rcap) { L->rcap = L->rcap ? 2 * L->rcap : 1024; L->r = (orc_region*)realloc(L->r, L->rcap * sizeof(orc_region)); }
+    L->r[L->nr++] = r;
+}
+
+/* one (subject, query) pair: coverage + X-drop -> HSPs -> regions
+ * (visit_chunk_inner / visit_scan / finish_subject_into, scan.rs:2084-2474) */
+static void scan_visit(void* vc, uint64_t g0, uint64_t g1, int tid) {
+    scan_ctx* c = (scan_ctx*)vc;
+    scan_local* L = &c->loc[tid];
+    const orc_scan_params* P = c->P;
+    const int32_t* matrix = c->matrix;
+    const surv_t* sv = c->sv;
+    for (uint64_t g = g0; g < g1; g++) {
+        const size_t i = c->grp[g], j = c->grp[g + 1];
+        const uint32_t q = sv[i].query, s = sv[i].subject;
+        const uint8_t* qc = c->qcodes + c->qoffs[q];
+        const int8_t* qb = c->qbias ? c->qbias + c->qoffs[q] : NULL;
+        const uint64_t qlen = c->qoffs[q + 1] - c->qoffs[q];
+        const uint8_t* sc = c->res + c->soffs[s];
+        const uint64_t sl = c->soffs[s + 1] - c->soffs[s];
+        uint32_t* cover = (uint32_t*)calloc(qlen + sl + 1, sizeof(uint32_t));
+        size_t nh = 0;
+        hsp_t* hs = (hsp_t*)malloc((j - i) * sizeof(hsp_t));
+        for (size_t k = i; k < j; k++) {
+            const uint32_t qp = sv[k].qp, sp = sv[k].sp;
+            const int64_t d = (int64_t)sp - (int64_t)qp;
+            const size_t di = (size_t)(d + (int64_t)qlen);
+            if (qp < cover[di]) { L->c.extensions_avoided++; continue; }
+            L->c.ungapped_extensions++;
+            uint64_t lo, hi;
+            int32_t score = orc_ungapped_xdrop(qc, qlen, sc, sl, qp, sp, matrix, qb, P->x_drop, &lo, &hi);
+            {
+                /* steps of xdrop_cat (scan.rs:904): right steps + left steps */
+                uint64_t nrt = qlen - qp < sl - sp ? qlen - qp : sl - sp;
+                uint64_t nlt = qp < sp ? qp : sp;
+                int32_t best = 0, cur = 0; uint64_t tr = 0;
+                while (tr < nrt) {
+                    cur += matrix[(qc[qp + tr] < 24 ? qc[qp + tr] : 22) * 24 + (sc[sp + tr] < 24 ? sc[sp + tr] : 22)] + (qb ? qb[qp + tr] : 0);
+                    tr++;
+                    if (cur > best) best = cur;
+                    if (cur < best - P->x_drop) break;
+                }
+                int32_t bl = 0, cl = 0; uint64_t tl = 1;
+                if (nlt > 0) {
+                    for (;;) {
+                        cl += matrix[(qc[qp - tl] < 24 ? qc[qp - tl] : 22) * 24 + (sc[sp - tl] < 24 ? sc[sp - tl] : 22)] + (qb ? qb[qp - tl] : 0);
+                        if (cl > bl) bl = cl;
+                        tl++;
+                        if (!(tl <= nlt && cl >= bl - P->x_drop)) break;
+                    }
+                }
+                L->c.xdrop_steps += tr + tl - 1;
+            }
+            cover[di] = (uint32_t)hi;
+            if (score >= P->hsp_threshold) {
+                hs[nh].diag = d; hs[nh].q_lo = (uint32_t)lo; hs[nh].q_hi = (uint32_t)hi; hs[nh].score = score;
+                nh++;
+            }
+        }
+        free(cover);
+        if (nh) {
+            /* finish_subject_into (scan.rs:2437-2474) */
+            L->c.hsps += nh;
+            qsort(hs, nh, sizeof(hsp_t), cmp_hsp);
+            const int64_t join = 2 * (int64_t)P->window_slack;
+            orc_region* rg = (orc_region*)malloc(nh * sizeof(orc_region));
+            uint32_t* ev_n = (uint32_t*)malloc(nh * sizeof(uint32_t));
+            int32_t* ev_s = (int32_t*)malloc(nh * sizeof(int32_t));
+            size_t ng = 0;
+            for (size_t k = 0; k < nh; k++) {
+                if (ng > 0 && hs[k].diag - rg[ng - 1].d_max <= join) {
+                    if (hs[k].diag > rg[ng - 1].d_max) rg[ng - 1].d_max = (int32_t)hs[k].diag;
+                    if (hs[k].score > rg[ng - 1].best) rg[ng - 1].best = hs[k].score;
+                    ev_n[ng - 1]++;
+                    int64_t sum = (int64_t)ev_s[ng - 1] + hs[k].score;
+                    ev_s[ng - 1] = sum > INT32_MAX ? INT32_MAX : (sum < INT32_MIN ? INT32_MIN : (int32_t)sum);
+                } else {
+                    rg[ng].query = q; rg[ng].subject = s;
+                    rg[ng].d_min = rg[ng].d_max = (int32_t)hs[k].diag; rg[ng].best = hs[k].score;
+                    ev_n[ng] = 1; ev_s[ng] = hs[k].score;
+                    ng++;
+                }
+            }
+            const int32_t thr = c->region_thr ? c->region_thr[q] : P->hsp_threshold;
+            size_t kept = ng;
+            if (thr > P->hsp_threshold) {
+                kept = 0;
+                for (size_t k = 0; k < ng; k++)
+                    if (rg[k].best >= thr || (ev_n[k] >= 2 && ev_s[k] >= thr)) rg[kept++] = rg[k];
+                L->c.regions_weak_dropped += ng - kept;
+            }
+            /* sort by (best desc, d_min asc), keep max_regions_per_subject */
+            for (size_t a = 1; a < kept; a++) {
+                orc_region x = rg[a];
+                size_t b2 = a;
+                while (b2 > 0 && (rg[b2 - 1].best < x.best || (rg[b2 - 1].best == x.best && rg[b2 - 1].d_min > x.d_min))) {
+                    rg[b2] = rg[b2 - 1];
+                    b2--;
+                }
+                rg[b2] = x;
+            }
+            size_t keep = kept < P->max_regions_per_subject ? kept : (P->max_regions_per_subject ? P->max_regions_per_subject : 1);
+            if (keep > kept) keep = kept;
+            for (size_t k = 0; k < keep; k++) push_region(L, rg[k]);
+            free(rg); free(ev_n); free(ev_s);
+        }
+        free(hs);
+    }
+}
+
+static void add_counters(orc_scan_counters* a, const orc_scan_counters* b) {
+    a->seed_positions += b->seed_positions; a->seeds_frequent_skipped += b->seeds_frequent_skipped;
+    a->hits += b->hits; a->hits_filtered += b->hits_filtered; a->ungapped_extensions += b->ungapped_extensions;
+    a->extensions_avoided += b->extensions_avoided; a->xdrop_steps += b->xdrop_steps; a->hsps += b->hsps;
+    a->regions += b->regions; a->regions_weak_dropped += b->regions_weak_dropped;
+    a->regions_dropped_by_cap += b->regions_dropped_by_cap;
+}
+
 int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsub, const uint8_t* db_mask,
                          const uint8_t* qcodes, const uint64_t* qoffs, uint32_t nq, const int8_t* qbias,
                          const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
                          const orc_scan_params* P, orc_region* out, uint64_t out_cap,
                          orc_scan_counters* ctr) {
+    return orc_scan_regions_mt(res, soffs, nsub, db_mask, qcodes, qoffs, nq, qbias, q_mask, region_thr, matrix, P,
+                               out, out_cap, ctr, 1);
+}
+
+int64_t orc_scan_regions_mt(const uint8_t* res, const uint64_t* soffs, uint64_t nsub, const uint8_t* db_mask,
+                            const uint8_t* qcodes, const uint64_t* qoffs, uint32_t nq, const int8_t* qbias,
+                            const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
+                            const orc_scan_params* P, orc_region* out, uint64_t out_cap,
+                            orc_scan_counters* ctr, int threads) {
     memset(ctr, 0, sizeof(*ctr));
+    if (threads < 1) threads = 1;
+    if (threads > 256) threads = 256;
     const uint64_t N = soffs[nsub];
     const uint32_t asize = P->alpha_size;
     /* database seed bytes (scan.rs:123-141, seed_map at 1072-1077) */
@@ -523,32 +776,31 @@ int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsu
     }
     uint32_t cmin = 1u << 30;
     for (uint32_t s = 0; s < P->nshapes; s++) if (P->shape_span[s] < cmin) cmin = P->shape_span[s];
-    const int64_t cfil = cmin / 2;
 
-    size_t ns_cap = 1024, ns = 0;
-    surv_t* sv = (surv_t*)malloc(ns_cap * sizeof(surv_t));
+    scan_local* loc = (scan_local*)calloc((size_t)threads, sizeof(scan_local));
+    scan_ctx cx;
+    memset(&cx, 0, sizeof(cx));
+    cx.res = res; cx.soffs = soffs; cx.sb = sb; cx.qred = qred; cx.qfull = qfull; cx.qcodes = qcodes;
+    cx.qoffs = qoffs; cx.qbias = qbias; cx.region_thr = region_thr; cx.matrix = matrix; cx.P = P;
+    cx.asize = asize; cx.cfil = cmin / 2; cx.loc = loc;
+    const uint64_t sub_chunk = 256;
     for (uint32_t si = 0; si < P->nshapes; si++) {
         const uint32_t span = P->shape_span[si], w = P->shape_weight[si];
         const uint16_t* offs = P->shape_off[si];
         uint64_t ncodes = 1;
         for (uint32_t k = 0; k < w; k++) ncodes *= asize;
+        cx.span = span; cx.w = w; cx.offs = offs; cx.shape = si;
         /* frequent codes (scan.rs:1184-1238) */
-        uint32_t* cnt = (uint32_t*)calloc(ncodes, sizeof(uint32_t));
-        uint64_t total = 0;
-        for (uint64_t s = 0; s < nsub; s++) {
-            uint64_t b = soffs[s], e = soffs[s + 1];
-            if (e - b < span) continue;
-            for (uint64_t p = b; p + span <= e; p++) {
-                int64_t c = code_at(sb + p, offs, w, asize);
-                if (c >= 0) { cnt[c]++; total++; }
-            }
-        }
+        cx.cnt = (uint32_t*)calloc(ncodes, sizeof(uint32_t));
+        cx.total = 0;
+        par_for(nsub, sub_chunk, threads, scan_count, &cx);
         uint64_t cap = P->seed_max_occ > 0 ? P->seed_max_occ
-                                           : orc_auto_occ_cap(total, ncodes, P->db_length, P->ref_db_residues);
+                                           : orc_auto_occ_cap(cx.total, ncodes, P->db_length, P->ref_db_residues);
         uint8_t* freq = (uint8_t*)calloc(ncodes, 1);
-        if (total > cap)
-            for (uint64_t c = 0; c < ncodes; c++) freq[c] = cnt[c] > cap;
-        free(cnt);
+        if (cx.total > cap)
+            for (uint64_t c = 0; c < ncodes; c++) freq[c] = cx.cnt[c] > cap;
+        free(cx.cnt);
+        cx.cnt = NULL;
         /* query seeds (scan.rs:1541-1562) */
         size_t nseed = 0, seed_cap = 1024;
         seed_t* seeds = (seed_t*)malloc(seed_cap * sizeof(seed_t));
@@ -567,161 +819,55 @@ int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsu
         free(freq);
         ctr->seed_positions += nseed;
         qsort(seeds, nseed, sizeof(seed_t), cmp_seed);
-        /* database positions: hits and window filter (scan.rs:1603-1856) */
-        for (uint64_t s = 0; s < nsub && nseed; s++) {
-            uint64_t b = soffs[s], e = soffs[s + 1];
-            const int64_t sl = (int64_t)(e - b);
-            if ((uint64_t)sl < span) continue;
-            for (int64_t p = 0; p + (int64_t)span <= sl; p++) {
-                int64_t c = code_at(sb + b + p, offs, w, asize);
-                if (c < 0) continue;
-                /* entries of code c */
-                size_t lo = 0, hi = nseed;
-                while (lo < hi) { size_t mid = (lo + hi) / 2; if (seeds[mid].code < (uint32_t)c) lo = mid + 1; else hi = mid; }
-                for (size_t k = lo; k < nseed && seeds[k].code == (uint32_t)c; k++) {
-                    const uint32_t q = seeds[k].q, qp = seeds[k].p;
-                    ctr->hits++;
-                    if (P->hit_filter_min_ids > 0) {
-                        const int64_t ss = p + cfil - 16;
-                        const int64_t qs = (int64_t)qp + cfil - 16;
-                        const int64_t qlen = (int64_t)(qoffs[q + 1] - qoffs[q]);
-                        uint32_t r = 0, ex = 0;
-                        for (int t = 0; t < 32; t++) {
-                            int64_t j = ss + t, i = qs + t;
-                            if (j < 0 || j >= sl) continue;
-                            if (i < 0 || i >= qlen) continue;
-                            uint8_t qr = qred[qoffs[q] + i];
-                            if (qr != 0xFE && qr == (sb[b + j] & 0x7F)) {
-                                r++;
-                                if (P->hit_filter_exact_weight > 0 && qfull[qoffs[q] + i] == res[b + j]) ex++;
-                            }
-                        }
-                        if (r + P->hit_filter_exact_weight * ex < P->hit_filter_min_ids) {
-                            ctr->hits_filtered++;
-                            continue;
-                        }
-                    }
-                    if (ns == ns_cap) { ns_cap *= 2; sv = (surv_t*)realloc(sv, ns_cap * sizeof(surv_t)); }
-                    sv[ns].subject = (uint32_t)s; sv[ns].query = q; sv[ns].qp = qp; sv[ns].sp = (uint32_t)p;
-                    sv[ns].shape = si;
-                    ns++;
-                }
-            }
-        }
+        cx.seeds = seeds;
+        cx.nseed = nseed;
+        if (nseed) par_for(nsub, sub_chunk, threads, scan_hits, &cx);
         free(seeds);
     }
     free(sb);
-    free(qred);
-    free(qfull);
+    /* survivors of all threads, in the (subject, query, qp, shape, sp) order */
+    size_t ns = 0;
+    for (int t = 0; t < threads; t++) ns += loc[t].n;
+    surv_t* sv = (surv_t*)malloc((ns ? ns : 1) * sizeof(surv_t));
+    {
+        size_t o = 0;
+        for (int t = 0; t < threads; t++) {
+            if (loc[t].n) memcpy(sv + o, loc[t].v, loc[t].n * sizeof(surv_t));
+            o += loc[t].n;
+            free(loc[t].v);
+            loc[t].v = NULL;
+        }
+    }
     qsort(sv, ns, sizeof(surv_t), cmp_surv);
-
-    /* visit every (subject, query) pair: coverage + X-drop -> HSPs -> regions */
-    size_t nr = 0, r_cap = 1024;
-    orc_region* regs_all = (orc_region*)malloc(r_cap * sizeof(orc_region));
-    size_t i = 0;
-    while (i < ns) {
+    /* (subject, query) groups, visited on all threads */
+    size_t ngrp = 0;
+    size_t* grp = (size_t*)malloc((ns + 1) * sizeof(size_t));
+    for (size_t i = 0; i < ns;) {
         size_t j = i + 1;
         while (j < ns && sv[j].subject == sv[i].subject && sv[j].query == sv[i].query) j++;
-        const uint32_t q = sv[i].query, s = sv[i].subject;
-        const uint8_t* qc = qcodes + qoffs[q];
-        const int8_t* qb = qbias ? qbias + qoffs[q] : NULL;
-        const uint64_t qlen = qoffs[q + 1] - qoffs[q];
-        const uint8_t* sc = res + soffs[s];
-        const uint64_t sl = soffs[s + 1] - soffs[s];
-        uint32_t* cover = (uint32_t*)calloc(qlen + sl + 1, sizeof(uint32_t));
-        size_t nh = 0;
-        hsp_t* hs = (hsp_t*)malloc((j - i) * sizeof(hsp_t));
-        for (size_t k = i; k < j; k++) {
-            const uint32_t qp = sv[k].qp, sp = sv[k].sp;
-            const int64_t d = (int64_t)sp - (int64_t)qp;
-            const size_t di = (size_t)(d + (int64_t)qlen);
-            if (qp < cover[di]) { ctr->extensions_avoided++; continue; }
-            ctr->ungapped_extensions++;
-            uint64_t lo, hi;
-            int32_t score = orc_ungapped_xdrop(qc, qlen, sc, sl, qp, sp, matrix, qb, P->x_drop, &lo, &hi);
-            /* steps of xdrop_cat (scan.rs:904): right steps + left steps */
-            {
-                /* recount the steps the way xdrop_cat counts them */
-                uint64_t nrt = qlen - qp < sl - sp ? qlen - qp : sl - sp;
-                uint64_t nlt = qp < sp ? qp : sp;
-                int32_t best = 0, cur = 0; uint64_t tr = 0;
-                while (tr < nrt) {
-                    cur += matrix[(qc[qp + tr] < 24 ? qc[qp + tr] : 22) * 24 + (sc[sp + tr] < 24 ? sc[sp + tr] : 22)] + (qb ? qb[qp + tr] : 0);
-                    tr++;
-                    if (cur > best) best = cur;
-                    if (cur < best - P->x_drop) break;
-                }
-                int32_t bl = 0, cl = 0; uint64_t tl = 1;
-                if (nlt > 0) {
-                    for (;;) {
-                        cl += matrix[(qc[qp - tl] < 24 ? qc[qp - tl] : 22) * 24 + (sc[sp - tl] < 24 ? sc[sp - tl] : 22)] + (qb ? qb[qp - tl] : 0);
-                        if (cl > bl) bl = cl;
-                        tl++;
-                        if (!(tl <= nlt && cl >= bl - P->x_drop)) break;
-                    }
-                }
-                ctr->xdrop_steps += tr + tl - 1;
-            }
-            cover[di] = (uint32_t)hi;
-            if (score >= P->hsp_threshold) {
-                hs[nh].diag = d; hs[nh].q_lo = (uint32_t)lo; hs[nh].q_hi = (uint32_t)hi; hs[nh].score = score;
-                nh++;
-            }
-        }
-        free(cover);
-        if (nh) {
-            /* finish_subject_into (scan.rs:2437-2474) */
-            ctr->hsps += nh;
-            qsort(hs, nh, sizeof(hsp_t), cmp_hsp);
-            const int64_t join = 2 * (int64_t)P->window_slack;
-            orc_region* rg = (orc_region*)malloc(nh * sizeof(orc_region));
-            uint32_t* ev_n = (uint32_t*)malloc(nh * sizeof(uint32_t));
-            int32_t* ev_s = (int32_t*)malloc(nh * sizeof(int32_t));
-            size_t ng = 0;
-            for (size_t k = 0; k < nh; k++) {
-                if (ng > 0 && hs[k].diag - rg[ng - 1].d_max <= join) {
-                    if (hs[k].diag > rg[ng - 1].d_max) rg[ng - 1].d_max = (int32_t)hs[k].diag;
-                    if (hs[k].score > rg[ng - 1].best) rg[ng - 1].best = hs[k].score;
-                    ev_n[ng - 1]++;
-                    int64_t sum = (int64_t)ev_s[ng - 1] + hs[k].score;
-                    ev_s[ng - 1] = sum > INT32_MAX ? INT32_MAX : (sum < INT32_MIN ? INT32_MIN : (int32_t)sum);
-                } else {
-                    rg[ng].query = q; rg[ng].subject = s;
-                    rg[ng].d_min = rg[ng].d_max = (int32_t)hs[k].diag; rg[ng].best = hs[k].score;
-                    ev_n[ng] = 1; ev_s[ng] = hs[k].score;
-                    ng++;
-                }
-            }
-            const int32_t thr = region_thr ? region_thr[q] : P->hsp_threshold;
-            size_t kept = ng;
-            if (thr > P->hsp_threshold) {
-                kept = 0;
-                for (size_t k = 0; k < ng; k++)
-                    if (rg[k].best >= thr || (ev_n[k] >= 2 && ev_s[k] >= thr)) rg[kept++] = rg[k];
-                ctr->regions_weak_dropped += ng - kept;
-            }
-            /* sort by (best desc, d_min asc), keep max_regions_per_subject */
-            for (size_t a = 1; a < kept; a++) {
-                orc_region x = rg[a];
-                size_t b2 = a;
-                while (b2 > 0 && (rg[b2 - 1].best < x.best || (rg[b2 - 1].best == x.best && rg[b2 - 1].d_min > x.d_min))) {
-                    rg[b2] = rg[b2 - 1];
-                    b2--;
-                }
-                rg[b2] = x;
-            }
-            size_t keep = kept < P->max_regions_per_subject ? kept : (P->max_regions_per_subject ? P->max_regions_per_subject : 1);
-            if (keep > kept) keep = kept;
-            for (size_t k = 0; k < keep; k++) {
-                if (nr == r_cap) { r_cap *= 2; regs_all = (orc_region*)realloc(regs_all, r_cap * sizeof(orc_region)); }
-                regs_all[nr++] = rg[k];
-            }
-            free(rg); free(ev_n); free(ev_s);
-        }
-        free(hs);
+        grp[ngrp++] = i;
         i = j;
     }
+    grp[ngrp] = ns;
+    cx.sv = sv;
+    cx.grp = grp;
+    par_for(ngrp, 64, threads, scan_visit, &cx);
     free(sv);
+    free(grp);
+    free(qred);
+    free(qfull);
+    size_t nr = 0;
+    for (int t = 0; t < threads; t++) { nr += loc[t].nr; add_counters(ctr, &loc[t].c); }
+    orc_region* regs_all = (orc_region*)malloc((nr ? nr : 1) * sizeof(orc_region));
+    {
+        size_t o = 0;
+        for (int t = 0; t < threads; t++) {
+            if (loc[t].nr) memcpy(regs_all + o, loc[t].r, loc[t].nr * sizeof(orc_region));
+            o += loc[t].nr;
+            free(loc[t].r);
+        }
+    }
+    free(loc);
     /* per query: region_order, cap at max_candidates */
     qsort(regs_all, nr, sizeof(orc_region), cmp_region);
     uint64_t w = 0;

@@ -118,6 +118,27 @@ int orc_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
                         int32_t* scores, int threads, uint64_t* cells_out);
 
 
+/* ---- SIMD-class restatement of the reference's CPU scoring (simd_band.cpp) ----
+ * score_banded_many (band_simd8.rs:78-185) per query: the inter-sequence
+ * unsigned 8-bit kernel batch_u8 (band_simd8.rs:236-388) for bands of width
+ * <= 126, the 16-bit row kernel banded_avx2_16 (banded_simd.rs:393-599) for
+ * wider bands and 8-bit overflows, and 32 bits (orc_banded_score) where the
+ * 16-bit range may not hold.  Same jobs and scores as orc_score_band_jobs;
+ * queries are spread over `threads` threads. */
+typedef struct {
+    uint64_t cells;        /* in-band cells of all jobs */
+    uint64_t u8_jobs;      /* jobs run through the 8-bit kernel */
+    uint64_t u8_overflows; /* of those, re-scored because the lane may have saturated */
+    uint64_t i16_jobs;     /* jobs finished by the 16-bit kernel */
+    uint64_t i32_jobs;     /* jobs re-run in 32 bits */
+} orc_simd_counters;
+
+int orc_simd_score_band_jobs(const uint8_t* residues, const uint8_t* qcodes,
+                             const uint64_t* qoffs, const int8_t* qbias,
+                             const orc_band_job* jobs, uint64_t njobs,
+                             const int32_t* matrix, int32_t gap_open, int32_t gap_extend,
+                             int32_t* scores, int threads, orc_simd_counters* counters);
+
 /* ---- scan schedule: seeds -> hits -> window filter -> X-drop -> regions ----
  * Restates Engine::search_scan for one query batch (src/search/engine/scan.rs:
  * build_scan_db 1066-1257, build_batch 1500-1596, scan_hits 1603-1804,
@@ -161,6 +182,15 @@ int64_t orc_scan_regions(const uint8_t* res, const uint64_t* soffs, uint64_t nsu
                          const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
                          const orc_scan_params* p, orc_region* out, uint64_t out_cap,
                          orc_scan_counters* ctr);
+
+/* orc_scan_regions with the subjects (counting and hit passes) and the
+ * (subject, query) pairs (coverage, X-drop, regions) spread over `threads`
+ * threads; the output does not depend on the thread count. */
+int64_t orc_scan_regions_mt(const uint8_t* res, const uint64_t* soffs, uint64_t nsub, const uint8_t* db_mask,
+                            const uint8_t* qcodes, const uint64_t* qoffs, uint32_t nq, const int8_t* qbias,
+                            const uint8_t* q_mask, const int32_t* region_thr, const int32_t* matrix,
+                            const orc_scan_params* p, orc_region* out, uint64_t out_cap,
+                            orc_scan_counters* ctr, int threads);
 
 /* auto_occ_cap (src/search/index.rs:329-336). */
 uint64_t orc_auto_occ_cap(uint64_t total, uint64_t ncodes, uint64_t db_residues, uint64_t ref_residues);

@@ -50,6 +50,8 @@ def lib():
         _lib.orc_ungapped_xdrop.argtypes = [P, U64, P, U64, U64, U64, P, P, I32, P, P]
         _lib.orc_score_band_jobs.restype = ctypes.c_int
         _lib.orc_score_band_jobs.argtypes = [P, P, P, P, P, U64, P, I32, I32, P, ctypes.c_int, P]
+        _lib.orc_simd_score_band_jobs.restype = ctypes.c_int
+        _lib.orc_simd_score_band_jobs.argtypes = [P, P, P, P, P, U64, P, I32, I32, P, ctypes.c_int, P]
     return _lib
 
 
@@ -159,6 +161,27 @@ def score_band_jobs(residues, qcodes, qoffs, qbias, jobs, matrix, go, ge, thread
     return out, int(cells.value)
 
 
+class SimdCounters(ctypes.Structure):
+    _fields_ = [("cells", ctypes.c_uint64), ("u8_jobs", ctypes.c_uint64), ("u8_overflows", ctypes.c_uint64),
+                ("i16_jobs", ctypes.c_uint64), ("i32_jobs", ctypes.c_uint64)]
+
+
+def simd_score_band_jobs(residues, qcodes, qoffs, qbias, jobs, matrix, go, ge, threads=1):
+    """The SIMD-class restatement of score_banded_many (simd_band.cpp): the
+    same jobs and scores as score_band_jobs -> (scores, counters dict)."""
+    res = _a(residues, np.uint8)
+    qc = _a(qcodes, np.uint8)
+    qo = _a(qoffs, np.uint64)
+    qb = None if qbias is None else _a(qbias, np.int8)
+    jb = np.ascontiguousarray(jobs)
+    m = _a(np.asarray(matrix).reshape(576), np.int32)
+    out = np.zeros(jb.size, np.int32)
+    ct = SimdCounters()
+    lib().orc_simd_score_band_jobs(_p(res), _p(qc), _p(qo), _p(qb) if qb is not None else None, _p(jb), jb.size,
+                                   _p(m), int(go), int(ge), _p(out), int(threads), ctypes.byref(ct))
+    return out, {k: int(getattr(ct, k)) for k, _ in SimdCounters._fields_}
+
+
 class ScanParams(ctypes.Structure):
     _fields_ = [("alpha_map", ctypes.c_uint8 * 24), ("alpha_size", ctypes.c_uint32), ("nshapes", ctypes.c_uint32),
                 ("shape_span", ctypes.c_uint32 * 32), ("shape_weight", ctypes.c_uint32 * 32),
@@ -205,13 +228,16 @@ def make_scan_params(alpha_map, alpha_size, shapes, min_ids=27, exact_weight=2, 
     return p
 
 
-def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, matrix, params, out_cap=None):
-    """Engine::search_scan's candidate regions for one batch -> (REGION_DTYPE array, counters dict)."""
+def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, matrix, params, out_cap=None,
+                 threads=1):
+    """Engine::search_scan's candidate regions for one batch -> (REGION_DTYPE array, counters dict);
+    `threads` host threads (the result does not depend on it)."""
     L = lib()
-    f = L.orc_scan_regions
+    f = L.orc_scan_regions_mt
     f.restype = ctypes.c_int64
     P = ctypes.c_void_p
-    f.argtypes = [P, P, ctypes.c_uint64, P, P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_uint64, P]
+    f.argtypes = [P, P, ctypes.c_uint64, P, P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_uint64, P,
+                  ctypes.c_int]
     res = _a(res, np.uint8)
     so = _a(soffs, np.uint64)
     dm = None if db_mask is None else _a(db_mask, np.uint8)
@@ -226,7 +252,8 @@ def scan_regions(res, soffs, db_mask, qcodes, qoffs, qbias, q_mask, region_thr, 
     ctr = ScanCounters()
     n = f(_p(res), _p(so), so.size - 1, _p(dm) if dm is not None else None, _p(qc), _p(qo), qo.size - 1,
           _p(qb) if qb is not None else None, _p(qm) if qm is not None else None,
-          _p(rt) if rt is not None else None, _p(m), ctypes.byref(params), _p(out), cap, ctypes.byref(ctr))
+          _p(rt) if rt is not None else None, _p(m), ctypes.byref(params), _p(out), cap, ctypes.byref(ctr),
+          int(threads))
     if n < 0:
         raise MemoryError("region buffer too small")
     return out[:n].copy(), {k: int(getattr(ctr, k)) for k, _ in ctr._fields_}
