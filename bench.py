@@ -41,15 +41,22 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample size (seconds of work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the microbench scores")
+    ap.add_argument("--no-config0", action="store_true", help="skip the 64 x 20,000 blastp search and its oracle check")
+    ap.add_argument("--parity-queries", type=int, default=100,
+                    help="batched search: queries whose hits are checked against the oracle pipeline")
     ap.add_argument("--strip-rows", type=int, default=16, help="rows per strip of the int16 kernel (8 or 16)")
     ap.add_argument("--no-autotune", action="store_true", help="keep --strip-rows and the default pairing")
     ap.add_argument("--no-search", action="store_true", help="skip the batched-search / learned-triage lines")
     ap.add_argument("--search-only", action="store_true",
                     help="only the batched-search section (printed as its own JSON line)")
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
+    ap.add_argument("--triage-recall", type=float, default=0.998,
+                    help="share of the held-out positive regions the triage threshold keeps")
+    ap.add_argument("--triage-margin", type=float, default=0.25, help="logits below that threshold point")
     ap.add_argument("--no-pool", action="store_true", help="search section without the two-batches-in-flight lines")
     ap.add_argument("--no-masking", action="store_true", help="search section without the tantan masking line")
-    ap.add_argument("--search-queries", type=int, default=2000)
+    ap.add_argument("--search-queries", type=int, default=11000)
     ap.add_argument("--search-subjects", type=int, default=500_000)
     ap.add_argument("--nn-search", action="store_true",
                     help="only the blastn (nn) batched search: DNA queries of 1-10 kb vs a synthetic genome-scale "
@@ -132,27 +139,58 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(qs, ss, bias, jobs, matrix, seconds):
-    """The oracle port on all host cores over a bounded sample of the jobs."""
+def simd_whole_workload(qs, ss, bias, jobs, matrix, min_seconds, max_runs=5):
+    """The SIMD-class restatement of the reference's CPU scoring (oracle/
+    simd_band.cpp) over the whole workload on all host cores: one warm run,
+    then timed runs until min_seconds have passed (at most max_runs).
+    Returns (scores, GCUPS of the median run, counters, run seconds, threads)."""
     from oracle import oracle as orc
     threads = os.cpu_count() or 1
-    n = min(jobs.size, 4000)
+    scores, ct = orc.simd_score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs, matrix, 11, 1, threads)
+    ts = []
+    while len(ts) < max_runs and (not ts or sum(ts) < min_seconds):
+        t0 = time.perf_counter()
+        orc.simd_score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs, matrix, 11, 1, threads)
+        ts.append(time.perf_counter() - t0)
+    dt = float(np.median(ts))
+    return scores, ct["cells"] / dt / 1e9, ct, ts, threads
+
+
+def cpu_baseline(qs, ss, bias, jobs, matrix, seconds):
+    """The reference's CPU scoring restated with its vector kernels (score_banded_many: 32-lane
+    8-bit batches, 16-bit rows, 32-bit re-runs; NEON on the aarch64 host) over all the jobs."""
+    scores, gcups, ct, ts, threads = simd_whole_workload(qs, ss, bias, jobs, matrix, seconds)
+    out = {"value": round(gcups, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
+           "per_core_gcups": round(gcups / threads, 3),
+           "reference_recorded_per_thread_gcups": "3.4-4.2 (16-bit), 12.8 (8-bit batches), AVX2 at 2.8 GHz",
+           "sample": "all %d jobs (%.3g cells) per run, median of %d runs (%.2f s each), SIMD-class restatement of "
+                     "score_banded_many (band_simd8.rs batch_u8 + banded_simd.rs banded_avx2_16 + 32-bit re-run) "
+                     "on %d threads; %d jobs through 8-bit batches (%d re-scored), %d in 16 bits, %d re-run in 32 bits"
+                     % (jobs.size, ct["cells"], len(ts), float(np.median(ts)), threads, ct["u8_jobs"],
+                        ct["u8_overflows"], ct["i16_jobs"], ct["i32_jobs"])}
+    return out, scores
+
+
+def parity_config1(qs, ss, bias, jobs, matrix, gpu_scores, simd_scores):
+    """Every GPU score of the microbench against the scalar oracle (banded_score_scalar,
+    banded.rs:134-224), all jobs, all host threads."""
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs[:n], matrix, 11, 1, threads)
+    want, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs, matrix, 11, 1, threads)
     dt = time.perf_counter() - t0
-    rate = cells / max(dt, 1e-9)
-    want_cells = rate * seconds
-    per_job = cells / max(n, 1)
-    n2 = int(min(jobs.size, max(n, want_cells / max(per_job, 1))))
-    t0 = time.perf_counter()
-    _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs[:n2], matrix, 11, 1, threads)
-    dt = time.perf_counter() - t0
-    return {"value": round(cells / dt / 1e9, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
-            "sample": "first %d of the %d jobs (%.3g cells, %.1f s), scalar C oracle (banded.rs restatement), "
-                      "%d threads" % (n2, jobs.size, cells, dt, threads)}
+    bad = np.nonzero(gpu_scores != want)[0]
+    return {"config": "sw-scoring-microbench", "jobs": int(jobs.size), "cells": int(cells),
+            "oracle": "scalar C restatement of banded_score_scalar, every job (%.1f s on %d threads)" % (dt, threads),
+            "mismatches": int(bad.size), "first_mismatches": [int(x) for x in bad[:5]],
+            "simd_baseline_mismatches": int(np.count_nonzero(simd_scores != want)) if simd_scores is not None
+            else None}
 
 
 def run_reference(a, rank, world):
+    """The reference arm: the reference's CPU scoring restated with its vector
+    kernels (oracle/simd_band.cpp; the reference itself is Rust and cannot be
+    built here) over the whole microbench workload each step, all host threads."""
     if rank != 0:
         return
     from saber_gb300.scoring import matrix
@@ -160,101 +198,197 @@ def run_reference(a, rank, world):
     qs, ss, planted, bias, jobs = workload(a.seed, a.queries, a.subjects, a.jobs)
     mat = matrix("BLOSUM62")
     threads = os.cpu_count() or 1
-    per_step = 30000
-    rng = np.random.default_rng(a.seed + 9)
     tot_cells, tot_t = 0, 0.0
+    ct = None
     for step in range(a.warmup + a.steps):
-        sel = jobs[rng.integers(0, jobs.size, size=min(per_step, jobs.size))]
         t0 = time.perf_counter()
-        _, cells = orc.score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, sel, mat, 11, 1, threads)
+        _, ct = orc.simd_score_band_jobs(ss.codes, qs.codes, qs.offsets, bias, jobs, mat, 11, 1, threads)
         dt = time.perf_counter() - t0
         if step >= a.warmup:
-            tot_cells += cells
+            tot_cells += ct["cells"]
             tot_t += dt
     v = tot_cells / tot_t / 1e9
     out = {"metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": "GCUPS", "n_gpus": world,
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(tot_t / a.steps * 1e3, 3),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 / i16 (i32 re-run)",
            "data": "synthetic", "config": config_dict(a, world),
            "cpu_baseline": {"value": round(v, 3), "unit": "GCUPS", "cores": threads, "kind": "port",
-                            "sample": "%d random jobs per step of the same workload, scalar C restatement of "
-                                      "banded_score (the reference is Rust; no cargo here)" % per_step},
+                            "per_core_gcups": round(v / threads, 3),
+                            "sample": "all %d jobs of the workload every step; SIMD-class restatement of "
+                                      "score_banded_many (band_simd8.rs batch_u8, banded_simd.rs banded_avx2_16, "
+                                      "32-bit re-run) on NEON; the reference is Rust and cannot be built here "
+                                      "(no cargo)" % jobs.size},
            "e2e": {"value": round(v, 3), "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
+def run_config0(a, dev):
+    """blastp (pp), default preset, plain method: 64 synthetic queries against
+    20,000 subjects, seed 0 (log-normal lengths, background residues, 10 %
+    planted homologs at about 40 % identity), BLOSUM62 11/1, E <= 10, -k 10,
+    tantan masking of the database (once, at load) and of the queries (every
+    call) on the GPU, through Searcher.search (host query codes in, hits out).
+    Parity: every m8 row must equal the oracle pipeline's (tantan masks by
+    oracle/tantan.c, scan, scores and tracebacks by the C oracle, statistics
+    and m8 formatting restated in Python), which is also the CPU baseline
+    (query masking + search, all host threads)."""
+    from oracle import engine as oeng
+    from oracle import oracle as orc
+    from saber_gb300 import synth
+    from saber_gb300.search import Searcher, SearchParams, m8_row
+    from saber_gb300.stats import gapped_protein
+    qs, ss, _ = synth.protein_db(0, 64, 20000)
+    se = Searcher(dev, ss.codes, ss.offsets, SearchParams("default"))
+    se.search(qs.codes, qs.offsets)
+    ts, hits = [], None
+    for _ in range(5):
+        t0 = time.perf_counter()
+        hits = se.search(qs.codes, qs.offsets)
+        ts.append(time.perf_counter() - t0)
+    tg = float(np.median(ts))
+    got = [m8_row("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(hits) for h in hl]
+    threads = os.cpu_count() or 1
+    dbm = orc.tantan_mask(ss.codes, ss.offsets, se.matrix)[0]
+    t0 = time.perf_counter()
+    qm = orc.tantan_mask(qs.codes, qs.offsets, se.matrix)[0]
+    want_h = oeng.search_batch(ss.codes, ss.offsets, qs.codes, qs.offsets, se.p, se.matrix, 11, 1,
+                               gapped_protein("BLOSUM62", 11, 1), se.scan_params, dbm, qm, threads=threads)
+    tc = time.perf_counter() - t0
+    want = [oeng.m8_line("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(want_h) for h in hl]
+    diff = sum(1 for x, y in zip(got, want) if x != y) + abs(len(got) - len(want))
+    nq = len(qs)
+    return {"workload": "blastp default preset, plain: %d queries (%d residues) vs %d subjects (%d residues), seed 0, "
+                        "tantan on both sides" % (nq, int(qs.codes.size), len(ss), int(ss.codes.size)),
+            "unit": "queries/s", "value": round(nq / tg, 1), "ms": round(tg * 1e3, 2),
+            "timing": "median of 5 calls of Searcher.search (query masking, scan, scores, tracebacks, hits)",
+            "hits": len(got), "database_residues_masked": int(se.db_residues_masked),
+            "cpu_baseline": {"value": round(nq / tc, 2), "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": "the whole batch (%.1f s): oracle pipeline (tantan, scan, banded scores, "
+                                       "tracebacks in C on %d threads; engine steps in Python)" % (tc, threads)},
+            "parity": {"config": "blastp 64 x 20,000, seed 0", "m8_rows": len(got), "oracle_m8_rows": len(want),
+                       "mismatching_rows": int(diff), "m8_identical": got == want}}
+
+
 def run_search(a, dev):
-    """Batched full search (config-2 style data: 50 % background, 25 % planted
-    homologs at 30-60 % identity, 25 % reversed decoys; the database at the
-    config's 150 M residues, fewer queries than its 11,000 to keep the run
-    short) through the C ABI's batch engine, plain and with the learned
-    triage; the triage network is trained on the GPU on a separately seeded
-    database from labels of the plain search."""
+    """Batched full search and learned triage on the batched-search workload:
+    a.search_queries (default 11,000) synthetic queries against a.search_subjects
+    (default 500,000) subjects, about 150 M residues (50 % background, 25 %
+    planted homologs at 30-60 % identity, 25 % reversed decoys), default preset
+    with masking none (the oracle legs then see the same seeds), through the C
+    ABI's batch engine (saber_gpu_search: query codes in, hit records out).
+
+    plain: the whole query set as one batch, and as two half batches in
+    flight on two handles (SearchPool).  parity: the first a.parity_queries
+    queries' hits from the whole-batch call against the oracle pipeline on
+    those queries and the whole database (m8 rows), which also gives the CPU
+    queries/s.  triage: the MLP trained on the GPU from plain-search labels of
+    a separately seeded database of the same size, its threshold calibrated on
+    the labels of other queries (held out from training), then the same
+    batches with the triage installed: hits kept with identical scores and
+    E-values, regions and cells saved, queries/s."""
+    from oracle import engine as oeng
     from saber_gb300 import synth
     from saber_gb300 import triage as tr
-    from saber_gb300.search import Searcher, SearchParams
+    from saber_gb300.search import Searcher, SearchParams, SearchPool, hits_from_records, m8_row
+    from saber_gb300.stats import gapped_protein
     triage = not a.no_triage
-    t0 = t1 = t2 = time.perf_counter()
+    nq = a.search_queries
+    P = SearchParams("default", masking="none")
+    out = {}
     if triage:
-        qa, sa, _ = synth.protein_db(a.seed + 501, max(a.search_queries // 2, 1), max(a.search_subjects * 2 // 5, 1),
-                                     reversed_frac=0.25, identity_range=(0.3, 0.6))
-        se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default", masking="none"))
-        rows, y, _ = tr.collect(se, qa.codes, qa.offsets)
+        t0 = time.perf_counter()
+        ntr, ncal = max(nq // 2, 1), max(nq // 5, 1)
+        qa, sa, _ = synth.protein_db(a.seed + 501, ntr + ncal, a.search_subjects, reversed_frac=0.25,
+                                     identity_range=(0.3, 0.6))
+        offs = qa.offsets.astype(np.int64)
+        se = Searcher(dev, sa.codes, sa.offsets, P)
+        rows, y, _ = tr.collect(se, qa.codes[:offs[ntr]], offs[:ntr + 1])
+        rows_c, y_c, _ = tr.collect(se, qa.codes[offs[ntr]:], offs[ntr:] - offs[ntr])
         t1 = time.perf_counter()
-        model, st = tr.train(dev, rows, y, seed=a.seed + 1)
+        # all positives and a seeded sample of the negatives (at most 3 M rows)
+        rng = np.random.default_rng(a.seed + 7)
+        neg = np.nonzero(y == 0)[0]
+        keep_neg = neg if neg.size + int(y.sum()) <= 3_000_000 else \
+            np.sort(rng.choice(neg, 3_000_000 - int(y.sum()), replace=False))
+        sel = np.sort(np.concatenate([np.nonzero(y > 0)[0], keep_neg]))
+        model, st = tr.train(dev, rows[sel], y[sel], seed=a.seed + 1)
         t2 = time.perf_counter()
-        thr = tr.threshold_for_recall(dev.triage_predict(model, rows), y, recall=0.999, margin=0.5)
-    qb, sb, _ = synth.protein_db(a.seed + 502, a.search_queries, a.search_subjects, reversed_frac=0.25,
-                                 identity_range=(0.3, 0.6))
+        z_c = dev.triage_predict(model, rows_c)
+        thr = tr.threshold_for_recall(z_c, y_c, recall=a.triage_recall, margin=a.triage_margin)
+        cal = {"regions": int(y_c.size), "positives": int(y_c.sum()),
+               "positives_kept": int(np.count_nonzero(z_c[y_c > 0] >= thr)),
+               "regions_dropped_frac": round(float(np.mean(z_c < thr)), 5),
+               "recall_target": a.triage_recall, "margin": a.triage_margin}
+        del rows, rows_c
+    qb, sb, _ = synth.protein_db(a.seed + 502, nq, a.search_subjects, reversed_frac=0.25, identity_range=(0.3, 0.6))
     if a.long_steps:
         dev.long_steps = a.long_steps
-    se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default", masking="none"))
+    se2 = Searcher(dev, sb.codes, sb.offsets, P)
     cpar = se2.cparams()
 
     def call():
-        # the C ABI's batch search (host buffers in, hit records out)
         return dev.search(cpar, se2.db_codes, se2.db_offsets, qb.codes, qb.offsets)
 
     call()  # warm: database state, scratch sizes
 
     def timed(reps=3):
-        ts, out = [], None
+        ts, res = [], None
         for _ in range(reps):
             t = time.perf_counter()
-            out = call()
+            res = call()
             ts.append(time.perf_counter() - t)
-        return out[0], float(np.median(ts)), out[2]
+        return res, float(np.median(ts))
 
-    def keyset(hits):
-        return {(int(r["query"]), int(r["subject"]), int(r["score"]), int(r["q_start"]), int(r["q_end"]),
+    def keyset(hits, qoff=0):
+        return {(int(r["query"]) + qoff, int(r["subject"]), int(r["score"]), int(r["q_start"]), int(r["q_end"]),
                  int(r["s_start"]), int(r["s_end"]), float(r["evalue"])) for r in hits}
 
-    plain, tp, cp = timed()
-    nq = a.search_queries
+    plain, tp = timed()
+    cp = plain[2]
     stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms",
               "t_score_calls_ms", "t_score_device_ms", "t_finish_tb_ms")
-    out = {
+    out.update({
         "workload": "batched search, default preset: %d synthetic queries vs %d subjects (%d residues; 50%% "
                     "background, 25%% planted 30-60%% identity, 25%% reversed), BLOSUM62 11/1, E<=10, -k 10"
                     % (nq, a.search_subjects, int(sb.codes.size)),
         "unit": "queries/s", "timing": "median of 3 calls, host wall clock around saber_gpu_search (query "
                                         "codes in, hit records out)",
-        "plain": {"value": round(nq / tp, 1), "hits": int(len(plain)), "regions": cp["regions"],
+        "plain": {"value": round(nq / tp, 1), "hits": int(len(plain[0])), "regions": cp["regions"],
                   "banded_cells": cp["banded_cells"], "stages_ms": {k: round(cp[k], 1) for k in stages},
+                  "counters": {k: int(cp[k]) for k in ("seed_positions", "hits", "hits_filtered",
+                                                       "ungapped_extensions", "xdrop_steps", "hsps") if k in cp},
                   # the scan stage as database bytes (1 per residue) per second; it is bound by
                   # the L1 data pipe and issue (seed-table lookups), not by HBM
                   "scan_db_gb_per_s": round(int(sb.codes.size) / (cp["t_scan_ms"] * 1e-3) / 1e9, 2)
                   if cp["t_scan_ms"] > 0 else None,
                   "score_device_gcups": round(cp["banded_cells"] / (cp["t_score_device_ms"] * 1e-3) / 1e9, 1)
                   if cp["t_score_device_ms"] > 0 else None},
-    }
-    # two batches in flight (SearchPool: two handles, host stages of one batch
-    # overlapping device stages of the other); the second batch is another
-    # 2,000 seeded queries of the same model
-    from saber_gb300.search import SearchPool
-    qc, _, _ = synth.protein_db(a.seed + 503, a.search_queries, 1, reversed_frac=0.25, identity_range=(0.3, 0.6))
-    batches = [(qb.codes, qb.offsets), (qc.codes, qc.offsets)]
-    pool = None if a.no_pool else SearchPool(sb.codes, sb.offsets, SearchParams("default", masking="none"), slots=2)
+    })
+    # parity sample: the first queries' hits of the whole-batch call against the oracle pipeline
+    k = min(a.parity_queries, nq)
+    if k > 0:
+        threads = os.cpu_count() or 1
+        qo = qb.offsets.astype(np.int64)
+        got_h = hits_from_records(plain[0], plain[1], nq, queries=k)
+        t0 = time.perf_counter()
+        want_h = oeng.search_batch(sb.codes, sb.offsets, qb.codes[:qo[k]], qo[:k + 1], P, se2.matrix, 11, 1,
+                                   gapped_protein("BLOSUM62", 11, 1), se2.scan_params, None, None, threads=threads)
+        tc = time.perf_counter() - t0
+        got = [m8_row("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(got_h) for h in hl]
+        want = [oeng.m8_line("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(want_h) for h in hl]
+        diff = sum(1 for x, y_ in zip(got, want) if x != y_) + abs(len(got) - len(want))
+        out["parity"] = {"config": "batched search, first %d of %d queries against the whole database" % (k, nq),
+                         "m8_rows": len(got), "oracle_m8_rows": len(want), "mismatching_rows": int(diff),
+                         "m8_identical": got == want}
+        out["cpu_baseline"] = {"value": round(k / tc, 2), "unit": "queries/s", "cores": threads, "kind": "port",
+                               "sample": "first %d queries against the whole database (%.1f s): oracle pipeline "
+                                         "(scan, banded scores and tracebacks in C on %d threads, engine steps "
+                                         "in Python)" % (k, tc, threads)}
+    # two half batches in flight on two handles
+    qo = qb.offsets.astype(np.int64)
+    h = nq // 2
+    batches = [(qb.codes[:qo[h]], qo[:h + 1]), (qb.codes[qo[h]:], qo[h:] - qo[h])]
+    pool = None if a.no_pool else SearchPool(sb.codes, sb.offsets, P, slots=2)
 
     def pooled(reps=3):
         pool.raw_batches(batches)
@@ -265,17 +399,21 @@ def run_search(a, dev):
             ts.append(time.perf_counter() - t)
         return res, float(np.median(ts))
 
-    nq2 = sum(len(b[1]) - 1 for b in batches)
+    def pooled_keys(res):
+        return keyset(res[0][0]) | keyset(res[1][0], h)
+
     if not a.no_masking:
         out["masking"] = run_masking(a, dev, sb, qb)
-    if not a.no_pool:
-        pres, pt = pooled()
+    tpp = None
+    if pool is not None:
+        pres, tpp = pooled()
         out["plain"]["two_batches_in_flight"] = {
-            "value": round(nq2 / pt, 1), "queries": nq2,
-            "same_hits_as_single_handle": bool(keyset(pres[0][0]) == keyset(plain))}
+            "value": round(nq / tpp, 1), "queries": nq, "batches": 2,
+            "same_hits_as_whole_batch": bool(pooled_keys(pres) == keyset(plain[0]))}
     if not triage:
         return out
-    if not a.no_pool:
+    tpt = None
+    if pool is not None:
         for se_ in pool.searchers:
             se_.dev.set_triage(model, thr)
         tres, tpt = pooled()
@@ -284,26 +422,30 @@ def run_search(a, dev):
     dev.set_triage(model, thr)
     try:
         call()
-        tri, tt, ct = timed()
+        tri, tt = timed()
     finally:
         dev.set_triage(None)
-    kp_, kt_ = keyset(plain), keyset(tri)
+    ct = tri[2]
+    kp_, kt_ = keyset(plain[0]), keyset(tri[0])
     total, kept = len(kp_), len(kp_ & kt_)
     out.update({
         "triage": {"value": round(nq / tt, 1), "regions_scored": ct["regions"], "regions_dropped": ct["triage_dropped"],
                    "banded_cells": ct["banded_cells"], "hits_kept": kept, "hits_plain": total,
                    "kept_frac": round(kept / max(total, 1), 5), "lost_hit_rate": round(1 - kept / max(total, 1), 5),
-                   "threshold": round(thr, 4), "stages_ms": {k: round(ct[k], 1) for k in stages}},
+                   "extra_hits": len(kt_ - kp_), "threshold": round(thr, 4), "calibration": cal,
+                   "stages_ms": {k_: round(ct[k_], 1) for k_ in stages}},
         "speedup": round(tp / tt, 3),
-        "training": {"regions": int(y.size), "positives": int(y.sum()), "steps": st["steps"],
-                     "final_loss": round(st["final_loss"], 5), "pos_weight": round(st["pos_weight"], 2),
-                     "collect_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 2),
-                     "data": "separately seeded database (%d queries x %d subjects)" % (len(qa.offsets) - 1,
-                                                                                          len(sa.offsets) - 1)},
+        "training": {"regions": int(y.size), "positives": int(y.sum()), "rows_trained": int(sel.size),
+                     "steps": st["steps"], "final_loss": round(st["final_loss"], 5),
+                     "pos_weight": round(st["pos_weight"], 2), "collect_s": round(t1 - t0, 1),
+                     "train_s": round(t2 - t1, 2),
+                     "data": "separately seeded database (%d subjects, %d residues): %d training queries, %d "
+                             "held-out calibration queries" % (len(sa), int(sa.codes.size), ntr, ncal)},
     })
-    if not a.no_pool:
-        out["triage"]["two_batches_in_flight"] = {"value": round(nq2 / tpt, 1), "queries": nq2,
-                                                  "same_hits_as_single_handle": bool(keyset(tres[0][0]) == kt_)}
+    if tpt is not None:
+        out["triage"]["two_batches_in_flight"] = {"value": round(nq / tpt, 1), "queries": nq, "batches": 2,
+                                                  "same_hits_as_whole_batch": bool(pooled_keys(tres) == kt_)}
+        out["speedup_two_batches_in_flight"] = round(tpp / tpt, 3)
     return out
 
 
@@ -579,12 +721,22 @@ def run_ours(a, rank, world, local_rank):
            "clocks": clk, "gpu_launches": int(launches),
            "library_launches": int(lib_launches), "i16_rescored": int(rescored),
            "cells_per_step": int(cells // max(a.steps, 1))}
+    simd_scores = None
     if not a.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(qs, ss, bias, jobs, mat, a.cpu_seconds)
+        out["cpu_baseline"], simd_scores = cpu_baseline(qs, ss, bias, jobs, mat, a.cpu_seconds)
+    if not a.no_parity:
+        out["parity"] = {"sw_microbench": parity_config1(qs, ss, bias, jobs, mat, d_scores.cpu().numpy(),
+                                                         simd_scores)}
+    if not a.no_config0 and world == 1:
+        out["blastp_64x20000"] = run_config0(a, dev)
+        if "parity" in out:
+            out["parity"]["blastp_64x20000"] = out["blastp_64x20000"]["parity"]
     # the search and translated sections run at N = 1 only (the other ranks
     # would wait at the barrier meanwhile)
     if not a.no_search and world == 1:
         out["search"] = run_search(a, dev)
+        if "parity" in out and "parity" in out["search"]:
+            out["parity"]["batched_search_sample"] = out["search"]["parity"]
     if not a.no_translated and world == 1:
         out["translated"] = run_translated(a, dev)
     print(json.dumps(out), flush=True)

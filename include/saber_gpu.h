@@ -508,21 +508,29 @@ int32_t saber_gpu_get_graphs(saber_gpu* h);
 uint64_t saber_gpu_graph_captures(saber_gpu* h);
 
 /* Allocation-free variant of saber_gpu_score_band_jobs_dev.  No counterpart
- * in the reference: it exists for callers that cannot allocate GPU memory at
- * scoring time — code between the nodes of a CUDA graph being captured, a
- * process whose device memory is held by another allocator or reserved in a
- * fixed budget, a latency-bound path where the device synchronisation of a
- * cudaMalloc is not acceptable.  It makes no cudaMalloc/cudaFree and calls no
- * allocating library routine: it reads the handle's resident database, query
- * set and scheme, the caller's device buffers d_jobs / d_scores, and uses a
- * fixed 16 MiB scratch array compiled into the library (held by every GPU
- * that loads the library until the process exits).  Scores equal those of the
- * other entry points (int32 recurrence of banded.rs:134-224).
+ * in the reference.  It exists for callers that cannot allocate GPU memory at
+ * scoring time: a process whose device memory is held by another allocator or
+ * reserved up front in a fixed budget, or a latency-bound path where the
+ * device synchronisation of a cudaMalloc is not acceptable.  It makes no
+ * cudaMalloc/cudaFree and calls no allocating library routine: it reads the
+ * handle's resident database, query set and scheme and the caller's device
+ * buffers d_jobs / d_scores, and uses a fixed 16 MiB scratch array compiled
+ * into the library (held by every GPU that loads the library until the
+ * process exits).  Scores equal those of the other entry points (int32
+ * recurrence of banded.rs:134-224).
  * max_band_width bounds the clipped band width of every job (1..4096; larger
- * is rejected with SABER_ERR_ARG; a job wider than it makes the call return
- * SABER_ERR_ARG).  The first call on a device looks up the scratch array's
- * address; make it before any stream capture.  Every call shares the scratch
- * and it keeps the last call's contents; calls that overlap on the GPU race. */
+ * is rejected with SABER_ERR_ARG; a job wider than it, or one outside the
+ * loaded queries or database, makes the call return SABER_ERR_ARG with the
+ * job's index in the message).  The scratch holds (16 MiB - 256 B) /
+ * (16 (max_band_width + 1)) scoring threads, about 4,000 at 257 and 255 at
+ * 4096, so a smaller max_band_width scores faster.
+ * The call runs on the handle's stream, which is not ordered after the
+ * caller's streams: finish writing d_jobs before the call.  It returns once
+ * d_scores is written (it reads a status word back and waits for the stream).
+ * The first call on a device looks up the scratch array's device address;
+ * make it before any stream capture.  Every call shares the scratch and it
+ * keeps the last call's contents (the status word is cleared by each call);
+ * calls that overlap on the GPU race on it. */
 int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs, uint64_t njobs,
                                       int32_t max_band_width, int32_t* d_scores);
 

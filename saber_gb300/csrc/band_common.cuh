@@ -117,7 +117,7 @@ struct NoAllocArgs {
     int go, ge;
     int32_t* scores;
 };
-int noalloc_score_band_jobs(int device, cudaStream_t s, const NoAllocArgs& a, const char** msg);
+int noalloc_score_band_jobs(int device, cudaStream_t s, const NoAllocArgs& a, const char** msg, uint32_t* bad_job);
 
 int band_fast_blocks_per_sm(int strip_rows);
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a);

@@ -1361,8 +1361,12 @@ int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs
     a.ge = h->scheme.ge;
     a.scores = d_scores;
     const char* msg = "";
-    int rc = noalloc_score_band_jobs(h->device, h->stream, a, &msg);
-    if (rc != SABER_OK) return fail(h, rc, "%s", msg);
+    uint32_t bad_job = UINT32_MAX;
+    int rc = noalloc_score_band_jobs(h->device, h->stream, a, &msg, &bad_job);
+    if (rc != SABER_OK) {
+        if (bad_job != UINT32_MAX) return fail(h, rc, "%s (job %u)", msg, bad_job);
+        return fail(h, rc, "%s", msg);
+    }
     return SABER_OK;
 }
 

@@ -347,8 +347,10 @@ class Device:
         return st.as_dict()
 
     def score_band_jobs_noalloc(self, d_jobs_ptr, njobs, max_band_width, d_scores_ptr):
-        """Allocation-free scoring of device-resident jobs (no device memory is
-        allocated by the call; scratch is a fixed 16 MiB array in the library)."""
+        """Allocation-free scoring of device-resident jobs: the call allocates no
+        device memory (its scratch is a fixed 16 MiB array in the library).  It
+        runs on the handle's stream and returns once the scores are written;
+        the jobs must be written before the call."""
         self._check(self.lib.saber_gpu_score_band_jobs_noalloc(self.h, ctypes.c_void_p(d_jobs_ptr), int(njobs),
                                                                int(max_band_width), ctypes.c_void_p(d_scores_ptr)),
                     "score_band_jobs_noalloc")

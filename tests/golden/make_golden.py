@@ -15,7 +15,8 @@ them).
   computed by the reference's own CUDA kernel source (src/gpu/kernels/sw.cu)
   compiled for the host by oracle/Makefile (`make -C oracle ref`).
 
-Usage:  python tests/golden/make_golden.py [--ref-root /root/reference]
+Usage:  python tests/golden/make_golden.py --ref-root <reference checkout>
+        (or SABER_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py)
 """
 import argparse
 import ctypes
@@ -182,8 +183,11 @@ def ref_scores(lib, case, mats):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", default=os.environ.get("SABER_REFERENCE_ROOT"),
+                    help="the reference checkout (default: $SABER_REFERENCE_ROOT)")
     a = ap.parse_args()
+    if not a.ref_root:
+        ap.error("give --ref-root or set SABER_REFERENCE_ROOT to the reference checkout")
     mats = parse_matrices(a.ref_root)
     with open(os.path.join(HERE, "matrices.json"), "w") as f:
         json.dump(mats, f)

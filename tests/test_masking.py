@@ -177,7 +177,8 @@ def test_search_with_tantan_matches_oracle_engine(dev):
     assert sum(len(h) for h in want) > 0
     _compare(got, want)
     # the python engine over the same device calls sees the same masks
-    _compare(se.search_py(qs.codes, qs.offsets), want)
+    from tests.py_engine import PyEngine
+    _compare(PyEngine(se).search(qs.codes, qs.offsets), want)
 
 
 @pytest.mark.gpu

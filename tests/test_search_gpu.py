@@ -9,6 +9,7 @@ from saber_gb300 import synth
 from saber_gb300.gpu import scan_params
 from saber_gb300.search import Searcher, SearchParams, m8_row
 from saber_gb300.stats import gapped_protein
+from tests.py_engine import PyEngine
 
 pytestmark = pytest.mark.gpu
 KEYS = ("subject", "score", "q_start", "q_end", "s_start", "s_end", "columns", "matches", "mismatches", "positives",
@@ -63,7 +64,7 @@ def test_native_engine_matches_python_engine(dev, preset, kw):
     qs, ss, planted = synth.protein_db(77, 16 if preset == "exhaustive" else 30, 500 if preset == "exhaustive" else 1500)
     se = Searcher(dev, ss.codes, ss.offsets, SearchParams(preset, **kw))
     got = se.search(qs.codes, qs.offsets)
-    want = se.search_py(qs.codes, qs.offsets)
+    want = PyEngine(se).search(qs.codes, qs.offsets)
     assert sum(len(h) for h in want) > 0
     _compare(got, want)
 
@@ -81,7 +82,7 @@ def test_nucleotide_search_matches_oracle(dev):
                              gapped_nucleotide(2, -3, 7, 2), se.scan_params, None, None, is_protein=False)
     assert sum(len(h) for h in want) >= 5
     _compare(got, want)
-    assert [len(h) for h in got] == [len(h) for h in se.search_py(qs.codes, qs.offsets)]
+    assert [len(h) for h in got] == [len(h) for h in PyEngine(se).search(qs.codes, qs.offsets)]
 
 
 @pytest.mark.gpu

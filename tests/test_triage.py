@@ -91,17 +91,20 @@ def test_gpu_training_learns_a_separable_rule(dev):
 
 @pytest.mark.gpu
 def test_triaged_search_keeps_the_plain_hits(dev):
-    """Train on one synthetic database, triage another: the triaged search
-    keeps >= 99 % of the plain search's hits with identical scores and
-    E-values while dropping a large share of the candidate regions (what the
-    trained network gains over the plain method)."""
+    """Train on one synthetic database, calibrate the threshold on the labels
+    of other queries (held out from training), triage a third data set: the
+    triaged search keeps >= 99.5 % of the plain search's hits with identical
+    scores and E-values while dropping a large share of the candidate
+    regions (what the trained network gains over the plain method)."""
     from saber_gb300.search import Searcher, SearchParams
-    qa, sa, _ = synth.protein_db(401, 300, 30000, reversed_frac=0.25, identity_range=(0.3, 0.6))
+    qa, sa, _ = synth.protein_db(401, 600, 30000, reversed_frac=0.25, identity_range=(0.3, 0.6))
+    offs = qa.offsets.astype(np.int64)
     se = Searcher(dev, sa.codes, sa.offsets, SearchParams("default"))
-    rows, y, _ = tr.collect(se, qa.codes, qa.offsets)
-    assert y.sum() > 100
+    rows, y, _ = tr.collect(se, qa.codes[:offs[300]], offs[:301])
+    rows_c, y_c, _ = tr.collect(se, qa.codes[offs[300]:], offs[300:] - offs[300])
+    assert y.sum() > 100 and y_c.sum() > 100
     model, st = tr.train(dev, rows, y, seed=1)
-    thr = tr.threshold_for_recall(dev.triage_predict(model, rows), y, recall=0.999, margin=0.5)
+    thr = tr.threshold_for_recall(dev.triage_predict(model, rows_c), y_c, recall=0.999, margin=0.5)
     qb, sb, _ = synth.protein_db(402, 300, 30000, reversed_frac=0.25, identity_range=(0.3, 0.6))
     se2 = Searcher(dev, sb.codes, sb.offsets, SearchParams("default"))
     plain = se2.search(qb.codes, qb.offsets)
@@ -114,7 +117,7 @@ def test_triaged_search_keeps_the_plain_hits(dev):
         dev.set_triage(None)
     kept, total, _ = tr.compare_hits(plain, tri)
     assert total > 100
-    assert kept >= 0.99 * total, (kept, total)
+    assert kept >= 0.995 * total, (kept, total)
     dropped = c_tri["triage_dropped"] / max(c_plain["regions"], 1)
     assert dropped > 0.3, dropped
     assert c_tri["banded_cells"] < c_plain["banded_cells"]
