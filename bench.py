@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--tr-subjects", type=int, default=100_000, help="nx protein subjects / pn DNA sequences")
     ap.add_argument("--nn-queries", type=int, default=2000)
     ap.add_argument("--nn-bases", type=float, default=500e6, help="database size in bases (subjects of 1-10 kb)")
+    ap.add_argument("--nn-parity-queries", type=int, default=10,
+                    help="blastn: queries whose hits are checked against the oracle pipeline")
+    ap.add_argument("--no-nn", action="store_true", help="skip the blastn (nn) batched-search section")
     ap.add_argument("--long-steps", type=int, default=0,
                     help="scoring: one-lane sweeps longer than this go to the warp-per-job kernel (0: library default)")
     return ap.parse_args()
@@ -296,7 +299,7 @@ def run_search(a, dev):
     P = SearchParams("default", masking="none")
     out = {}
     if triage:
-        t0 = time.perf_counter()
+        tc0 = time.perf_counter()
         ntr, ncal = max(nq // 2, 1), max(nq // 5, 1)
         qa, sa, _ = synth.protein_db(a.seed + 501, ntr + ncal, a.search_subjects, reversed_frac=0.25,
                                      identity_range=(0.3, 0.6))
@@ -304,7 +307,7 @@ def run_search(a, dev):
         se = Searcher(dev, sa.codes, sa.offsets, P)
         rows, y, _ = tr.collect(se, qa.codes[:offs[ntr]], offs[:ntr + 1])
         rows_c, y_c, _ = tr.collect(se, qa.codes[offs[ntr]:], offs[ntr:] - offs[ntr])
-        t1 = time.perf_counter()
+        tc1 = time.perf_counter()
         # all positives and a seeded sample of the negatives (at most 3 M rows)
         rng = np.random.default_rng(a.seed + 7)
         neg = np.nonzero(y == 0)[0]
@@ -312,13 +315,17 @@ def run_search(a, dev):
             np.sort(rng.choice(neg, 3_000_000 - int(y.sum()), replace=False))
         sel = np.sort(np.concatenate([np.nonzero(y > 0)[0], keep_neg]))
         model, st = tr.train(dev, rows[sel], y[sel], seed=a.seed + 1)
-        t2 = time.perf_counter()
+        tc2 = time.perf_counter()
         z_c = dev.triage_predict(model, rows_c)
         thr = tr.threshold_for_recall(z_c, y_c, recall=a.triage_recall, margin=a.triage_margin)
         cal = {"regions": int(y_c.size), "positives": int(y_c.sum()),
                "positives_kept": int(np.count_nonzero(z_c[y_c > 0] >= thr)),
                "regions_dropped_frac": round(float(np.mean(z_c < thr)), 5),
-               "recall_target": a.triage_recall, "margin": a.triage_margin}
+               "recall_target": a.triage_recall, "margin": a.triage_margin,
+               # the held-out trade-off: regions dropped at other recall targets (no margin)
+               "curve": [{"recall": r, "threshold": round(t_, 4), "regions_dropped_frac": round(float(np.mean(z_c < t_)), 5)}
+                         for r in (0.99, 0.995, 0.996, 0.997, 0.998, 0.999)
+                         for t_ in [tr.threshold_for_recall(z_c, y_c, recall=r, margin=0.0)]]}
         del rows, rows_c
     qb, sb, _ = synth.protein_db(a.seed + 502, nq, a.search_subjects, reversed_frac=0.25, identity_range=(0.3, 0.6))
     if a.long_steps:
@@ -437,8 +444,8 @@ def run_search(a, dev):
         "speedup": round(tp / tt, 3),
         "training": {"regions": int(y.size), "positives": int(y.sum()), "rows_trained": int(sel.size),
                      "steps": st["steps"], "final_loss": round(st["final_loss"], 5),
-                     "pos_weight": round(st["pos_weight"], 2), "collect_s": round(t1 - t0, 1),
-                     "train_s": round(t2 - t1, 2),
+                     "pos_weight": round(st["pos_weight"], 2), "collect_s": round(tc1 - tc0, 1),
+                     "train_s": round(tc2 - tc1, 2),
                      "data": "separately seeded database (%d subjects, %d residues): %d training queries, %d "
                              "held-out calibration queries" % (len(sa), int(sa.codes.size), ntr, ncal)},
     })
@@ -501,50 +508,81 @@ def run_masking(a, dev, sb, qb):
     }
 
 
-def run_nn_search(a, local_rank):
-    """blastn (nn) batched search: DNA queries of 1-10 kb (uniform ACGT)
-    against a database of 1-10 kb subjects, 10 % of them planted homologs at
-    80-95 % identity with indels at 0.01 per base; +2/-3 with SABER gaps 7/2,
-    one contiguous 11-mer shape, no window filter, E <= 10, -k 10; through
-    the C ABI batch engine, median of 2 calls after a warm-up."""
+def run_nn(a, local_rank):
+    """blastn (nn) batched search: a.nn_queries DNA queries of 1-10 kb
+    (uniform ACGT) against about a.nn_bases bases of 1-10 kb subjects, 10 % of
+    them planted homologs at 80-95 % identity with indels at 0.01 per base;
+    +2/-3 with SABER gaps 7/2, one contiguous 11-mer shape, no window filter,
+    E <= 10, -k 10; through the C ABI batch engine (query codes in, hit
+    records out), median of 2 calls after a warm-up, on a handle of its own
+    (closed afterwards).  Parity: the first a.nn_parity_queries queries' hits
+    of the whole-batch call against the oracle pipeline on those queries and
+    the whole database (m8 rows), which also gives the CPU queries/s."""
+    from oracle import engine as oeng
     from saber_gb300 import Device, synth
-    from saber_gb300.search import Searcher, SearchParams
-    dev = Device(local_rank)
-    if a.long_steps:
-        dev.long_steps = a.long_steps
+    from saber_gb300.search import Searcher, SearchParams, hits_from_records, m8_row
+    from saber_gb300.stats import gapped_nucleotide
     nsub = max(1, int(a.nn_bases / 5500))
     t0 = time.perf_counter()
     qs, ss, _ = synth.dna_db(a.seed + 700, a.nn_queries, nsub)
     t1 = time.perf_counter()
-    se = Searcher(dev, ss.codes, ss.offsets, SearchParams.nucleotide(), gap_open=7, gap_extend=2,
-                  nucleotide=(2, -3))
-    cpar = se.cparams()
+    P = SearchParams.nucleotide()
+    with Device(local_rank) as dev:
+        if a.long_steps:
+            dev.long_steps = a.long_steps
+        se = Searcher(dev, ss.codes, ss.offsets, P, gap_open=7, gap_extend=2, nucleotide=(2, -3))
+        cpar = se.cparams()
 
-    def call():
-        return dev.search(cpar, se.db_codes, se.db_offsets, qs.codes, qs.offsets)
+        def call():
+            return dev.search(cpar, se.db_codes, se.db_offsets, qs.codes, qs.offsets)
 
-    call()
-    ts, out = [], None
-    for _ in range(2):
-        t = time.perf_counter()
-        out = call()
-        ts.append(time.perf_counter() - t)
-    tp = float(np.median(ts))
-    st = out[2]
-    keys = ("seed_positions", "hits", "ungapped_extensions", "extensions_avoided", "xdrop_steps", "hsps",
-            "regions", "banded_cells", "tb_tracebacks")
-    print(json.dumps({"metric": "batched nn search queries/s", "nn": {
-        "workload": "blastn (nn) batched search: %d DNA queries (%d bases) vs %d subjects (%d bases; 10%% planted "
-                    "80-95%% identity homologs, indels 0.01), +2/-3, gaps 7/2, 11-mers, E<=10, -k 10"
-                    % (len(qs.offsets) - 1, int(qs.codes.size), nsub, int(ss.codes.size)),
-        "unit": "queries/s", "value": round((len(qs.offsets) - 1) / tp, 1), "s_per_search": round(tp, 3),
-        "hits": int(len(out[0])), "counters": {k: int(st[k]) for k in keys if k in st},
-        "stages_ms": {k: round(v, 1) for k, v in st.items() if k.startswith("t_")},
-        "score_device_gcups": round(st["banded_cells"] / (st["t_score_device_ms"] * 1e-3) / 1e9, 1)
-        if st.get("t_score_device_ms", 0) > 0 else None,
-        "data_gen_s": round(t1 - t0, 1), "long_steps": dev.long_steps,
-        "timing": "median of 2 calls, host wall clock around saber_gpu_search"}}),
-        flush=True)
+        call()
+        ts, res = [], None
+        for _ in range(2):
+            t = time.perf_counter()
+            res = call()
+            ts.append(time.perf_counter() - t)
+        tp = float(np.median(ts))
+        st = res[2]
+        nq = len(qs.offsets) - 1
+        keys = ("seed_positions", "hits", "ungapped_extensions", "extensions_avoided", "xdrop_steps", "hsps",
+                "regions", "banded_cells", "tb_tracebacks")
+        out = {
+            "workload": "blastn (nn) batched search: %d DNA queries (%d bases) vs %d subjects (%d bases; 10%% planted "
+                        "80-95%% identity homologs, indels 0.01), +2/-3, gaps 7/2, 11-mers, E<=10, -k 10"
+                        % (nq, int(qs.codes.size), nsub, int(ss.codes.size)),
+            "unit": "queries/s", "value": round(nq / tp, 1), "s_per_search": round(tp, 3),
+            "hits": int(len(res[0])), "counters": {k: int(st[k]) for k in keys if k in st},
+            "stages_ms": {k: round(v, 1) for k, v in st.items() if k.startswith("t_")},
+            "score_device_gcups": round(st["banded_cells"] / (st["t_score_device_ms"] * 1e-3) / 1e9, 1)
+            if st.get("t_score_device_ms", 0) > 0 else None,
+            "data_gen_s": round(t1 - t0, 1), "long_steps": dev.long_steps,
+            "timing": "median of 2 calls, host wall clock around saber_gpu_search"}
+        k = min(a.nn_parity_queries, nq)
+        if k > 0:
+            threads = os.cpu_count() or 1
+            qo = qs.offsets.astype(np.int64)
+            got_h = hits_from_records(res[0], res[1], nq, queries=k)
+            t0 = time.perf_counter()
+            want_h = oeng.search_batch(ss.codes, ss.offsets, qs.codes[:qo[k]], qo[:k + 1], P, se.matrix, 7, 2,
+                                       gapped_nucleotide(2, -3, 7, 2), se.scan_params, None, None, is_protein=False,
+                                       threads=threads)
+            tc = time.perf_counter() - t0
+            got = [m8_row("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(got_h) for h in hl]
+            want = [oeng.m8_line("q%d" % qi, "s%d" % h["subject"], h) for qi, hl in enumerate(want_h) for h in hl]
+            diff = sum(1 for x, y in zip(got, want) if x != y) + abs(len(got) - len(want))
+            out["parity"] = {"config": "blastn, first %d of %d queries against the whole database" % (k, nq),
+                             "m8_rows": len(got), "oracle_m8_rows": len(want), "mismatching_rows": int(diff),
+                             "m8_identical": got == want}
+            out["cpu_baseline"] = {"value": round(k / tc, 3), "unit": "queries/s", "cores": threads, "kind": "port",
+                                   "sample": "first %d queries against the whole database (%.1f s): oracle pipeline "
+                                             "(scan, banded scores and tracebacks in C on %d threads, engine steps "
+                                             "in Python)" % (k, tc, threads)}
+    return out
+
+
+def run_nn_search(a, local_rank):
+    print(json.dumps({"metric": "batched nn search queries/s", "nn": run_nn(a, local_rank)}), flush=True)
 
 
 def run_translated(a, dev):
@@ -739,6 +777,11 @@ def run_ours(a, rank, world, local_rank):
             out["parity"]["batched_search_sample"] = out["search"]["parity"]
     if not a.no_translated and world == 1:
         out["translated"] = run_translated(a, dev)
+    if not a.no_nn and world == 1:
+        dev.close()
+        out["blastn_2000x500M"] = run_nn(a, local_rank)
+        if "parity" in out and "parity" in out["blastn_2000x500M"]:
+            out["parity"]["blastn_sample"] = out["blastn_2000x500M"]["parity"]
     print(json.dumps(out), flush=True)
 
 

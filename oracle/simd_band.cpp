@@ -221,10 +221,23 @@ const int16_t NEG16 = -31000; /* banded_simd.rs:336 */
 struct I16Scratch {
     std::vector<int16_t> hp, fp, hc, fc;
     std::vector<int8_t> prof;
+    std::vector<uint8_t> codes;
 };
 
+/* tbl[a]: S(a, x) clamped to a signed byte, for x < 24 (banded_simd.rs:433-443) */
+static void score_tables(const int32_t* matrix, Tbl32* tbl) {
+    for (int a = 0; a < 24; a++) {
+        uint8_t t[32] = {0};
+        for (int x = 0; x < 24; x++) {
+            const int32_t v = matrix[a * 24 + x];
+            t[x] = (uint8_t)(int8_t)(v < -128 ? -128 : (v > 127 ? 127 : v));
+        }
+        tbl_make(&tbl[a], t);
+    }
+}
+
 static bool banded16(const uint8_t* qc, size_t m, const uint8_t* s, size_t n, const int8_t* bias,
-                     const int32_t* matrix, int32_t go, int32_t ge, int64_t lo, int64_t w, I16Scratch& sc,
+                     const Tbl32* tbl, int32_t go, int32_t ge, int64_t lo, int64_t w, I16Scratch& sc,
                      int32_t* score) {
     if (go < 0 || go > 1000 || ge < 0 || ge > 1000 || ge > go) return false;
     const int32_t limit = 32767 - 16 * ge - 192;
@@ -239,14 +252,12 @@ static bool banded16(const uint8_t* qc, size_t m, const uint8_t* s, size_t n, co
     uint32_t present = 0;
     for (size_t i = 0; i < m; i++) present |= 1u << qc[i];
     sc.prof.resize(24 * stride);
+    sc.codes.resize(stride);
+    for (size_t j = 0; j < stride; j++) sc.codes[j] = j < n ? code_index(s[j]) : 23;
     for (int a = 0; a < 24; a++) {
         if (!(present & (1u << a))) continue;
-        int8_t* row = &sc.prof[(size_t)a * stride];
-        const int32_t* mr = matrix + a * 24;
-        for (size_t j = 0; j < stride; j++) {
-            int32_t v = mr[j < n ? code_index(s[j]) : 23];
-            row[j] = (int8_t)(v < -128 ? -128 : (v > 127 ? 127 : v));
-        }
+        uint8_t* row = reinterpret_cast<uint8_t*>(&sc.prof[(size_t)a * stride]);
+        for (size_t j = 0; j < stride; j += 16) u8_store(row + j, tbl_lookup(tbl[a], u8_load(&sc.codes[j])));
     }
     int16_t* hp = sc.hp.data();
     int16_t* fp = sc.fp.data();
@@ -352,6 +363,7 @@ struct Ctx {
     int32_t go, ge;
     int32_t* scores;
     int32_t smin, smax;
+    Tbl32 tbl16[24]; /* signed-byte score tables of the 16-bit kernel's profiles */
 };
 
 struct Counts {
@@ -421,7 +433,7 @@ static void score_query(const Ctx& cx, uint32_t q, const uint64_t* idx, size_t n
         const orc_band_job& jb = cx.jobs[jj.k];
         const uint8_t* s = cx.residues + jb.win_begin;
         int32_t sc = 0;
-        if (banded16(qc, m, s, (size_t)jj.n, bias, cx.matrix, cx.go, cx.ge, jj.lo, jj.hi - jj.lo + 1, i16s, &sc)) {
+        if (banded16(qc, m, s, (size_t)jj.n, bias, cx.tbl16, cx.go, cx.ge, jj.lo, jj.hi - jj.lo + 1, i16s, &sc)) {
             ct.i16_jobs++;
         } else {
             orc_band_score r;
@@ -459,7 +471,8 @@ extern "C" int orc_simd_score_band_jobs(const uint8_t* residues, const uint8_t* 
         const uint64_t wb = (start[b + 1] - start[b]) * (qoffs[b + 1] - qoffs[b]);
         return wa != wb ? wa > wb : a < b;
     });
-    Ctx cx{residues, qcodes, qoffs, qbias, jobs, matrix, gap_open, gap_extend, scores, 0, 0};
+    Ctx cx{residues, qcodes, qoffs, qbias, jobs, matrix, gap_open, gap_extend, scores, 0, 0, {}};
+    score_tables(matrix, cx.tbl16);
     cx.smin = cx.smax = matrix[0];
     for (int t = 0; t < 576; t++) { cx.smin = std::min(cx.smin, matrix[t]); cx.smax = std::max(cx.smax, matrix[t]); }
     std::atomic<size_t> next(0);
