@@ -437,8 +437,17 @@ __device__ __forceinline__ uint32_t stage_word(const uint8_t* __restrict__ buf, 
     return v;
 }
 
+// Resident blocks per SM the scan and chain kernels are compiled for (a
+// register budget); tuning constants.
+#ifndef SABER_SCAN_MIN_BLOCKS
+#define SABER_SCAN_MIN_BLOCKS 4
+#endif
+#ifndef SABER_CHAINS_MIN_BLOCKS
+#define SABER_CHAINS_MIN_BLOCKS 4
+#endif
+
 template <bool COMB>
-__global__ void __launch_bounds__(256, 4) k_scan(ScanArgs a) {
+__global__ void __launch_bounds__(256, SABER_SCAN_MIN_BLOCKS) k_scan(ScanArgs a) {
     __shared__ uint32_t s_n[kScanWarps][kSegCap], s_eb[kScanWarps][kSegCap];
     __shared__ uint8_t s_rl[kScanWarps][kSegCap], s_sh[kScanWarps][kSegCap];
     __shared__ uint2 s_sv[kScanWarps][kSurvStage];
@@ -693,7 +702,7 @@ __device__ __forceinline__ uint2 load8(const uint8_t* __restrict__ buf, int64_t 
     return make_uint2(v[0], v[1]);
 }
 
-__global__ void __launch_bounds__(256, 4) k_chains(ChainArgs a) {
+__global__ void __launch_bounds__(256, SABER_CHAINS_MIN_BLOCKS) k_chains(ChainArgs a) {
     __shared__ int32_t smat[576];
     for (int t = threadIdx.x; t < 576; t += blockDim.x) smat[t] = a.matrix[t];
     __syncthreads();
