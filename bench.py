@@ -27,6 +27,7 @@ sys.path.insert(0, REPO)
 
 METRIC = "banded SW GCUPS (bit-exact)"
 ALGO_OPS_PER_CELL = 11  # E: 2 sub + max, F: 2 sub + max, H: add + 3 max, best: max
+K_BAND_FAST_DRAM_BYTES = 2.63e9 + 2.90e9  # dram__bytes_read.sum + dram__bytes_write.sum, one launch
 
 
 def parse():
@@ -51,9 +52,9 @@ def parse():
     ap.add_argument("--search-only", action="store_true",
                     help="only the batched-search section (printed as its own JSON line)")
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
-    ap.add_argument("--triage-recall", type=float, default=0.998,
+    ap.add_argument("--triage-recall", type=float, default=0.997,
                     help="share of the held-out positive regions the triage threshold keeps")
-    ap.add_argument("--triage-margin", type=float, default=0.25, help="logits below that threshold point")
+    ap.add_argument("--triage-margin", type=float, default=0.0, help="logits below that threshold point")
     ap.add_argument("--no-pool", action="store_true", help="search section without the two-batches-in-flight lines")
     ap.add_argument("--no-masking", action="store_true", help="search section without the tantan masking line")
     ap.add_argument("--search-queries", type=int, default=11000)
@@ -353,7 +354,8 @@ def run_search(a, dev):
     plain, tp = timed()
     cp = plain[2]
     stages = ("t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms", "t_finish_ms", "t_total_ms",
-              "t_score_calls_ms", "t_score_device_ms", "t_finish_tb_ms")
+              "t_score_calls_ms", "t_score_device_ms", "t_finish_tb_ms", "t_score_build_ms", "t_score_stage2_ms",
+              "t_finish_order_ms")
     out.update({
         "workload": "batched search, default preset: %d synthetic queries vs %d subjects (%d residues; 50%% "
                     "background, 25%% planted 30-60%% identity, 25%% reversed), BLOSUM62 11/1, E<=10, -k 10"
@@ -750,7 +752,11 @@ def run_ours(a, rank, world, local_rank):
            "roofline": {"bound": "int", "kernel": "k_band_fast",
                         "achieved": round(achieved, 3) if achieved else None, "peak": round(peak, 3),
                         "unit": "Tops/s", "frac": round(achieved / peak, 3) if achieved else None,
-                        "traffic": None,
+                        # DRAM bytes (read + write) of one k_band_fast<16> launch on this workload, from one
+                        # ncu capture of the same command (profiles/k_band_fast16_traffic_1M.md)
+                        "traffic": K_BAND_FAST_DRAM_BYTES if a.jobs == 1_000_000 and a.seed == 0 else None,
+                        "traffic_unit": "bytes per launch",
+                        "algorithmic_bytes": int(jobs.nbytes + jobs.size * 4 + ss.codes.size + 50 * qs.codes.size),
                         "basis": "11 algorithmic int ops per in-band cell; peak = measured DPX s16x2 "
                                  "lane-instructions/s x 2 (probe kernel, this run)",
                         "fast_kernel_gcups": round(fast_cells / fast_s / 1e9, 2) if fast_s > 0 else None,

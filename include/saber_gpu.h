@@ -396,6 +396,10 @@ typedef struct {
     double t_finish_tb_ms;
     /* the scoring calls' device time by part (saber_score_stats) */
     double t_score_prep_ms, t_score_fast_ms, t_score_generic_ms;
+    /* host parts: inside t_score_ms, building the first-stage jobs and the
+     * second-stage decisions and jobs; inside t_finish_ms, the per-query
+     * E-value order */
+    double t_score_build_ms, t_score_stage2_ms, t_finish_order_ms;
 } saber_search_stats;
 
 /* Hits of every query of the batch, ordered by query, then (E-value, score

@@ -488,6 +488,7 @@ struct Engine {
             int kind;  // 0 full, 1 narrow, 2 band
         };
         const size_t nq = per_q.size();
+        const double tb0 = now_ms();
         scores.resize(nq);
         std::vector<size_t> base(nq + 1, 0);
         for (size_t qi = 0; qi < nq; qi++) base[qi + 1] = base[qi] + per_q[qi].size();
@@ -522,9 +523,11 @@ struct Engine {
             }
         });
         for (uint64_t v : banded) st.band_scored_regions += v;
+        st.t_score_build_ms += now_ms() - tb0;
         const int32_t* sc1 = nullptr;
         int rc = score(s1, n1, 2, &sc1);
         if (rc != SABER_OK) return rc;
+        const double ts0 = now_ms();
         // stage-2 decision per region (f64 threshold of the region's subject length)
         const double re = region_evalue();
         std::vector<uint8_t> again(n1, 0);
@@ -570,6 +573,7 @@ struct Engine {
                 w++;
             }
         });
+        st.t_score_stage2_ms += now_ms() - ts0;
         const int32_t* sc2 = nullptr;
         rc = score(s2, n2, 3, &sc2);
         if (rc != SABER_OK) return rc;
@@ -669,6 +673,7 @@ struct Engine {
                std::vector<uint64_t>* hit_src) {
         const double ecut = (P.evalue > 0.0 && std::isfinite(P.evalue)) ? P.evalue : kInf;
         const size_t nq = per_q.size();
+        const double to0 = now_ms();
         std::vector<std::vector<std::pair<double, uint32_t>>> orders(nq);
         parallel_for(nq, [&](size_t qi) {
             const QStats& qs = preps[qi].qs;
@@ -701,6 +706,7 @@ struct Engine {
                 return x.dmax < y.dmax;
             });
         });
+        st.t_finish_order_ms += now_ms() - to0;
         std::unordered_map<uint64_t, Aln> tb;
         std::vector<QState> state(nq);
         for (size_t qi = 0; qi < nq; qi++) state[qi].done = orders[qi].empty();

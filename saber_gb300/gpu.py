@@ -107,7 +107,8 @@ class SearchStats(ctypes.Structure):
                                        "banded_cells", "score_launches", "alignments")] + [
         (n, ctypes.c_double) for n in ("t_prep_ms", "t_scan_ms", "t_triage_ms", "t_plan_ms", "t_score_ms",
                                        "t_finish_ms", "t_total_ms", "t_score_calls_ms", "t_score_device_ms",
-                                       "t_finish_tb_ms", "t_score_prep_ms", "t_score_fast_ms", "t_score_generic_ms")]
+                                       "t_finish_tb_ms", "t_score_prep_ms", "t_score_fast_ms", "t_score_generic_ms",
+                                       "t_score_build_ms", "t_score_stage2_ms", "t_finish_order_ms")]
 
     def as_dict(self):
         d = {}
