@@ -76,7 +76,8 @@ double now_ms() {
 // Memo of a pure function of the subject length (per query): direct-mapped,
 // so a collision only recomputes.
 struct LenMemo {
-    static constexpr int kSlots = 512;
+    // a query's candidate subjects have up to a few thousand distinct lengths
+    static constexpr int kSlots = 8192;
     int64_t key[kSlots];
     double val[kSlots];
     LenMemo() {
@@ -84,7 +85,7 @@ struct LenMemo {
     }
     template <class F>
     double get(int64_t n, F f) {
-        const int i = (int)(((uint64_t)n * 0x9E3779B97F4A7C15ull) >> 55);
+        const int i = (int)(((uint64_t)n * 0x9E3779B97F4A7C15ull) >> 51);
         if (key[i] != n) {
             key[i] = n;
             val[i] = f();
@@ -359,18 +360,32 @@ struct Engine {
     // engine.rs:1247-1324
     std::vector<Plan> plan_windows(const std::vector<Region>& regs, int64_t qlen) const {
         const size_t n = regs.size();
-        std::vector<int64_t> span_lo(n), span_hi(n);
+        // per-thread work buffers (a query's regions are planned on one thread)
+        thread_local std::vector<int64_t> span_lo, span_hi;
+        thread_local std::vector<uint32_t> by, tmp;
+        thread_local std::vector<size_t> idx;
+        span_lo.resize(n);
+        span_hi.resize(n);
         for (size_t i = 0; i < n; i++) {
             span_lo[i] = regs[i].dmin;
             span_hi[i] = regs[i].dmax;
         }
-        // group by subject (stable: the index breaks ties)
-        std::vector<uint64_t> keyed(n);
-        for (size_t i = 0; i < n; i++) keyed[i] = ((uint64_t)regs[i].subject << 32) | (uint64_t)i;
-        std::sort(keyed.begin(), keyed.end());
-        std::vector<size_t> by(n);
-        for (size_t i = 0; i < n; i++) by[i] = (size_t)(keyed[i] & 0xFFFFFFFFu);
-        std::vector<size_t> idx;
+        // group by subject, stable (the index breaks ties): 12-bit counting
+        // passes over the subject ids, least significant digit first
+        by.resize(n);
+        tmp.resize(n);
+        uint32_t smax = 0;
+        for (size_t i = 0; i < n; i++) {
+            by[i] = (uint32_t)i;
+            smax = std::max(smax, regs[i].subject);
+        }
+        for (int sh = 0; sh == 0 || (sh < 32 && (smax >> sh) != 0); sh += 12) {
+            uint32_t cnt[4097] = {0};
+            for (size_t i = 0; i < n; i++) cnt[((regs[by[i]].subject >> sh) & 4095u) + 1]++;
+            for (int b = 0; b < 4096; b++) cnt[b + 1] += cnt[b];
+            for (size_t i = 0; i < n; i++) tmp[cnt[(regs[by[i]].subject >> sh) & 4095u]++] = by[i];
+            std::swap(by, tmp);
+        }
         for (size_t a = 0; a < n;) {
             size_t b = a;
             while (b < n && regs[by[b]].subject == regs[by[a]].subject) b++;
