@@ -264,7 +264,9 @@ void composition_bias(const uint8_t* q, int64_t n, const int32_t* mat, int8_t* o
 struct Region {
     uint32_t subject;
     int64_t dmin, dmax, best;
-    uint64_t src;  // index among the scan's regions of the batch
+    uint64_t src;    // index among the scan's regions of the batch
+    uint64_t sbase;  // the subject's first residue in the database
+    int64_t sl;      // the subject's length
 };
 struct Plan {
     int64_t lo, hi;
@@ -347,8 +349,8 @@ struct Engine {
     }
 
     // engine.rs:1223-1234
-    void window(int64_t dmin, int64_t dmax, uint32_t s, int64_t qlen, int64_t& lo, int64_t& hi) const {
-        const int64_t sl = slen(s), slack = P.window_slack;
+    void window(int64_t dmin, int64_t dmax, int64_t sl, int64_t qlen, int64_t& lo, int64_t& hi) const {
+        const int64_t slack = P.window_slack;
         lo = std::min(std::max<int64_t>(dmin - slack, 0), sl);
         hi = std::max(std::min(qlen + dmax + slack, sl), lo);
         if ((hi - lo) * 4 >= sl * 3) {
@@ -420,14 +422,14 @@ struct Engine {
         for (size_t ri = 0; ri < n; ri++) {
             const Region& r = regs[ri];
             int64_t lo, hi;
-            window(r.dmin, r.dmax, r.subject, qlen, lo, hi);
+            window(r.dmin, r.dmax, r.sl, qlen, lo, hi);
             Plan own{lo, hi, false, 0, 0};
             if (P.exhaustive || r.best == 0 || (int64_t)P.window_slack >= kI64Max / 8) {
                 plans[ri] = own;
                 continue;
             }
             if (P.score_band > 0) {
-                const int64_t w = P.score_band, dmin = span_lo[ri], dmax = span_hi[ri], sl = slen(r.subject);
+                const int64_t w = P.score_band, dmin = span_lo[ri], dmax = span_hi[ri], sl = r.sl;
                 const int64_t lo2 = std::min(std::max<int64_t>(dmin - w, 0), sl);
                 const int64_t hi2 = std::max(std::min(qlen + dmax + w, sl), lo2);
                 const int64_t nn = hi2 - lo2;
@@ -442,7 +444,7 @@ struct Engine {
                 continue;
             }
             int64_t ulo, uhi;
-            window(span_lo[ri], span_hi[ri], r.subject, qlen, ulo, uhi);
+            window(span_lo[ri], span_hi[ri], r.sl, qlen, ulo, uhi);
             const int64_t nn = uhi - ulo;
             int64_t blo = span_lo[ri] - ulo - P.window_slack, bhi = span_hi[ri] - ulo + P.window_slack;
             band_clip(blo, bhi, qlen, nn);
@@ -458,11 +460,11 @@ struct Engine {
         return plans;
     }
 
-    saber_band_job job(uint32_t qi, uint32_t s, int64_t lo, int64_t hi, int64_t blo, int64_t bhi) const {
+    saber_band_job job(uint32_t qi, const Region& r, int64_t lo, int64_t hi, int64_t blo, int64_t bhi) const {
         saber_band_job j{};
         j.query = qi;
-        j.subject = s;
-        j.win_begin = soff[s] + (uint64_t)lo;
+        j.subject = r.subject;
+        j.win_begin = r.sbase + (uint64_t)lo;
         j.win_len = (uint32_t)(hi - lo);
         j.band_lo = (int32_t)std::max<int64_t>(std::min(blo, kI32Max), -kI32Max - 1);
         j.band_hi = (int32_t)std::max<int64_t>(std::min(bhi, kI32Max), -kI32Max - 1);
@@ -522,16 +524,16 @@ struct Engine {
                 const int64_t n = pl.hi - pl.lo;
                 const size_t k = base[qi] + ri;
                 if (!pl.band) {
-                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, -m, n);
+                    s1[k] = job(qi, r, pl.lo, pl.hi, -m, n);
                     r1[k] = {qi, ri, 0};
                 } else if (0 < wn && wn < full_band) {
                     int64_t blo = r.dmin - wn - pl.lo, bhi = r.dmax + wn - pl.lo;
                     band_clip(blo, bhi, m, n);
-                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, blo, bhi);
+                    s1[k] = job(qi, r, pl.lo, pl.hi, blo, bhi);
                     r1[k] = {qi, ri, 1};
                     banded[qi]++;
                 } else {
-                    s1[k] = job(qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi);
+                    s1[k] = job(qi, r, pl.lo, pl.hi, pl.blo, pl.bhi);
                     r1[k] = {qi, ri, 2};
                     banded[qi]++;
                 }
@@ -558,7 +560,7 @@ struct Engine {
                 }
                 const Region& r = per_q[x.qi][x.ri];
                 const Prep& pr = preps[x.qi];
-                const int64_t sl = slen(r.subject);
+                const int64_t sl = r.sl;
                 const double thr = memo.get(sl, [&]() {
                     return P.score_prefilter_frac * pr.qs.floor_lower_bound(re, false, 0.0, sl, pr.region_floor);
                 });
@@ -583,7 +585,7 @@ struct Engine {
                 const Ref& x = r1[k];
                 const Region& r = per_q[x.qi][x.ri];
                 const Plan& pl = plans[x.qi][x.ri];
-                s2[w] = job(x.qi, r.subject, pl.lo, pl.hi, pl.blo, pl.bhi);
+                s2[w] = job(x.qi, r, pl.lo, pl.hi, pl.blo, pl.bhi);
                 r2[w] = x;
                 w++;
             }
@@ -702,7 +704,7 @@ struct Engine {
                     continue;
                 }
                 if (sc <= 0 || (has_bits && qs.bitscore(sc) < P.min_bitscore)) continue;
-                const int64_t n = slen(regs[i].subject);
+                const int64_t n = regs[i].sl;
                 if (qs.evalue_in(sc, lb.get(n, [&]() { return qs.space_lower_bound(n); })) > ecut) continue;
                 const double e = qs.evalue_in(sc, sp.get(n, [&]() { return qs.space_for(n); }));
                 if (e <= ecut) order.push_back({e, i});
@@ -840,7 +842,7 @@ struct Engine {
             std::memset(&j, 0, sizeof(j));
             j.query = qi;
             j.subject = r.subject;
-            j.win_begin = soff[r.subject] + (uint64_t)pl.lo;
+            j.win_begin = r.sbase + (uint64_t)pl.lo;
             j.win_len = (uint32_t)(pl.hi - pl.lo);
             j.d_min = (int32_t)(r.dmin - pl.lo);
             j.d_max = (int32_t)(r.dmax - pl.lo);
@@ -932,7 +934,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
     if (P.exhaustive) {
         for (uint32_t qi = 0; qi < nq; qi++)
             if (qlens[qi] > 0)
-                for (uint32_t s = 0; s < nsub; s++) per_q[qi].push_back({s, -qlens[qi], E.slen(s), 0, 0});
+                for (uint32_t s = 0; s < nsub; s++)
+                    per_q[qi].push_back({s, -qlens[qi], E.slen(s), 0, 0, db_offsets[s], E.slen(s)});
     } else if (nq && nsub) {
         std::vector<int32_t> thr(nq);
         for (uint32_t qi = 0; qi < nq; qi++) thr[qi] = (int32_t)preps[qi].region_thr;
@@ -949,6 +952,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
         if (sink.triaged) E.st.triage_dropped += sink.ncap - sink.n;
         const saber_region* R = sink.regs;
         const uint32_t* src = sink.src;
+        const uint64_t* sbase = sink.sbase;
+        const uint32_t* slen = sink.slen;
         const uint64_t nr = sink.n;
         parallel_for(nq, [&](size_t qi) {
             auto by_query = [](const saber_region& r, uint64_t q) { return r.query < q; };
@@ -956,7 +961,8 @@ extern "C" int saber_gpu_search(saber_gpu* h, const saber_search_params* params,
             const uint64_t e = (uint64_t)(std::lower_bound(R + b, R + nr, (uint64_t)qi + 1, by_query) - R);
             auto& v = per_q[qi];
             v.reserve(e - b);
-            for (uint64_t t = b; t < e; t++) v.push_back({R[t].subject, R[t].d_min, R[t].d_max, R[t].best, src[t]});
+            for (uint64_t t = b; t < e; t++)
+                v.push_back({R[t].subject, R[t].d_min, R[t].d_max, R[t].best, src[t], sbase[t], (int64_t)slen[t]});
         });
     }
     for (uint32_t qi = 0; qi < nq; qi++) {

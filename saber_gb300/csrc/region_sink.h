@@ -15,6 +15,8 @@ struct RegionSink {
     float lambda = 0.f, logk = 0.f;  // for the triage features
     const saber_region* regs = nullptr;
     const uint32_t* src = nullptr;
+    const uint64_t* sbase = nullptr;  // per kept region: its subject's first residue
+    const uint32_t* slen = nullptr;   // and length
     uint64_t n = 0;                  // kept regions
     uint64_t ncap = 0;               // regions after the per-query cap
     bool triaged = false;            // a model dropped regions

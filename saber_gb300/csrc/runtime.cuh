@@ -162,8 +162,8 @@ struct saber_gpu {
     std::vector<uint64_t> sc_caps;  // per shape
     std::vector<uint64_t> sc_freq_off;
     // device-side region cap / triage / compaction, pinned host staging
-    saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out;
-    saber::HostBuf pin_reg, pin_src;
+    saber::DevBuf rg_qcnt, rg_qstart, rg_rank, rg_flag, rg_idx, rg_idx2, rg_out, rg_sbase, rg_slen;
+    saber::HostBuf pin_reg, pin_src, pin_sbase, pin_slen;
     saber::HostBuf pin_scratch[4];  // the batch engine's staging (pinned_scratch)
     saber::DevBuf mask_runs;  // database mask runs being expanded
     // six-frame translation scratch

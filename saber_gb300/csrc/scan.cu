@@ -1165,6 +1165,19 @@ __global__ void k_keep_flags(const float* __restrict__ logit, uint32_t n, float 
         flag[i] = logit[i] >= thr;
 }
 
+// the subject's first residue and length of each region (the host engine's
+// windows and jobs need them for every region)
+__global__ void k_region_subject_spans(const saber_region* __restrict__ reg, uint32_t n,
+                                       const uint64_t* __restrict__ soffs, uint64_t* __restrict__ sbase,
+                                       uint32_t* __restrict__ slen) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t sj = reg[i].subject;
+        const uint64_t b = soffs[sj];
+        sbase[i] = b;
+        slen[i] = (uint32_t)(soffs[sj + 1] - b);
+    }
+}
+
 __global__ void k_iota(uint32_t* __restrict__ v, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
 }
@@ -1275,13 +1288,25 @@ static int region_sink(saber_gpu* h, const saber_scan_params* p, bool has_thr, u
     CU(h, cudaGetLastError());
     CUALLOC(h, h->pin_reg, (uint64_t)std::max<uint32_t>(nout, 1) * sizeof(saber_region));
     CUALLOC(h, h->pin_src, (uint64_t)std::max<uint32_t>(nout, 1) * 4);
+    CUALLOC(h, h->pin_sbase, (uint64_t)std::max<uint32_t>(nout, 1) * 8);
+    CUALLOC(h, h->pin_slen, (uint64_t)std::max<uint32_t>(nout, 1) * 4);
+    CUALLOC(h, h->rg_sbase, (uint64_t)std::max<uint32_t>(nout, 1) * 8);
+    CUALLOC(h, h->rg_slen, (uint64_t)std::max<uint32_t>(nout, 1) * 4);
     if (nout) {
+        k_region_subject_spans<<<nblocks(nout, 256), 256, 0, s>>>(oreg, nout, h->main.soff.as<uint64_t>(),
+                                                                 h->rg_sbase.as<uint64_t>(),
+                                                                 h->rg_slen.as<uint32_t>());
+        CU(h, cudaGetLastError());
         CU(h, cudaMemcpyAsync(h->pin_reg.p, oreg, (uint64_t)nout * sizeof(saber_region), cudaMemcpyDeviceToHost, s));
         CU(h, cudaMemcpyAsync(h->pin_src.p, osrc, (uint64_t)nout * 4, cudaMemcpyDeviceToHost, s));
+        CU(h, cudaMemcpyAsync(h->pin_sbase.p, h->rg_sbase.p, (uint64_t)nout * 8, cudaMemcpyDeviceToHost, s));
+        CU(h, cudaMemcpyAsync(h->pin_slen.p, h->rg_slen.p, (uint64_t)nout * 4, cudaMemcpyDeviceToHost, s));
     }
     CU(h, cudaStreamSynchronize(s));
     sk.regs = h->pin_reg.as<saber_region>();
     sk.src = h->pin_src.as<uint32_t>();
+    sk.sbase = h->pin_sbase.as<uint64_t>();
+    sk.slen = h->pin_slen.as<uint32_t>();
     sk.n = nout;
     return SABER_OK;
 }
