@@ -741,6 +741,7 @@ def run_ours(a, rank, world, local_rank):
     cfg = config_dict(a, world)
     cfg["strip_rows"] = dev.strip_rows
     cfg["pair_steps"] = dev.pair_steps
+    cfg["long_steps"] = dev.long_steps
     if tuned is not None:
         cfg["autotune"] = tuned["candidates"]
     out = {"metric": METRIC, "value": round(value, 2), "unit": "GCUPS", "n_gpus": world, "steps": a.steps,

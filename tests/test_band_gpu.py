@@ -270,3 +270,33 @@ def test_captured_graphs_match_step_launches(tuned):
         assert st_g["banded_cells"] == st_w["banded_cells"] and st_g["i16_rescored"] == st_w["i16_rescored"]
         assert dev.graph_captures == n0
     dev.graphs = True
+
+
+def test_autotuner_keeps_scores_and_leaves_a_candidate_setting(dev):
+    """autotune_scoring times launch shapes on the caller's batch by
+    coordinate descent over strip rows, the pairing bin edge and the long-job
+    bin edge; every timed setting scores identically (it raises otherwise),
+    the chosen one is left on the device and the scores after it equal the
+    oracle's."""
+    torch = pytest.importorskip("torch")
+    from saber_gb300.tune import KNOBS, LONG_AUTO, autotune_scoring
+    qs, ss, planted = synth.protein_db(61, 40, 2000)
+    bias = synth.query_bias(62, qs)
+    jobs = synth.band_jobs(63, qs, ss, planted, 6000, half_min=2, half_max=128)
+    dev.set_scheme(B62, 11, 1)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    d_jobs = torch.from_numpy(jobs.view(np.uint8).copy()).cuda()
+    d_scores = torch.zeros(jobs.size, dtype=torch.int32, device="cuda")
+    try:
+        res = autotune_scoring(dev, d_jobs, d_scores, reps=1)
+        for name, cands in KNOBS:
+            assert res[name] in cands and getattr(dev, name) == res[name]
+        assert len(res["candidates"]) >= sum(len(c) for _, c in KNOBS) - len(KNOBS) + 1
+        got, _ = dev.score_band_jobs(jobs)
+        want, _ = _oracle_jobs(qs, ss, bias, jobs, B62, 11, 1)
+        assert np.array_equal(got, want), _report(got, want, jobs)
+    finally:
+        dev.strip_rows = 16
+        dev.pair_steps = PAIR_DEFAULT
+        dev.long_steps = LONG_AUTO
