@@ -672,8 +672,10 @@ struct ChainArgs {
 // visit_scan (scan.rs:2384-2431), HSPs of at least thr appended with the
 // number of the chain's seed hits they cover.  The ungapped X-drop
 // (ungapped_xdrop, engine.rs:2460-2494; step count of xdrop_cat,
-// scan.rs:859-904) runs as a per-lane state machine, 8 positions per warp
-// iteration: position t (0-based) of a direction scores
+// scan.rs:859-904) runs as a per-lane state machine, 8 positions of each
+// direction per warp iteration, the two directions side by side (they are
+// independent: the HSP takes the sum of their bests and their extents):
+// position t (0-based) of a direction scores
 // P[s[sp + dir (t + off)]][qp + dir (t + off)] (off = 0 rightwards, 1
 // leftwards); a strictly greater running sum is a new best and sets the
 // extent to t + 1, a sum more than x below the best stops the direction
@@ -702,6 +704,68 @@ __device__ __forceinline__ uint2 load8(const uint8_t* __restrict__ buf, int64_t 
     return make_uint2(v[0], v[1]);
 }
 
+// One direction of an extension: position t of the next block, positions
+// available n, running sum, best, extent, positions evaluated when it
+// stopped, and whether it still runs.
+struct XDir {
+    int t, n, cur, best, xe, done;
+    bool run;
+};
+
+// The block's 8 positions of one direction as byte runs of query codes,
+// biases and subject residues (ascending addresses; leftwards reads them
+// backwards).
+struct XBlock {
+    uint2 q, s, b;
+};
+
+__device__ __forceinline__ void xdrop_load(XBlock& L, const XDir& d, bool right, int64_t gq0, int64_t gs0,
+                                           const ChainArgs& a) {
+    const int64_t gq = gq0 + (right ? d.t : -(d.t + kXBlock));
+    const int64_t gs = gs0 + (right ? d.t : -(d.t + kXBlock));
+    L.q = load8(a.qcodes, gq, a.qn + 16);
+    L.s = load8(a.res, gs, a.n_res + 64);
+    L.b = a.qbias ? load8(reinterpret_cast<const uint8_t*>(a.qbias), gq, a.qn + 16) : make_uint2(0u, 0u);
+}
+
+// Scores from the matrix in shared memory plus the query bias, as the
+// profile P[c][i] = S(q_i, c) + bias_i holds them; then the X-drop rule.
+__device__ __forceinline__ void xdrop_eval(XDir& d, const XBlock& L, bool right, const int32_t* smat, int x) {
+    int sv[kXBlock];
+#pragma unroll
+    for (int u = 0; u < kXBlock; u++) {
+        const int b = right ? u : kXBlock - 1 - u;  // byte of position t + u
+        const uint32_t wq = b < 4 ? L.q.x : L.q.y, ws = b < 4 ? L.s.x : L.s.y, wb = b < 4 ? L.b.x : L.b.y;
+        const int sh = 8 * (b & 3);
+        int qcode = (int)((wq >> sh) & 0xFFu);
+        qcode = qcode < 24 ? qcode : 22;
+        const int scode = (int)((ws >> sh) & 0xFFu);
+        const int bias = (int)(int8_t)((wb >> sh) & 0xFFu);
+        sv[u] = smat[qcode * 24 + (scode < 24 ? scode : 22)] + bias;
+    }
+    bool stop = false;
+    int done = 0;
+#pragma unroll
+    for (int u = 0; u < kXBlock; u++) {
+        const int tt = d.t + u;
+        if (!stop && tt < d.n) {
+            d.cur += sv[u];
+            if (d.cur > d.best) {
+                d.best = d.cur;
+                d.xe = tt + 1;
+            } else if (d.cur < d.best - x) {
+                stop = true;
+                done = tt + 1;
+            }
+        }
+    }
+    d.t += kXBlock;
+    if (stop || d.t >= d.n) {
+        d.run = false;
+        d.done = stop ? done : d.n;
+    }
+}
+
 __global__ void __launch_bounds__(256, SABER_CHAINS_MIN_BLOCKS) k_chains(ChainArgs a) {
     __shared__ int32_t smat[576];
     for (int t = threadIdx.x; t < 576; t += blockDim.x) smat[t] = a.matrix[t];
@@ -711,20 +775,20 @@ __global__ void __launch_bounds__(256, SABER_CHAINS_MIN_BLOCKS) k_chains(ChainAr
     unsigned long long ext = 0, avoided = 0, steps = 0;
     uint32_t i = 0, e = 0;  // survivors left in this lane's chain
     bool retired = false;
-    int phase = 0;          // 0: next survivor, 1: rightwards, 2: leftwards
+    bool extending = false;  // an extension (both directions at once) is in progress
     unsigned long long hkey = 0;
     // positions fit 32 bits: queries and subjects are shorter than 2^19,
     // residue offsets below 2^32
     uint32_t q0 = 0;
     int qlen = 0, sl = 0, cover = 0;
     const uint8_t* subj = nullptr;
-    int qp = 0, sp = 0, n = 0, t = 0, xe = 0, end_r = 0, done_r = 0;
-    int cur = 0, best = 0, best_r = 0;
+    int qp = 0, sp = 0;
+    XDir R{0, 0, 0, 0, 0, 0, false}, Lf{0, 0, 0, 0, 0, 0, false};
     uint2 vnext = make_uint2(0, 0);
     bool have_next = false;  // vnext holds survivor i + 1 of this lane's chain
     const uint32_t m27 = (1u << 27) - 1u;
     while (true) {
-        const bool need = !retired && phase == 0 && i >= e;
+        const bool need = !retired && !extending && i >= e;
         const uint32_t nb = __ballot_sync(0xffffffffu, need);
         if (nb) {
             const int leader = __ffs(nb) - 1;
@@ -757,92 +821,47 @@ __global__ void __launch_bounds__(256, SABER_CHAINS_MIN_BLOCKS) k_chains(ChainAr
         bool emit = false;
         uint4 hsp = make_uint4(0, 0, 0, 0);
         if (!retired) {
-            if (phase == 0) {
+            if (!extending) {
                 const uint2 v = have_next ? vnext : a.surv[i];
                 // the chain's next survivor, for the coverage test at the end
                 have_next = i + 1 < e;
                 if (have_next) vnext = a.surv[i + 1];
                 qp = (int)((v.y & m27) - q0);
                 sp = (int)(v.x - (uint32_t)(subj - a.res));
-                n = qlen - qp < sl - sp ? qlen - qp : sl - sp;
-                t = 0;
-                cur = best = 0;
-                xe = 0;
-                phase = 1;
+                R = XDir{0, qlen - qp < sl - sp ? qlen - qp : sl - sp, 0, 0, 0, 0, true};
+                Lf = XDir{0, qp < sp ? qp : sp, 0, 0, 0, 0, false};
+                Lf.run = Lf.n > 0;
+                extending = true;
             }
-            // the block's 8 positions as byte runs of query codes, biases and
-            // subject residues (ascending addresses; leftwards reads them
-            // backwards); scores from the matrix in shared memory, as the
-            // profile P[c][i] = S(q_i, c) + bias_i holds them
-            const bool right = phase == 1;
-            const int64_t gq = (int64_t)q0 + qp + (right ? t : -(t + kXBlock));
-            const int64_t gs = (int64_t)(subj - a.res) + sp + (right ? t : -(t + kXBlock));
-            const uint2 qc8 = load8(a.qcodes, gq, a.qn + 16);
-            const uint2 sc8 = load8(a.res, gs, a.n_res + 64);
-            const uint2 qb8 = a.qbias ? load8(reinterpret_cast<const uint8_t*>(a.qbias), gq, a.qn + 16)
-                                      : make_uint2(0u, 0u);
-            int sv[kXBlock];
-#pragma unroll
-            for (int u = 0; u < kXBlock; u++) {
-                const int b = right ? u : kXBlock - 1 - u;  // byte of position t + u
-                const uint32_t wq = b < 4 ? qc8.x : qc8.y, ws = b < 4 ? sc8.x : sc8.y, wb = b < 4 ? qb8.x : qb8.y;
-                const int sh = 8 * (b & 3);
-                int qcode = (int)((wq >> sh) & 0xFFu);
-                qcode = qcode < 24 ? qcode : 22;
-                const int scode = (int)((ws >> sh) & 0xFFu);
-                const int bias = (int)(int8_t)((wb >> sh) & 0xFFu);
-                sv[u] = smat[qcode * 24 + (scode < 24 ? scode : 22)] + bias;
-            }
-            bool stop = false;
-            int done = 0;
-#pragma unroll
-            for (int u = 0; u < kXBlock; u++) {
-                const int tt = t + u;
-                if (!stop && tt < n) {
-                    cur += sv[u];
-                    if (cur > best) {
-                        best = cur;
-                        xe = tt + 1;
-                    } else if (cur < best - a.x) {
-                        stop = true;
-                        done = tt + 1;
-                    }
+            // both directions advance a block per iteration: their loads are
+            // issued together, then both are evaluated
+            const int64_t gq0 = (int64_t)q0 + qp, gs0 = (int64_t)(subj - a.res) + sp;
+            XBlock BR, BL;
+            if (R.run) xdrop_load(BR, R, true, gq0, gs0, a);
+            if (Lf.run) xdrop_load(BL, Lf, false, gq0, gs0, a);
+            if (R.run) xdrop_eval(R, BR, true, smat, a.x);
+            if (Lf.run) xdrop_eval(Lf, BL, false, smat, a.x);
+            if (!R.run && !Lf.run) {
+                steps += (uint64_t)(R.done + Lf.done);
+                ext++;
+                const int hi = qp + R.xe, lo = qp - Lf.xe;
+                cover = hi;
+                const int score = R.best + Lf.best;
+                // the chain's next hits below hi are covered (query
+                // positions ascend along the chain); the HSP counts them
+                uint32_t j = i + 1;
+                if (j < e && (int)((vnext.y & m27) - q0) < cover) {
+                    j++;
+                    have_next = false;
+                    while (j < e && (int)((a.surv[j].y & m27) - q0) < cover) j++;
                 }
-            }
-            t += kXBlock;
-            if (stop || t >= n) {
-                if (!stop) done = n;
-                if (phase == 1) {
-                    best_r = best;
-                    end_r = xe;
-                    done_r = done;
-                    phase = 2;
-                    n = qp < sp ? qp : sp;
-                    t = 0;
-                    cur = best = 0;
-                    xe = 0;
-                } else {
-                    steps += (uint64_t)(done_r + done);
-                    ext++;
-                    const int hi = qp + end_r, lo = qp - xe;
-                    cover = hi;
-                    const int score = best_r + best;
-                    // the chain's next hits below hi are covered (query
-                    // positions ascend along the chain); the HSP counts them
-                    uint32_t j = i + 1;
-                    if (j < e && (int)((vnext.y & m27) - q0) < cover) {
-                        j++;
-                        have_next = false;
-                        while (j < e && (int)((a.surv[j].y & m27) - q0) < cover) j++;
-                    }
-                    avoided += j - (i + 1);
-                    if (score >= a.thr) {
-                        emit = true;
-                        hsp = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, j - i);
-                    }
-                    i = j;
-                    phase = 0;
+                avoided += j - (i + 1);
+                if (score >= a.thr) {
+                    emit = true;
+                    hsp = make_uint4((uint32_t)lo, (uint32_t)hi, (uint32_t)score, j - i);
                 }
+                i = j;
+                extending = false;
             }
         }
         const uint32_t eb = __ballot_sync(0xffffffffu, emit);
