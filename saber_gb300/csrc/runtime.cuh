@@ -142,6 +142,7 @@ struct saber_gpu {
         scores_dev;
     // scan state: per-residue seed bytes / distances of the database, the
     // database mask, per-shape frequent-code bitmaps, and per-call buffers
+    saber::DevBuf sc_sblk, sc_qblk;  // owner tables of 256-position blocks (database, batch)
     saber::DevBuf db_mask, sc_sb, sc_rem, sc_dst, sc_freq, sc_counts, sc_qsb, sc_qfull, sc_qrem, sc_qdst,
         sc_qcnt, sc_qoff, sc_qent, sc_qpres, sc_surv, sc_key1, sc_key2, sc_val, sc_key1o, sc_key2o, sc_valo,
         sc_chains, sc_hsp, sc_hkey, sc_hkeyo, sc_hval, sc_hvalo, sc_pairs, sc_regions, sc_rthr, sc_ctr, sc_tmp,

@@ -589,15 +589,6 @@ __global__ void k_gather_regions(const saber_region* __restrict__ src, const uin
 }
 
 // ---- chains ------------------------------------------------------------------------
-__device__ __forceinline__ uint64_t upper_idx(const uint64_t* offs, uint64_t n, uint64_t x) {
-    uint64_t lo = 0, hi = n;  // last k with offs[k] <= x
-    while (hi - lo > 1) {
-        uint64_t mid = (lo + hi) >> 1;
-        if (offs[mid] <= x) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
 
 // Bit layout of the chain keys: (query, subject, diagonal + dbias) above
 // `low` bits.  In the composite layout the low bits hold (query position,
@@ -609,15 +600,37 @@ struct KeyLayout {
     int64_t dbias;
 };
 
+// Owner tables: blk[b] is the sequence holding position b * 256 of a
+// concatenation with offsets offs[nseq + 1]; one thread per sequence writes
+// the blocks that start inside it.
+constexpr int kOwnerShift = 8;
+__global__ void k_block_owner(const uint64_t* __restrict__ offs, uint64_t nseq, uint32_t* __restrict__ blk) {
+    for (uint64_t sq = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; sq < nseq;
+         sq += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b0 = (offs[sq] + (1ull << kOwnerShift) - 1) >> kOwnerShift;
+        const uint64_t b1 = (offs[sq + 1] + (1ull << kOwnerShift) - 1) >> kOwnerShift;
+        for (uint64_t b = b0; b < b1; b++) blk[b] = (uint32_t)sq;
+    }
+}
+
+// The sequence holding position x (< offs[nseq]): the owner of x's block,
+// then forward over the sequences that start later in the block.
+__device__ __forceinline__ uint64_t owner_of(const uint64_t* offs, const uint32_t* blk, uint64_t x) {
+    uint64_t sq = blk[x >> kOwnerShift];
+    while (offs[sq + 1] <= x) sq++;
+    return sq;
+}
+
 __global__ void k_surv_keys(const uint2* __restrict__ surv, uint32_t n, const uint64_t* __restrict__ soffs,
-                            uint64_t nsub, const uint64_t* __restrict__ qoffs, uint32_t nq, KeyLayout L,
+                            const uint32_t* __restrict__ sblk, const uint64_t* __restrict__ qoffs,
+                            const uint32_t* __restrict__ qblk, KeyLayout L,
                             unsigned long long* __restrict__ key1, uint32_t* __restrict__ key2,
                             uint32_t* __restrict__ val) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint2 v = surv[i];
         const uint32_t g = v.y & ((1u << 27) - 1), shape = v.y >> 27;
-        const uint64_t s = upper_idx(soffs, nsub, v.x);
-        const uint64_t q = upper_idx(qoffs, nq, g);
+        const uint64_t s = owner_of(soffs, sblk, v.x);
+        const uint64_t q = owner_of(qoffs, qblk, g);
         const int64_t qp = (int64_t)g - (int64_t)qoffs[q], sp = (int64_t)v.x - (int64_t)soffs[s];
         const int64_t d = sp - qp;
         const unsigned long long ck =
@@ -1074,6 +1087,10 @@ int scan_build_db(saber_gpu* h, const saber_scan_params* p) {
             CU(h, cudaGetLastError());
         }
     }
+    CUALLOC(h, h->sc_sblk, ((N >> kOwnerShift) + 2) * 4);
+    if (ds.nsub)
+        k_block_owner<<<nblocks(ds.nsub, 256, h->sm_count * 32), 256, 0, s>>>(ds.soff.as<uint64_t>(), ds.nsub,
+                                                                            h->sc_sblk.as<uint32_t>());
     CUALLOC(h, h->sc_sb, N + 128);
     CUALLOC(h, h->sc_rem, N + 64);
     CUALLOC(h, h->sc_dst, N + 64);
@@ -1576,8 +1593,14 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             }
         }
         const int chain_bits = bits_for(qs.nq ? qs.nq - 1 : 0) + kl.bs + kl.bd;
-        k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(), ds.nsub,
-                                                     qs.offsets.as<uint64_t>(), qs.nq, kl,
+        // owner table of the batch positions (the database's is built with the scan state)
+        CUALLOC(h, h->sc_qblk, ((QN >> kOwnerShift) + 2) * 4);
+        if (qs.nq)
+            k_block_owner<<<nblocks(qs.nq, 256), 256, 0, s>>>(qs.offsets.as<uint64_t>(), qs.nq,
+                                                              h->sc_qblk.as<uint32_t>());
+        k_surv_keys<<<nblocks(ns, 256), 256, 0, s>>>(h->sc_surv.as<uint2>(), ns, ds.soff.as<uint64_t>(),
+                                                     h->sc_sblk.as<uint32_t>(), qs.offsets.as<uint64_t>(),
+                                                     h->sc_qblk.as<uint32_t>(), kl,
                                                      kl.low ? h->sc_key1o.as<unsigned long long>()
                                                             : h->sc_key1.as<unsigned long long>(),
                                                      h->sc_key2.as<uint32_t>(),
