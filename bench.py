@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--search-only", action="store_true",
                     help="only the batched-search section (printed as its own JSON line)")
     ap.add_argument("--no-triage", action="store_true", help="search section without the learned triage")
-    ap.add_argument("--triage-recall", type=float, default=0.997,
+    ap.add_argument("--triage-recall", type=float, default=0.998,
                     help="share of the held-out positive regions the triage threshold keeps")
     ap.add_argument("--triage-margin", type=float, default=0.0, help="logits below that threshold point")
     ap.add_argument("--no-pool", action="store_true", help="search section without the two-batches-in-flight lines")

@@ -60,3 +60,30 @@ def test_scan_caps_and_no_filter(dev):
                                max_candidates=7)
     assert ost["seeds_frequent_skipped"] > 0 and ost["regions_dropped_by_cap"] > 0
     _check(got, gst, want, ost)
+
+
+def test_scan_with_empty_and_tiny_sequences(dev):
+    """Subjects and queries of length 0 and 1-7 beside long ones (many
+    sequences start inside one 256-position block of the owner tables, and
+    long ones span several blocks): regions and counters still equal the
+    oracle's."""
+    from saber_gb300.synth import ProteinSet
+    qs, ss, _ = synth.protein_db(27, 12, 600)
+    rng = np.random.default_rng(28)
+
+    def splice(seqs, n_tiny):
+        parts = [seqs.seq(i) for i in range(len(seqs))]
+        for _ in range(n_tiny):
+            k = int(rng.integers(0, len(parts) + 1))
+            parts.insert(k, rng.integers(0, 20, size=int(rng.integers(0, 8))).astype(np.uint8))
+        parts.append(np.concatenate([seqs.seq(0)] * 12))  # one sequence over several blocks
+        offs = np.zeros(len(parts) + 1, np.uint64)
+        offs[1:] = np.cumsum([p.size for p in parts])
+        return ProteinSet(np.concatenate(parts).astype(np.uint8), offs)
+
+    q2, s2 = splice(qs, 6), splice(ss, 400)
+    assert np.any(np.diff(s2.offsets.astype(np.int64)) == 0)
+    got, gst, want, ost = _run(dev, q2, s2, None, None, None, None, presets.DS16, presets.alphabet_map(),
+                               min_ids=27, exact_weight=2)
+    assert want.size > 0
+    _check(got, gst, want, ost)
