@@ -1635,12 +1635,12 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         uint32_t* nchains = h->sc_ctr.as<uint32_t>() + 40;
         CU(h, cub::DeviceSelect::Flagged(h->cub_tmp.p, tb, thrust::counting_iterator<uint32_t>(0),
                                          h->sc_flags.as<uint8_t>(), h->sc_chains.as<uint32_t>(), nchains, (int)ns, s));
-        uint64_t hcap = std::max<uint64_t>(1024, ns);
-        CUALLOC(h, h->sc_hsp, hcap * 16);
-        CUALLOC(h, h->sc_hkey, hcap * 8);
-        CUALLOC(h, h->sc_hkeyo, hcap * 8);
-        CUALLOC(h, h->sc_hval, hcap * 4);
-        CUALLOC(h, h->sc_hvalo, hcap * 4);
+        // HSP buffers: at most one HSP per survivor, usually far fewer (7 % of
+        // the survivors of a protein batch, 0.01 % in nn), so they start at an
+        // eighth of the survivors (or what earlier calls needed) and are grown
+        // and the chains rerun when an HSP count exceeds them
+        uint64_t hcap = std::max<uint64_t>(std::max<uint64_t>(1u << 20, h->sc_hsp.cap / 16), (uint64_t)ns / 8);
+        hcap = std::min<uint64_t>(hcap, std::max<uint64_t>(1024, ns));
         // survivors in chain order (one gather, so the chains read them directly)
         CUALLOC(h, h->sc_surv2, (uint64_t)ns * 8);
         k_gather_u64_by<<<nblocks(ns, 256), 256, 0, s>>>(
@@ -1663,22 +1663,35 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         c.matrix = h->scheme.d_matrix.as<int32_t>();
         c.thr = p->hsp_threshold;
         c.x = p->x_drop;
-        c.hsp = h->sc_hsp.as<uint4>();
-        c.hkey = h->sc_hkey.as<unsigned long long>();
-        c.hval = h->sc_hval.as<uint32_t>();
         c.nhsp = ctr + 11;
-        c.hcap = hcap;
         c.ctr = ctr;
         c.next = reinterpret_cast<uint32_t*>(ctr + 14);
-        CU(h, cudaMemsetAsync(c.next, 0, 4, s));
         int chain_bps = 0;
         CU(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&chain_bps, k_chains, 256, 0));
-        k_chains<<<(unsigned)std::max(1, chain_bps) * (unsigned)h->sm_count, 256, 0, s>>>(c);
-        CU(h, cudaGetLastError());
         unsigned long long nh = 0;
-        CU(h, cudaMemcpyAsync(&nh, ctr + 11, 8, cudaMemcpyDeviceToHost, s));
-        CU(h, cudaStreamSynchronize(s));
-        if (nh > hcap) return fail(h, SABER_ERR_DEVICE, "HSP buffer overflow");
+        for (int attempt = 0;; attempt++) {
+            CUALLOC(h, h->sc_hsp, hcap * 16);
+            CUALLOC(h, h->sc_hkey, hcap * 8);
+            CUALLOC(h, h->sc_hkeyo, hcap * 8);
+            CUALLOC(h, h->sc_hval, hcap * 4);
+            CUALLOC(h, h->sc_hvalo, hcap * 4);
+            c.hsp = h->sc_hsp.as<uint4>();
+            c.hkey = h->sc_hkey.as<unsigned long long>();
+            c.hval = h->sc_hval.as<uint32_t>();
+            c.hcap = hcap;
+            // extensions, avoided, steps; HSP count; chain work counter
+            CU(h, cudaMemsetAsync(ctr + 4, 0, 3 * 8, s));
+            CU(h, cudaMemsetAsync(ctr + 11, 0, 8, s));
+            CU(h, cudaMemsetAsync(c.next, 0, 4, s));
+            k_chains<<<(unsigned)std::max(1, chain_bps) * (unsigned)h->sm_count, 256, 0, s>>>(c);
+            CU(h, cudaGetLastError());
+            CU(h, cudaMemcpyAsync(&nh, ctr + 11, 8, cudaMemcpyDeviceToHost, s));
+            CU(h, cudaStreamSynchronize(s));
+            if (nh <= hcap) break;
+            // the HSP count of a batch does not depend on the buffer: one rerun fits
+            if (attempt >= 1) return fail(h, SABER_ERR_DEVICE, "HSP buffer overflow");
+            hcap = nh + nh / 4 + 1024;
+        }
         CU(h, cudaEventRecord(ev[3], s));
         const uint32_t nhsp = (uint32_t)nh;
         if (nhsp) {
