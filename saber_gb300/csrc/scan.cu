@@ -1565,8 +1565,6 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
     if (ns) {
         CUALLOC(h, h->sc_key1, (uint64_t)ns * 8);
         CUALLOC(h, h->sc_key1o, (uint64_t)ns * 8);
-        CUALLOC(h, h->sc_key2, (uint64_t)ns * 4);
-        CUALLOC(h, h->sc_key2o, (uint64_t)ns * 4);
         CUALLOC(h, h->sc_val, (uint64_t)ns * 4);
         CUALLOC(h, h->sc_valo, (uint64_t)ns * 4);
         CUALLOC(h, h->sc_flags, (uint64_t)ns + 8);
@@ -1592,6 +1590,10 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
                 kl = KeyLayout{0, 24, 20, 5, (int64_t)kDBias};
             }
         }
+        if (!kl.low) {  // the second key of the two-sort layout
+            CUALLOC(h, h->sc_key2, (uint64_t)ns * 4);
+            CUALLOC(h, h->sc_key2o, (uint64_t)ns * 4);
+        }
         const int chain_bits = bits_for(qs.nq ? qs.nq - 1 : 0) + kl.bs + kl.bd;
         // owner table of the batch positions (the database's is built with the scan state)
         CUALLOC(h, h->sc_qblk, ((QN >> kOwnerShift) + 2) * 4);
@@ -1608,9 +1610,10 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
         const int k2_end = std::min(32, 5 + bits_for(qmax));
         const int k1_end = std::min(64, chain_bits + kl.low);
         size_t t1 = 0, t2 = 0, t3 = 0;
-        CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t1, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
-                                              h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0, k2_end,
-                                              s));
+        if (!kl.low)
+            CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t1, h->sc_key2.as<uint32_t>(), h->sc_key2o.as<uint32_t>(),
+                                                  h->sc_val.as<uint32_t>(), h->sc_valo.as<uint32_t>(), (int)ns, 0,
+                                                  k2_end, s));
         CU(h, cub::DeviceRadixSort::SortPairs(nullptr, t2, h->sc_key1o.as<unsigned long long>(),
                                               h->sc_key1.as<unsigned long long>(), h->sc_valo.as<uint32_t>(),
                                               h->sc_val.as<uint32_t>(), (int)ns, 0, k1_end, s));
