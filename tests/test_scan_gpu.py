@@ -87,3 +87,14 @@ def test_scan_with_empty_and_tiny_sequences(dev):
                                min_ids=27, exact_weight=2)
     assert want.size > 0
     _check(got, gst, want, ost)
+
+
+def test_scan_filter_with_the_full_alphabet(dev):
+    """The window filter with the 20-letter alphabet (too many letters for
+    the combined one-byte codes: separate letter and full-code records)."""
+    qs, ss, planted = synth.protein_db(37, 12, 900)
+    bias = synth.query_bias(38, qs)
+    got, gst, want, ost = _run(dev, qs, ss, bias, None, None, None, ["1111", "11011", "110101"],
+                               presets.full_alphabet(), min_ids=27, exact_weight=2)
+    assert want.size > 0 and ost["hits_filtered"] > 0
+    _check(got, gst, want, ost)
