@@ -12,8 +12,8 @@
 // two independent jobs in the two int16 halves of every register and
 // updates both with one DPX s16x2 instruction per operation.  A job is swept
 // as strips of R query rows along its subject window: per strip the lane
-// keeps H(i, j-1) and E(i, j-1) of its R rows in registers, and the H/F
-// values of the row above the strip come from a per-lane boundary buffer
+// keeps G(i, j-1) = H(i, j-1) - go and E(i, j-1) of its R rows in registers,
+// and the G/F values of the row above the strip come from a per-lane boundary buffer
 // indexed by band offset k = j - i - lo, laid out [k][lane] so the warp
 // reads and writes 256 contiguous bytes per step.  All lanes run the same
 // column schedule: the rows entering the band at its left edge are handled
@@ -21,12 +21,14 @@
 // right edge (band widths differ within a warp) is masked per half.  The
 // boundary value, residue codes and substitution scores of a step are
 // fetched one to two steps ahead.  Substitution scores come from per-query
-// profiles P[c][i] = S(q_i, c) + bias_i (int16, built at query upload): two
-// 16-byte loads per 8 rows and step.
+// profiles P[c][i] = S(q_i, c) + bias_i + go (int16, built at query upload;
+// the packed cell adds them to G = H - go): one 32-byte load per 16 rows and
+// step.
 //
 // Cells outside the window (j < 0 or j >= n), rows past the query end and
 // the strips of a half that has finished use a sentinel code / sentinel
-// profile whose value is kSent16: such cells only ever hold values below the
+// profile whose value is kSent16 (+ go in the query profiles): such cells
+// only ever hold values below the
 // band optimum and never feed an in-window cell (except the j = -1 column,
 // which holds exactly H = 0 as the reference's "hd = 0 when j == 0" rule
 // requires), so they need no masks.
@@ -62,31 +64,38 @@ __device__ __align__(32) int16_t g_sent_profile[64] = {
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16};
 
 struct PackedConsts {
-    uint32_t ngo2, nge2, neg2;
+    uint32_t ngo2, nge2, neg2, go2;
 };
 
-// One cell pair of one row.  E and F are carried shifted by the gap-open
-// cost, X = E + go and Y = F + go, so that each updates with one fused DPX op:
-//   X(i,j) = max(X(i,j-1) - ge, H(i,j-1))
-//   Y(i,j) = max(Y(i-1,j) - ge, H(i-1,j))
-//   H(i,j) = max(max(X, Y) - go, H(i-1,j-1) + S, 0)
-// X and Y never fall below kNeg16 (H >= kNeg16 everywhere), and where the
-// reference holds E or F at its NEG sentinel (the band's first cell, row 0)
-// these hold values <= 0, which no H can tell apart (H is clamped at 0).
-__device__ __forceinline__ void cell(uint32_t& X, uint32_t Hleft, uint32_t Hup, uint32_t Yup,
-                                     uint32_t diag, uint32_t sub, const PackedConsts& c,
-                                     uint32_t& H, uint32_t& Y) {
-    X = __viaddmax_s16x2(X, c.nge2, Hleft);
-    Y = __viaddmax_s16x2(Yup, c.nge2, Hup);
-    const uint32_t z = __vimax_s16x2_relu(X, Y);
-    const uint32_t ds = __viaddmax_s16x2(diag, sub, c.neg2);
-    H = __viaddmax_s16x2_relu(z, c.ngo2, ds);
+// One cell pair of one row.  The kernel keeps G = H - go instead of H (the
+// value both gap recurrences open from) and E, F unshifted, and the profile
+// holds S + bias + go:
+//   E(i,j) = max(E(i,j-1) - ge, G(i,j-1))
+//   F(i,j) = max(F(i-1,j) - ge, G(i-1,j))
+//   H(i,j) = max(E, F, G(i-1,j-1) + (S + go), 0),   G(i,j) = H(i,j) - go
+// so that a cell is three DPX instructions on the ALU pipe (two fused
+// add-max, one three-input max with relu) and two packed adds on the FMA
+// pipe (the diagonal sum and G), which issue beside them.  In-band values
+// stay inside int16 without clamping: G >= kNeg16 (the unreachable value of
+// cells outside the band) and the profile >= kSent16, so the diagonal sum is
+// >= -32000; below kLimit16 it is < 32767 (|S + bias| <= 767, go <= 1000).
+// E and F start at kNeg16 and never fall below it (E >= G), and where the
+// reference holds E or F at its NEG sentinel these hold values <= 0, which
+// no H can tell apart (H is clamped at 0).
+__device__ __forceinline__ void cell(uint32_t& E, uint32_t Gleft, uint32_t Gup, uint32_t Fup,
+                                     uint32_t gdiag, uint32_t sub, const PackedConsts& c,
+                                     uint32_t& G, uint32_t& F) {
+    E = __viaddmax_s16x2(E, c.nge2, Gleft);
+    F = __viaddmax_s16x2(Fup, c.nge2, Gup);
+    const uint32_t ds = __vadd2(gdiag, sub);
+    const uint32_t H = __vimax3_s16x2_relu(E, F, ds);
+    G = __vadd2(H, c.ngo2);
 }
 
 template <int R>
 struct StripState {
-    uint32_t Hd[R];  // H(row r, previous column)
-    uint32_t X[R];   // E(row r, previous column) + go
+    uint32_t Hd[R];  // G = H - go of (row r, previous column)
+    uint32_t X[R];   // E(row r, previous column)
 };
 
 // One job of a half: its window, clipped band and rows.
@@ -159,7 +168,7 @@ template <int R>
 struct StepLoads {
     uint4 a[R / 8];
     uint4 b[R / 8];
-    uint2 top;  // (H, F + go) of the row above at band offset u + 1
+    uint2 top;  // (G, F) of the row above at band offset u + 1
 };
 
 // 32-byte read-only load (sm_100 and later): one request per lane for the
@@ -206,36 +215,37 @@ __device__ __forceinline__ uint32_t ragged_mask(int r, int thr_a, int thr_b) {
 
 // One column step of a strip.  MODE 0: left triangle, rows 0..U computed
 // (compile-time U); MODE 1: all rows, no masks; MODE 2: all rows, ragged
-// right-edge masks.
+// right-edge masks.  `best` is the running maximum of G (H - go) over the
+// lane's in-band cells.
 template <int R, int MODE, int U>
 __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, uint2* __restrict__ buf, int u,
                                            const StepLoads<R>& L, const PackedConsts& c, uint32_t& best,
                                            int thr_a, int thr_b) {
-    uint32_t Hup = L.top.x, Yup = L.top.y;
+    uint32_t Gup = L.top.x, Fup = L.top.y;
     uint32_t diag = diag0;
     diag0 = L.top.x;
-    uint32_t hprev = 0;
+    uint32_t gprev = 0;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (MODE == 0 && r > U) break;
-        uint32_t H, Y;
-        uint32_t hold = st.Hd[r];
-        cell(st.X[r], hold, Hup, Yup, diag, sub_of<R>(L, r), c, H, Y);
+        uint32_t G, F;
+        uint32_t gold = st.Hd[r];
+        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R>(L, r), c, G, F);
         if (MODE == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
-            H = (H & mk) | (c.neg2 & ~mk);
-            Y = (Y & mk) | (c.neg2 & ~mk);
+            G = (G & mk) | (c.neg2 & ~mk);
+            F = (F & mk) | (c.neg2 & ~mk);
         }
-        diag = hold;
-        st.Hd[r] = H;
-        Hup = H;
-        Yup = Y;
+        diag = gold;
+        st.Hd[r] = G;
+        Gup = G;
+        Fup = F;
         // running best over row pairs: one three-input max per two rows
-        if (r & 1) best = __vimax3_s16x2_relu(best, hprev, H);
-        else if (r == R - 1 || (MODE == 0 && r == U)) best = __vimax_s16x2_relu(best, H);
-        else hprev = H;
+        if (r & 1) best = __vimax3_s16x2(best, gprev, G);
+        else if (r == R - 1 || (MODE == 0 && r == U)) best = __vmaxs2(best, G);
+        else gprev = G;
     }
-    if (MODE != 0 || U == R - 1) stbuf(buf + (size_t)(u - R + 1) * 32, make_uint2(Hup, Yup));
+    if (MODE != 0 || U == R - 1) stbuf(buf + (size_t)(u - R + 1) * 32, make_uint2(Gup, Fup));
 }
 
 // The pipelined column loop state of one strip: the loads of step u + 1 are
@@ -290,7 +300,7 @@ struct LeftTriangle<R, -1> {
 // rows R .. 2R-1 in the high halves one column behind, so the high half's row
 // above (the low half's last row) comes from the previous step's registers
 // and its residue code is the low half's code of the previous step.  The
-// boundary buffer then carries one job per lane: 32-bit words H | (F + go) << 16
+// boundary buffer then carries one job per lane: 32-bit words G | F << 16
 // of the super-strip's last row.  A warp task is 32 such jobs; the job's
 // critical path is about half of its R-row sweep.
 template <int R>
@@ -323,42 +333,43 @@ __device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha
 // One step g of a super-strip.  PH 0: compile-time step G <= 2R (low rows
 // r > G not yet in band, high rows r > G - R - 1 not yet in band); PH 1: every
 // row of both halves in band; PH 2: right-edge masks from the thresholds.
+// Values are G = H - go and F, as in strip_step.
 template <int R, int PH, int G>
-__device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, uint32_t& lastH, uint32_t& lastY,
+__device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, uint32_t& lastG, uint32_t& lastF,
                                           uint32_t* __restrict__ pbuf, int g, const StepLoads<R>& L,
                                           const PackedConsts& c, uint32_t& best, int thr_a, int thr_b) {
     const uint32_t top = L.top.x;
-    uint32_t Hup = __byte_perm(top, lastH, 0x5410);
-    uint32_t Yup = __byte_perm(top, lastY, 0x5432);
+    uint32_t Gup = __byte_perm(top, lastG, 0x5410);
+    uint32_t Fup = __byte_perm(top, lastF, 0x5432);
     uint32_t diag = diag0;
-    diag0 = Hup;
-    uint32_t hprev = 0;
+    diag0 = Gup;
+    uint32_t gprev = 0;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (PH == 0 && r > G) break;
-        uint32_t H, Y;
-        uint32_t hold = st.Hd[r];
-        cell(st.X[r], hold, Hup, Yup, diag, sub_of<R>(L, r), c, H, Y);
+        uint32_t Gv, F;
+        uint32_t gold = st.Hd[r];
+        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R>(L, r), c, Gv, F);
         if (PH == 0 && r > G - R - 1) {
-            H = (H & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
-            Y = (Y & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
+            Gv = (Gv & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
+            F = (F & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
         }
         if (PH == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
-            H = (H & mk) | (c.neg2 & ~mk);
-            Y = (Y & mk) | (c.neg2 & ~mk);
+            Gv = (Gv & mk) | (c.neg2 & ~mk);
+            F = (F & mk) | (c.neg2 & ~mk);
         }
-        diag = hold;
-        st.Hd[r] = H;
-        Hup = H;
-        Yup = Y;
-        if (r & 1) best = __vimax3_s16x2_relu(best, hprev, H);
-        else if (r == R - 1 || (PH == 0 && r == G)) best = __vimax_s16x2_relu(best, H);
-        else hprev = H;
+        diag = gold;
+        st.Hd[r] = Gv;
+        Gup = Gv;
+        Fup = F;
+        if (r & 1) best = __vimax3_s16x2(best, gprev, Gv);
+        else if (r == R - 1 || (PH == 0 && r == G)) best = __vmaxs2(best, Gv);
+        else gprev = Gv;
     }
-    lastH = Hup;
-    lastY = Yup;
-    if (g >= 2 * R) stbuf(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Hup, Yup, 0x7632));
+    lastG = Gup;
+    lastF = Fup;
+    if (g >= 2 * R) stbuf(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Gup, Fup, 0x7632));
 }
 
 template <int R, int G>
@@ -418,11 +429,11 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
     const int wmax = __reduce_max_sync(0xffffffffu, has ? J.w : 0);
     const int nsmax = __reduce_max_sync(0xffffffffu, J.ns);
     if (!has) J.w = wmin;
-    const uint32_t top0 = (uint32_t)(uint16_t)kNeg16 << 16;  // H = 0, F + go unreachable
+    const uint32_t top0 = (c.neg2 & 0xFFFF0000u) | (c.ngo2 & 0x0000FFFFu);  // G = -go (H = 0), F unreachable
     for (int k = 0; k < wmax; k++) stbuf(pbuf + (size_t)k * 32, top0);
     stbuf(pbuf + (size_t)wmax * 32, c.neg2);
 
-    uint32_t best = 0;
+    uint32_t best = c.ngo2;  // G of H = 0
     const int gfull = wmax + 2 * R;
     for (int t = 0; t < nsmax; t++) {
         const HalfStrip ha = half_strip(J, t, 2 * R);
@@ -430,7 +441,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
         // Step g reads window column col0 + g in the low half and col0 + g - 1
         // in the high half.  As in the two-job lanes, the warp sweeps only the
         // steps that reach a window column of one of its jobs, a late start
-        // being = 1 (mod 4) past the triangle, from H = 0 rows, with the
+        // being = 1 (mod 4) past the triangle, from rows of H = 0, with the
         // boundary entries of the skipped steps set as those steps would set
         // them.
         int s_lo = 1 << 30, s_hi = -1;
@@ -449,7 +460,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             gend = w_hi + 1 < gfull ? w_hi + 1 : gfull;
         }
         StripState<R> st;
-        uint32_t diag0, lastH, lastY;
+        uint32_t diag0, lastG, lastF;
         PairPipe<R> p;
         int g;
         if (g0 == 0) {
@@ -459,8 +470,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
                 st.X[r] = c.neg2;
             }
             diag0 = __byte_perm(__ldca(pbuf), c.neg2, 0x5410);
-            lastH = c.neg2;
-            lastY = c.neg2;
+            lastG = c.neg2;
+            lastF = c.neg2;
             p.w = code_word(ha, 0);
             p.w2 = code_word(ha, 4);
             const int ca0 = (int)(p.w & 0xFFu);
@@ -468,19 +479,19 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)kSentCode * ha.mpad);
             p.nxt.top.x = __ldca(pbuf + 32);
             p.cprev = ca0;
-            PairTriangle<R, 2 * R>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
+            PairTriangle<R, 2 * R>::run(p, st, diag0, lastG, lastF, pbuf, wmax, ha, hb_rows, c, best);
             g = 2 * R + 1;
         } else {
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                st.Hd[r] = 0u;
+                st.Hd[r] = c.ngo2;
                 st.X[r] = c.neg2;
             }
             const int kskip = min(g0 - 2 * R, wmax);
             for (int k = 0; k < kskip; k++) stbuf(pbuf + (size_t)k * 32, top0);
-            diag0 = 0u;
-            lastH = 0u;
-            lastY = c.neg2;
+            diag0 = c.ngo2;
+            lastG = c.ngo2;
+            lastF = c.neg2;
             // code words of the groups holding steps g0 - 1 .. g0 + 2 and the next
             p.w = code_word(ha, g0 - 1);
             p.w2 = code_word(ha, g0 + 3);
@@ -496,20 +507,20 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
         // (g + 1) & 3 runs 2, 3, 0, 1 from g = 1 (mod 4) (R a multiple of 4)
         for (; g + 4 <= gmid; g += 4) {
             pair_advance<R, 2>(p, ha, hb_rows, pbuf, g, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g, p.cur, c, best, 0, 0);
+            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, 0, 0);
             pair_advance<R, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 1, p.cur, c, best, 0, 0);
+            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 1, p.cur, c, best, 0, 0);
             pair_advance<R, 0>(p, ha, hb_rows, pbuf, g + 2, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 2, p.cur, c, best, 0, 0);
+            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 2, p.cur, c, best, 0, 0);
             pair_advance<R, 1>(p, ha, hb_rows, pbuf, g + 3, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastH, lastY, pbuf, g + 3, p.cur, c, best, 0, 0);
+            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 3, p.cur, c, best, 0, 0);
         }
         for (; g < gend; g++) {
             pair_advance<R, -1>(p, ha, hb_rows, pbuf, g, wmax);
-            pair_step<R, 2, 0>(st, diag0, lastH, lastY, pbuf, g, p.cur, c, best, g - J.w + 1, g - R - J.w);
+            pair_step<R, 2, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, g - J.w + 1, g - R - J.w);
         }
     }
-    const int sc = max(lo16(best), hi16(best));
+    const int sc = max(lo16(best), hi16(best)) + lo16(c.go2);
     if (has) {
         if (sc >= kLimit16) rescue[atomicAdd(rescue_count, 1u)] = jidx;
         else scores[jidx] = sc;
@@ -543,6 +554,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
     c.ngo2 = pk2(-go);
     c.nge2 = pk2(-ge);
     c.neg2 = pk2(kNeg16);
+    c.go2 = pk2(go);
 
     for (;;) {
         uint32_t wt = 0;
@@ -576,12 +588,12 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         if (!has_b) B.w = wmin;
 
         // Boundary of the row above each job's first strip: H = 0 (the
-        // reference's hd = 0 on row 0), F + go unreachable; position wmax
-        // lies outside every band.
-        for (int k = 0; k < wmax; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
+        // reference's hd = 0 on row 0, stored as G = -go), F unreachable;
+        // position wmax lies outside every band.
+        for (int k = 0; k < wmax; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(c.ngo2, c.neg2));
         stbuf(mybuf + (size_t)wmax * 32, make_uint2(c.neg2, c.neg2));
 
-        uint32_t best = 0;
+        uint32_t best = c.ngo2;  // G of H = 0
         const int ufull = wmax + R - 1;
         for (int t = 0; t < nsmax; t++) {
             const HalfStrip ha = half_strip(A, t, R), hb = half_strip(B, t, R);
@@ -633,18 +645,18 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
                 u = R;
             } else {
-                // the skipped columns are sentinel columns: H = 0 to the left
-                // and on the diagonal, E below zero; the boundary entries the
+                // the skipped columns are sentinel columns: H = 0 (G = -go) to
+                // the left and on the diagonal, E below zero; the boundary entries the
                 // skipped steps would have written get those values too (a
                 // later strip that sweeps from step 0 reads them)
 #pragma unroll
                 for (int r = 0; r < R; r++) {
-                    st.Hd[r] = 0u;
+                    st.Hd[r] = c.ngo2;
                     st.X[r] = c.neg2;
                 }
                 const int kskip = min(u0 - R + 1, wmax);
-                for (int k = 0; k < kskip; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(0u, c.neg2));
-                diag0 = 0u;
+                for (int k = 0; k < kskip; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(c.ngo2, c.neg2));
+                diag0 = c.ngo2;
                 p.wa = code_word(ha, u0);
                 p.wb = code_word(hb, u0);
                 p.wa2 = code_word(ha, u0 + 4);
@@ -672,7 +684,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 strip_step<R, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);
             }
         }
-        const int sa = lo16(best), sb = hi16(best);
+        const int sa = lo16(best) + go, sb = hi16(best) + go;
         if (has_a) {
             if (sa >= kLimit16) rescue[atomicAdd(rescue_count, 1u)] = ja_idx;
             else scores[ja_idx] = sa;
@@ -749,7 +761,7 @@ __device__ __forceinline__ void band_pipe_job(const int16_t* __restrict__ qprof,
                 const uint4 pv = *reinterpret_cast<const uint4*>(qprof + (size_t)code * mpad + i0);
                 const uint32_t wv[4] = {pv.x, pv.y, pv.z, pv.w};
 #pragma unroll
-                for (int r = 0; r < RR; r++) sub[r] = (int)(int16_t)((wv[r >> 1] >> (16 * (r & 1))) & 0xFFFFu);
+                for (int r = 0; r < RR; r++) sub[r] = (int)(int16_t)((wv[r >> 1] >> (16 * (r & 1))) & 0xFFFFu) - go;
             }
             const int2 top = buf[u + 1 < w ? u + 1 : w];  // entry w stays NEG
             int Hup = top.x, Fup = top.y;
@@ -852,7 +864,7 @@ __global__ void __launch_bounds__(128) k_band_generic(
         int32_t best = 0;
         for (int64_t i = 0; i < m; i++) {
             __syncwarp();
-            if (lane < 24) col[wib][lane] = qprof[(size_t)lane * mpad + i];
+            if (lane < 24) col[wib][lane] = qprof[(size_t)lane * mpad + i] - go;
             __syncwarp();
             int64_t kmin64 = -(i + lo);
             if (kmin64 < 0) kmin64 = 0;

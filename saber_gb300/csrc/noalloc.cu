@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kNoAllocBlock) k_band_noalloc(
                     e = k > kmin ? ecand : NEG;
                     int32_t f = i >= 1 ? max(AT(a_hp, k + 1) - go, AT(a_fp, k + 1) - ge) : NEG;
                     int32_t hd = (i >= 1 && j >= 1) ? AT(a_hp, k) : 0;
-                    int32_t h = max(max(max(hd + (int32_t)qprof[(size_t)s[j] * mpad + i], e), f), 0);
+                    int32_t h = max(max(max(hd + ((int32_t)qprof[(size_t)s[j] * mpad + i] - go), e), f), 0);
                     AT(a_hc, k) = h;
                     AT(a_fc, k) = f;
                     h_left = h;

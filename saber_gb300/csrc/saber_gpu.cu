@@ -44,15 +44,17 @@ __global__ void k_canon(uint8_t* __restrict__ r, uint64_t n) {
     }
 }
 
-// Query profile P[c][i] = S(q_i, c) + bias_i for c < 24 and i < m, the
-// sentinel score elsewhere (row 24 and rows past the query end).  The
-// reference builds the same per-query table for its ungapped extension
-// (engine.rs:387-388) and a per-subject one in its int16 kernel
+// Query profile P[c][i] = S(q_i, c) + bias_i + go for c < 24 and i < m, the
+// sentinel score + go elsewhere (row 24 and rows past the query end).  The
+// gap-open cost is folded in for the packed kernel, which adds the profile
+// to H - go; the int32 kernels and the traceback subtract it again.  The
+// reference builds the same per-query table (without go) for its ungapped
+// extension (engine.rs:387-388) and a per-subject one in its int16 kernel
 // (banded_simd.rs:425-469).
 __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __restrict__ qoffs,
                           const int8_t* __restrict__ bias, const int32_t* __restrict__ matrix,
                           const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
-                          int16_t* __restrict__ prof) {
+                          int go, int16_t* __restrict__ prof) {
     const uint32_t q = blockIdx.x;
     const uint64_t q0 = qoffs[q];
     const int m = (int)(qoffs[q + 1] - q0);
@@ -66,7 +68,7 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
             if (qc >= 24) qc = 22;
             v = matrix[qc * 24 + c] + (bias ? (int)bias[q0 + i] : 0);
         }
-        P[t] = (int16_t)v;
+        P[t] = (int16_t)(v + go);
     }
 }
 
@@ -606,7 +608,8 @@ static int build_profiles(saber_gpu* h, const Scheme& sch, QuerySet& q) {
     if (!q.has || !sch.has || q.nq == 0) return SABER_OK;
     k_profile<<<q.nq, 256, 0, h->stream>>>(q.codes.as<uint8_t>(), q.offsets.as<uint64_t>(),
                                            q.has_bias ? q.bias.as<int8_t>() : nullptr, sch.d_matrix.as<int32_t>(),
-                                           q.prof_off.as<uint64_t>(), q.prof_mpad.as<uint32_t>(), q.prof.as<int16_t>());
+                                           q.prof_off.as<uint64_t>(), q.prof_mpad.as<uint32_t>(), sch.go,
+                                           q.prof.as<int16_t>());
     CU(h, cudaGetLastError());
     CU(h, cudaStreamSynchronize(h->stream));
     return SABER_OK;

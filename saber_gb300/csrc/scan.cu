@@ -741,8 +741,8 @@ __device__ __forceinline__ void xdrop_load(XBlock& L, const XDir& d, bool right,
     L.b = a.qbias ? load8(reinterpret_cast<const uint8_t*>(a.qbias), gq, a.qn + 16) : make_uint2(0u, 0u);
 }
 
-// Scores from the matrix in shared memory plus the query bias, as the
-// profile P[c][i] = S(q_i, c) + bias_i holds them; then the X-drop rule.
+// Scores S(q_i, s_j) + bias_i from the matrix in shared memory plus the
+// query bias; then the X-drop rule.
 __device__ __forceinline__ void xdrop_eval(XDir& d, const XBlock& L, bool right, const int32_t* smat, int x) {
     int sv[kXBlock];
 #pragma unroll

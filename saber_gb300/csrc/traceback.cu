@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128) k_band_align_warp(const AlignReq* __restr
                     fe = fp[k + 1] - ge;
                     f = i >= 1 ? max(fe, fo) : NEG;
                     const int32_t hd = (i >= 1 && j >= 1) ? hp[k] : 0;
-                    const int32_t diag = hd + (int32_t)rq.prof[(size_t)rq.win[j] * rq.mpad + i];
+                    const int32_t diag = hd + ((int32_t)rq.prof[(size_t)rq.win[j] * rq.mpad + i] - go);
                     c1 = diag > 0;
                     h1 = max(diag, 0);
                     hstar = max(h1, f);
