@@ -71,6 +71,8 @@ typedef struct {
     double t_prep_ms;         /* device time: classify, sort, pairing (CUDA events) */
     double t_fast_ms;         /* device time of the packed int16 kernel */
     double t_generic_ms;      /* device time of the int32 kernel */
+    uint64_t prof8;           /* 1: the packed kernel read the int8 copy of the query profiles (every
+                                 S + bias + go of the query set in [-127, 127]), 0: the int16 profiles */
 } saber_score_stats;
 
 /* ---- handle ---------------------------------------------------------- */

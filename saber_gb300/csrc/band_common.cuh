@@ -70,6 +70,7 @@ __host__ __device__ inline uint64_t band_cells(int64_t m, int64_t n, int64_t lo,
 struct FastArgs {
     const uint8_t* res;
     const int16_t* prof;
+    const int8_t* prof8;    // int8 copy of the profile (every entry fits), or null: the int16 kernel
     const uint64_t* prof_off;
     const uint32_t* prof_mpad;
     const uint64_t* qoffs;
@@ -119,7 +120,7 @@ struct NoAllocArgs {
 };
 int noalloc_score_band_jobs(int device, cudaStream_t s, const NoAllocArgs& a, const char** msg, uint32_t* bad_job);
 
-int band_fast_blocks_per_sm(int strip_rows);
+int band_fast_blocks_per_sm(int strip_rows, bool prof8);
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a);
 cudaError_t launch_band_generic(unsigned grid, unsigned block, cudaStream_t s, const GenericArgs& a);
 

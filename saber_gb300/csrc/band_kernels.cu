@@ -21,9 +21,12 @@
 // right edge (band widths differ within a warp) is masked per half.  The
 // boundary value, residue codes and substitution scores of a step are
 // fetched one to two steps ahead.  Substitution scores come from per-query
-// profiles P[c][i] = S(q_i, c) + bias_i + go (int16, built at query upload;
-// the packed cell adds them to G = H - go): one 32-byte load per 16 rows and
-// step.
+// profiles P[c][i] = S(q_i, c) + bias_i + go built at query upload (the
+// packed cell adds them to G = H - go): an int8 copy (sentinel -128) when
+// every entry of the query set lies in [-127, 127], one 16-byte load per 16
+// rows and step, else the int16 profile, one 32-byte load.  The L1 data pipe
+// bounds the kernel, so the int8 copy's half-size loads are what set its
+// speed; one byte permute with sign replication widens them.
 //
 // Cells outside the window (j < 0 or j >= n), rows past the query end and
 // the strips of a half that has finished use a sentinel code / sentinel
@@ -63,6 +66,22 @@ __device__ __align__(32) int16_t g_sent_profile[64] = {
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16,
     kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16, kSent16};
 
+// The same for the int8 profiles: -128 is their sentinel score (S + bias +
+// go of every real entry lies in [-127, 127]).
+__device__ __align__(32) int8_t g_sent_profile8[64] = {
+    -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128,
+    -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128,
+    -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128,
+    -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128, -128,
+};
+
+template <class T>
+__device__ __forceinline__ const T* sent_profile();
+template <>
+__device__ __forceinline__ const int16_t* sent_profile<int16_t>() { return g_sent_profile; }
+template <>
+__device__ __forceinline__ const int8_t* sent_profile<int8_t>() { return g_sent_profile8; }
+
 struct PackedConsts {
     uint32_t ngo2, nge2, neg2, go2;
 };
@@ -98,9 +117,11 @@ struct StripState {
     uint32_t X[R];   // E(row r, previous column)
 };
 
-// One job of a half: its window, clipped band and rows.
+// One job of a half: its window, clipped band and rows.  T is the profile's
+// element type: int16 S + bias + go, or int8 where every entry fits.
+template <class T>
 struct HalfJob {
-    const int16_t* prof;  // query profile (rows c = 0..24, stride mpad)
+    const T* prof;        // query profile (rows c = 0..24, stride mpad)
     const uint8_t* win;   // window start (unused when n == 0)
     int mpad;
     int n;                // window length (0: every column is a sentinel)
@@ -111,16 +132,18 @@ struct HalfJob {
 };
 
 // Per-strip view of a half: profile row base for this strip's rows.
+template <class T>
 struct HalfStrip {
-    const int16_t* rows;  // prof + i0 (sentinel block when the half is done)
+    const T* rows;        // prof + i0 (sentinel block when the half is done)
     const uint8_t* win;
     int mpad;
     int n;
     int col0;             // window column of step 0 (= lo + i0)
 };
 
-__device__ __forceinline__ HalfStrip half_strip(const HalfJob& h, int t, int R) {
-    HalfStrip v;
+template <class T>
+__device__ __forceinline__ HalfStrip<T> half_strip(const HalfJob<T>& h, int t, int R) {
+    HalfStrip<T> v;
     if (t < h.ns) {
         int i0 = (h.s0 + t) * R;
         v.rows = h.prof + i0;
@@ -129,7 +152,7 @@ __device__ __forceinline__ HalfStrip half_strip(const HalfJob& h, int t, int R) 
         v.n = h.n;
         v.col0 = h.lo + i0;
     } else {
-        v.rows = g_sent_profile;
+        v.rows = sent_profile<T>();
         v.win = nullptr;
         v.mpad = 0;
         v.n = 0;
@@ -142,7 +165,8 @@ __device__ __forceinline__ HalfStrip half_strip(const HalfJob& h, int t, int R) 
 // one byte each, the sentinel code outside the window.  Interior groups take
 // one or two aligned 32-bit loads; the residue buffer is padded past its end,
 // so the second word never leaves the allocation.
-__device__ __forceinline__ uint32_t code_word(const HalfStrip& h, int u) {
+template <class T>
+__device__ __forceinline__ uint32_t code_word(const HalfStrip<T>& h, int u) {
     const int c = h.col0 + u;
     if (c >= 0 && c + 4 <= h.n) {
         const uintptr_t a = reinterpret_cast<uintptr_t>(h.win + c);
@@ -163,46 +187,68 @@ __device__ __forceinline__ uint32_t code_word(const HalfStrip& h, int u) {
     return r;
 }
 
-// Raw profile vectors of one step for both halves (R/8 x 16 bytes each).
-template <int R>
+// Raw profile words of one step for both halves (R rows of T each: 32, 16
+// or 8 bytes).
+template <int R, class T>
 struct StepLoads {
-    uint4 a[R / 8];
-    uint4 b[R / 8];
+    static constexpr int kW = R * (int)sizeof(T) / 4;
+    uint32_t a[kW];
+    uint32_t b[kW];
     uint2 top;  // (G, F) of the row above at band offset u + 1
 };
 
-// 32-byte read-only load (sm_100 and later): one request per lane for the
-// 16 profile rows of a step.
-__device__ __forceinline__ void ld256(uint4& lo, uint4& hi, const void* p) {
-    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=r"(lo.x), "=r"(lo.y), "=r"(lo.z), "=r"(lo.w), "=r"(hi.x), "=r"(hi.y), "=r"(hi.z), "=r"(hi.w)
-        : "l"(p));
+// Read-only load of one half's profile words for a step: one request per
+// lane (32-byte loads exist on sm_100 and later).
+template <int W>
+__device__ __forceinline__ void ld_prof(uint32_t (&d)[W], const void* p) {
+    if constexpr (W == 8) {
+        asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7])
+            : "l"(p));
+    } else if constexpr (W == 4) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+        d[0] = v.x;
+        d[1] = v.y;
+        d[2] = v.z;
+        d[3] = v.w;
+    } else {
+        static_assert(W == 2, "8, 16 or 32 bytes of profile per half and step");
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+        d[0] = v.x;
+        d[1] = v.y;
+    }
 }
 
-template <int R>
-__device__ __forceinline__ void fetch_step(StepLoads<R>& L, const HalfStrip& ha, const HalfStrip& hb, int ca,
-                                           int cb, const uint2* __restrict__ buf, int kin) {
-    const int16_t* pa = ha.rows + (size_t)ca * ha.mpad;
-    const int16_t* pb = hb.rows + (size_t)cb * hb.mpad;
-    if constexpr (R == 16) {
-        ld256(L.a[0], L.a[1], pa);
-        ld256(L.b[0], L.b[1], pb);
-    } else {
-        static_assert(R == 8, "strip rows are 8 or 16");
-        L.a[0] = __ldg(reinterpret_cast<const uint4*>(pa));
-        L.b[0] = __ldg(reinterpret_cast<const uint4*>(pb));
-    }
+template <int R, class T>
+__device__ __forceinline__ void fetch_step(StepLoads<R, T>& L, const HalfStrip<T>& ha, const HalfStrip<T>& hb,
+                                           int ca, int cb, const uint2* __restrict__ buf, int kin) {
+    static_assert(R == 8 || R == 16, "strip rows are 8 or 16");
+    ld_prof(L.a, ha.rows + (size_t)ca * ha.mpad);
+    ld_prof(L.b, hb.rows + (size_t)cb * hb.mpad);
     L.top = __ldca(buf + (size_t)kin * 32);  // boundary rows: the lane's own writes, cached in L1
 }
 
-template <int R>
-__device__ __forceinline__ uint32_t sub_of(const StepLoads<R>& L, int r) {
-    const uint4& a = L.a[r / 8];
-    const uint4& b = L.b[r / 8];
-    const int q = (r % 8) / 2;
-    uint32_t x = q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : a.w;
-    uint32_t y = q == 0 ? b.x : q == 1 ? b.y : q == 2 ? b.z : b.w;
-    return (r & 1) ? __byte_perm(x, y, 0x7632) : __byte_perm(x, y, 0x5410);
+// Byte permute with the selector's sign-replicate bit (PTX prmt, default
+// mode): a selector nibble 8 | b writes the sign of source byte b.
+__device__ __forceinline__ uint32_t prmt(uint32_t x, uint32_t y, uint32_t sel) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(x), "r"(y), "r"(sel));
+    return d;
+}
+
+// Packed substitution scores (half a low, half b high) of row r of a step:
+// one byte permute per row, from int16 pairs or, with sign extension, from
+// int8 quads.
+template <int R, class T>
+__device__ __forceinline__ uint32_t sub_of(const StepLoads<R, T>& L, int r) {
+    if constexpr (sizeof(T) == 2) {
+        const uint32_t x = L.a[r / 2], y = L.b[r / 2];
+        return (r & 1) ? __byte_perm(x, y, 0x7632) : __byte_perm(x, y, 0x5410);
+    } else {
+        const uint32_t x = L.a[r / 4], y = L.b[r / 4];
+        const uint32_t k = (uint32_t)(r & 3);
+        return prmt(x, y, k | ((8u | k) << 4) | ((4u + k) << 8) | ((12u + k) << 12));
+    }
 }
 
 // Mask of the halves whose row r is still inside its band at this step
@@ -217,9 +263,9 @@ __device__ __forceinline__ uint32_t ragged_mask(int r, int thr_a, int thr_b) {
 // (compile-time U); MODE 1: all rows, no masks; MODE 2: all rows, ragged
 // right-edge masks.  `best` is the running maximum of G (H - go) over the
 // lane's in-band cells.
-template <int R, int MODE, int U>
+template <int R, class T, int MODE, int U>
 __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, uint2* __restrict__ buf, int u,
-                                           const StepLoads<R>& L, const PackedConsts& c, uint32_t& best,
+                                           const StepLoads<R, T>& L, const PackedConsts& c, uint32_t& best,
                                            int thr_a, int thr_b) {
     uint32_t Gup = L.top.x, Fup = L.top.y;
     uint32_t diag = diag0;
@@ -230,7 +276,7 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
         if (MODE == 0 && r > U) break;
         uint32_t G, F;
         uint32_t gold = st.Hd[r];
-        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R>(L, r), c, G, F);
+        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, G, F);
         if (MODE == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
             G = (G & mk) | (c.neg2 & ~mk);
@@ -251,17 +297,17 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
 // The pipelined column loop state of one strip: the loads of step u + 1 are
 // in flight while step u computes; the residue codes come four steps to a
 // word, the word of the next group loaded a group ahead.
-template <int R>
+template <int R, class T>
 struct Pipe {
-    StepLoads<R> cur, nxt;
+    StepLoads<R, T> cur, nxt;
     uint32_t wa, wb;    // codes of the group of step u + 1 (byte i: step 4g + i)
     uint32_t wa2, wb2;  // codes of the group after it
 };
 
 // Called before computing step u: cur <- nxt (step u), issue step u + 1.
 // K = (u + 1) & 3 when known at compile time, else -1.
-template <int R, int K>
-__device__ __forceinline__ void pipe_advance(Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
+template <int R, class T, int K>
+__device__ __forceinline__ void pipe_advance(Pipe<R, T>& p, const HalfStrip<T>& ha, const HalfStrip<T>& hb,
                                              const uint2* buf, int u, int wmax) {
     p.cur = p.nxt;
     const int v = u + 1;
@@ -275,23 +321,24 @@ __device__ __forceinline__ void pipe_advance(Pipe<R>& p, const HalfStrip& ha, co
     const uint32_t sel = 0x4440u | (uint32_t)k;
     const int ca = (int)__byte_perm(p.wa, 0u, sel), cb = (int)__byte_perm(p.wb, 0u, sel);
     const int k1 = u + 2 <= wmax ? u + 2 : wmax;
-    fetch_step<R>(p.nxt, ha, hb, ca, cb, buf, k1);
+    fetch_step<R, T>(p.nxt, ha, hb, ca, cb, buf, k1);
 }
 
-template <int R, int U>
+template <int R, class T, int U>
 struct LeftTriangle {
     __device__ __forceinline__ static void run(StripState<R>& st, uint32_t& diag0, uint2* buf, int wmax,
-                                               Pipe<R>& p, const HalfStrip& ha, const HalfStrip& hb,
+                                               Pipe<R, T>& p, const HalfStrip<T>& ha, const HalfStrip<T>& hb,
                                                const PackedConsts& c, uint32_t& best) {
-        LeftTriangle<R, U - 1>::run(st, diag0, buf, wmax, p, ha, hb, c, best);
-        pipe_advance<R, (U + 1) & 3>(p, ha, hb, buf, U, wmax);
-        strip_step<R, 0, U>(st, diag0, buf, U, p.cur, c, best, 0, 0);
+        LeftTriangle<R, T, U - 1>::run(st, diag0, buf, wmax, p, ha, hb, c, best);
+        pipe_advance<R, T, (U + 1) & 3>(p, ha, hb, buf, U, wmax);
+        strip_step<R, T, 0, U>(st, diag0, buf, U, p.cur, c, best, 0, 0);
     }
 };
-template <int R>
-struct LeftTriangle<R, -1> {
-    __device__ __forceinline__ static void run(StripState<R>&, uint32_t&, uint2*, int, Pipe<R>&, const HalfStrip&,
-                                               const HalfStrip&, const PackedConsts&, uint32_t&) {}
+template <int R, class T>
+struct LeftTriangle<R, T, -1> {
+    __device__ __forceinline__ static void run(StripState<R>&, uint32_t&, uint2*, int, Pipe<R, T>&,
+                                               const HalfStrip<T>&, const HalfStrip<T>&, const PackedConsts&,
+                                               uint32_t&) {}
 };
 
 // ---- paired strips (one job per lane) --------------------------------------
@@ -303,16 +350,16 @@ struct LeftTriangle<R, -1> {
 // boundary buffer then carries one job per lane: 32-bit words G | F << 16
 // of the super-strip's last row.  A warp task is 32 such jobs; the job's
 // critical path is about half of its R-row sweep.
-template <int R>
+template <int R, class T>
 struct PairPipe {
-    StepLoads<R> cur, nxt;  // top.x: boundary word of the low half's row above
+    StepLoads<R, T> cur, nxt;  // top.x: boundary word of the low half's row above
     uint32_t w, w2;         // code words of the low half: group of step g + 1, next group
     int cprev;              // low half's code at step g (the high half's at step g + 1)
 };
 
 // Called before computing step g: cur <- nxt (step g), issue step g + 1.
-template <int R, int K>
-__device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha, const int16_t* hb_rows,
+template <int R, class T, int K>
+__device__ __forceinline__ void pair_advance(PairPipe<R, T>& p, const HalfStrip<T>& ha, const T* hb_rows,
                                              const uint32_t* pbuf, int g, int wmax) {
     p.cur = p.nxt;
     const int v = g + 1;
@@ -325,8 +372,8 @@ __device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha
     const int cb = p.cprev;
     p.cprev = ca;
     const int kin = g + 2 <= wmax ? g + 2 : wmax;
-    ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca * ha.mpad);
-    ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb * ha.mpad);
+    ld_prof(p.nxt.a, ha.rows + (size_t)ca * ha.mpad);
+    ld_prof(p.nxt.b, hb_rows + (size_t)cb * ha.mpad);
     p.nxt.top.x = __ldca(pbuf + (size_t)kin * 32);
 }
 
@@ -334,9 +381,9 @@ __device__ __forceinline__ void pair_advance(PairPipe<R>& p, const HalfStrip& ha
 // r > G not yet in band, high rows r > G - R - 1 not yet in band); PH 1: every
 // row of both halves in band; PH 2: right-edge masks from the thresholds.
 // Values are G = H - go and F, as in strip_step.
-template <int R, int PH, int G>
+template <int R, class T, int PH, int G>
 __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, uint32_t& lastG, uint32_t& lastF,
-                                          uint32_t* __restrict__ pbuf, int g, const StepLoads<R>& L,
+                                          uint32_t* __restrict__ pbuf, int g, const StepLoads<R, T>& L,
                                           const PackedConsts& c, uint32_t& best, int thr_a, int thr_b) {
     const uint32_t top = L.top.x;
     uint32_t Gup = __byte_perm(top, lastG, 0x5410);
@@ -349,7 +396,7 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
         if (PH == 0 && r > G) break;
         uint32_t Gv, F;
         uint32_t gold = st.Hd[r];
-        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R>(L, r), c, Gv, F);
+        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, Gv, F);
         if (PH == 0 && r > G - R - 1) {
             Gv = (Gv & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
             F = (F & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
@@ -372,24 +419,26 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
     if (g >= 2 * R) stbuf(pbuf + (size_t)(g - 2 * R) * 32, __byte_perm(Gup, Fup, 0x7632));
 }
 
-template <int R, int G>
+template <int R, class T, int G>
 struct PairTriangle {
-    __device__ __forceinline__ static void run(PairPipe<R>& p, StripState<R>& st, uint32_t& diag0, uint32_t& lastH,
-                                               uint32_t& lastY, uint32_t* pbuf, int wmax, const HalfStrip& ha,
-                                               const int16_t* hb_rows, const PackedConsts& c, uint32_t& best) {
-        PairTriangle<R, G - 1>::run(p, st, diag0, lastH, lastY, pbuf, wmax, ha, hb_rows, c, best);
-        pair_advance<R, (G + 1) & 3>(p, ha, hb_rows, pbuf, G, wmax);
-        pair_step<R, 0, G>(st, diag0, lastH, lastY, pbuf, G, p.cur, c, best, 0, 0);
+    __device__ __forceinline__ static void run(PairPipe<R, T>& p, StripState<R>& st, uint32_t& diag0,
+                                               uint32_t& lastG, uint32_t& lastF, uint32_t* pbuf, int wmax,
+                                               const HalfStrip<T>& ha, const T* hb_rows, const PackedConsts& c,
+                                               uint32_t& best) {
+        PairTriangle<R, T, G - 1>::run(p, st, diag0, lastG, lastF, pbuf, wmax, ha, hb_rows, c, best);
+        pair_advance<R, T, (G + 1) & 3>(p, ha, hb_rows, pbuf, G, wmax);
+        pair_step<R, T, 0, G>(st, diag0, lastG, lastF, pbuf, G, p.cur, c, best, 0, 0);
     }
 };
-template <int R>
-struct PairTriangle<R, -1> {
-    __device__ __forceinline__ static void run(PairPipe<R>&, StripState<R>&, uint32_t&, uint32_t&, uint32_t&,
-                                               uint32_t*, int, const HalfStrip&, const int16_t*,
-                                               const PackedConsts&, uint32_t&) {}
+template <int R, class T>
+struct PairTriangle<R, T, -1> {
+    __device__ __forceinline__ static void run(PairPipe<R, T>&, StripState<R>&, uint32_t&, uint32_t&, uint32_t&,
+                                               uint32_t*, int, const HalfStrip<T>&, const T*, const PackedConsts&,
+                                               uint32_t&) {}
 };
 
-__device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, const int16_t* prof,
+template <class T>
+__device__ __forceinline__ void load_half(HalfJob<T>& h, const saber_band_job& j, const T* prof,
                                           const uint64_t* prof_off, const uint32_t* prof_mpad,
                                           const uint64_t* qoffs, const uint8_t* res, int R) {
     const uint32_t q = j.query;
@@ -411,8 +460,8 @@ __device__ __forceinline__ void load_half(HalfJob& h, const saber_band_job& j, c
 
 // One paired task: sorted positions [32t, 32t + 32) of the paired range,
 // lane l takes position 32t + l.
-template <int R>
-__device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
+template <int R, class T>
+__device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T* __restrict__ prof,
                                        const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
                                        const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
                                        const uint32_t* __restrict__ porder, uint32_t n_pair, uint32_t task, int lane,
@@ -422,7 +471,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
     const uint32_t pos = task * 32 + lane;
     const bool has = pos < n_pair;
     const uint32_t jidx = has ? porder[pos] : 0u;
-    HalfJob J{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0};
+    HalfJob<T> J{sent_profile<T>(), nullptr, 0, 0, 0, 0, 0, 0};
     if (has) load_half(J, jobs[jidx], prof, prof_off, prof_mpad, qoffs, res, 2 * R);
     const int big = 1 << 30;
     const int wmin = __reduce_min_sync(0xffffffffu, has ? J.w : big);
@@ -436,8 +485,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
     uint32_t best = c.ngo2;  // G of H = 0
     const int gfull = wmax + 2 * R;
     for (int t = 0; t < nsmax; t++) {
-        const HalfStrip ha = half_strip(J, t, 2 * R);
-        const int16_t* hb_rows = ha.rows + R;
+        const HalfStrip<T> ha = half_strip(J, t, 2 * R);
+        const T* hb_rows = ha.rows + R;
         // Step g reads window column col0 + g in the low half and col0 + g - 1
         // in the high half.  As in the two-job lanes, the warp sweeps only the
         // steps that reach a window column of one of its jobs, a late start
@@ -461,7 +510,7 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
         }
         StripState<R> st;
         uint32_t diag0, lastG, lastF;
-        PairPipe<R> p;
+        PairPipe<R, T> p;
         int g;
         if (g0 == 0) {
 #pragma unroll
@@ -475,11 +524,11 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             p.w = code_word(ha, 0);
             p.w2 = code_word(ha, 4);
             const int ca0 = (int)(p.w & 0xFFu);
-            ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
-            ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)kSentCode * ha.mpad);
+            ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
+            ld_prof(p.nxt.b, hb_rows + (size_t)kSentCode * ha.mpad);
             p.nxt.top.x = __ldca(pbuf + 32);
             p.cprev = ca0;
-            PairTriangle<R, 2 * R>::run(p, st, diag0, lastG, lastF, pbuf, wmax, ha, hb_rows, c, best);
+            PairTriangle<R, T, 2 * R>::run(p, st, diag0, lastG, lastF, pbuf, wmax, ha, hb_rows, c, best);
             g = 2 * R + 1;
         } else {
 #pragma unroll
@@ -497,8 +546,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
             p.w2 = code_word(ha, g0 + 3);
             const int ca0 = (int)((p.w >> 8) & 0xFFu);  // step g0 (= 1 mod 4)
             const int cb0 = (int)(p.w & 0xFFu);         // the high half's: the low half's at g0 - 1
-            ld256(p.nxt.a[0], p.nxt.a[1], ha.rows + (size_t)ca0 * ha.mpad);
-            ld256(p.nxt.b[0], p.nxt.b[1], hb_rows + (size_t)cb0 * ha.mpad);
+            ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
+            ld_prof(p.nxt.b, hb_rows + (size_t)cb0 * ha.mpad);
             p.nxt.top.x = __ldca(pbuf + (size_t)(g0 + 1 <= wmax ? g0 + 1 : wmax) * 32);
             p.cprev = ca0;
             g = g0;
@@ -506,18 +555,18 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
         const int gmid = wmin < gend ? wmin : gend;
         // (g + 1) & 3 runs 2, 3, 0, 1 from g = 1 (mod 4) (R a multiple of 4)
         for (; g + 4 <= gmid; g += 4) {
-            pair_advance<R, 2>(p, ha, hb_rows, pbuf, g, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, 0, 0);
-            pair_advance<R, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 1, p.cur, c, best, 0, 0);
-            pair_advance<R, 0>(p, ha, hb_rows, pbuf, g + 2, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 2, p.cur, c, best, 0, 0);
-            pair_advance<R, 1>(p, ha, hb_rows, pbuf, g + 3, wmax);
-            pair_step<R, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 3, p.cur, c, best, 0, 0);
+            pair_advance<R, T, 2>(p, ha, hb_rows, pbuf, g, wmax);
+            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, 0, 0);
+            pair_advance<R, T, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
+            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 1, p.cur, c, best, 0, 0);
+            pair_advance<R, T, 0>(p, ha, hb_rows, pbuf, g + 2, wmax);
+            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 2, p.cur, c, best, 0, 0);
+            pair_advance<R, T, 1>(p, ha, hb_rows, pbuf, g + 3, wmax);
+            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 3, p.cur, c, best, 0, 0);
         }
         for (; g < gend; g++) {
-            pair_advance<R, -1>(p, ha, hb_rows, pbuf, g, wmax);
-            pair_step<R, 2, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, g - J.w + 1, g - R - J.w);
+            pair_advance<R, T, -1>(p, ha, hb_rows, pbuf, g, wmax);
+            pair_step<R, T, 2, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, g - J.w + 1, g - R - J.w);
         }
     }
     const int sc = max(lo16(best), hi16(best)) + lo16(c.go2);
@@ -530,9 +579,9 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const in
 // Persistent warps over warp tasks: task t = sorted positions [64t, 64t + 64)
 // of the fast class, taken largest first; lane l takes positions 64t + 2l
 // (low half) and 64t + 2l + 1 (high half).
-template <int R>
+template <int R, class T>
 __global__ void __launch_bounds__(256, 2) k_band_fast(
-    const uint8_t* __restrict__ res, const int16_t* __restrict__ prof,
+    const uint8_t* __restrict__ res, const T* __restrict__ prof,
     const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
     const uint64_t* __restrict__ qoffs, const saber_band_job* __restrict__ jobs,
     const uint32_t* __restrict__ order, const uint32_t* __restrict__ n_ptr, const uint32_t* __restrict__ np_ptr,
@@ -567,7 +616,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         if constexpr (R == 16) paired = wt < n_ptasks;
         if (paired) {
             if constexpr (R == 16)
-                pair_task<R>(res, prof, prof_off, prof_mpad, qoffs, jobs, order + n_fast, n_pair, n_ptasks - 1 - wt,
+                pair_task<R, T>(res, prof, prof_off, prof_mpad, qoffs, jobs, order + n_fast, n_pair, n_ptasks - 1 - wt,
                              lane, reinterpret_cast<uint32_t*>(bufs + (size_t)gwarp * buf_stride * 32) + lane, c,
                              scores, rescue, rescue_count);
             continue;
@@ -577,7 +626,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         const bool has_a = pa < n_fast, has_b = pb < n_fast;
         const uint32_t ja_idx = has_a ? order[pa] : 0u;
         const uint32_t jb_idx = has_b ? order[pb] : 0u;
-        HalfJob A{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0}, B{g_sent_profile, nullptr, 0, 0, 0, 0, 0, 0};
+        HalfJob<T> A{sent_profile<T>(), nullptr, 0, 0, 0, 0, 0, 0}, B{sent_profile<T>(), nullptr, 0, 0, 0, 0, 0, 0};
         if (has_a) load_half(A, jobs[ja_idx], prof, prof_off, prof_mpad, qoffs, res, R);
         if (has_b) load_half(B, jobs[jb_idx], prof, prof_off, prof_mpad, qoffs, res, R);
         const int big = 1 << 30;
@@ -596,7 +645,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
         uint32_t best = c.ngo2;  // G of H = 0
         const int ufull = wmax + R - 1;
         for (int t = 0; t < nsmax; t++) {
-            const HalfStrip ha = half_strip(A, t, R), hb = half_strip(B, t, R);
+            const HalfStrip<T> ha = half_strip(A, t, R), hb = half_strip(B, t, R);
             // Step u reads window column col0 + u in every row of a half.  The
             // warp sweeps only the steps that reach a window column of one of
             // its halves: steps left of column -1 hold sentinel cells only (H =
@@ -628,7 +677,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
             }
             StripState<R> st;
             uint32_t diag0;
-            Pipe<R> p;
+            Pipe<R, T> p;
             int u;
             if (u0 == 0) {
 #pragma unroll
@@ -641,8 +690,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 p.wb = code_word(hb, 0);
                 p.wa2 = code_word(ha, 4);
                 p.wb2 = code_word(hb, 4);
-                fetch_step<R>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf, 1);
-                LeftTriangle<R, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
+                fetch_step<R, T>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf, 1);
+                LeftTriangle<R, T, R - 1>::run(st, diag0, mybuf, wmax, p, ha, hb, c, best);
                 u = R;
             } else {
                 // the skipped columns are sentinel columns: H = 0 (G = -go) to
@@ -661,7 +710,7 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 p.wb = code_word(hb, u0);
                 p.wa2 = code_word(ha, u0 + 4);
                 p.wb2 = code_word(hb, u0 + 4);
-                fetch_step<R>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf,
+                fetch_step<R, T>(p.nxt, ha, hb, (int)(p.wa & 0xFFu), (int)(p.wb & 0xFFu), mybuf,
                               u0 + 1 <= wmax ? u0 + 1 : wmax);
                 u = u0;
             }
@@ -669,19 +718,19 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
             // so that the code bytes are selected at compile time
             const int umid = wmin < uend ? wmin : uend;
             for (; u + 4 <= umid; u += 4) {
-                pipe_advance<R, 1>(p, ha, hb, mybuf, u, wmax);
-                strip_step<R, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
-                pipe_advance<R, 2>(p, ha, hb, mybuf, u + 1, wmax);
-                strip_step<R, 1, 0>(st, diag0, mybuf, u + 1, p.cur, c, best, 0, 0);
-                pipe_advance<R, 3>(p, ha, hb, mybuf, u + 2, wmax);
-                strip_step<R, 1, 0>(st, diag0, mybuf, u + 2, p.cur, c, best, 0, 0);
-                pipe_advance<R, 0>(p, ha, hb, mybuf, u + 3, wmax);
-                strip_step<R, 1, 0>(st, diag0, mybuf, u + 3, p.cur, c, best, 0, 0);
+                pipe_advance<R, T, 1>(p, ha, hb, mybuf, u, wmax);
+                strip_step<R, T, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
+                pipe_advance<R, T, 2>(p, ha, hb, mybuf, u + 1, wmax);
+                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 1, p.cur, c, best, 0, 0);
+                pipe_advance<R, T, 3>(p, ha, hb, mybuf, u + 2, wmax);
+                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 2, p.cur, c, best, 0, 0);
+                pipe_advance<R, T, 0>(p, ha, hb, mybuf, u + 3, wmax);
+                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 3, p.cur, c, best, 0, 0);
             }
             // the rest, with the right-edge masks (all ones while u < wmin)
             for (; u < uend; u++) {
-                pipe_advance<R, -1>(p, ha, hb, mybuf, u, wmax);
-                strip_step<R, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);
+                pipe_advance<R, T, -1>(p, ha, hb, mybuf, u, wmax);
+                strip_step<R, T, 2, 0>(st, diag0, mybuf, u, p.cur, c, best, u - A.w + 1, u - B.w + 1);
             }
         }
         const int sa = lo16(best) + go, sb = hi16(best) + go;
@@ -918,26 +967,35 @@ __global__ void __launch_bounds__(128) k_band_generic(
 }
 
 // ---- host-side launch wrappers (the runtime TU calls these) ----
-template <int R>
+template <int R, class T>
 static int fast_blocks_per_sm() {
     int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_band_fast<R>, 256, 0) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_band_fast<R, T>, 256, 0) != cudaSuccess) return 1;
     return bps < 1 ? 1 : bps;
 }
 
-int band_fast_blocks_per_sm(int strip_rows) {
-    return strip_rows == 8 ? fast_blocks_per_sm<8>() : fast_blocks_per_sm<16>();
+int band_fast_blocks_per_sm(int strip_rows, bool prof8) {
+    if (prof8) return strip_rows == 8 ? fast_blocks_per_sm<8, int8_t>() : fast_blocks_per_sm<16, int8_t>();
+    return strip_rows == 8 ? fast_blocks_per_sm<8, int16_t>() : fast_blocks_per_sm<16, int16_t>();
 }
 
+template <int R, class T>
+static void launch_fast(unsigned grid, cudaStream_t s, const FastArgs& a, const T* prof) {
+    k_band_fast<R, T><<<grid, 256, 0, s>>>(a.res, prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order, a.n_ptr,
+                                           a.np_ptr, a.order_skip, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge,
+                                           a.scores, a.rescue, a.rescue_count);
+}
+
+// The int8 profile when the query set has one (every entry fits), else the
+// int16 profile.
 cudaError_t launch_band_fast(unsigned grid, cudaStream_t s, const FastArgs& a) {
-    if (a.strip_rows == 8)
-        k_band_fast<8><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                            a.n_ptr, a.np_ptr, a.order_skip, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
-                                            a.rescue, a.rescue_count);
-    else
-        k_band_fast<16><<<grid, 256, 0, s>>>(a.res, a.prof, a.prof_off, a.prof_mpad, a.qoffs, a.jobs, a.order,
-                                             a.n_ptr, a.np_ptr, a.order_skip, a.wt_counter, a.bufs, a.buf_stride, a.go, a.ge, a.scores,
-                                             a.rescue, a.rescue_count);
+    if (a.prof8) {
+        if (a.strip_rows == 8) launch_fast<8>(grid, s, a, a.prof8);
+        else launch_fast<16>(grid, s, a, a.prof8);
+    } else {
+        if (a.strip_rows == 8) launch_fast<8>(grid, s, a, a.prof);
+        else launch_fast<16>(grid, s, a, a.prof);
+    }
     return cudaGetLastError();
 }
 

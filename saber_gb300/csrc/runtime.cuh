@@ -81,8 +81,12 @@ struct QuerySet {
     std::vector<uint64_t> poff;  // host copy of the profile offsets
     std::vector<uint32_t> pmpad; // host copy of the profile row strides
     DevBuf codes, offsets, bias, prof, prof_off, prof_mpad;
+    DevBuf prof8;              // int8 copy of prof, valid when p8
+    uint64_t prof_elems = 0;   // entries of prof
+    int bias_min = 0, bias_max = 0;
     bool has = false;
     bool has_bias = false;
+    bool p8 = false;           // every profile entry fits in [-127, 127]
 };
 
 // Residues + subject offsets + a query set with profiles for one scheme.
@@ -101,6 +105,7 @@ struct GraphKey {
     int32_t rows, go, ge;
     uint32_t pair_steps, nq, long_steps;
     const void* ptrs[16];
+    const void* prof8;
     bool operator==(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 struct GraphEntry {

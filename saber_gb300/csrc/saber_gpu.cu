@@ -47,14 +47,16 @@ __global__ void k_canon(uint8_t* __restrict__ r, uint64_t n) {
 // Query profile P[c][i] = S(q_i, c) + bias_i + go for c < 24 and i < m, the
 // sentinel score + go elsewhere (row 24 and rows past the query end).  The
 // gap-open cost is folded in for the packed kernel, which adds the profile
-// to H - go; the int32 kernels and the traceback subtract it again.  The
-// reference builds the same per-query table (without go) for its ungapped
-// extension (engine.rs:387-388) and a per-subject one in its int16 kernel
-// (banded_simd.rs:425-469).
+// to H - go; the int32 kernels and the traceback subtract it again.  When
+// every real entry lies in [-127, 127], an int8 copy with sentinel -128 is
+// written too (prof8, else null): the packed kernel then reads half the
+// bytes.  The reference builds the same per-query table (without go) for its
+// ungapped extension (engine.rs:387-388) and a per-subject one in its int16
+// kernel (banded_simd.rs:425-469).
 __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __restrict__ qoffs,
                           const int8_t* __restrict__ bias, const int32_t* __restrict__ matrix,
                           const uint64_t* __restrict__ prof_off, const uint32_t* __restrict__ prof_mpad,
-                          int go, int16_t* __restrict__ prof) {
+                          int go, int16_t* __restrict__ prof, int8_t* __restrict__ prof8) {
     const uint32_t q = blockIdx.x;
     const uint64_t q0 = qoffs[q];
     const int m = (int)(qoffs[q + 1] - q0);
@@ -63,12 +65,14 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
     for (int t = threadIdx.x; t < kProfRows * mpad; t += blockDim.x) {
         int c = t / mpad, i = t - c * mpad;
         int v = kSent16;
-        if (c < 24 && i < m) {
+        const bool real = c < 24 && i < m;
+        if (real) {
             int qc = codes[q0 + i];
             if (qc >= 24) qc = 22;
             v = matrix[qc * 24 + c] + (bias ? (int)bias[q0 + i] : 0);
         }
         P[t] = (int16_t)(v + go);
+        if (prof8) prof8[prof_off[q] + t] = real ? (int8_t)(v + go) : (int8_t)-128;
     }
 }
 
@@ -256,7 +260,7 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
 // warp-pipelined int32 kernel; larger batches keep every job on the lanes.
 static uint32_t long_steps_for(const saber_gpu* h, uint64_t njobs) {
     if (h->long_steps != kLongStepsAuto) return h->long_steps;
-    const uint64_t slots = (uint64_t)h->sm_count * band_fast_blocks_per_sm(h->strip_rows) * 256 / 32 * 64;
+    const uint64_t slots = (uint64_t)h->sm_count * band_fast_blocks_per_sm(h->strip_rows, false) * 256 / 32 * 64;
     return njobs < slots ? kLongStepsSmall : kLongStepsNever;
 }
 
@@ -349,7 +353,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         const uint32_t nj = pass == 0 ? n_fast : n_fast8;
         if (nj == 0) continue;
         const int rows = pass == 0 ? h->strip_rows : kStripRowsMin;
-        const int bps = band_fast_blocks_per_sm(rows);
+        const int bps = band_fast_blocks_per_sm(rows, qs.p8);
         const unsigned grid = (unsigned)(h->sm_count * bps);
         const uint64_t warps = (uint64_t)grid * 256 / 32;
         const uint32_t stride = (uint32_t)(wmax_fast + 1);
@@ -357,6 +361,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
         FastArgs a;
         a.res = ds.res.as<uint8_t>();
         a.prof = qs.prof.as<int16_t>();
+        a.prof8 = qs.p8 ? qs.prof8.as<int8_t>() : nullptr;
         a.prof_off = qs.prof_off.as<uint64_t>();
         a.prof_mpad = qs.prof_mpad.as<uint32_t>();
         a.qoffs = qs.offsets.as<uint64_t>();
@@ -414,6 +419,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     local.t_prep_ms = t01;
     local.t_fast_ms = t12;
     local.t_generic_ms = t23;
+    local.prof8 = qs.p8 ? 1 : 0;
     if (st) *st = local;
     return SABER_OK;
 }
@@ -458,8 +464,8 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     CUALLOC(h, h->list, npad * 4);
     CUALLOC(h, h->g_nreal, 16);
     const int rows0 = h->strip_rows;
-    const unsigned grid0 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(rows0));
-    const unsigned grid8 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(kStripRowsMin));
+    const unsigned grid0 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(rows0, qs.p8));
+    const unsigned grid8 = (unsigned)(h->sm_count * band_fast_blocks_per_sm(kStripRowsMin, qs.p8));
     const uint64_t warps = (uint64_t)std::max(grid0, grid8) * 256 / 32;
     CUALLOC(h, h->bufs, warps * wcap * 32 * sizeof(uint2));
     const unsigned gT = 128, gGrid = (unsigned)(h->sm_count * 4);
@@ -479,6 +485,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     key.long_steps = long_steps_for(h, njobs);
     key.n_res = ds.n_res;  // scalar kernel parameters baked into the graph
     key.nq = qs.nq;
+    key.prof8 = qs.p8 ? qs.prof8.p : nullptr;  // which packed kernel the graph launches
     const void* ptrs[16] = {h->jobs_dev.p, h->scores_dev.p, h->keys_in.p, h->keys_out.p, h->vals_in.p,
                             h->vals_out.p, h->counts.p, h->stats.p, h->list.p, h->bufs.p, h->slabs.p,
                             h->cub_tmp.p, ds.res.p, qs.prof.p, qs.offsets.p, qs.prof_off.p};
@@ -515,6 +522,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
             FastArgs a;
             a.res = ds.res.as<uint8_t>();
             a.prof = qs.prof.as<int16_t>();
+            a.prof8 = qs.p8 ? qs.prof8.as<int8_t>() : nullptr;
             a.prof_off = qs.prof_off.as<uint64_t>();
             a.prof_mpad = qs.prof_mpad.as<uint32_t>();
             a.qoffs = qs.offsets.as<uint64_t>();
@@ -599,19 +607,31 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
         local.kernel_launches = 5;
         local.library_launches = 9;
         local.t_fast_ms = ms;
+        local.prof8 = qs.p8 ? 1 : 0;
         *st = local;
     }
     return SABER_OK;
 }
 
 static int build_profiles(saber_gpu* h, const Scheme& sch, QuerySet& q) {
+    q.p8 = false;
     if (!q.has || !sch.has || q.nq == 0) return SABER_OK;
+    // int8 copy when every real entry S + bias + go lies in [-127, 127]
+    // (bounded over the whole matrix and the set's bias range)
+    int smin = sch.matrix[0], smax = sch.matrix[0];
+    for (int i = 1; i < 576; i++) {
+        smin = std::min(smin, (int)sch.matrix[i]);
+        smax = std::max(smax, (int)sch.matrix[i]);
+    }
+    const bool fits8 = smin + q.bias_min + sch.go >= -127 && smax + q.bias_max + sch.go <= 127;
+    if (fits8) CUALLOC(h, q.prof8, q.prof_elems + 64);
     k_profile<<<q.nq, 256, 0, h->stream>>>(q.codes.as<uint8_t>(), q.offsets.as<uint64_t>(),
                                            q.has_bias ? q.bias.as<int8_t>() : nullptr, sch.d_matrix.as<int32_t>(),
                                            q.prof_off.as<uint64_t>(), q.prof_mpad.as<uint32_t>(), sch.go,
-                                           q.prof.as<int16_t>());
+                                           q.prof.as<int16_t>(), fits8 ? q.prof8.as<int8_t>() : nullptr);
     CU(h, cudaGetLastError());
     CU(h, cudaStreamSynchronize(h->stream));
+    q.p8 = fits8;
     return SABER_OK;
 }
 
@@ -651,10 +671,20 @@ static int load_queries(saber_gpu* h, const Scheme& sch, QuerySet& q, const uint
     CU(h, cudaMemcpyAsync(q.prof_off.p, poff.data(), poff.size() * 8, cudaMemcpyHostToDevice, s));
     CU(h, cudaMemcpyAsync(q.prof_mpad.p, pm.data(), pm.size() * 4, cudaMemcpyHostToDevice, s));
     q.has_bias = bias != nullptr && total > 0;
+    q.bias_min = 0;
+    q.bias_max = 0;
     if (q.has_bias) {
         CUALLOC(h, q.bias, total + 16);
         CU(h, cudaMemcpyAsync(q.bias.p, bias, total, cudaMemcpyHostToDevice, s));
+        int bmin = bias[0], bmax = bias[0];
+        for (uint64_t i = 1; i < total; i++) {
+            bmin = std::min(bmin, (int)bias[i]);
+            bmax = std::max(bmax, (int)bias[i]);
+        }
+        q.bias_min = bmin;
+        q.bias_max = bmax;
     }
+    q.prof_elems = acc;
     CU(h, cudaStreamSynchronize(s));
     q.poff.assign(poff.begin(), poff.begin() + nq);
     q.pmpad.assign(pm.begin(), pm.begin() + nq);

@@ -178,7 +178,7 @@ class ScoreStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "jobs", "banded_cells", "fast_cells", "fast_jobs", "generic_jobs", "i16_rescored", "empty_jobs",
         "kernel_launches", "library_launches")] + [
-        (n, ctypes.c_double) for n in ("t_prep_ms", "t_fast_ms", "t_generic_ms")]
+        (n, ctypes.c_double) for n in ("t_prep_ms", "t_fast_ms", "t_generic_ms")] + [("prof8", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: (float(getattr(self, n)) if n.startswith("t_") else int(getattr(self, n)))

@@ -85,3 +85,36 @@ def test_headers_compile_as_plain_c(tmp_path):
     r = subprocess.run([cc, "-std=c99", "-I", os.path.join(REPO, "include"), "-c", str(src), "-o",
                         str(tmp_path / "use.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """Every ctypes mirror of a header struct has the C struct's size and
+    field offsets (compiled against include/saber_gpu.h)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"saber_score_stats": gpu.ScoreStats, "saber_scan_params": gpu.ScanParams,
+             "saber_scan_stats": gpu.ScanStats, "saber_alignment": gpu.Alignment,
+             "saber_traceback_stats": gpu.TracebackStats, "saber_search_params": gpu.SearchParamsC,
+             "saber_search_stats": gpu.SearchStats, "saber_triage_train_cfg": gpu.TriageTrainCfg,
+             "saber_triage_train_stats": gpu.TriageTrainStats}
+    cfield = {"lambda_": "lambda"}  # Python keyword
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "saber_gpu.h"', 'int main(void) {']
+    for cname, py in pairs.items():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, cfield.get(f, f)))
+    lines.append("  return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    for cname, py in pairs.items():
+        assert int(out[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(out[cname + "." + f]) == getattr(py, f).offset, (cname, f)

@@ -81,6 +81,42 @@ def test_random_band_jobs_match_oracle(tuned, gaps, mode):
     assert st["fast_jobs"] > 0 and st["generic_jobs"] > 0
 
 
+# (gap open, extend, bias levels, int8 profile expected): BLOSUM62 scores lie
+# in [-4, 11], so S + bias + go spans [-4 + bmin + go, 11 + bmax + go]
+PROFILE_KINDS = [
+    (11, 1, (-110, 0, 105), 1),  # up to exactly 127
+    (1, 1, (-124, 0, 115), 1),   # down to exactly -127 and up to 127
+    (1, 1, (-125, 0, 0), 0),     # -128 is the int8 sentinel: int16 profile
+    (11, 1, (-1, 0, 106), 0),    # 128: int16 profile
+]
+
+
+@pytest.mark.parametrize("mode", KERNEL_MODES)
+@pytest.mark.parametrize("go,ge,levels,prof8", PROFILE_KINDS)
+def test_int8_and_int16_profiles(tuned, mode, go, ge, levels, prof8):
+    """The packed kernel reads an int8 copy of the query profiles when every
+    S + bias + go of the query set lies in [-127, 127], else the int16
+    profiles; both give the oracle's scores, at the range's ends too."""
+    dev = tuned
+    qs, ss, planted = synth.protein_db(81, 30, 2000)
+    bias = synth.query_bias(82, qs, levels=levels)
+    jobs = synth.band_jobs(83, qs, ss, planted, 4000, half_min=1, half_max=140)
+    dev.strip_rows, dev.pair_steps = mode
+    dev.set_scheme(B62, go, ge)
+    dev.load_db(ss.codes, ss.offsets)
+    dev.load_queries(qs.codes, qs.offsets, bias)
+    want, cells = _oracle_jobs(qs, ss, bias, jobs, B62, go, ge)
+    try:
+        for graphs in (True, False):  # captured scoring graph and step launches
+            dev.graphs = graphs
+            got, st = dev.score_band_jobs(jobs)
+            assert np.array_equal(got, want), _report(got, want, jobs)
+            assert st["banded_cells"] == cells and st["fast_jobs"] > 0
+            assert st["prof8"] == prof8
+    finally:
+        dev.graphs = True
+
+
 @pytest.mark.parametrize("mode", KERNEL_MODES)
 def test_step_windows_mixed_geometry(tuned, mode):
     """Wide bands on long queries, windows anywhere in the subject: many
