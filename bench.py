@@ -27,7 +27,7 @@ sys.path.insert(0, REPO)
 
 METRIC = "banded SW GCUPS (bit-exact)"
 ALGO_OPS_PER_CELL = 11  # E: 2 sub + max, F: 2 sub + max, H: add + 3 max, best: max
-K_BAND_FAST_DRAM_BYTES = 2.63e9 + 2.90e9  # dram__bytes_read.sum + dram__bytes_write.sum, one launch
+K_BAND_FAST_DRAM_BYTES = 1.73e9 + 2.34e9  # dram__bytes_read.sum + dram__bytes_write.sum, one launch (int8 profile)
 
 
 def parse():
@@ -696,6 +696,7 @@ def run_ours(a, rank, world, local_rank):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     tot_ms, fast_ms, cells, fast_cells, launches, lib_launches, rescored = 0.0, 0.0, 0, 0, 0, 0, 0
+    prof8 = 0
     for _ in range(a.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1)
@@ -711,6 +712,7 @@ def run_ours(a, rank, world, local_rank):
         launches += st["kernel_launches"]
         lib_launches += st["library_launches"]
         rescored += st["i16_rescored"]
+        prof8 = int(st["prof8"])
     torch.cuda.synchronize()
     clk = clocks.stop()
     all_cells, max_ms = whole_job(cells, tot_ms, world)
@@ -757,7 +759,10 @@ def run_ours(a, rank, world, local_rank):
                         # ncu capture of the same command (profiles/k_band_fast16_traffic_1M.md)
                         "traffic": K_BAND_FAST_DRAM_BYTES if a.jobs == 1_000_000 and a.seed == 0 else None,
                         "traffic_unit": "bytes per launch",
-                        "algorithmic_bytes": int(jobs.nbytes + jobs.size * 4 + ss.codes.size + 50 * qs.codes.size),
+                        # jobs, scores, the database, the query profiles (25 codes x 1 or 2 bytes per residue)
+                        "algorithmic_bytes": int(jobs.nbytes + jobs.size * 4 + ss.codes.size
+                                                 + (25 if prof8 else 50) * qs.codes.size),
+                        "profile": "int8" if prof8 else "int16",
                         "basis": "11 algorithmic int ops per in-band cell; peak = measured DPX s16x2 "
                                  "lane-instructions/s x 2 (probe kernel, this run)",
                         "fast_kernel_gcups": round(fast_cells / fast_s / 1e9, 2) if fast_s > 0 else None,
