@@ -677,6 +677,7 @@ def run_ours(a, rank, world, local_rank):
     d_scores = torch.empty(jobs.size, dtype=torch.int32, device="cuda:%d" % local_rank)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda:%d" % local_rank)
     dpx_peak, i32_peak = dev.probe_int_peak()
+    pipe_rates = dev.probe_pipe_rates()
 
     def step_dev():
         return dev.score_band_jobs_dev(d_jobs.data_ptr(), jobs.size, d_scores.data_ptr())
@@ -767,7 +768,11 @@ def run_ours(a, rank, world, local_rank):
                                  "lane-instructions/s x 2 (probe kernel, this run)",
                         "fast_kernel_gcups": round(fast_cells / fast_s / 1e9, 2) if fast_s > 0 else None,
                         "fast_share_of_step": round(fast_ms / tot_ms, 3) if tot_ms else None,
-                        "int32_max_lane_ops_per_s": i32_peak},
+                        "int32_max_lane_ops_per_s": i32_peak,
+                        # the packed cell pair (two cells): 3 DPX + 1 prmt + 0.5 vimax3 on the ALU pipe, 2 vadd2
+                        # on the FMA pipe; each instruction's measured rate (alone, and add-max beside vadd2)
+                        "cell_pair_instructions": {"alu_pipe": 4.5, "fma_pipe": 2.0},
+                        "pipe_rates_lane_instr_per_s": {k: round(v, -8) for k, v in pipe_rates.items()}},
            "clocks": clk, "gpu_launches": int(launches),
            "library_launches": int(lib_launches), "i16_rescored": int(rescored),
            "cells_per_step": int(cells // max(a.steps, 1))}

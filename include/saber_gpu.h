@@ -547,6 +547,14 @@ int saber_gpu_score_band_jobs_noalloc(saber_gpu* h, const saber_band_job* d_jobs
 int saber_gpu_probe_int_peak(saber_gpu* h, double* dpx_s16x2_lane_ops_per_s,
                              double* i32_lane_ops_per_s);
 
+/* Lane-instructions per second of the packed cell's instructions, each timed
+ * alone in independent chains: rates[0] DPX fused add-max (viaddmax s16x2),
+ * rates[1] DPX three-input max with relu, rates[2] packed add (vadd2),
+ * rates[3] byte permute, rates[4] a fused add-max chain and a packed-add
+ * chain side by side (together, when they issue to different pipes, above
+ * either alone).  Measurement utility; no reference counterpart. */
+int saber_gpu_probe_pipe_rates(saber_gpu* h, double rates[5]);
+
 /* In-band cell count of one job after clipping the band to the m x n
  * rectangle, counted as the reference counts banded cells (the row_range span
  * summed over rows, src/algorithm/banded.rs:123-131,208).  Host-only helper;

@@ -1178,6 +1178,7 @@ static int traceback_driver(saber_gpu* h, const saber_traceback_job* jobs, uint6
 using namespace saber;
 
 extern "C" int saber_probe_int_peak_impl(int device, cudaStream_t s, double* dpx, double* i32);
+extern "C" int saber_probe_pipe_rates_impl(int device, cudaStream_t s, double* rates);
 
 // ---------------------------------------------------------------------------
 // exported C ABI
@@ -1368,6 +1369,14 @@ int saber_gpu_probe_int_peak(saber_gpu* h, double* dpx, double* i32) {
     ENTER(h);
     int rc = saber_probe_int_peak_impl(h->device, h->stream, dpx, i32);
     if (rc != SABER_OK) return fail(h, rc, "integer peak probe failed");
+    return SABER_OK;
+}
+
+int saber_gpu_probe_pipe_rates(saber_gpu* h, double rates[5]) {
+    ENTER(h);
+    if (!rates) return fail(h, SABER_ERR_ARG, "null argument");
+    int rc = saber_probe_pipe_rates_impl(h->device, h->stream, rates);
+    if (rc != SABER_OK) return fail(h, rc, "pipe rate probe failed");
     return SABER_OK;
 }
 

@@ -214,6 +214,7 @@ def load_library():
         "saber_gpu_score_windows": (ctypes.c_int, [P, P, U32, P, P, P, U32, P, I32, I32, P]),
         "saber_band_cells": (U64, [U64, U64, I64, I64]),
         "saber_gpu_probe_int_peak": (ctypes.c_int, [P, P, P]),
+        "saber_gpu_probe_pipe_rates": (ctypes.c_int, [P, P]),
         "saber_gpu_set_strip_rows": (ctypes.c_int, [P, I32]),
         "saber_gpu_banded_align": (ctypes.c_int, [P, P, U64, U64, P, P, U64]),
         "saber_gpu_banded_align_one": (ctypes.c_int, [P, P, U32, P, P, U32, I64, I64, U64, I32, P, P, U64]),
@@ -592,6 +593,15 @@ class Device:
         a, b = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.saber_gpu_probe_int_peak(self.h, ctypes.byref(a), ctypes.byref(b)), "probe_int_peak")
         return a.value, b.value
+
+    PIPE_OPS = ("viaddmax_s16x2", "vimax3_s16x2_relu", "vadd2", "prmt", "viaddmax_s16x2 + vadd2")
+
+    def probe_pipe_rates(self):
+        """Lane-instructions/s of the packed cell's instructions, each alone, and a
+        fused add-max chain beside a packed-add chain (dict by PIPE_OPS name)."""
+        r = (ctypes.c_double * 5)()
+        self._check(self.lib.saber_gpu_probe_pipe_rates(self.h, r), "probe_pipe_rates")
+        return dict(zip(self.PIPE_OPS, list(r)))
 
     def score_banded_many(self, query, bias, subjects, bands):
         """One query against banded windows: list of (window codes, (lo, hi))."""

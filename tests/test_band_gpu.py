@@ -63,7 +63,7 @@ def tuned(dev):
 
 
 @pytest.mark.parametrize("mode", KERNEL_MODES)
-@pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8)])
+@pytest.mark.parametrize("gaps", [(11, 1), (10, 2), (6, 3), (15, 1), (8, 8), (0, 0), (1000, 1000), (1000, 0)])
 def test_random_band_jobs_match_oracle(tuned, gaps, mode):
     dev = tuned
     go, ge = gaps
@@ -336,3 +336,17 @@ def test_autotuner_keeps_scores_and_leaves_a_candidate_setting(dev):
         dev.strip_rows = 16
         dev.pair_steps = PAIR_DEFAULT
         dev.long_steps = LONG_AUTO
+
+
+def test_pipe_rate_probe(dev):
+    """The per-instruction probe behind the kernel's cell design: every rate
+    is positive and below the issue ceiling, and a fused add-max chain beside
+    a packed-add chain is not slower than either alone."""
+    r = dev.probe_pipe_rates()
+    assert set(r) == set(dev.PIPE_OPS)
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    ceiling = props.multi_processor_count * 4 * 32 * 2.2e9  # one warp instruction per SMSP and cycle
+    for k, v in r.items():
+        assert 0 < v < ceiling, (k, v)
+    assert r["viaddmax_s16x2 + vadd2"] >= 0.9 * max(r["viaddmax_s16x2"], r["vadd2"])
