@@ -553,16 +553,11 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T*
             g = g0;
         }
         const int gmid = wmin < gend ? wmin : gend;
-        // (g + 1) & 3 runs 2, 3, 0, 1 from g = 1 (mod 4) (R a multiple of 4)
-        for (; g + 4 <= gmid; g += 4) {
-            pair_advance<R, T, 2>(p, ha, hb_rows, pbuf, g, wmax);
+        // middle steps, one per iteration (the code byte's selector is a
+        // register; a short loop body keeps the hot code in the instruction cache)
+        for (; g < gmid; g++) {
+            pair_advance<R, T, -1>(p, ha, hb_rows, pbuf, g, wmax);
             pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g, p.cur, c, best, 0, 0);
-            pair_advance<R, T, 3>(p, ha, hb_rows, pbuf, g + 1, wmax);
-            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 1, p.cur, c, best, 0, 0);
-            pair_advance<R, T, 0>(p, ha, hb_rows, pbuf, g + 2, wmax);
-            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 2, p.cur, c, best, 0, 0);
-            pair_advance<R, T, 1>(p, ha, hb_rows, pbuf, g + 3, wmax);
-            pair_step<R, T, 1, 0>(st, diag0, lastG, lastF, pbuf, g + 3, p.cur, c, best, 0, 0);
         }
         for (; g < gend; g++) {
             pair_advance<R, T, -1>(p, ha, hb_rows, pbuf, g, wmax);
@@ -714,18 +709,13 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                               u0 + 1 <= wmax ? u0 + 1 : wmax);
                 u = u0;
             }
-            // middle steps (every row in band for every half), four at a time
-            // so that the code bytes are selected at compile time
+            // middle steps (every row in band for every half), one step per
+            // iteration: the code byte's selector is a register, and the
+            // short loop body keeps the hot code in the instruction cache
             const int umid = wmin < uend ? wmin : uend;
-            for (; u + 4 <= umid; u += 4) {
-                pipe_advance<R, T, 1>(p, ha, hb, mybuf, u, wmax);
+            for (; u < umid; u++) {
+                pipe_advance<R, T, -1>(p, ha, hb, mybuf, u, wmax);
                 strip_step<R, T, 1, 0>(st, diag0, mybuf, u, p.cur, c, best, 0, 0);
-                pipe_advance<R, T, 2>(p, ha, hb, mybuf, u + 1, wmax);
-                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 1, p.cur, c, best, 0, 0);
-                pipe_advance<R, T, 3>(p, ha, hb, mybuf, u + 2, wmax);
-                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 2, p.cur, c, best, 0, 0);
-                pipe_advance<R, T, 0>(p, ha, hb, mybuf, u + 3, wmax);
-                strip_step<R, T, 1, 0>(st, diag0, mybuf, u + 3, p.cur, c, best, 0, 0);
             }
             // the rest, with the right-edge masks (all ones while u < wmin)
             for (; u < uend; u++) {
