@@ -485,9 +485,11 @@ uint32_t saber_gpu_get_pair_steps(saber_gpu* h);
  * steps (strips x the steps of a strip, window columns only) is scored by
  * the int32 kernel instead, which pipelines a long job's strips over a
  * warp's lanes, so one long job does not set the launch's length.
- * 0xFFFFFFFF keeps every job on the int16 lanes (the faster choice for large
- * batches); 0xFFFFFFFE (the default) picks 2048 for batches smaller than the
- * lanes' job slots and 0xFFFFFFFF otherwise.  Results do not depend on it.
+ * 0xFFFFFFFF keeps every job on the int16 lanes; 0xFFFFFFFE (the default)
+ * picks, per call, the power of two at or above four times the sweep steps
+ * of one int16 lane if the batch's in-band cells were spread evenly over
+ * the lanes (32 cells per step), and at least 2048.  Results do not depend
+ * on it.
  * No reference counterpart. */
 int saber_gpu_set_long_steps(saber_gpu* h, uint32_t steps);
 uint32_t saber_gpu_get_long_steps(saber_gpu* h);

@@ -19,7 +19,7 @@ constexpr int kProfPad = 32;
 // many column steps (strips x (width + R - 1)) is swept as paired strips.
 constexpr uint32_t kPairStepsDefault = 2048;
 constexpr uint32_t kLongStepsNever = 0xFFFFFFFFu;
-constexpr uint32_t kLongStepsAuto = 0xFFFFFFFEu;  // kLongStepsSmall for batches smaller than the lanes' job slots
+constexpr uint32_t kLongStepsAuto = 0xFFFFFFFEu;  // from the batch's cells per lane, at least kLongStepsSmall
 constexpr uint32_t kLongStepsSmall = 2048;
 constexpr uint32_t kLongStepsDefault = kLongStepsAuto;
 // Residue code used for positions outside a window or a query: its profile

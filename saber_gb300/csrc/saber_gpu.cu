@@ -76,20 +76,29 @@ __global__ void k_profile(const uint8_t* __restrict__ codes, const uint64_t* __r
     }
 }
 
-// Widest clipped band of the jobs that reference a loaded query.
+// Widest clipped band (out[0]) and in-band cell total (out[1]) of the jobs
+// that reference a loaded query.
 __global__ void k_job_wmax(const saber_band_job* __restrict__ jobs, uint64_t njobs,
-                           const uint64_t* __restrict__ qoffs, uint32_t nq, unsigned long long* __restrict__ wmax) {
-    unsigned long long wm = 0;
+                           const uint64_t* __restrict__ qoffs, uint32_t nq, unsigned long long* __restrict__ out) {
+    unsigned long long wm = 0, cells = 0;
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < njobs; t += (uint64_t)gridDim.x * blockDim.x) {
         const saber_band_job j = jobs[t];
         if (j.query >= nq) continue;
+        const int64_t m = (int64_t)(qoffs[j.query + 1] - qoffs[j.query]);
         int64_t lo = j.band_lo, hi = j.band_hi;
-        const int64_t w = clip_band((int64_t)(qoffs[j.query + 1] - qoffs[j.query]), j.win_len, lo, hi);
+        const int64_t w = clip_band(m, j.win_len, lo, hi);
         wm = max(wm, (unsigned long long)w);
+        if (w > 0) cells += band_cells(m, j.win_len, lo, hi);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-    if ((threadIdx.x & 31) == 0 && wm) atomicMax(wmax, wm);
+    for (int o = 16; o > 0; o >>= 1) {
+        wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+        cells += __shfl_xor_sync(0xffffffffu, cells, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (wm) atomicMax(out, wm);
+        if (cells) atomicAdd(out + 1, cells);
+    }
 }
 
 // stats layout (uint64): 0 cells, 1 wmax of the R-row class, 2 wmax of the
@@ -254,14 +263,42 @@ __global__ void k_classify(const saber_band_job* __restrict__ jobs, uint64_t njo
 // ---------------------------------------------------------------------------
 // the scoring pipeline (device-resident jobs and scores)
 // ---------------------------------------------------------------------------
-// The long-job threshold of a call: in the automatic mode, a batch smaller
-// than the int16 lanes' job slots leaves most lanes idle while its longest
-// sweeps run alone, so sweeps above kLongStepsSmall steps go to the
-// warp-pipelined int32 kernel; larger batches keep every job on the lanes.
-static uint32_t long_steps_for(const saber_gpu* h, uint64_t njobs) {
+// The long-job threshold of a call.  In the automatic mode a one-lane sweep
+// goes to the warp-pipelined int32 kernel when it is longer than about four
+// times the sweep steps each int16 lane gets if the batch's cells were
+// spread evenly (a lane sweeps 32 cells per step), as a power of two, at
+// least kLongStepsSmall: such a job would otherwise set the launch's length
+// while most lanes are done.  Measured on one GB300 (threshold -> result):
+// the blastn batch (26.8 k kilobase regions, about 6.9 k steps per lane)
+// 2048 / 16384 / 32768 / none -> scoring 80 / 61 / 56 / 82 ms; the 1 M-job
+// microbench (about 11.6 k) 16384 / 65536 / none -> 8.66 / 8.71 / 8.67 ms;
+// the 11,000-query protein search (about 60 k) 32768 / none -> 64.1 /
+// 64.1 ms of device scoring.
+static uint32_t long_steps_for(const saber_gpu* h, uint64_t cells) {
     if (h->long_steps != kLongStepsAuto) return h->long_steps;
-    const uint64_t slots = (uint64_t)h->sm_count * band_fast_blocks_per_sm(h->strip_rows, false) * 256 / 32 * 64;
-    return njobs < slots ? kLongStepsSmall : kLongStepsNever;
+    const uint64_t lanes = (uint64_t)h->sm_count * band_fast_blocks_per_sm(h->strip_rows, false) * 256;
+    const uint64_t load = cells / 32 / (lanes ? lanes : 1);
+    uint64_t t = kLongStepsSmall;
+    while (t < 4 * load && t < (1ull << 30)) t <<= 1;
+    return (uint32_t)t;
+}
+
+// In-band cells of the device jobs (for the automatic long-job threshold):
+// one reduction and an 8-byte read-back, only in the automatic mode.
+static int jobs_cells(saber_gpu* h, const QuerySet& qs, const saber_band_job* d_jobs, uint64_t njobs,
+                      uint64_t* cells) {
+    *cells = 0;
+    if (h->long_steps != kLongStepsAuto || !qs.has || njobs == 0) return SABER_OK;
+    CUALLOC(h, h->g_wmax, 16);
+    CU(h, cudaMemsetAsync(h->g_wmax.p, 0, 16, h->stream));
+    k_job_wmax<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, h->stream>>>(
+        d_jobs, njobs, qs.offsets.as<uint64_t>(), qs.nq, h->g_wmax.as<unsigned long long>());
+    CU(h, cudaGetLastError());
+    unsigned long long r[2] = {0, 0};
+    CU(h, cudaMemcpyAsync(r, h->g_wmax.p, 16, cudaMemcpyDeviceToHost, h->stream));
+    CU(h, cudaStreamSynchronize(h->stream));
+    *cells = r[1];
+    return SABER_OK;
 }
 
 static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, const saber_band_job* d_jobs,
@@ -291,6 +328,10 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     CU(h, cudaMemsetAsync(stats, 0, 8 * 8, s));
 
     const QuerySet& qs = ds.qs;
+    uint64_t job_cells = 0;
+    int rc0 = jobs_cells(h, qs, d_jobs, njobs, &job_cells);
+    if (rc0 != SABER_OK) return rc0;
+    const uint32_t long_steps = long_steps_for(h, job_cells);
     cudaEvent_t ev[4];
     for (int i = 0; i < 4; i++) CU(h, cudaEventCreate(&ev[i]));
     struct EvGuard {
@@ -301,7 +342,7 @@ static int score_pipeline(saber_gpu* h, const Scheme& sch, const Dataset& ds, co
     } evg{ev};
     CU(h, cudaEventRecord(ev[0], s));
     k_classify<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, s>>>(
-        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, long_steps_for(h, njobs), qs.offsets.as<uint64_t>(), qs.nq,
+        d_jobs, njobs, nullptr, h->strip_rows, h->pair_steps, long_steps, qs.offsets.as<uint64_t>(), qs.nq,
         ds.n_res,
         h->keys_in.as<uint64_t>(),
         h->vals_in.as<uint32_t>(), d_scores, counts, stats);
@@ -446,7 +487,7 @@ static uint64_t pow2_at_least(uint64_t v, uint64_t lo) {
 // job count and band width, captured once per (size bucket, buffers,
 // settings) and replayed.  Jobs and scores live in the handle's buffers.
 static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& ds, uint64_t njobs, uint64_t wmax,
-                                saber_score_stats* st) {
+                                uint64_t job_cells, saber_score_stats* st) {
     if (!sch.has) return fail(h, SABER_ERR_STATE, "no scoring scheme set");
     if (!ds.has_db) return fail(h, SABER_ERR_STATE, "no database loaded");
     if (!ds.qs.has) return fail(h, SABER_ERR_STATE, "no query set loaded");
@@ -482,7 +523,8 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
     key.go = sch.go;
     key.ge = sch.ge;
     key.pair_steps = h->pair_steps;
-    key.long_steps = long_steps_for(h, njobs);
+    const uint32_t long_steps = long_steps_for(h, job_cells);
+    key.long_steps = long_steps;
     key.n_res = ds.n_res;  // scalar kernel parameters baked into the graph
     key.nq = qs.nq;
     key.prof8 = qs.p8 ? qs.prof8.p : nullptr;  // which packed kernel the graph launches
@@ -507,7 +549,7 @@ static int score_pipeline_graph(saber_gpu* h, const Scheme& sch, const Dataset& 
         chk(cudaMemsetAsync(counts, 0, 16 * 4, s));
         chk(cudaMemsetAsync(stats, 0, 8 * 8, s));
         k_classify<<<nblocks(npad, 256, h->sm_count * 8), 256, 0, s>>>(
-            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, long_steps_for(h, njobs),
+            d_jobs, npad, h->g_nreal.as<uint32_t>(), rows0, h->pair_steps, long_steps,
             qs.offsets.as<uint64_t>(), qs.nq,
             ds.n_res, h->keys_in.as<uint64_t>(), h->vals_in.as<uint32_t>(), d_scores, counts, stats);
         chk(cudaGetLastError());
@@ -1312,24 +1354,25 @@ int saber_gpu_score_band_jobs(saber_gpu* h, const saber_band_job* jobs, uint64_t
     }
     int rc;
     if (h->use_graphs) {
-        // the widest clipped band sizes the graph's scratch: one reduction on
-        // the device after the copy, 8 bytes read back
+        // the widest clipped band sizes the graph's scratch and the cell total
+        // sets the automatic long-job threshold: one reduction on the device
+        // after the copy, 16 bytes read back
         const QuerySet& qs = h->main.qs;
         const uint64_t npad = pow2_at_least(njobs, 1 << 12);
         CUALLOC(h, h->jobs_dev, npad * sizeof(saber_band_job));
         CUALLOC(h, h->scores_dev, npad * 4);
-        CUALLOC(h, h->g_wmax, 8);
+        CUALLOC(h, h->g_wmax, 16);
         CU(h, cudaMemcpyAsync(h->jobs_dev.p, jobs, njobs * sizeof(saber_band_job), cudaMemcpyHostToDevice, h->stream));
-        CU(h, cudaMemsetAsync(h->g_wmax.p, 0, 8, h->stream));
+        CU(h, cudaMemsetAsync(h->g_wmax.p, 0, 16, h->stream));
         if (qs.has)
             k_job_wmax<<<nblocks(njobs, 256, h->sm_count * 8), 256, 0, h->stream>>>(
                 h->jobs_dev.as<saber_band_job>(), njobs, qs.offsets.as<uint64_t>(), qs.nq,
                 h->g_wmax.as<unsigned long long>());
         CU(h, cudaGetLastError());
-        unsigned long long wmax = 0;
-        CU(h, cudaMemcpyAsync(&wmax, h->g_wmax.p, 8, cudaMemcpyDeviceToHost, h->stream));
+        unsigned long long r[2] = {0, 0};
+        CU(h, cudaMemcpyAsync(r, h->g_wmax.p, 16, cudaMemcpyDeviceToHost, h->stream));
         CU(h, cudaStreamSynchronize(h->stream));
-        rc = score_pipeline_graph(h, h->scheme, h->main, njobs, wmax, stats);
+        rc = score_pipeline_graph(h, h->scheme, h->main, njobs, r[0], r[1], stats);
     } else {
         CUALLOC(h, h->jobs_dev, njobs * sizeof(saber_band_job));
         CUALLOC(h, h->scores_dev, njobs * 4);

@@ -13,7 +13,9 @@ never results:
 * the long-job bin edge (`Device.long_steps`): a job whose one-lane sweep is
   longer than this goes to the warp-per-job int32 kernel's pipelined strips
   (a whole warp on one job) instead of a lane of the int16 kernel; the
-  default picks it from the batch size.
+  default picks it per call from the batch's in-band cells per lane (the
+  power of two at or above four times a lane's even share of the sweep
+  steps, at least 2048).
 
 `autotune_scoring` times settings on the caller's own batch (the
 device-resident entry point, same stream) by coordinate descent: starting
@@ -34,7 +36,7 @@ LONG_AUTO = 0xFFFFFFFE
 KNOBS = (
     ("strip_rows", (16, 8)),
     ("pair_steps", (2048, 1024, 4096, 8192, PAIR_NEVER)),
-    ("long_steps", (LONG_AUTO, 4096, 8192, 16384, 32768)),
+    ("long_steps", (LONG_AUTO, 4096, 8192, 16384, 65536)),
 )
 
 
