@@ -113,8 +113,8 @@ __device__ __forceinline__ void cell(uint32_t& E, uint32_t Gleft, uint32_t Gup, 
 
 template <int R>
 struct StripState {
-    uint32_t Hd[R];  // G = H - go of (row r, previous column)
-    uint32_t X[R];   // E(row r, previous column)
+    uint32_t Gd[R];  // G = H - go of (row r, previous column)
+    uint32_t E[R];   // E(row r, previous column)
 };
 
 // One job of a half: its window, clipped band and rows.  T is the profile's
@@ -275,15 +275,15 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
     for (int r = 0; r < R; r++) {
         if (MODE == 0 && r > U) break;
         uint32_t G, F;
-        uint32_t gold = st.Hd[r];
-        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, G, F);
+        uint32_t gold = st.Gd[r];
+        cell(st.E[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, G, F);
         if (MODE == 2) {
             uint32_t mk = ragged_mask(r, thr_a, thr_b);
             G = (G & mk) | (c.neg2 & ~mk);
             F = (F & mk) | (c.neg2 & ~mk);
         }
         diag = gold;
-        st.Hd[r] = G;
+        st.Gd[r] = G;
         Gup = G;
         Fup = F;
         // running best over row pairs: one three-input max per two rows
@@ -395,8 +395,8 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
     for (int r = 0; r < R; r++) {
         if (PH == 0 && r > G) break;
         uint32_t Gv, F;
-        uint32_t gold = st.Hd[r];
-        cell(st.X[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, Gv, F);
+        uint32_t gold = st.Gd[r];
+        cell(st.E[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, Gv, F);
         if (PH == 0 && r > G - R - 1) {
             Gv = (Gv & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
             F = (F & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
@@ -407,7 +407,7 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
             F = (F & mk) | (c.neg2 & ~mk);
         }
         diag = gold;
-        st.Hd[r] = Gv;
+        st.Gd[r] = Gv;
         Gup = Gv;
         Fup = F;
         if (r & 1) best = __vimax3_s16x2(best, gprev, Gv);
@@ -515,8 +515,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T*
         if (g0 == 0) {
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                st.Hd[r] = c.neg2;
-                st.X[r] = c.neg2;
+                st.Gd[r] = c.neg2;
+                st.E[r] = c.neg2;
             }
             diag0 = __byte_perm(__ldca(pbuf), c.neg2, 0x5410);
             lastG = c.neg2;
@@ -533,8 +533,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T*
         } else {
 #pragma unroll
             for (int r = 0; r < R; r++) {
-                st.Hd[r] = c.ngo2;
-                st.X[r] = c.neg2;
+                st.Gd[r] = c.ngo2;
+                st.E[r] = c.neg2;
             }
             const int kskip = min(g0 - 2 * R, wmax);
             for (int k = 0; k < kskip; k++) stbuf(pbuf + (size_t)k * 32, top0);
@@ -677,8 +677,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
             if (u0 == 0) {
 #pragma unroll
                 for (int r = 0; r < R; r++) {
-                    st.Hd[r] = c.neg2;
-                    st.X[r] = c.neg2;
+                    st.Gd[r] = c.neg2;
+                    st.E[r] = c.neg2;
                 }
                 diag0 = __ldca(mybuf).x;
                 p.wa = code_word(ha, 0);
@@ -695,8 +695,8 @@ __global__ void __launch_bounds__(256, 2) k_band_fast(
                 // later strip that sweeps from step 0 reads them)
 #pragma unroll
                 for (int r = 0; r < R; r++) {
-                    st.Hd[r] = c.ngo2;
-                    st.X[r] = c.neg2;
+                    st.Gd[r] = c.ngo2;
+                    st.E[r] = c.neg2;
                 }
                 const int kskip = min(u0 - R + 1, wmax);
                 for (int k = 0; k < kskip; k++) stbuf(mybuf + (size_t)k * 32, make_uint2(c.ngo2, c.neg2));
