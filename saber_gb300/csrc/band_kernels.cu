@@ -251,12 +251,18 @@ __device__ __forceinline__ uint32_t sub_of(const StepLoads<R, T>& L, int r) {
     }
 }
 
-// Mask of the halves whose row r is still inside its band at this step
-// (row r is in band while r >= thr_half, thr = u - w + 1).
-__device__ __forceinline__ uint32_t ragged_mask(int r, int thr_a, int thr_b) {
-    uint32_t ma = (r >= thr_a) ? 0x0000FFFFu : 0u;
-    uint32_t mb = (r >= thr_b) ? 0xFFFF0000u : 0u;
-    return ma | mb;
+// Right-edge masks: a half's row r is in band while r >= thr (thr = u - w +
+// 1).  ragged_nthr packs -thr of both halves, thr clamped to [0, rows] so
+// that r - thr fits int16 (once per step); ragged_out gives 0xFFFF in the
+// halves whose row r is out of band: one packed add (FMA pipe) and one
+// permute that replicates each half's sign.
+__device__ __forceinline__ uint32_t ragged_nthr(int thr_a, int thr_b, int rows) {
+    thr_a = min(max(thr_a, 0), rows);
+    thr_b = min(max(thr_b, 0), rows);
+    return (uint32_t)(uint16_t)(-thr_a) | ((uint32_t)(uint16_t)(-thr_b) << 16);
+}
+__device__ __forceinline__ uint32_t ragged_out(int r, uint32_t nthr2) {
+    return prmt(__vadd2((uint32_t)r * 0x10001u, nthr2), 0u, 0xBB99u);
 }
 
 // One column step of a strip.  MODE 0: left triangle, rows 0..U computed
@@ -271,6 +277,7 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
     uint32_t diag = diag0;
     diag0 = L.top.x;
     uint32_t gprev = 0;
+    const uint32_t nthr2 = MODE == 2 ? ragged_nthr(thr_a, thr_b, R) : 0u;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (MODE == 0 && r > U) break;
@@ -278,9 +285,9 @@ __device__ __forceinline__ void strip_step(StripState<R>& st, uint32_t& diag0, u
         uint32_t gold = st.Gd[r];
         cell(st.E[r], gold, Gup, Fup, diag, sub_of<R, T>(L, r), c, G, F);
         if (MODE == 2) {
-            uint32_t mk = ragged_mask(r, thr_a, thr_b);
-            G = (G & mk) | (c.neg2 & ~mk);
-            F = (F & mk) | (c.neg2 & ~mk);
+            const uint32_t out = ragged_out(r, nthr2);
+            G = (G & ~out) | (c.neg2 & out);
+            F = (F & ~out) | (c.neg2 & out);
         }
         diag = gold;
         st.Gd[r] = G;
@@ -391,6 +398,7 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
     uint32_t diag = diag0;
     diag0 = Gup;
     uint32_t gprev = 0;
+    const uint32_t nthr2 = PH == 2 ? ragged_nthr(thr_a, thr_b, R) : 0u;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         if (PH == 0 && r > G) break;
@@ -402,9 +410,9 @@ __device__ __forceinline__ void pair_step(StripState<R>& st, uint32_t& diag0, ui
             F = (F & 0x0000FFFFu) | (c.neg2 & 0xFFFF0000u);
         }
         if (PH == 2) {
-            uint32_t mk = ragged_mask(r, thr_a, thr_b);
-            Gv = (Gv & mk) | (c.neg2 & ~mk);
-            F = (F & mk) | (c.neg2 & ~mk);
+            const uint32_t out = ragged_out(r, nthr2);
+            Gv = (Gv & ~out) | (c.neg2 & out);
+            F = (F & ~out) | (c.neg2 & out);
         }
         diag = gold;
         st.Gd[r] = Gv;
