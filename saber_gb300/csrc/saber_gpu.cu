@@ -884,7 +884,10 @@ struct AlignResult {
 using RunPools = std::vector<std::vector<uint32_t>>;
 
 // Budget of the direction-byte pool per launch (larger batches are split).
-constexpr uint64_t kDirPoolBudget = 2ull << 30;
+// A launch ends with its longest job, so few launches per round matter: the
+// blastn batch's first round (14.6 k alignments of kilobase windows, about
+// 6.6 GB of direction bytes) fits one launch.
+constexpr uint64_t kDirPoolBudget = 8ull << 30;
 constexpr uint64_t kAlignSlabBudget = 512ull << 20;
 
 static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const std::vector<AlignHostReq>& in,
@@ -908,6 +911,32 @@ static int align_batch(saber_gpu* h, const Scheme& sch, const Dataset& ds, const
             continue;
         }
         todo.push_back(t);
+    }
+    // largest size class first (classes of log2 of the band cells, input
+    // order within a class, one counting pass): warp w takes jobs w, w +
+    // warps, ..., so the longest ones start together and the short ones fill
+    // in behind them; within a class jobs of one query stay together.  Each
+    // job is independent and results go back by index.
+    {
+        std::vector<uint8_t> cls(todo.size());
+        size_t count[65] = {0};
+        for (size_t k = 0; k < todo.size(); k++) {
+            const AlignHostReq& r = in[todo[k]];
+            int64_t lo = r.lo, hi = r.hi;
+            const int64_t m = (int64_t)(qs.offs[r.query + 1] - qs.offs[r.query]);
+            const uint64_t cells = (uint64_t)m * (uint64_t)clip_band(m, r.win_len, lo, hi);
+            cls[k] = (uint8_t)(cells ? 64 - __builtin_clzll(cells) : 0);  // 1 + floor(log2), 0 for none
+            count[cls[k]]++;
+        }
+        size_t start[65];
+        size_t acc = 0;
+        for (int c = 64; c >= 0; c--) {
+            start[c] = acc;
+            acc += count[c];
+        }
+        std::vector<size_t> sorted(todo.size());
+        for (size_t k = 0; k < todo.size(); k++) sorted[start[cls[k]]++] = todo[k];
+        todo.swap(sorted);
     }
     cudaStream_t s = h->stream;
     size_t pos = 0;
