@@ -916,6 +916,91 @@ struct RegionArgs {
     unsigned long long* ctr;          // [7] hsps, [8] weak dropped
 };
 
+// Top list of one pair's regions by (best desc, d_min asc), with each
+// region's HSP count, score sum and seed hits.  TopLocal holds up to 64 (the
+// largest max_regions_per_subject) in local memory; TopReg holds up to K in
+// registers, inserted by a compile-time network (the default cap is 4).  A
+// new region goes after every entry that is not worse than it, as the
+// reference's stable order does.
+struct TopLocal {
+    saber_region top[64];
+    uint4 tst[64];
+    uint32_t ntop = 0;
+    __device__ __forceinline__ void insert(const saber_region& r, uint4 st, uint32_t kmax) {
+        uint32_t pos = ntop;
+        while (pos > 0 && (top[pos - 1].best < r.best || (top[pos - 1].best == r.best && top[pos - 1].d_min > r.d_min)))
+            pos--;
+        if (pos >= kmax) return;
+        uint32_t last = ntop < kmax ? ntop : kmax - 1;
+        for (uint32_t k = last; k > pos; k--) {
+            top[k] = top[k - 1];
+            tst[k] = tst[k - 1];
+        }
+        top[pos] = r;
+        tst[pos] = st;
+        if (ntop < kmax) ntop++;
+    }
+    __device__ __forceinline__ saber_region region(uint32_t k, uint32_t, uint32_t) const { return top[k]; }
+    __device__ __forceinline__ uint4 stat(uint32_t k) const { return tst[k]; }
+};
+
+template <int K>
+struct TopReg {
+    int32_t dmin[K], dmax[K], best[K];
+    uint4 tst[K];
+    uint32_t ntop = 0;
+    __device__ __forceinline__ void insert(const saber_region& r, uint4 st, uint32_t kmax) {
+        uint32_t pos = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const bool worse = best[k] < r.best || (best[k] == r.best && dmin[k] > r.d_min);
+            pos += ((uint32_t)k < ntop && !worse) ? 1u : 0u;
+        }
+        if (pos >= kmax) return;
+#pragma unroll
+        for (int k = K - 1; k > 0; k--) {
+            if ((uint32_t)k > pos) {
+                dmin[k] = dmin[k - 1];
+                dmax[k] = dmax[k - 1];
+                best[k] = best[k - 1];
+                tst[k] = tst[k - 1];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if ((uint32_t)k == pos) {
+                dmin[k] = r.d_min;
+                dmax[k] = r.d_max;
+                best[k] = r.best;
+                tst[k] = st;
+            }
+        }
+        if (ntop < kmax) ntop++;
+    }
+    __device__ __forceinline__ saber_region region(uint32_t k, uint32_t q, uint32_t s) const {
+        saber_region r;
+        r.query = q;
+        r.subject = s;
+        r.d_min = r.d_max = r.best = 0;
+#pragma unroll
+        for (int j = 0; j < K; j++)
+            if ((uint32_t)j == k) {
+                r.d_min = dmin[j];
+                r.d_max = dmax[j];
+                r.best = best[j];
+            }
+        return r;
+    }
+    __device__ __forceinline__ uint4 stat(uint32_t k) const {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+        for (int j = 0; j < K; j++)
+            if ((uint32_t)j == k) v = tst[j];
+        return v;
+    }
+};
+
+template <class Top>
 __global__ void k_regions(RegionArgs a) {
     unsigned long long hsps = 0, weak = 0;
     const uint32_t np = *a.npairs;
@@ -927,9 +1012,7 @@ __global__ void k_regions(RegionArgs a) {
         const int thr = a.region_thr ? a.region_thr[q] : a.hsp_thr;
         hsps += e - b;
         // top kmax regions by (best desc, d_min asc)
-        saber_region top[64];
-        uint4 tst[64];
-        uint32_t ntop = 0;
+        Top top;
         int64_t dmin = 0, dmax = 0;
         int best = 0;
         uint32_t evn = 0, evh = 0;
@@ -946,19 +1029,7 @@ __global__ void k_regions(RegionArgs a) {
             r.d_min = (int32_t)dmin;
             r.d_max = (int32_t)dmax;
             r.best = best;
-            // insert into the top list
-            uint32_t pos = ntop;
-            while (pos > 0 && (top[pos - 1].best < r.best || (top[pos - 1].best == r.best && top[pos - 1].d_min > r.d_min)))
-                pos--;
-            if (pos >= a.kmax) return;
-            uint32_t last = ntop < a.kmax ? ntop : a.kmax - 1;
-            for (uint32_t k = last; k > pos; k--) {
-                top[k] = top[k - 1];
-                tst[k] = tst[k - 1];
-            }
-            top[pos] = r;
-            tst[pos] = make_uint4(evn, (uint32_t)evs, evh, 0u);
-            if (ntop < a.kmax) ntop++;
+            top.insert(r, make_uint4(evn, (uint32_t)evs, evh, 0u), a.kmax);
         };
         for (uint32_t i = b; i < e; i++) {
             const uint4 h = a.hsp[a.order[i]];
@@ -982,12 +1053,12 @@ __global__ void k_regions(RegionArgs a) {
             }
         }
         if (open) close();
-        if (ntop) {
-            const unsigned long long base = atomicAdd(a.nout, (unsigned long long)ntop);
-            for (uint32_t k = 0; k < ntop; k++)
+        if (top.ntop) {
+            const unsigned long long base = atomicAdd(a.nout, (unsigned long long)top.ntop);
+            for (uint32_t k = 0; k < top.ntop; k++)
                 if (base + k < a.cap) {
-                    a.out[base + k] = top[k];
-                    a.rstat[base + k] = tst[k];
+                    a.out[base + k] = top.region(k, q, s);
+                    a.rstat[base + k] = top.stat(k);
                 }
         }
     }
@@ -1732,7 +1803,10 @@ int scan_regions(saber_gpu* h, const saber_scan_params* p, const uint8_t* q_mask
             r.nout = ctr + 12;
             r.cap = rcap;
             r.ctr = ctr;
-            k_regions<<<nblocks(nhsp, 128), 128, 0, s>>>(r);
+            if (r.kmax <= 4)
+                k_regions<TopReg<4>><<<nblocks(nhsp, 128), 128, 0, s>>>(r);
+            else
+                k_regions<TopLocal><<<nblocks(nhsp, 128), 128, 0, s>>>(r);
             CU(h, cudaGetLastError());
             unsigned long long nr = 0;
             CU(h, cudaMemcpyAsync(&nr, ctr + 12, 8, cudaMemcpyDeviceToHost, s));

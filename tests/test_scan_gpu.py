@@ -51,12 +51,15 @@ def test_scan_regions_match_oracle(dev, preset):
     _check(got, gst, want, ost)
 
 
-def test_scan_caps_and_no_filter(dev):
+@pytest.mark.parametrize("per_subject", [2, 9])
+def test_scan_caps_and_no_filter(dev, per_subject):
     """Small frequent-seed cap, no window filter, tiny per-subject and
-    per-query region caps, full 20-letter alphabet with contiguous seeds."""
+    per-query region caps, full 20-letter alphabet with contiguous seeds.
+    Per-subject caps up to 4 keep the top list in registers, larger ones in
+    local memory."""
     qs, ss, planted = synth.protein_db(17, 10, 800)
     got, gst, want, ost = _run(dev, qs, ss, None, None, None, None, ["1111", "11011"], presets.full_alphabet(),
-                               min_ids=0, exact_weight=0, seed_max_occ=6, max_regions_per_subject=2,
+                               min_ids=0, exact_weight=0, seed_max_occ=6, max_regions_per_subject=per_subject,
                                max_candidates=7)
     assert ost["seeds_frequent_skipped"] > 0 and ost["regions_dropped_by_cap"] > 0
     _check(got, gst, want, ost)
