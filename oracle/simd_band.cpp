@@ -1,6 +1,6 @@
 /*
  * SIMD-class CPU restatement of the reference's banded scoring — TEST AND
- * BASELINE INFRASTRUCTURE ONLY.  bench.py times it as the CPU baseline and
+ * CPU-BASELINE INFRASTRUCTURE ONLY.  bench.py times it as the CPU baseline and
  * as the reference arm; tests/test_simd_baseline.py holds it to the scalar
  * oracle (orc_banded_score).  The product library never links it.
  *
