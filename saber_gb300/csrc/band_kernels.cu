@@ -362,7 +362,25 @@ struct PairPipe {
     StepLoads<R, T> cur, nxt;  // top.x: boundary word of the low half's row above
     uint32_t w, w2;         // code words of the low half: group of step g + 1, next group
     int cprev;              // low half's code at step g (the high half's at step g + 1)
+    // int8 profiles: rows R .. 2R-1 of the low half's last 32-byte block, the
+    // high half's rows at the next step (one load serves both halves)
+    uint32_t hi[sizeof(T) == 1 ? StepLoads<R, T>::kW : 1];
 };
+
+// One aligned 2R-row block of an int8 profile at code c: rows 0 .. R-1 to lo,
+// rows R .. 2R-1 to hi.
+template <int R, class T>
+__device__ __forceinline__ void ld_block(uint32_t (&lo)[StepLoads<R, T>::kW], uint32_t (&hi)[StepLoads<R, T>::kW],
+                                         const T* p) {
+    static_assert(sizeof(T) == 1 && R == 16, "one 32-byte load covers 32 int8 rows");
+    uint32_t d[8];
+    ld_prof(d, p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        lo[i] = d[i];
+        hi[i] = d[4 + i];
+    }
+}
 
 // Called before computing step g: cur <- nxt (step g), issue step g + 1.
 template <int R, class T, int K>
@@ -379,8 +397,15 @@ __device__ __forceinline__ void pair_advance(PairPipe<R, T>& p, const HalfStrip<
     const int cb = p.cprev;
     p.cprev = ca;
     const int kin = g + 2 <= wmax ? g + 2 : wmax;
-    ld_prof(p.nxt.a, ha.rows + (size_t)ca * ha.mpad);
-    ld_prof(p.nxt.b, hb_rows + (size_t)cb * ha.mpad);
+    if constexpr (sizeof(T) == 1) {
+        // the high half's rows at code cb came with the low half's block last step
+#pragma unroll
+        for (int i = 0; i < StepLoads<R, T>::kW; i++) p.nxt.b[i] = p.hi[i];
+        ld_block<R, T>(p.nxt.a, p.hi, ha.rows + (size_t)ca * ha.mpad);
+    } else {
+        ld_prof(p.nxt.a, ha.rows + (size_t)ca * ha.mpad);
+        ld_prof(p.nxt.b, hb_rows + (size_t)cb * ha.mpad);
+    }
     p.nxt.top.x = __ldca(pbuf + (size_t)kin * 32);
 }
 
@@ -532,7 +557,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T*
             p.w = code_word(ha, 0);
             p.w2 = code_word(ha, 4);
             const int ca0 = (int)(p.w & 0xFFu);
-            ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
+            if constexpr (sizeof(T) == 1) ld_block<R, T>(p.nxt.a, p.hi, ha.rows + (size_t)ca0 * ha.mpad);
+            else ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
             ld_prof(p.nxt.b, hb_rows + (size_t)kSentCode * ha.mpad);
             p.nxt.top.x = __ldca(pbuf + 32);
             p.cprev = ca0;
@@ -554,7 +580,8 @@ __device__ __noinline__ void pair_task(const uint8_t* __restrict__ res, const T*
             p.w2 = code_word(ha, g0 + 3);
             const int ca0 = (int)((p.w >> 8) & 0xFFu);  // step g0 (= 1 mod 4)
             const int cb0 = (int)(p.w & 0xFFu);         // the high half's: the low half's at g0 - 1
-            ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
+            if constexpr (sizeof(T) == 1) ld_block<R, T>(p.nxt.a, p.hi, ha.rows + (size_t)ca0 * ha.mpad);
+            else ld_prof(p.nxt.a, ha.rows + (size_t)ca0 * ha.mpad);
             ld_prof(p.nxt.b, hb_rows + (size_t)cb0 * ha.mpad);
             p.nxt.top.x = __ldca(pbuf + (size_t)(g0 + 1 <= wmax ? g0 + 1 : wmax) * 32);
             p.cprev = ca0;
